@@ -1,0 +1,339 @@
+/*
+ * lue_oracle.c — CPU restatement of LUE's flow-routing hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle that the CUDA path is checked against: only
+ * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it.  The product library
+ * (liblue_gb300.so) never links, calls or falls back to it.
+ *
+ * Parity pinning: tests/test_oracle_golden.py runs every known-answer case extracted from the
+ * reference's own unit tests (tests/golden/reference_cases.json) through this file.  The reference
+ * itself cannot be built here (it needs HPX and Boost), so those vectors are the pin.
+ *
+ * What is restated (paths within computationalgeography/lue; ALG/ = source/framework/algorithm/
+ * include/lue/framework/algorithm/):
+ *
+ *   - D8 decoding with the partition-exit flag ............ ALG/detail/flow_direction.hpp:11-112
+ *   - per-partition inflow count + no-data marking ......... ALG/detail/inflow_count.hpp:9-351
+ *   - partition input cells (+1 per cross-partition inflow)  ALG/definition/inflow_count.hpp:97-577
+ *   - domain decomposition (last partition absorbs rest) .. source/framework/core/include/lue/
+ *                                                            framework/core/domain_decomposition.hpp:90-175
+ *   - the ridge-walk ("accumulate") ........................ ALG/definition/accumulating_router.hpp:525-599
+ *   - intra-partition row-major ridge scan ................. ALG/definition/accumulating_router.hpp:866-882
+ *   - inter-partition hand-off of (cell, outflow) .......... ALG/definition/accumulating_router.hpp:467-506,
+ *                                                            602-645, 984-1010
+ *   - cell functors: accu ................................. ALG/definition/accu.hpp:27-197
+ *                    accu_threshold ....................... ALG/definition/accu_threshold.hpp:29-260
+ *                    accu_fraction ........................ ALG/definition/accu_fraction.hpp:29-253
+ *                    kinematic_wave ....................... ALG/definition/kinematic_wave.hpp:13-456
+ *   - value-policy domains ................................ ALG/value_policies/{accu,accu_threshold,
+ *                                                            accu_fraction,kinematic_wave}.hpp:15-21
+ *
+ * Kinematic wave calls Boost.Math's newton_raphson_iterate (boost/math/tools/roots.hpp; Boost is
+ * unpinned by the reference: Conan "boost/[1.74 || >1.75]", Conda libboost-devel).  Boost is not in
+ * the reference tree; lue_oracle_newton_raphson() below restates its documented contract (Newton
+ * steps; a step that leaves the bracket is replaced by bisection towards the violated bound; stop when
+ * the last step is below |x| * 2^(1 - digits), when f(x) == 0, or after max_iter evaluations).
+ *
+ * The inter-partition arrival order in the reference is whatever order HPX channels deliver; here it
+ * is a FIFO (single-threaded) or per-partition mailboxes drained by worker threads (threaded mode).
+ * Float results therefore agree with the reference up to summation order.
+ */
+#include <math.h>
+#include <float.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define U8_NO_DATA 255u
+
+/* ------------------------------------------------------------------------------------------------ */
+/* D8                                                                                                */
+/* ------------------------------------------------------------------------------------------------ */
+
+/* Keypad codes (ALG/flow_direction.hpp:7-35): 7 8 9 / 4 5 6 / 1 2 3; any other code is a sink. */
+static inline void d8_offset(uint8_t code, int* dr, int* dc)
+{
+    switch (code) {
+        case 7: *dr = -1; *dc = -1; return;
+        case 8: *dr = -1; *dc = 0; return;
+        case 9: *dr = -1; *dc = 1; return;
+        case 4: *dr = 0; *dc = -1; return;
+        case 6: *dr = 0; *dc = 1; return;
+        case 1: *dr = 1; *dc = -1; return;
+        case 2: *dr = 1; *dc = 0; return;
+        case 3: *dr = 1; *dc = 1; return;
+        default: *dr = 0; *dc = 0; return;
+    }
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Partitioning                                                                                      */
+/* ------------------------------------------------------------------------------------------------ */
+
+typedef struct {
+    int64_t rows, cols;      /* array */
+    int64_t nprow, npcol;    /* partition grid */
+    int64_t prow, pcol;      /* nominal partition extent */
+} Grid;
+
+static int grid_init(Grid* g, int64_t rows, int64_t cols, int64_t prow, int64_t pcol)
+{
+    if (rows <= 0 || cols <= 0 || prow <= 0 || pcol <= 0 || prow > rows || pcol > cols) return -1;
+    g->rows = rows; g->cols = cols; g->prow = prow; g->pcol = pcol;
+    g->nprow = rows / prow; g->npcol = cols / pcol;
+    return 0;
+}
+
+/* Row range [r0, r1) of partition row pr: the last partition absorbs the remainder. */
+static inline void part_rows(const Grid* g, int64_t pr, int64_t* r0, int64_t* r1)
+{
+    *r0 = pr * g->prow;
+    *r1 = (pr == g->nprow - 1) ? g->rows : *r0 + g->prow;
+}
+static inline void part_cols(const Grid* g, int64_t pc, int64_t* c0, int64_t* c1)
+{
+    *c0 = pc * g->pcol;
+    *c1 = (pc == g->npcol - 1) ? g->cols : *c0 + g->pcol;
+}
+static inline int64_t part_of_row(const Grid* g, int64_t r)
+{
+    int64_t p = r / g->prow;
+    return p >= g->nprow ? g->nprow - 1 : p;
+}
+static inline int64_t part_of_col(const Grid* g, int64_t c)
+{
+    int64_t p = c / g->pcol;
+    return p >= g->npcol ? g->npcol - 1 : p;
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Inflow count                                                                                      */
+/* ------------------------------------------------------------------------------------------------ */
+
+/*
+ * Router-internal counts (int8 in the reference, no-data -128): per partition, count upstream
+ * neighbours inside the partition (ALG/detail/inflow_count.hpp:9-351), then add one per partition
+ * input cell arrival from a neighbouring partition (ALG/definition/inflow_count.hpp:558-574).
+ * A cell whose flow leaves the array contributes nothing (no neighbour partition, no message).
+ */
+static void router_counts(const Grid* g, const uint8_t* fd, int value_policies, int8_t* cnt)
+{
+    const int64_t cols = g->cols;
+    memset(cnt, 0, (size_t)(g->rows * cols));
+    for (int64_t pr = 0; pr < g->nprow; ++pr) {
+        int64_t r0, r1;
+        part_rows(g, pr, &r0, &r1);
+        for (int64_t pc = 0; pc < g->npcol; ++pc) {
+            int64_t c0, c1;
+            part_cols(g, pc, &c0, &c1);
+            for (int64_t r = r0; r < r1; ++r) {
+                for (int64_t c = c0; c < c1; ++c) {
+                    uint8_t code = fd[r * cols + c];
+                    if (value_policies && code == U8_NO_DATA) {
+                        cnt[r * cols + c] = INT8_MIN;
+                        continue;
+                    }
+                    int dr, dc;
+                    d8_offset(code, &dr, &dc);
+                    if (dr == 0 && dc == 0) continue;
+                    int64_t rd = r + dr, cd = c + dc;
+                    if (rd >= r0 && rd < r1 && cd >= c0 && cd < c1) cnt[rd * cols + cd] += 1;
+                }
+            }
+        }
+    }
+    /* partition input cells: flow that crosses a partition boundary but stays in the array */
+    for (int64_t r = 0; r < g->rows; ++r) {
+        for (int64_t c = 0; c < cols; ++c) {
+            uint8_t code = fd[r * cols + c];
+            if (value_policies && code == U8_NO_DATA) continue;
+            int dr, dc;
+            d8_offset(code, &dr, &dc);
+            if (dr == 0 && dc == 0) continue;
+            int64_t rd = r + dr, cd = c + dc;
+            if (rd < 0 || rd >= g->rows || cd < 0 || cd >= cols) continue;
+            if (part_of_row(g, rd) != part_of_row(g, r) || part_of_col(g, cd) != part_of_col(g, c))
+                cnt[rd * cols + cd] += 1;
+        }
+    }
+}
+
+/*
+ * Public inflow_count<uint8> (ALG/definition/inflow_count.hpp:665-726).  With value policies
+ * (DefaultValuePolicies) a no-data flow direction gives count 255; with DefaultPolicies the value 255
+ * is just an unknown code, i.e. a sink.
+ */
+int lue_oracle_inflow_count(const uint8_t* fd, int64_t rows, int64_t cols, int64_t prow, int64_t pcol,
+                            int value_policies, uint8_t* out)
+{
+    Grid g;
+    if (grid_init(&g, rows, cols, prow, pcol)) return -1;
+    int8_t* cnt = (int8_t*)malloc((size_t)(rows * cols));
+    if (!cnt) return -2;
+    router_counts(&g, fd, value_policies, cnt);
+    for (int64_t i = 0; i < rows * cols; ++i)
+        out[i] = (cnt[i] == INT8_MIN && value_policies && fd[i] == U8_NO_DATA) ? U8_NO_DATA : (uint8_t)cnt[i];
+    free(cnt);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Newton-Raphson (restated contract of boost::math::tools::newton_raphson_iterate)                 */
+/* ------------------------------------------------------------------------------------------------ */
+
+typedef struct {
+    double k;             /* time_step_duration / channel_length */
+    double alpha, beta, alpha_beta;
+    double known;         /* k * Qup + alpha * Qcur^beta + dt * q */
+} KwSolve;
+
+static inline void kw_eval(const KwSolve* s, double q, double* f, double* df)
+{
+    double qb1 = pow(q, s->beta - 1.0);
+    *f = s->k * q + s->alpha * pow(q, s->beta) - s->known;
+    *df = s->k + s->alpha_beta * qb1;
+}
+
+/*
+ * Newton iteration on [lo, hi] with the documented stopping rule.  Returns the last iterate; *iters
+ * receives the number of function evaluations used.
+ */
+double lue_oracle_newton_raphson_kw(double k, double alpha, double beta, double known, double guess,
+                                    double lo, double hi, int digits, int max_iter, int* iters)
+{
+    KwSolve s = {k, alpha, beta, alpha * beta, known};
+    double factor = ldexp(1.0, 1 - digits);
+    double x = guess;
+    int n = 0;
+    while (n < max_iter) {
+        double f, df;
+        kw_eval(&s, x, &f, &df);
+        ++n;
+        if (f == 0.0) break;
+        double step;
+        if (df == 0.0 || !isfinite(df)) {
+            /* no usable slope: bisect towards the bound on the side the residual points to */
+            step = f > 0.0 ? 0.5 * (x - lo) : 0.5 * (x - hi);
+        } else {
+            step = f / df;
+        }
+        double next = x - step;
+        if (next <= lo) {
+            step = 0.5 * (x - lo);
+            next = x - step;
+        } else if (next >= hi) {
+            step = 0.5 * (x - hi);
+            next = x - step;
+        }
+        /* shrink the bracket: the root lies on the side the step points to */
+        if (step > 0.0) hi = x; else lo = x;
+        x = next;
+        if (fabs(step) <= fabs(x) * factor) break;
+        if (x == lo || x == hi) break;
+    }
+    if (iters) *iters = n;
+    return x;
+}
+
+/* iterate_to_new_discharge (ALG/definition/kinematic_wave.hpp:145-254), F = double. */
+double lue_oracle_iterate_to_new_discharge_f64(double upstream, double current, double lateral,
+                                               double alpha, double beta, double dt, double dx)
+{
+    double new_q = 0.0;
+    if (upstream + current > 0.0 || lateral > 0.0) {
+        double inflow = lateral >= 0.0 ? lateral : 0.0;
+        double k = dt / dx;
+        double known = k * upstream + alpha * pow(current, beta) + dt * inflow;
+        /* guess (kinematic_wave.hpp:61-91) */
+        double guess = DBL_MIN;
+        if (current + upstream != 0.0 || beta >= 1.0) {
+            double a_b_pq = alpha * beta * pow((current + upstream) / 2.0, beta - 1.0);
+            guess = (k * upstream + a_b_pq * current + dt * inflow) / (k + a_b_pq);
+            if (!(guess > DBL_MIN)) guess = DBL_MIN;
+        }
+        int digits = (int)(DBL_MANT_DIG * 0.6);
+        new_q = lue_oracle_newton_raphson_kw(k, alpha, beta, known, guess, 0.0, DBL_MAX, digits, 10, NULL);
+    }
+    if (lateral < 0.0) {
+        double extraction = fmin(dx * fabs(lateral), new_q);
+        new_q -= extraction;
+    }
+    return new_q;
+}
+
+/* Same in float: digits = int(24 * 0.6) = 14, bracket [0, FLT_MAX], float arithmetic. */
+static double newton_f32(float k, float alpha, float beta, float known, float guess, int* iters)
+{
+    float factor = ldexpf(1.0f, 1 - (int)(FLT_MANT_DIG * 0.6));
+    float lo = 0.0f, hi = FLT_MAX, x = guess, ab = alpha * beta;
+    int n = 0;
+    while (n < 10) {
+        float f = k * x + alpha * powf(x, beta) - known;
+        float df = k + ab * powf(x, beta - 1.0f);
+        ++n;
+        if (f == 0.0f) break;
+        float step = (df == 0.0f || !isfinite(df)) ? (f > 0.0f ? 0.5f * (x - lo) : 0.5f * (x - hi)) : f / df;
+        float next = x - step;
+        if (next <= lo) { step = 0.5f * (x - lo); next = x - step; }
+        else if (next >= hi) { step = 0.5f * (x - hi); next = x - step; }
+        if (step > 0.0f) hi = x; else lo = x;
+        x = next;
+        if (fabsf(step) <= fabsf(x) * factor) break;
+        if (x == lo || x == hi) break;
+    }
+    if (iters) *iters = n;
+    return x;
+}
+
+float lue_oracle_iterate_to_new_discharge_f32(float upstream, float current, float lateral, float alpha,
+                                              float beta, float dt, float dx)
+{
+    float new_q = 0.0f;
+    if (upstream + current > 0.0f || lateral > 0.0f) {
+        float inflow = lateral >= 0.0f ? lateral : 0.0f;
+        float k = dt / dx;
+        float known = k * upstream + alpha * powf(current, beta) + dt * inflow;
+        float guess = FLT_MIN;
+        if (current + upstream != 0.0f || beta >= 1.0f) {
+            float a_b_pq = alpha * beta * powf((current + upstream) / 2.0f, beta - 1.0f);
+            guess = (k * upstream + a_b_pq * current + dt * inflow) / (k + a_b_pq);
+            if (!(guess > FLT_MIN)) guess = FLT_MIN;
+        }
+        new_q = (float)newton_f32(k, alpha, beta, known, guess, NULL);
+    }
+    if (lateral < 0.0f) {
+        float extraction = fminf(dx * fabsf(lateral), new_q);
+        new_q -= extraction;
+    }
+    return new_q;
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* The accumulating router, instantiated for float and double                                       */
+/* ------------------------------------------------------------------------------------------------ */
+
+enum { OP_ACCU = 0, OP_THRESHOLD = 1, OP_FRACTION = 2, OP_KINEMATIC_WAVE = 3 };
+
+#define REAL float
+#define SFX f32
+#define REAL_MIN FLT_MIN
+#define ITERATE lue_oracle_iterate_to_new_discharge_f32
+#include "router_impl.h"
+#undef REAL
+#undef SFX
+#undef REAL_MIN
+#undef ITERATE
+
+#define REAL double
+#define SFX f64
+#define REAL_MIN DBL_MIN
+#define ITERATE lue_oracle_iterate_to_new_discharge_f64
+#include "router_impl.h"
+#undef REAL
+#undef SFX
+#undef REAL_MIN
+#undef ITERATE
+
+/* Symbols the Python wrapper checks for, so a stale build is caught early. */
+int lue_oracle_abi_version(void) { return 1; }
