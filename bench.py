@@ -1,0 +1,393 @@
+#!/usr/bin/env python3
+"""Benchmark of the flow-routing hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (default ``accu_16k``): accu over a 16384 x 16384 D8 raster (268,435,456 cells) built from a
+seeded fBm DEM (amplitude 200 m, 1 % tilt to the south, Priority-Flood+epsilon filled, the reference's
+D8 rule), float32 lognormal(0, 1) material, partitions 2048 x 2048.  A step is one accu pass over the
+whole raster.  The flow topology is built once (timed and reported separately) and stays resident, as
+for a model that routes many inputs over one flow-direction raster.
+
+Reported (one JSON line, rank 0):
+  value      Mcells/s of the device-resident step (inputs in HBM), K steps timed with CUDA events on
+             the launching stream between barriers + synchronize; max over ranks.
+  e2e        the same metric through the public API (lue_gb300.framework) with host buffers: per step
+             the float32 material goes host->device from pinned memory and the outflow comes back
+             device->host.
+  roofline   algorithmic bytes (fd 1 + material 4 + outflow 4 = 9 B/cell) / mean step time against the
+             measured HBM copy bandwidth; traffic from the committed ncu summary when present.
+  cpu_baseline  the CPU oracle (a restatement of the reference's partitioned ridge walk, threaded
+             one task per partition) on a bounded sample, rank 0 only.
+  extra.kinematic_wave  kinematic_wave steps over the 8192 x 8192 workload (float64 discharge).
+
+--impl reference times the reference algorithm on the CPU (the oracle port, every host core), since
+the reference (HPX + Boost) cannot be built here; each step is the bounded sample described in
+``cpu_baseline.sample``.  Multi-GPU (torchrun): each rank routes its own replica of the workload; no
+collective is involved (replicas only; scaling "weak").
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ACCU_BYTES_PER_CELL = 9      # fd 1 + material 4 + outflow 4
+KW_BYTES_PER_CELL = 25       # fd 1 + Q_cur 8 + lateral 4 + alpha 4 + Q_new 8
+REF_SAMPLE_ROWS = 4096       # reference-arm / cpu_baseline sample: the top 4096 rows, all columns
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(kernel):
+    """Per-launch DRAM bytes of `kernel` from a committed ncu summary line
+    'traffic_per_launch <kernel> <bytes> <units_per_launch>'; scaled to a launch of this workload."""
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return None
+    for name in sorted(os.listdir(d)):
+        if not name.endswith((".md", ".txt")):
+            continue
+        for line in open(os.path.join(d, name)):
+            parts = line.strip().strip("`").split()
+            if len(parts) == 4 and parts[0] == "traffic_per_launch" and parts[1] == kernel:
+                return float(parts[2]), float(parts[3])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def outlet_mask(fd):
+    """Cells whose flow leaves the array or stops (sinks): where all routed material ends up."""
+    import torch
+    lut_dr = torch.zeros(256, dtype=torch.int32, device=fd.device)
+    lut_dc = torch.zeros(256, dtype=torch.int32, device=fd.device)
+    for code, (dr, dc) in {7: (-1, -1), 8: (-1, 0), 9: (-1, 1), 4: (0, -1), 6: (0, 1), 1: (1, -1), 2: (1, 0),
+                           3: (1, 1)}.items():
+        lut_dr[code], lut_dc[code] = dr, dc
+    rows, cols = fd.shape
+    idx = fd.long()
+    rr = torch.arange(rows, device=fd.device, dtype=torch.int32)[:, None] + lut_dr[idx]
+    cc = torch.arange(cols, device=fd.device, dtype=torch.int32)[None, :] + lut_dc[idx]
+    sink = (lut_dr[idx] == 0) & (lut_dc[idx] == 0) & (fd != 255)
+    off = (rr < 0) | (rr >= rows) | (cc < 0) | (cc >= cols)
+    return sink | off
+
+
+def cpu_sample(inputs, partition):
+    """The bounded CPU sample: the top REF_SAMPLE_ROWS rows (flow leaving the band is dropped, as at
+    the array edge), same partitioning."""
+    fd = np.ascontiguousarray(inputs["flow_direction"][:REF_SAMPLE_ROWS])
+    m = np.ascontiguousarray(inputs["material"][:REF_SAMPLE_ROWS])
+    return fd, m, (min(partition[0], fd.shape[0]), min(partition[1], fd.shape[1]))
+
+
+def run_cpu_accu(fd, m, partition, nthreads):
+    from oracle import oracle
+    t0 = time.perf_counter()
+    oracle.accu(fd, m, partition, dtype=np.float32, nthreads=nthreads)
+    return time.perf_counter() - t0
+
+
+def workload_inputs(name):
+    from lue_gb300 import synthetic
+    w = synthetic.WORKLOADS[name]
+    inputs = synthetic.accu_inputs(w["rows"], w["cols"], w["seed"], w["amplitude"])
+    return w, inputs
+
+
+def bench_reference(args, world, rank):
+    """CPU reference arm: the oracle port of the reference's algorithm on every host core."""
+    if rank != 0:
+        return
+    w, inputs = workload_inputs(args.workload)
+    fd, m, ps = cpu_sample(inputs, w["partition"])
+    nthreads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        run_cpu_accu(fd, m, ps, nthreads)
+    times = [run_cpu_accu(fd, m, ps, nthreads) for _ in range(args.steps)]
+    total = sum(times)
+    value = fd.size * args.steps / total / 1e6
+    sample = (f"accu over rows 0-{fd.shape[0] - 1} of the {w['rows']}x{w['cols']} raster "
+              f"({fd.shape[0]}x{fd.shape[1]} cells, partitions {ps[0]}x{ps[1]}) per step")
+    line = {
+        "impl": "reference", "metric": "accu Mcells/s (16384^2 D8 raster, float32 material)", "value": round(value, 3),
+        "unit": "Mcells/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1000 * total / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fBm DEM, lognormal material)",
+        "config": {"workload": args.workload, "rows": w["rows"], "cols": w["cols"],
+                   "partition_shape": list(w["partition"]), "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": round(value, 3), "unit": "Mcells/s", "cores": nthreads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 3), "unit": "Mcells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference (HPX + Boost) not buildable offline; oracle/lue_oracle.c restates its partitioned "
+                "ridge walk, one thread task per partition",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def bench_ours(args, world, rank, local):
+    import torch
+
+    from lue_gb300 import framework as lfr
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w, inputs = workload_inputs(args.workload)
+    rows, cols, ps = w["rows"], w["cols"], w["partition"]
+    n = rows * cols
+    stream = torch.cuda.current_stream(dev)
+
+    # resident inputs
+    fd_d = lfr.from_numpy(inputs["flow_direction"], ps, device=dev)
+    m_host = torch.from_numpy(inputs["material"]).pin_memory()
+    m_d = lfr.PartitionedArray(m_host.to(dev, non_blocking=True), ps)
+    torch.cuda.synchronize()
+
+    t0 = time.perf_counter()
+    topo = fd_d.topology()
+    torch.cuda.synchronize()
+    topology_ms = 1000 * (time.perf_counter() - t0)
+    stats = topo.stats()
+
+    # warm-up (also checks the mass balance once)
+    out = None
+    for _ in range(args.warmup):
+        out = lfr.accu(fd_d, m_d)
+    torch.cuda.synchronize()
+
+    # timed, device-resident
+    sampler = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    sampler.start()
+    time.sleep(0.3)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    ev[0].record(stream)
+    for k in range(args.steps):
+        out = lfr.accu(fd_d, m_d)
+        ev[k + 1].record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    barrier(world)
+    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    total_s = max_over_ranks(sum(step_ms) / 1000.0, world)
+    value = world * n * args.steps / total_s / 1e6
+
+    # mass balance: the material reaching outlets and sinks equals the material put in
+    mask = outlet_mask(fd_d.data)
+    total_in = float(m_d.data.double().sum())
+    total_out = float(out.data.double()[mask].sum())
+    del mask
+
+    # end to end through the public API with host buffers
+    e2e_steps = max(1, min(args.steps, 5))
+    out_host = torch.empty((rows, cols), dtype=torch.float32).pin_memory()
+    torch.cuda.synchronize()
+    barrier(world)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        m_step = lfr.PartitionedArray(m_host.to(dev, non_blocking=True), ps)
+        o = lfr.accu(fd_d, m_step)
+        out_host.copy_(o.data, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(e0.elapsed_time(e1) / 1000.0, world)
+    e2e_value = world * n * e2e_steps / e2e_s / 1e6
+
+    # roofline of the dominant kernel (the routing walk; one launch per step)
+    peak, peak_kind = peaks()
+    mean_step_s = statistics.mean(step_ms) / 1000.0
+    achieved = ACCU_BYTES_PER_CELL * n / mean_step_s / 1e9
+    tr = profile_traffic("k_walk_accu_f32")
+    traffic = None if tr is None else tr[0] / tr[1] * n
+
+    extra = {}
+    if args.kinematic_wave_steps > 0 and rank == 0:
+        extra["kinematic_wave"] = bench_kinematic_wave(args, dev)
+
+    if rank != 0:
+        return
+    cpu = None
+    if world == 1 and not args.skip_cpu:
+        fd_s, m_s, ps_s = cpu_sample(inputs, ps)
+        nthreads = os.cpu_count() or 1
+        t_cpu = run_cpu_accu(fd_s, m_s, ps_s, nthreads)
+        cpu = {"value": round(fd_s.size / t_cpu / 1e6, 3), "unit": "Mcells/s", "cores": nthreads, "kind": "port",
+               "sample": f"accu over rows 0-{fd_s.shape[0] - 1} of the raster ({fd_s.shape[0]}x{fd_s.shape[1]} "
+                         f"cells, partitions {ps_s[0]}x{ps_s[1]}), one pass, oracle/lue_oracle.c threaded"}
+    line = {
+        "metric": "accu Mcells/s (16384^2 D8 raster, float32 material)", "value": round(value, 3),
+        "unit": "Mcells/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1000 * total_s / args.steps, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fBm DEM, lognormal material)",
+        "config": {"workload": args.workload, "rows": rows, "cols": cols, "partition_shape": list(ps),
+                   "l2": "inputs larger than L2 (268 MB fd + 1 GB material per step)",
+                   "topology": "resident, built once", "topology_build_ms": round(topology_ms, 2),
+                   "longest_flow_path_cells": stats["max_level"] + 1, "engine": "walk"},
+        "e2e": {"value": round(e2e_value, 3), "unit": "Mcells/s", "h2d_bytes_per_step": 4 * n,
+                "d2h_bytes_per_step": 4 * n},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "kernel": "k_walk<RouteF32<accu>>", "peak_kind": peak_kind,
+                     "bytes_per_cell": ACCU_BYTES_PER_CELL},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": args.steps,
+        "mass_balance": {"material_in": total_in, "outlet_outflow": total_out,
+                         "rel_err": abs(total_out - total_in) / total_in},
+        "extra": extra,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def bench_kinematic_wave(args, dev):
+    import torch
+
+    from lue_gb300 import framework as lfr
+    from lue_gb300 import synthetic
+
+    w = synthetic.WORKLOADS["kw_8k"]
+    d = synthetic.kinematic_wave_inputs(w["rows"], w["cols"], w["seed"], w["amplitude"])
+    ps = w["partition"]
+    fd = lfr.from_numpy(d["flow_direction"], ps, device=dev)
+    q = lfr.from_numpy(d["discharge"], ps, device=dev)
+    lat = lfr.from_numpy(d["lateral_inflow"], ps, device=dev)
+    alpha = lfr.from_numpy(d["alpha"], ps, device=dev)
+    fd.topology()
+    q = lfr.kinematic_wave(fd, q, lat, alpha, 0.6, 3600.0, 100.0)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.kinematic_wave_steps):
+        q = lfr.kinematic_wave(fd, q, lat, alpha, 0.6, 3600.0, 100.0)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    s = e0.elapsed_time(e1) / 1000.0
+    n = w["rows"] * w["cols"]
+    return {"workload": "kw_8k", "steps": args.kinematic_wave_steps, "ms_per_step": round(1000 * s / args.kinematic_wave_steps, 3),
+            "value": round(n * args.kinematic_wave_steps / s / 1e6, 3), "unit": "Mcells/s",
+            "roofline_frac": round(KW_BYTES_PER_CELL * n * args.kinematic_wave_steps / s / 1e9 / peaks()[0], 4),
+            "longest_flow_path_cells": fd.topology().stats()["max_level"] + 1}
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="accu_16k")
+    ap.add_argument("--kinematic-wave-steps", type=int, default=5)
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_init(args)
+    if args.impl == "reference":
+        bench_reference(args, world, rank)
+    else:
+        bench_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,150 @@
+/*
+ * lue_gb300.h — C ABI of the GB300-native flow-routing path.
+ *
+ * Drop-in boundary for LUE's routing operations on D8 rasters (computationalgeography/lue, paths
+ * below are relative to source/framework/algorithm/include/lue/framework/algorithm/):
+ *
+ *   LUE operation (C++ template, PartitionedArray in/out)        entry point here
+ *   ----------------------------------------------------------   -----------------------------------
+ *   inflow_count<uint8>(policies, fd)  inflow_count.hpp:29-42      lue_gpu_inflow_count_u8
+ *   value_policies::accu(fd, inflow)   value_policies/accu.hpp:33-55   lue_gpu_accu_f32 / _f64
+ *   value_policies::accu_threshold(fd, inflow, threshold)
+ *                                      value_policies/accu_threshold.hpp:33-90
+ *                                                                  lue_gpu_accu_threshold_f32 / _f64
+ *   value_policies::accu_fraction(fd, inflow, fraction)
+ *                                      value_policies/accu_fraction.hpp:33-90
+ *                                                                  lue_gpu_accu_fraction_f32 / _f64
+ *   value_policies::kinematic_wave(fd, current_outflow, inflow, alpha, beta,
+ *                                  time_step_duration, channel_length)
+ *                                      value_policies/kinematic_wave.hpp:43-91
+ *                                                                  lue_gpu_kinematic_wave_f64
+ *                                                                  (+ _f64_f32in: float32 lateral
+ *                                                                   inflow and alpha rasters)
+ *
+ * The per-call inflow-count pass and the partition-connectivity exchange of the reference
+ * (definition/accumulating_router.hpp:1212-1247, definition/inflow_count.hpp:97-577) become a resident
+ * topology built once per flow-direction raster (lue_gpu_topology_create) and reused by every call.
+ *
+ * Conventions
+ *   - Rasters are row-major (the reference's mdspan layout_right), in device memory, owned by the
+ *     caller.  Flow direction is uint8 with the keypad D8 codes (flow_direction.hpp:7-35); 255 is
+ *     no-data.  Float no-data is NaN (policy/default_value_policies.hpp:18-29).
+ *   - A raster argument that may also be a scalar (the reference's PartitionedArray | Scalar
+ *     overloads) is a pointer plus a value: a NULL pointer selects the scalar.
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).  Routing calls are asynchronous on it;
+ *     lue_gpu_topology_create synchronises its stream before returning.
+ *   - Every function returns a status (LUE_GPU_OK on success) and never throws;
+ *     lue_gpu_last_error() describes the last failure of the calling thread.
+ *   - Invalid values do not fail a call: they become NaN (floats) or 255 (counts) in the output,
+ *     exactly like the reference's value policies.  A shape mismatch fails with LUE_GPU_ESHAPE, where
+ *     the reference throws std::runtime_error (detail/verify_compatible.hpp:23-40).
+ *   - The partition shape is kept for interface parity and validated like the reference's domain
+ *     decomposition (partition extents must be positive and not larger than the array); results do
+ *     not depend on it beyond floating-point summation order.
+ *   - A topology holds per-call scratch memory: calls that use the same topology must not overlap in
+ *     time (issue them on one stream).  lue_gpu_topology_clone gives another handle that shares the
+ *     immutable flow topology and has its own scratch.
+ */
+#ifndef LUE_GB300_H
+#define LUE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LUE_GPU_ABI_VERSION 1
+
+enum lue_gpu_status {
+    LUE_GPU_OK = 0,
+    LUE_GPU_EINVAL = 1,    /* bad argument: NULL pointer, non-positive extent, bad partition shape */
+    LUE_GPU_ESHAPE = 2,    /* arrays of different shape / partitioning */
+    LUE_GPU_ECUDA = 3,     /* a CUDA runtime call failed */
+    LUE_GPU_ENOMEM = 4,    /* device allocation failed */
+    LUE_GPU_ETIMEDOUT = 5, /* a bounded device-side wait gave up (no result written) */
+    LUE_GPU_ERANGE = 6     /* a size beyond a documented maximum */
+};
+
+typedef struct lue_gpu_topology lue_gpu_topology;
+
+typedef struct lue_gpu_topology_stats {
+    int64_t rows, cols;
+    int64_t partition_rows, partition_cols;
+    int64_t valid_cells;       /* flow direction is not no-data */
+    int64_t ridge_cells;       /* valid cells without inflow */
+    int64_t outlet_cells;      /* valid cells whose flow leaves the array */
+    int64_t sink_cells;        /* valid cells with code 5 or an unknown code */
+    int64_t cycle_cells;       /* valid cells on or downstream of a flow cycle (never routed) */
+    int64_t max_level;         /* largest downstream level (longest flow path minus one) */
+    int64_t device_bytes;      /* device memory held by this handle */
+} lue_gpu_topology_stats;
+
+/* Library */
+int lue_gpu_abi_version(void);
+const char* lue_gpu_last_error(void);
+
+/* Topology: built once per flow-direction raster, resident on the device. */
+int lue_gpu_topology_create(const uint8_t* flow_direction, int64_t rows, int64_t cols,
+                            int64_t partition_rows, int64_t partition_cols, void* stream,
+                            lue_gpu_topology** topology);
+int lue_gpu_topology_clone(const lue_gpu_topology* topology, lue_gpu_topology** clone);
+int lue_gpu_topology_destroy(lue_gpu_topology* topology);
+int lue_gpu_topology_get_stats(const lue_gpu_topology* topology, lue_gpu_topology_stats* stats);
+
+/* inflow_count<uint8>(DefaultValuePolicies, fd): number of neighbours draining into each cell,
+ * 255 where the flow direction is no-data.  value_policies = 0 gives DefaultPolicies (255 is an
+ * unknown code, i.e. a sink; definition/inflow_count.hpp:9-15). */
+int lue_gpu_inflow_count_u8(const lue_gpu_topology* topology, int value_policies, uint8_t* inflow_count,
+                            void* stream);
+
+/* Downstream level of each cell: 0 for cells without inflow, else 1 + the largest level upstream;
+ * -1 for no-data and for cells on or below a cycle.  No reference counterpart: it exposes the
+ * downstream ordering the routing kernels use. */
+int lue_gpu_downstream_level_i32(const lue_gpu_topology* topology, int32_t* level, void* stream);
+
+/* accu: outflow = upstream outflow + inflow (inflow >= 0, else NaN). */
+int lue_gpu_accu_f32(lue_gpu_topology* topology, const float* inflow, float inflow_scalar, float* outflow,
+                     void* stream);
+int lue_gpu_accu_f64(lue_gpu_topology* topology, const double* inflow, double inflow_scalar, double* outflow,
+                     void* stream);
+
+/* accu_threshold: total = upstream + inflow; if total > threshold: (flux, state) = (total - threshold,
+ * threshold) else (0, total).  Domain inflow >= 0 && threshold >= 0. */
+int lue_gpu_accu_threshold_f32(lue_gpu_topology* topology, const float* inflow, float inflow_scalar,
+                               const float* threshold, float threshold_scalar, float* flux, float* state,
+                               void* stream);
+int lue_gpu_accu_threshold_f64(lue_gpu_topology* topology, const double* inflow, double inflow_scalar,
+                               const double* threshold, double threshold_scalar, double* flux, double* state,
+                               void* stream);
+
+/* accu_fraction: total = upstream + inflow; flux = fraction * total; state = total - flux.
+ * Domain inflow >= 0 && 0 <= fraction <= 1. */
+int lue_gpu_accu_fraction_f32(lue_gpu_topology* topology, const float* inflow, float inflow_scalar,
+                              const float* fraction, float fraction_scalar, float* flux, float* state,
+                              void* stream);
+int lue_gpu_accu_fraction_f64(lue_gpu_topology* topology, const double* inflow, double inflow_scalar,
+                              const double* fraction, double fraction_scalar, double* flux, double* state,
+                              void* stream);
+
+/* kinematic_wave: one time step of non-linear kinematic-wave routing; per cell the Newton-Raphson
+ * solve of definition/kinematic_wave.hpp:145-254 with the upstream new discharge.
+ * Domain current_outflow >= 0 && inflow >= 0 && channel_length > 0, else NaN. */
+int lue_gpu_kinematic_wave_f64(lue_gpu_topology* topology, const double* current_outflow,
+                               double current_outflow_scalar, const double* inflow, double inflow_scalar,
+                               const double* alpha, double alpha_scalar, const double* beta,
+                               double beta_scalar, double time_step_duration, const double* channel_length,
+                               double channel_length_scalar, double* outflow, void* stream);
+/* Same with float32 lateral inflow and alpha rasters, promoted exactly to double per cell. */
+int lue_gpu_kinematic_wave_f64_f32in(lue_gpu_topology* topology, const double* current_outflow,
+                                     double current_outflow_scalar, const float* inflow, double inflow_scalar,
+                                     const float* alpha, double alpha_scalar, double beta,
+                                     double time_step_duration, double channel_length, double* outflow,
+                                     void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LUE_GB300_H */

@@ -1,0 +1,40 @@
+// topology.cuh — the resident flow topology of one D8 raster and its per-handle scratch.
+#pragma once
+
+#include <atomic>
+
+#include "common.cuh"
+
+namespace lue_gb300 {
+
+// Immutable part, shared by a topology and its clones.
+struct TopologyCore {
+    int64_t rows = 0, cols = 0, prow = 0, pcol = 0, n = 0;
+    uint8_t* fd = nullptr;      // device copy of the flow direction raster
+    uint8_t* count = nullptr;   // inflow count, 255 where the flow direction is no-data
+    uint8_t* upmask = nullptr;  // bit k set: neighbour k (NW, N, NE, W, E, SW, S, SE) drains here
+    int32_t* level = nullptr;   // downstream level, -1 for no-data and cycle cells
+    lue_gpu_topology_stats stats{};
+    int64_t bytes = 0;
+    std::atomic<int> refs{1};
+};
+
+}  // namespace lue_gb300
+
+struct lue_gpu_topology {
+    lue_gb300::TopologyCore* core = nullptr;
+    uint32_t* work_count = nullptr;  // per-call copy of the counts, 4 cells per word
+    float* lo = nullptr;             // per-call float-float residuals of f32 routing
+    int64_t scratch_bytes = 0;
+};
+
+namespace lue_gb300 {
+
+int allocate_scratch(lue_gpu_topology* t);
+
+// Launch of the walk engine: one thread per cell; cells without inflow start a downstream walk that
+// continues through a cell once all its upstream neighbours are done (definition/accumulating_router.hpp:
+// 525-599, run by many threads at once).
+inline int64_t words_for(int64_t n) { return (n + 3) / 4; }
+
+}  // namespace lue_gb300

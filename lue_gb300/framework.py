@@ -1,0 +1,238 @@
+"""Python mirror of LUE's routing operations (``lue.framework``) on the GB300 C ABI.
+
+Same operation names, argument names and order, and the same raster-or-scalar overloads as the
+reference's pybind11 module (source/framework/python/source/algorithm/routing_operation/{accu,
+accu_threshold,accu_fraction,kinematic_wave,inflow_count}.cpp).  ``from_numpy`` / ``to_numpy`` mirror
+source/framework/python/source/numpy/{from_numpy,to_numpy}.cpp.  Device memory is held in torch
+CUDA tensors; every operation runs the CUDA kernels of liblue_gb300.so on torch's current stream.
+
+The flow topology of a flow-direction array is built on first use and kept with that array, so
+repeated calls (for example one kinematic_wave call per time step) do not redo it.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+
+FLOW_DIRECTION_NO_DATA = 255
+
+
+class PartitionedArray:
+    """A 2-D raster resident on the GPU, with the reference's partition shape kept for parity."""
+
+    def __init__(self, data, partition_shape=None):
+        if not isinstance(data, torch.Tensor) or not data.is_cuda:
+            raise TypeError("PartitionedArray data must be a CUDA tensor")
+        if data.dim() != 2:
+            raise ValueError("PartitionedArray must be 2-D")
+        self.data = data.contiguous()
+        shape = tuple(self.data.shape)
+        ps = tuple(int(v) for v in (partition_shape or shape))
+        if len(ps) != 2 or ps[0] <= 0 or ps[1] <= 0:
+            raise ValueError("Partition shape must not be empty")
+        if ps[0] > shape[0] or ps[1] > shape[1]:
+            raise ValueError("Partition size must be smaller than or equal to array size")
+        self.partition_shape = ps
+        self._topology = None
+
+    @property
+    def shape(self):
+        return tuple(self.data.shape)
+
+    @property
+    def dtype(self):
+        return self.data.dtype
+
+    @property
+    def shape_in_partitions(self):
+        return (self.shape[0] // self.partition_shape[0], self.shape[1] // self.partition_shape[1])
+
+    def topology(self):
+        if self._topology is None:
+            if self.dtype != torch.uint8:
+                raise TypeError("flow direction must be uint8")
+            self._topology = Topology(self.data, self.partition_shape)
+        return self._topology
+
+
+class Topology:
+    """Owner of a lue_gpu_topology handle (resident inflow counts, upstream masks, levels, scratch)."""
+
+    def __init__(self, flow_direction, partition_shape):
+        L = _lib.lib()
+        h = ctypes.c_void_p()
+        fd = flow_direction.contiguous()
+        stream = torch.cuda.current_stream(fd.device).cuda_stream
+        _lib.check(L.lue_gpu_topology_create(fd.data_ptr(), fd.shape[0], fd.shape[1], partition_shape[0],
+                                             partition_shape[1], stream, ctypes.byref(h)))
+        self.handle = h
+        self.shape = tuple(fd.shape)
+        self.device = fd.device
+
+    @classmethod
+    def _from_handle(cls, handle, shape, device):
+        t = cls.__new__(cls)
+        t.handle, t.shape, t.device = handle, shape, device
+        return t
+
+    def clone(self):
+        """Another handle on the same flow topology, with its own scratch (for concurrent calls)."""
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().lue_gpu_topology_clone(self.handle, ctypes.byref(h)))
+        return Topology._from_handle(h, self.shape, self.device)
+
+    def stats(self):
+        s = _lib.TopologyStats()
+        _lib.check(_lib.lib().lue_gpu_topology_get_stats(self.handle, ctypes.byref(s)))
+        return s.as_dict()
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            _lib.lib().lue_gpu_topology_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def from_numpy(array, partition_shape=None, no_data_value=None, device="cuda"):
+    """Copy a 2-D numpy array to the GPU.  For floats, ``no_data_value`` cells become NaN; for
+    integers they become the element type's no-data value (255 for uint8)."""
+    a = np.ascontiguousarray(array)
+    if no_data_value is not None:
+        a = a.copy()
+        mask = a == no_data_value
+        if np.issubdtype(a.dtype, np.floating):
+            a[mask] = np.nan
+        else:
+            a[mask] = np.iinfo(a.dtype).max
+    return PartitionedArray(torch.from_numpy(a).to(device), partition_shape)
+
+
+def to_numpy(array):
+    return array.data.cpu().numpy()
+
+
+def _stream(t):
+    return torch.cuda.current_stream(t.device).cuda_stream
+
+
+def _raster_or_scalar(x, shape, dtype, name):
+    """(device pointer or None, scalar, keep-alive tensor) for an argument of the reference's
+    PartitionedArray | Scalar | value overloads."""
+    if isinstance(x, PartitionedArray):
+        if x.shape != shape:
+            raise _lib.LueGpuError(2, f"{name}: shape {x.shape} differs from flow direction shape {shape}")
+        t = x.data if x.data.dtype == dtype else x.data.to(dtype)
+        return t.data_ptr(), 0.0, t
+    if isinstance(x, torch.Tensor):
+        if x.dim() == 0:
+            return None, float(x), None
+        return _raster_or_scalar(PartitionedArray(x), shape, dtype, name)
+    return None, float(x), None
+
+
+def _check_partitioning(flow_direction, *arrays):
+    for a in arrays:
+        if isinstance(a, PartitionedArray) and a.shape_in_partitions != flow_direction.shape_in_partitions:
+            raise _lib.LueGpuError(2, "arrays are not partitioned in the same way")
+
+
+def _material_dtype(*args):
+    for a in args:
+        if isinstance(a, PartitionedArray) and a.dtype in (torch.float32, torch.float64):
+            return a.dtype
+    return torch.float32
+
+
+def _empty(flow_direction, dtype):
+    return torch.empty(flow_direction.shape, dtype=dtype, device=flow_direction.data.device)
+
+
+def inflow_count(flow_direction, value_policies=True):
+    t = flow_direction.topology()
+    out = _empty(flow_direction, torch.uint8)
+    _lib.check(_lib.lib().lue_gpu_inflow_count_u8(t.handle, int(value_policies), out.data_ptr(),
+                                                  _stream(flow_direction.data)))
+    return PartitionedArray(out, flow_direction.partition_shape)
+
+
+def downstream_level(flow_direction):
+    t = flow_direction.topology()
+    out = _empty(flow_direction, torch.int32)
+    _lib.check(_lib.lib().lue_gpu_downstream_level_i32(t.handle, out.data_ptr(), _stream(flow_direction.data)))
+    return PartitionedArray(out, flow_direction.partition_shape)
+
+
+def accu(flow_direction, inflow):
+    _check_partitioning(flow_direction, inflow)
+    dtype = _material_dtype(inflow)
+    t = flow_direction.topology()
+    p, s, keep = _raster_or_scalar(inflow, flow_direction.shape, dtype, "inflow")
+    out = _empty(flow_direction, dtype)
+    fn = _lib.lib().lue_gpu_accu_f32 if dtype == torch.float32 else _lib.lib().lue_gpu_accu_f64
+    _lib.check(fn(t.handle, p, s, out.data_ptr(), _stream(flow_direction.data)))
+    del keep
+    return PartitionedArray(out, flow_direction.partition_shape)
+
+
+def _two_output(fn32, fn64, flow_direction, inflow, other, name):
+    _check_partitioning(flow_direction, inflow, other)
+    dtype = _material_dtype(inflow, other)
+    t = flow_direction.topology()
+    p0, s0, k0 = _raster_or_scalar(inflow, flow_direction.shape, dtype, "inflow")
+    p1, s1, k1 = _raster_or_scalar(other, flow_direction.shape, dtype, name)
+    flux, state = _empty(flow_direction, dtype), _empty(flow_direction, dtype)
+    fn = fn32 if dtype == torch.float32 else fn64
+    _lib.check(fn(t.handle, p0, s0, p1, s1, flux.data_ptr(), state.data_ptr(), _stream(flow_direction.data)))
+    del k0, k1
+    ps = flow_direction.partition_shape
+    return PartitionedArray(flux, ps), PartitionedArray(state, ps)
+
+
+def accu_threshold(flow_direction, inflow, threshold):
+    L = _lib.lib()
+    return _two_output(L.lue_gpu_accu_threshold_f32, L.lue_gpu_accu_threshold_f64, flow_direction, inflow,
+                       threshold, "threshold")
+
+
+def accu_fraction(flow_direction, inflow, fraction):
+    L = _lib.lib()
+    return _two_output(L.lue_gpu_accu_fraction_f32, L.lue_gpu_accu_fraction_f64, flow_direction, inflow,
+                       fraction, "fraction")
+
+
+def kinematic_wave(flow_direction, current_outflow, inflow, alpha, beta, time_step_duration, channel_length):
+    """One time step; float64 discharge.  Float32 inflow/alpha rasters with scalar beta and channel
+    length take the mixed-precision entry point (exact float32 -> float64 promotion per cell)."""
+    _check_partitioning(flow_direction, current_outflow, inflow, alpha, beta, channel_length)
+    t = flow_direction.topology()
+    shape = flow_direction.shape
+    out = _empty(flow_direction, torch.float64)
+    L = _lib.lib()
+    stream = _stream(flow_direction.data)
+    f32_in = (isinstance(inflow, PartitionedArray) and inflow.dtype == torch.float32 and
+              (not isinstance(alpha, PartitionedArray) or alpha.dtype == torch.float32) and
+              not isinstance(beta, PartitionedArray) and not isinstance(channel_length, PartitionedArray))
+    pq, sq, kq = _raster_or_scalar(current_outflow, shape, torch.float64, "current_outflow")
+    if f32_in:
+        pl, sl, kl = _raster_or_scalar(inflow, shape, torch.float32, "inflow")
+        pa, sa, ka = _raster_or_scalar(alpha, shape, torch.float32, "alpha")
+        _lib.check(L.lue_gpu_kinematic_wave_f64_f32in(t.handle, pq, sq, pl, sl, pa, sa, float(beta),
+                                                      float(time_step_duration), float(channel_length),
+                                                      out.data_ptr(), stream))
+    else:
+        pl, sl, kl = _raster_or_scalar(inflow, shape, torch.float64, "inflow")
+        pa, sa, ka = _raster_or_scalar(alpha, shape, torch.float64, "alpha")
+        pb, sb, kb = _raster_or_scalar(beta, shape, torch.float64, "beta")
+        pd, sd, kd = _raster_or_scalar(channel_length, shape, torch.float64, "channel_length")
+        _lib.check(L.lue_gpu_kinematic_wave_f64(t.handle, pq, sq, pl, sl, pa, sa, pb, sb,
+                                                float(time_step_duration), pd, sd, out.data_ptr(), stream))
+        del kb, kd
+    del kq, kl, ka
+    return PartitionedArray(out, flow_direction.partition_shape)

@@ -337,3 +337,50 @@ enum { OP_ACCU = 0, OP_THRESHOLD = 1, OP_FRACTION = 2, OP_KINEMATIC_WAVE = 3 };
 
 /* Symbols the Python wrapper checks for, so a stale build is caught early. */
 int lue_oracle_abi_version(void) { return 1; }
+
+/*
+ * Downstream level of every cell (no reference counterpart; the CPU definition the GPU's
+ * downstream ordering is pinned to): 0 for a valid cell without inflow, else 1 + the largest level
+ * among the cells draining into it; -1 for no-data cells and for cells on or below a cycle.
+ * Kahn's peel over the whole array (flow off the array ends a path).
+ */
+int lue_oracle_downstream_level(const uint8_t* fd, int64_t rows, int64_t cols, int32_t* level)
+{
+    int64_t n = rows * cols;
+    uint8_t* cnt = (uint8_t*)calloc((size_t)n, 1);
+    int64_t* queue = (int64_t*)malloc((size_t)n * sizeof(int64_t));
+    if (!cnt || !queue) { free(cnt); free(queue); return -2; }
+    for (int64_t i = 0; i < n; ++i) level[i] = -1;
+    for (int64_t r = 0; r < rows; ++r)
+        for (int64_t c = 0; c < cols; ++c) {
+            uint8_t code = fd[r * cols + c];
+            if (code == U8_NO_DATA) continue;
+            int dr, dc;
+            d8_offset(code, &dr, &dc);
+            if (dr == 0 && dc == 0) continue;
+            int64_t rd = r + dr, cd = c + dc;
+            if (rd < 0 || rd >= rows || cd < 0 || cd >= cols) continue;
+            cnt[rd * cols + cd]++;
+        }
+    int64_t head = 0, tail = 0;
+    for (int64_t i = 0; i < n; ++i)
+        if (fd[i] != U8_NO_DATA && cnt[i] == 0) { queue[tail++] = i; level[i] = 0; }
+    while (head < tail) {
+        int64_t i = queue[head++];
+        int dr, dc;
+        d8_offset(fd[i], &dr, &dc);
+        if (dr == 0 && dc == 0) continue;
+        int64_t rd = i / cols + dr, cd = i % cols + dc;
+        if (rd < 0 || rd >= rows || cd < 0 || cd >= cols) continue;
+        int64_t j = rd * cols + cd;
+        if (fd[j] == U8_NO_DATA) continue;
+        if (level[i] + 1 > level[j]) level[j] = level[i] + 1;
+        if (--cnt[j] == 0) queue[tail++] = j;
+    }
+    /* cells left with a positive count were never peeled: on or below a cycle */
+    for (int64_t i = 0; i < n; ++i)
+        if (fd[i] != U8_NO_DATA && cnt[i] != 0) level[i] = -1;
+    free(cnt);
+    free(queue);
+    return 0;
+}

@@ -48,6 +48,7 @@ def lib():
             f = getattr(L, f"lue_oracle_kinematic_wave_{sfx}")
             f.argtypes = [p, i64, i64, i64, i64, p, real, p, real, p, real, p, real, real, p, real, p, i32]
         L.lue_oracle_inflow_count.argtypes = [p, i64, i64, i64, i64, i32, p]
+        L.lue_oracle_downstream_level.argtypes = [p, i64, i64, p]
         d = ctypes.c_double
         L.lue_oracle_iterate_to_new_discharge_f64.argtypes = [d] * 7
         L.lue_oracle_iterate_to_new_discharge_f64.restype = d
@@ -95,6 +96,13 @@ def inflow_count(fd, partition_shape=None, value_policies=True):
     out = np.empty(fd.shape, np.uint8)
     _check(lib().lue_oracle_inflow_count(fd.ctypes.data, fd.shape[0], fd.shape[1], pr, pc,
                                          int(value_policies), out.ctypes.data))
+    return out
+
+
+def downstream_level(fd):
+    fd = _fd(fd)
+    out = np.empty(fd.shape, np.int32)
+    _check(lib().lue_oracle_downstream_level(fd.ctypes.data, fd.shape[0], fd.shape[1], out.ctypes.data))
     return out
 
 

@@ -1,0 +1,204 @@
+"""GPU results against the CPU oracle on seeded synthetic rasters and on edge cases.
+
+All calls go through liblue_gb300.so's C ABI (lue_gb300.framework).  Tolerances: tests/parity.py.
+"""
+import numpy as np
+import pytest
+
+from lue_gb300 import synthetic
+from oracle import oracle
+from tests import parity
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lfr():
+    import torch
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    from lue_gb300 import framework
+    return framework
+
+
+@pytest.fixture(scope="module")
+def c1():
+    """The 1024 x 1024 workload in 256 x 256 partitions: amplitude 50 m, material U[0, 1)."""
+    w = synthetic.WORKLOADS["accu_1k"]
+    d = synthetic.accu_inputs(w["rows"], w["cols"], w["seed"], w["amplitude"], distribution="uniform",
+                              cached=False)
+    d["partition"] = w["partition"]
+    return d
+
+
+def ragged(rows, cols, seed, amplitude=30.0):
+    fd = synthetic.flow_direction(rows, cols, seed, amplitude, wavelength=max(rows, cols) / 2)
+    rng = np.random.default_rng(seed)
+    return fd, rng.lognormal(0.0, 1.0, (rows, cols)).astype(np.float32), rng
+
+
+def test_inflow_count_and_levels_bit_exact(lfr, c1):
+    fd = c1["flow_direction"]
+    a = lfr.from_numpy(fd, c1["partition"])
+    assert np.array_equal(lfr.to_numpy(lfr.inflow_count(a)), oracle.inflow_count(fd, c1["partition"]))
+    assert np.array_equal(lfr.to_numpy(lfr.inflow_count(a, value_policies=False)),
+                          oracle.inflow_count(fd, c1["partition"], value_policies=False))
+    assert np.array_equal(lfr.to_numpy(lfr.downstream_level(a)), oracle.downstream_level(fd))
+    s = a.topology().stats()
+    v = synthetic.validate(fd)
+    assert s["cycle_cells"] == 0 and s["max_level"] + 1 == v["longest_path"]
+    assert s["outlet_cells"] == v["edge_outlets"]
+
+
+def test_accu_f32_against_fp64_oracle(lfr, c1):
+    fd, m, ps = c1["flow_direction"], c1["material"], c1["partition"]
+    got = lfr.to_numpy(lfr.accu(lfr.from_numpy(fd, ps), lfr.from_numpy(m, ps)))
+    want = oracle.accu(fd, m.astype(np.float64), ps, dtype=np.float64)
+    parity.assert_close32(got, want, "accu_f32")
+    # compensated accumulation is at least as close to float64 as the reference's float32 walk
+    ref32 = oracle.accu(fd, m, ps, dtype=np.float32)
+    assert parity.rel_error(got, want, parity.FLOOR32)[0] <= parity.rel_error(ref32, want, parity.FLOOR32)[0] + 1e-7
+
+
+def test_accu_f64_against_fp64_oracle(lfr, c1):
+    fd, m, ps = c1["flow_direction"], c1["material"].astype(np.float64), c1["partition"]
+    got = lfr.to_numpy(lfr.accu(lfr.from_numpy(fd, ps), lfr.from_numpy(m, ps)))
+    parity.assert_close64(got, oracle.accu(fd, m, ps, dtype=np.float64), "accu_f64")
+
+
+def test_accu_scalar_inflow(lfr, c1):
+    fd, ps = c1["flow_direction"], c1["partition"]
+    got = lfr.to_numpy(lfr.accu(lfr.from_numpy(fd, ps), 1.0))
+    want = oracle.accu(fd, 1.0, ps, dtype=np.float64)
+    assert np.array_equal(got, want.astype(np.float32))  # integer counts of upstream cells: exact
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+def test_accu_threshold_and_fraction(lfr, dtype):
+    fd, m, rng = ragged(777, 1001, 11)
+    thr = (rng.random(fd.shape, dtype=np.float32) * 0.5).astype(np.float32)
+    frac = rng.random(fd.shape, dtype=np.float32)
+    ps = (256, 300)
+    a = lfr.from_numpy(fd, ps)
+    check = parity.assert_close32 if dtype == np.float32 else parity.assert_close64
+    for fn_gpu, fn_cpu, other in ((lfr.accu_threshold, oracle.accu_threshold, thr),
+                                  (lfr.accu_fraction, oracle.accu_fraction, frac)):
+        flux, state = fn_gpu(a, lfr.from_numpy(m.astype(dtype), ps), lfr.from_numpy(other.astype(dtype), ps))
+        wf, ws = fn_cpu(fd, m.astype(np.float64), other.astype(np.float64), ps, dtype=np.float64)
+        check(lfr.to_numpy(flux), wf, fn_gpu.__name__ + " flux")
+        check(lfr.to_numpy(state), ws, fn_gpu.__name__ + " state")
+    # scalar threshold / fraction overloads
+    flux, state = lfr.accu_threshold(a, lfr.from_numpy(m.astype(dtype), ps), 0.25)
+    wf, ws = oracle.accu_threshold(fd, m.astype(np.float64), 0.25, ps, dtype=np.float64)
+    check(lfr.to_numpy(flux), wf, "threshold scalar")
+
+
+def kw_inputs(rows, cols, seed):
+    d = synthetic.kinematic_wave_inputs(rows, cols, seed, 100.0, cached=False)
+    return d
+
+
+@pytest.mark.parametrize("f32_inputs", [True, False], ids=["f32in", "f64in"])
+def test_kinematic_wave_three_steps(lfr, f32_inputs):
+    d = kw_inputs(512, 640, 5)
+    fd, ps = d["flow_direction"], (128, 160)
+    a = lfr.from_numpy(fd, ps)
+    lat = d["lateral_inflow"] if f32_inputs else d["lateral_inflow"].astype(np.float64)
+    alpha = d["alpha"] if f32_inputs else d["alpha"].astype(np.float64)
+    q_gpu = lfr.from_numpy(d["discharge"], ps)
+    q_cpu = d["discharge"]
+    lat_d, alpha_d = lfr.from_numpy(lat, ps), lfr.from_numpy(alpha, ps)
+    for step in range(3):
+        q_gpu = lfr.kinematic_wave(a, q_gpu, lat_d, alpha_d, 0.6, 3600.0, 100.0)
+        q_cpu = oracle.kinematic_wave(fd, q_cpu, lat.astype(np.float64), alpha.astype(np.float64), 0.6, 3600.0,
+                                      100.0, ps, dtype=np.float64)
+        parity.assert_close64(lfr.to_numpy(q_gpu), q_cpu, f"kinematic_wave step {step}")
+
+
+def test_kinematic_wave_raster_beta_and_channel_length(lfr):
+    d = kw_inputs(200, 300, 9)
+    fd = d["flow_direction"]
+    rng = np.random.default_rng(3)
+    beta = rng.uniform(0.5, 0.7, fd.shape)
+    dx = rng.uniform(50, 150, fd.shape)
+    q0 = d["discharge"]
+    q0[::17, ::13] = 0.0  # dry cells
+    lat = d["lateral_inflow"].astype(np.float64)
+    lat[::29, ::31] = 0.0
+    got = lfr.kinematic_wave(lfr.from_numpy(fd), lfr.from_numpy(q0), lfr.from_numpy(lat),
+                             lfr.from_numpy(d["alpha"].astype(np.float64)), lfr.from_numpy(beta), 900.0,
+                             lfr.from_numpy(dx))
+    want = oracle.kinematic_wave(fd, q0, lat, d["alpha"].astype(np.float64), beta, 900.0, dx, dtype=np.float64)
+    parity.assert_close64(lfr.to_numpy(got), want, "kinematic_wave raster beta/dx")
+
+
+def test_no_data_propagation(lfr):
+    fd, m, rng = ragged(300, 301, 4)
+    fd = fd.copy()
+    fd[rng.random(fd.shape) < 0.002] = 255  # no-data flow directions (flow into them is undefined:
+    m = m.copy()                              # the comparison below is with the oracle on the same input)
+    m[rng.random(fd.shape) < 0.003] = np.nan
+    m[rng.random(fd.shape) < 0.003] = -1.0  # outside the domain
+    a = lfr.from_numpy(fd)
+    got = lfr.to_numpy(lfr.accu(a, lfr.from_numpy(m)))
+    want = oracle.accu(fd, m.astype(np.float64), dtype=np.float64)
+    parity.assert_close32(got, want, "accu with no-data")
+    assert np.isnan(got).sum() > 0
+
+
+def test_all_no_data(lfr):
+    fd = np.full((37, 41), 255, np.uint8)
+    a = lfr.from_numpy(fd)
+    assert (lfr.to_numpy(lfr.inflow_count(a)) == 255).all()
+    assert np.isnan(lfr.to_numpy(lfr.accu(a, 1.0))).all()
+    assert (lfr.to_numpy(lfr.downstream_level(a)) == -1).all()
+
+
+def test_cycles_sinks_and_unknown_codes(lfr):
+    """Cells on or below a cycle keep the sum of what entered upstream cells pushed into them (the
+    reference never enters them); sinks (5) and unknown codes keep their material."""
+    rng = np.random.default_rng(2)
+    fd = rng.choice(np.array([1, 2, 3, 4, 6, 7, 8, 9, 5, 0, 17], np.uint8), size=(64, 48))
+    fd[10, 10], fd[10, 11], fd[11, 11], fd[11, 10] = 6, 2, 4, 8  # 4-cycle
+    fd[30, 5], fd[30, 6] = 6, 4  # 2-cycle
+    m = rng.random(fd.shape, dtype=np.float32)
+    a = lfr.from_numpy(fd)
+    assert a.topology().stats()["cycle_cells"] > 0
+    got = lfr.to_numpy(lfr.accu(a, lfr.from_numpy(m)))
+    want = oracle.accu(fd, m.astype(np.float64), dtype=np.float64)
+    parity.assert_close32(got, want, "accu with cycles")
+    assert np.array_equal(lfr.to_numpy(lfr.downstream_level(a)), oracle.downstream_level(fd))
+    flux, state = lfr.accu_threshold(a, lfr.from_numpy(m), 0.3)
+    wf, ws = oracle.accu_threshold(fd, m.astype(np.float64), 0.3, dtype=np.float64)
+    parity.assert_close32(lfr.to_numpy(flux), wf, "threshold with cycles")
+    parity.assert_close32(lfr.to_numpy(state), ws, "threshold state with cycles")
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (1, 257), (263, 1), (3, 2)])
+def test_degenerate_shapes(lfr, shape):
+    rng = np.random.default_rng(sum(shape))
+    fd = rng.choice(np.array([1, 2, 3, 4, 5, 6, 7, 8, 9], np.uint8), size=shape)
+    m = rng.random(shape, dtype=np.float32)
+    a = lfr.from_numpy(fd)
+    parity.assert_close32(lfr.to_numpy(lfr.accu(a, lfr.from_numpy(m))),
+                          oracle.accu(fd, m.astype(np.float64), dtype=np.float64), f"accu {shape}")
+    assert np.array_equal(lfr.to_numpy(lfr.inflow_count(a)), oracle.inflow_count(fd))
+
+
+def test_shape_mismatch_is_an_error(lfr):
+    from lue_gb300._lib import LueGpuError
+    a = lfr.from_numpy(np.full((8, 8), 6, np.uint8), (4, 4))
+    with pytest.raises(LueGpuError):
+        lfr.accu(a, lfr.from_numpy(np.ones((8, 9), np.float32)))
+    with pytest.raises(LueGpuError):
+        lfr.accu(a, lfr.from_numpy(np.ones((8, 8), np.float32), (8, 8)))
+    with pytest.raises(ValueError):
+        lfr.from_numpy(np.ones((8, 8), np.float32), (9, 1))
+
+
+def test_repeated_calls_are_identical(lfr, c1):
+    fd, m, ps = c1["flow_direction"], c1["material"], c1["partition"]
+    a = lfr.from_numpy(fd, ps)
+    md = lfr.from_numpy(m, ps)
+    r1 = lfr.to_numpy(lfr.accu(a, md))
+    r2 = lfr.to_numpy(lfr.accu(a, md))
+    assert np.array_equal(r1, r2)  # the pull order is fixed: bitwise reproducible
