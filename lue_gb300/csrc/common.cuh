@@ -101,6 +101,14 @@ void set_error(const std::string& msg);
 int fail(int status, const std::string& msg);
 int cuda_status(cudaError_t err, const char* what);
 
+// One thread per element, no grid-stride reuse (walk kernels: a thread that walks a long path must not
+// also own later cells, or the walks chain up behind each other).
+inline unsigned grid_all(int64_t n, int threads)
+{
+    int64_t b = (n + threads - 1) / threads;
+    return (unsigned)(b < 1 ? 1 : b);
+}
+
 inline int grid_for(int64_t n, int threads, int max_blocks = 152 * 16)
 {
     int64_t b = (n + threads - 1) / threads;

@@ -268,7 +268,7 @@ static int run(lue_gpu_topology* t, Visitor v, T* out, T* rem, bool use_lo, cuda
         cudaMemcpyAsync(t->work_count, core->count, words_for(n) * 4, cudaMemcpyDeviceToDevice, stream), what);
     if (rc) return rc;
     WalkGrid g{core->fd, core->count, t->work_count, core->rows, core->cols, n};
-    k_walk<<<grid_for(n, 256), 256, 0, stream>>>(g, v);
+    k_walk<<<grid_all(n, 256), 256, 0, stream>>>(g, v);
     if (core->stats.cycle_cells > 0) {
         k_cycle_cells<T><<<grid_for(n, 256), 256, 0, stream>>>(core->fd, core->upmask, t->work_count, n, core->cols,
                                                                out, rem, use_lo ? t->lo : nullptr);

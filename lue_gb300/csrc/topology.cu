@@ -218,7 +218,7 @@ extern "C" int lue_gpu_topology_create(const uint8_t* flow_direction, int64_t ro
     {
         WalkGrid g{core->fd, core->count, t->work_count, rows, cols, n};
         LevelVisitor v{core->upmask, core->level, cols};
-        k_walk<<<grid_for(n, 256), 256, 0, stream>>>(g, v);
+        k_walk<<<grid_all(n, 256), 256, 0, stream>>>(g, v);
     }
     if ((rc = cuda_status(cudaMemsetAsync(dstats, 0, sizeof hstats, stream), "memset"))) goto error;
     k_stats<<<grid_for(n, 256), 256, 0, stream>>>(core->fd, core->count, core->level, rows, cols, dstats);

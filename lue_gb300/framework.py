@@ -144,9 +144,14 @@ def _check_partitioning(flow_direction, *arrays):
 
 
 def _material_dtype(*args):
+    """Element type of the operation: that of the first float raster, else of a numpy float64 scalar,
+    else float32 (the reference binds the float overload first)."""
     for a in args:
         if isinstance(a, PartitionedArray) and a.dtype in (torch.float32, torch.float64):
             return a.dtype
+    for a in args:
+        if isinstance(a, np.float64) or (isinstance(a, torch.Tensor) and a.dtype == torch.float64):
+            return torch.float64
     return torch.float32
 
 

@@ -30,4 +30,4 @@ def arg(spec, dtype=np.float32):
     if "raster" in spec:
         return np.array([[np.nan if v is None else v for v in row] for row in spec["raster"]], dtype=dtype)
     v = spec["scalar"]
-    return float("nan") if v is None else float(v)
+    return np.dtype(dtype).type(float("nan") if v is None else v)

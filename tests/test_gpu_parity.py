@@ -87,8 +87,8 @@ def test_accu_threshold_and_fraction(lfr, dtype):
         check(lfr.to_numpy(flux), wf, fn_gpu.__name__ + " flux")
         check(lfr.to_numpy(state), ws, fn_gpu.__name__ + " state")
     # scalar threshold / fraction overloads
-    flux, state = lfr.accu_threshold(a, lfr.from_numpy(m.astype(dtype), ps), 0.25)
-    wf, ws = oracle.accu_threshold(fd, m.astype(np.float64), 0.25, ps, dtype=np.float64)
+    flux, state = lfr.accu_threshold(a, lfr.from_numpy(m.astype(dtype), ps), dtype(0.25))
+    wf, ws = oracle.accu_threshold(fd, m.astype(np.float64), float(dtype(0.25)), ps, dtype=np.float64)
     check(lfr.to_numpy(flux), wf, "threshold scalar")
 
 
@@ -167,8 +167,9 @@ def test_cycles_sinks_and_unknown_codes(lfr):
     want = oracle.accu(fd, m.astype(np.float64), dtype=np.float64)
     parity.assert_close32(got, want, "accu with cycles")
     assert np.array_equal(lfr.to_numpy(lfr.downstream_level(a)), oracle.downstream_level(fd))
-    flux, state = lfr.accu_threshold(a, lfr.from_numpy(m), 0.3)
-    wf, ws = oracle.accu_threshold(fd, m.astype(np.float64), 0.3, dtype=np.float64)
+    thr = np.float32(0.3)  # the float32 entry point sees 0.3f: give the float64 oracle the same value
+    flux, state = lfr.accu_threshold(a, lfr.from_numpy(m), thr)
+    wf, ws = oracle.accu_threshold(fd, m.astype(np.float64), float(thr), dtype=np.float64)
     parity.assert_close32(lfr.to_numpy(flux), wf, "threshold with cycles")
     parity.assert_close32(lfr.to_numpy(state), ws, "threshold state with cycles")
 
