@@ -143,6 +143,21 @@ int lue_gpu_kinematic_wave_f64_f32in(lue_gpu_topology* topology, const double* c
                                      double time_step_duration, double channel_length, double* outflow,
                                      void* stream);
 
+/* accu (float32) that allocates no device memory.  No counterpart in the reference: it is for callers
+ * that must not allocate on their call path (a model step inside a host framework that owns the
+ * device memory pool, or a latency-critical loop in which cudaMalloc/cudaFree would synchronise the
+ * device).  It takes the flow direction itself (no topology) and keeps its scratch in one fixed,
+ * file-scope device array of 7 * LUE_GPU_NOALLOC_MAX_CELLS bytes (about 29 MB) that every GPU which
+ * loads the library holds until the process exits.  Rasters above LUE_GPU_NOALLOC_MAX_CELLS cells fail
+ * with LUE_GPU_ERANGE.  The first call on each device resolves that array's device address
+ * (cudaGetSymbolAddress, with the device current); make the first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race and must be serialised by the caller.
+ * Results equal lue_gpu_accu_f32's. */
+#define LUE_GPU_NOALLOC_MAX_CELLS 4194304
+int lue_gpu_accu_f32_noalloc(const uint8_t* flow_direction, int64_t rows, int64_t cols, int64_t partition_rows,
+                             int64_t partition_cols, const float* inflow, float inflow_scalar, float* outflow,
+                             void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -57,6 +57,7 @@ def _declare(L):
         "lue_gpu_accu_fraction_f64": ([p, p, d, p, d, p, p, p], i32),
         "lue_gpu_kinematic_wave_f64": ([p, p, d, p, d, p, d, p, d, d, p, d, p, p], i32),
         "lue_gpu_kinematic_wave_f64_f32in": ([p, p, d, p, d, p, d, d, d, d, p, p], i32),
+        "lue_gpu_accu_f32_noalloc": ([p, i64, i64, i64, i64, p, f, p, p], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)

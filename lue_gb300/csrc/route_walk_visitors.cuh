@@ -1,0 +1,249 @@
+// route_walk_visitors.cuh — cell rules of accu, accu_threshold, accu_fraction and kinematic_wave as
+// visitors of the walk engine (walk.cuh), and the pass that finishes cells on or below flow cycles.
+// See route_walk.cu for the reference counterparts.
+#pragma once
+
+#include <cfloat>
+
+#include "kinematic_wave.cuh"
+#include "walk.cuh"
+
+namespace lue_gb300 {
+
+template <class T>
+__device__ __forceinline__ T value_at(const T* p, T s, int64_t i)
+{
+    return p ? __ldg(p + i) : s;
+}
+
+template <class T>
+__device__ __forceinline__ T qnan();
+template <>
+__device__ __forceinline__ float qnan<float>() { return __int_as_float(0x7fc00000); }
+template <>
+__device__ __forceinline__ double qnan<double>() { return __longlong_as_double(0x7ff8000000000000ll); }
+
+enum class Rule { accu, threshold, fraction };
+
+// --- float32: float-float running values ---------------------------------------------------------
+
+template <Rule R>
+struct RouteF32 {
+    const uint8_t* upmask;
+    const float* a;   // inflow
+    float as;
+    const float* b;   // threshold / fraction
+    float bs;
+    float* out;       // outflow / flux
+    float* rem;       // state (threshold, fraction)
+    float* lo;        // residual of out
+    int64_t cols;
+
+    __device__ void no_data(int64_t c)
+    {
+        out[c] = qnan<float>();
+        lo[c] = 0.0f;
+        if (R != Rule::accu) rem[c] = qnan<float>();
+    }
+
+    __device__ void enter(int64_t c)
+    {
+        unsigned m = __ldg(upmask + c);
+        FF t{0.0f, 0.0f};
+        bool nan = false;
+        while (m) {
+            int k = __ffs(m) - 1;
+            m &= m - 1;
+            int64_t u = c + nb_dr(k) * cols + nb_dc(k);
+            float h = load_cg(out + u);
+            if (isnan(h)) nan = true;
+            else t.add(h, load_cg(lo + u));
+        }
+        float x = value_at(a, as, c);
+        if (R == Rule::accu) {
+            if (nan || isnan(x) || !(x >= 0.0f)) {
+                no_data(c);
+                return;
+            }
+            t.add(x);
+            t.normalise();
+            out[c] = t.hi;
+            lo[c] = t.lo;
+        } else if (R == Rule::threshold) {
+            float th = value_at(b, bs, c);
+            if (nan || isnan(x) || isnan(th) || !(x >= 0.0f && th >= 0.0f)) {
+                no_data(c);
+                return;
+            }
+            t.add(x);
+            t.normalise();
+            // strict '>' on the compensated total (accu_threshold.hpp:157)
+            if (t.hi > th || (t.hi == th && t.lo > 0.0f)) {
+                FF d{0.0f, 0.0f};
+                two_sum(t.hi, -th, d.hi, d.lo);
+                d.lo = __fadd_rn(d.lo, t.lo);
+                d.normalise();
+                rem[c] = th;
+                out[c] = d.hi;
+                lo[c] = d.lo;
+            } else {
+                rem[c] = __fadd_rn(t.hi, t.lo);
+                out[c] = 0.0f;
+                lo[c] = 0.0f;
+            }
+        } else {
+            float f = value_at(b, bs, c);
+            if (nan || isnan(x) || isnan(f) || !(x >= 0.0f && f >= 0.0f && f <= 1.0f)) {
+                no_data(c);
+                return;
+            }
+            t.add(x);
+            t.normalise();
+            // flux = fraction * total, state = total - flux (accu_fraction.hpp:157-159)
+            float ph = __fmul_rn(f, t.hi);
+            float pl = __fmaf_rn(f, t.hi, -ph);
+            pl = __fmaf_rn(f, t.lo, pl);
+            FF d{ph, pl};
+            d.normalise();
+            FF r{0.0f, 0.0f};
+            two_sum(t.hi, -d.hi, r.hi, r.lo);
+            r.lo = __fadd_rn(r.lo, __fsub_rn(t.lo, d.lo));
+            rem[c] = __fadd_rn(r.hi, r.lo);
+            out[c] = d.hi;
+            lo[c] = d.lo;
+        }
+    }
+};
+
+// --- float64: plain double arithmetic, like the reference's double instantiation ---------------------
+
+template <Rule R>
+struct RouteF64 {
+    const uint8_t* upmask;
+    const double* a;
+    double as;
+    const double* b;
+    double bs;
+    double* out;
+    double* rem;
+    int64_t cols;
+
+    __device__ void no_data(int64_t c)
+    {
+        out[c] = qnan<double>();
+        if (R != Rule::accu) rem[c] = qnan<double>();
+    }
+
+    __device__ void enter(int64_t c)
+    {
+        unsigned m = __ldg(upmask + c);
+        double t = 0.0;
+        bool nan = false;
+        while (m) {
+            int k = __ffs(m) - 1;
+            m &= m - 1;
+            double h = load_cg(out + c + nb_dr(k) * cols + nb_dc(k));
+            if (isnan(h)) nan = true;
+            else t += h;
+        }
+        double x = value_at(a, as, c);
+        if (R == Rule::accu) {
+            if (nan || isnan(x) || !(x >= 0.0)) return no_data(c);
+            out[c] = t + x;
+        } else if (R == Rule::threshold) {
+            double th = value_at(b, bs, c);
+            if (nan || isnan(x) || isnan(th) || !(x >= 0.0 && th >= 0.0)) return no_data(c);
+            t += x;
+            if (t > th) {
+                rem[c] = th;
+                out[c] = t - th;
+            } else {
+                rem[c] = t;
+                out[c] = 0.0;
+            }
+        } else {
+            double f = value_at(b, bs, c);
+            if (nan || isnan(x) || isnan(f) || !(x >= 0.0 && f >= 0.0 && f <= 1.0)) return no_data(c);
+            t += x;
+            double d = f * t;
+            rem[c] = t - d;
+            out[c] = d;
+        }
+    }
+};
+
+// --- kinematic wave (float64 discharge; lateral inflow and alpha as TIn) ------------------------------
+
+template <class TIn>
+struct RouteKW {
+    const uint8_t* upmask;
+    const double* qcur;
+    double qcur_s;
+    const TIn* lateral;
+    double lateral_s;
+    const TIn* alpha;
+    double alpha_s;
+    const double* beta;
+    double beta_s;
+    double dt;
+    const double* dx;
+    double dx_s;
+    double* out;
+    int64_t cols;
+
+    __device__ void no_data(int64_t c) { out[c] = qnan<double>(); }
+
+    __device__ void enter(int64_t c)
+    {
+        unsigned m = __ldg(upmask + c);
+        double up = 0.0;
+        bool nan = false;
+        while (m) {
+            int k = __ffs(m) - 1;
+            m &= m - 1;
+            double h = load_cg(out + c + nb_dr(k) * cols + nb_dc(k));
+            if (isnan(h)) nan = true;
+            else up += h;
+        }
+        double qc = qcur ? __ldg(qcur + c) : qcur_s;
+        double q = lateral ? (double)__ldg(lateral + c) : lateral_s;
+        double al = alpha ? (double)__ldg(alpha + c) : alpha_s;
+        double be = beta ? __ldg(beta + c) : beta_s;
+        double len = dx ? __ldg(dx + c) : dx_s;
+        if (nan || isnan(qc) || isnan(q) || isnan(al) || isnan(be) || isnan(dt) || isnan(len) ||
+            !(qc >= 0.0 && q >= 0.0 && len > 0.0)) {
+            out[c] = qnan<double>();
+            return;
+        }
+        out[c] = iterate_to_new_discharge(up, qc, q, al, be, dt, len);
+    }
+};
+
+// Cells never entered (on or below a cycle): sum of the outflow of entered upstream cells.
+template <class T>
+__global__ void __launch_bounds__(256)
+    k_cycle_cells(const uint8_t* fd, const uint8_t* upmask, const uint32_t* work, int64_t n, int64_t cols, T* out,
+                  T* rem, float* lo)
+{
+    for (int64_t c = grid_stride_begin(); c < n; c += grid_stride()) {
+        if (fd[c] == kNoData) continue;
+        if (((work[c >> 2] >> ((c & 3) * 8)) & 0xFFu) == 0u) continue;  // entered
+        unsigned m = upmask[c];
+        T s = 0;
+        bool nan = false;
+        while (m) {
+            int k = __ffs(m) - 1;
+            m &= m - 1;
+            int64_t u = c + nb_dr(k) * cols + nb_dc(k);
+            if (((work[u >> 2] >> ((u & 3) * 8)) & 0xFFu) != 0u) continue;  // not entered: pushed nothing
+            T h = out[u];
+            if (isnan(h)) nan = true;
+            else s += h;
+        }
+        out[c] = nan ? qnan<T>() : s;
+        if (rem) rem[c] = nan ? qnan<T>() : T(0);
+        if (lo) lo[c] = 0.0f;
+    }
+}
+
+}  // namespace lue_gb300
