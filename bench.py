@@ -243,11 +243,13 @@ def bench_ours(args, world, rank, local):
     topology_ms = 1000 * (time.perf_counter() - t0)
     stats = topo.stats()
 
-    # warm-up (also checks the mass balance once)
+    from lue_gb300 import _lib
+    engine = "tiles" if stats.get("tile_exits", 0) > 0 else "walk"
     out = None
     for _ in range(args.warmup):
         out = lfr.accu(fd_d, m_d)
     torch.cuda.synchronize()
+    launches0 = _lib.lib().lue_gpu_kernel_launches()
 
     # timed, device-resident
     sampler = ClockSampler(local)
@@ -262,6 +264,7 @@ def bench_ours(args, world, rank, local):
         ev[k + 1].record(stream)
     torch.cuda.synchronize()
     clocks = sampler.stop()
+    launches = _lib.lib().lue_gpu_kernel_launches() - launches0
     barrier(world)
     step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
     total_s = max_over_ranks(sum(step_ms) / 1000.0, world)
@@ -294,8 +297,8 @@ def bench_ours(args, world, rank, local):
     peak, peak_kind = peaks()
     mean_step_s = statistics.mean(step_ms) / 1000.0
     achieved = ACCU_BYTES_PER_CELL * n / mean_step_s / 1e9
-    tr = profile_traffic("k_walk_accu_f32")
-    traffic = None if tr is None else tr[0] / tr[1] * n
+    tr = profile_traffic(f"accu_f32_{engine}")
+    traffic = None if tr is None else round(tr[0] / tr[1] * n)
 
     extra = {}
     if args.kinematic_wave_steps > 0 and rank == 0:
@@ -319,16 +322,19 @@ def bench_ours(args, world, rank, local):
         "config": {"workload": args.workload, "rows": rows, "cols": cols, "partition_shape": list(ps),
                    "l2": "inputs larger than L2 (268 MB fd + 1 GB material per step)",
                    "topology": "resident, built once", "topology_build_ms": round(topology_ms, 2),
-                   "longest_flow_path_cells": stats["max_level"] + 1, "engine": "walk"},
+                   "longest_flow_path_cells": stats["max_level"] + 1, "engine": engine,
+                   "tile_exits": stats.get("tile_exits", 0), "exit_forest_depth": stats.get("exit_forest_depth", 0)},
         "e2e": {"value": round(e2e_value, 3), "unit": "Mcells/s", "h2d_bytes_per_step": 4 * n,
                 "d2h_bytes_per_step": 4 * n},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "kernel": "k_walk<RouteF32<accu>>", "peak_kind": peak_kind,
-                     "bytes_per_cell": ACCU_BYTES_PER_CELL},
+                     "kernel": ("accu_f32 call: k_tile_local + exit-forest scan + k_tile_fixup" if engine == "tiles"
+                                else "k_walk<RouteF32<accu>>"),
+                     "timed": "whole call per step (all its kernels), CUDA events on the launching stream",
+                     "peak_kind": peak_kind, "bytes_per_cell": ACCU_BYTES_PER_CELL},
         "cpu_baseline": cpu,
         "clocks": clocks,
-        "gpu_launches": args.steps,
+        "gpu_launches": int(launches),
         "mass_balance": {"material_in": total_in, "outlet_outflow": total_out,
                          "rel_err": abs(total_out - total_in) / total_in},
         "extra": extra,

@@ -79,11 +79,15 @@ typedef struct lue_gpu_topology_stats {
     int64_t cycle_cells;       /* valid cells on or downstream of a flow cycle (never routed) */
     int64_t max_level;         /* largest downstream level (longest flow path minus one) */
     int64_t device_bytes;      /* device memory held by this handle */
+    int64_t tile_exits;        /* cells whose flow leaves their 64 x 64 tile (0: tile engine off) */
+    int64_t exit_forest_depth; /* depth of the forest of those exits */
 } lue_gpu_topology_stats;
 
 /* Library */
 int lue_gpu_abi_version(void);
 const char* lue_gpu_last_error(void);
+/* Number of CUDA kernels this library has launched in this process (for benchmarks and tests). */
+unsigned long long lue_gpu_kernel_launches(void);
 
 /* Topology: built once per flow-direction raster, resident on the device. */
 int lue_gpu_topology_create(const uint8_t* flow_direction, int64_t rows, int64_t cols,
@@ -103,6 +107,15 @@ int lue_gpu_inflow_count_u8(const lue_gpu_topology* topology, int value_policies
  * -1 for no-data and for cells on or below a cycle.  No reference counterpart: it exposes the
  * downstream ordering the routing kernels use. */
 int lue_gpu_downstream_level_i32(const lue_gpu_topology* topology, int32_t* level, void* stream);
+
+/* d8_flow_direction: steepest-descent D8 code per cell from an elevation raster, the reference's rule
+ * (ALG/definition/d8_flow_direction.hpp:45-147): unweighted drop, candidates N, W, E, S, NW, NE, SW, SE,
+ * strict '>', sink (5) without a positive drop, 255 for NaN elevation; outside the array the smallest
+ * positive normal value of the element type, so edge cells above it drain off the array. */
+int lue_gpu_d8_flow_direction_f32(const float* elevation, int64_t rows, int64_t cols, uint8_t* flow_direction,
+                                  void* stream);
+int lue_gpu_d8_flow_direction_f64(const double* elevation, int64_t rows, int64_t cols, uint8_t* flow_direction,
+                                  void* stream);
 
 /* accu: outflow = upstream outflow + inflow (inflow >= 0, else NaN). */
 int lue_gpu_accu_f32(lue_gpu_topology* topology, const float* inflow, float inflow_scalar, float* outflow,

@@ -91,5 +91,21 @@ def synth_library(force=False):
     return target
 
 
+def cpp_example(force=False):
+    """The C++ mirror's example program (examples/accu_example.cpp), linked against liblue_gb300.so."""
+    lib = gpu_library()
+    target = os.path.join(BUILD, "accu_example")
+    src = os.path.join(PKG, "examples", "accu_example.cpp")
+    hpp = os.path.join(CSRC, "lue_gb300.hpp")
+    if force or _stale(target, [src, hpp, lib, __file__]):
+        cuda = os.path.dirname(os.path.dirname(nvcc()))
+        tmp = target + f".tmp{os.getpid()}"
+        _run(["g++", "-std=c++17", "-O2", "-I" + INCLUDE, "-I" + CSRC, "-I" + os.path.join(cuda, "include"), src,
+              "-o", tmp, "-L" + BUILD, "-llue_gb300", "-L" + os.path.join(cuda, "lib64"), "-lcudart",
+              "-Wl,-rpath," + BUILD])
+        os.replace(tmp, target)
+    return target
+
+
 def build_all(force=False, verbose=False):
-    return {"gpu": gpu_library(force, verbose), "synth": synth_library(force)}
+    return {"gpu": gpu_library(force, verbose), "synth": synth_library(force), "cpp_example": cpp_example(force)}

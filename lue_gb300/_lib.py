@@ -22,7 +22,7 @@ class LueGpuError(RuntimeError):
 class TopologyStats(ctypes.Structure):
     _fields_ = [(name, ctypes.c_int64) for name in (
         "rows", "cols", "partition_rows", "partition_cols", "valid_cells", "ridge_cells", "outlet_cells",
-        "sink_cells", "cycle_cells", "max_level", "device_bytes")]
+        "sink_cells", "cycle_cells", "max_level", "device_bytes", "tile_exits", "exit_forest_depth")]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -43,6 +43,7 @@ def _declare(L):
     sig = {
         "lue_gpu_abi_version": ([], i32),
         "lue_gpu_last_error": ([], ctypes.c_char_p),
+        "lue_gpu_kernel_launches": ([], ctypes.c_ulonglong),
         "lue_gpu_topology_create": ([p, i64, i64, i64, i64, p, ctypes.POINTER(p)], i32),
         "lue_gpu_topology_clone": ([p, ctypes.POINTER(p)], i32),
         "lue_gpu_topology_destroy": ([p], i32),
@@ -58,6 +59,8 @@ def _declare(L):
         "lue_gpu_kinematic_wave_f64": ([p, p, d, p, d, p, d, p, d, d, p, d, p, p], i32),
         "lue_gpu_kinematic_wave_f64_f32in": ([p, p, d, p, d, p, d, d, d, d, p, p], i32),
         "lue_gpu_accu_f32_noalloc": ([p, i64, i64, i64, i64, p, f, p, p], i32),
+        "lue_gpu_d8_flow_direction_f32": ([p, i64, i64, p, p], i32),
+        "lue_gpu_d8_flow_direction_f64": ([p, i64, i64, p, p], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)

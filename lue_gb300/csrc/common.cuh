@@ -62,24 +62,36 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
     e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
-// Float-float accumulator: value = hi + lo with |lo| <= ulp(hi) / 2 after normalise().
+// Float-float accumulator: value = hi + lo with |lo| <= ulp(hi) / 2 after normalise().  A sum that is
+// not finite keeps IEEE semantics (inf stays inf, NaN stays NaN) with lo = 0; the error terms of
+// two_sum would otherwise turn inf into NaN.
 struct FF {
     float hi, lo;
     __device__ __forceinline__ void add(float x)
     {
         float s, e;
         two_sum(hi, x, s, e);
+        if (!isfinite(s)) {
+            hi = s;
+            lo = 0.0f;
+            return;
+        }
         hi = s;
         lo = __fadd_rn(lo, e);
     }
     __device__ __forceinline__ void add(float xh, float xl)
     {
         add(xh);
-        lo = __fadd_rn(lo, xl);
+        if (isfinite(hi)) lo = __fadd_rn(lo, xl);
     }
     __device__ __forceinline__ void normalise()
     {
         float s = __fadd_rn(hi, lo);
+        if (!isfinite(s)) {
+            hi = s;
+            lo = 0.0f;
+            return;
+        }
         lo = __fsub_rn(lo, __fsub_rn(s, hi));
         hi = s;
     }
@@ -98,6 +110,8 @@ __device__ __forceinline__ int64_t grid_stride() { return (int64_t)gridDim.x * b
 // Host side -----------------------------------------------------------------------------------------
 
 void set_error(const std::string& msg);
+// Kernel launches made by this library in this process (reported by lue_gpu_kernel_launches).
+void count_launches(int n);
 int fail(int status, const std::string& msg);
 int cuda_status(cudaError_t err, const char* what);
 

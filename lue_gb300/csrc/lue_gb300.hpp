@@ -1,0 +1,290 @@
+// lue_gb300.hpp — C++ mirror of LUE's routing operations over the C ABI of include/lue_gb300.h.
+//
+// Same operation names, parameter order and raster/scalar overloads as the reference's
+// lue::value_policies:: functions (source/framework/algorithm/include/lue/framework/algorithm/
+// value_policies/{accu,accu_threshold,accu_fraction,kinematic_wave}.hpp) and lue::inflow_count
+// (.../algorithm/inflow_count.hpp:29-42).  A PartitionedArray here is a device-resident, row-major
+// raster with the reference's (shape, partition_shape); like the reference's it is move-only.  A shape
+// or partitioning mismatch throws std::runtime_error, as ALG/detail/verify_compatible.hpp:23-40 does;
+// invalid values become NaN in the result, never an exception.
+//
+// Header-only; link with liblue_gb300.so and the CUDA runtime.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <array>
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <type_traits>
+#include <utility>
+
+#include "lue_gb300.h"
+
+namespace lue_gb300 {
+
+using Shape = std::array<std::int64_t, 2>;
+
+inline void check(int status, const char* what)
+{
+    if (status != LUE_GPU_OK)
+        throw std::runtime_error(std::string(what) + ": " + lue_gpu_last_error());
+}
+
+inline void check_cuda(cudaError_t err, const char* what)
+{
+    if (err != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(err));
+}
+
+// Resident flow topology of one flow-direction raster (inflow counts, downstream ordering, scratch).
+class Topology {
+   public:
+    Topology(const std::uint8_t* fd, Shape shape, Shape partition_shape, cudaStream_t stream)
+    {
+        check(lue_gpu_topology_create(fd, shape[0], shape[1], partition_shape[0], partition_shape[1], stream, &_h),
+              "topology");
+    }
+    Topology(const Topology&) = delete;
+    Topology& operator=(const Topology&) = delete;
+    ~Topology() { lue_gpu_topology_destroy(_h); }
+    lue_gpu_topology* handle() const { return _h; }
+
+   private:
+    lue_gpu_topology* _h = nullptr;
+};
+
+template <typename Element>
+class PartitionedArray {
+   public:
+    PartitionedArray() = default;
+
+    PartitionedArray(Shape shape, Shape partition_shape) : _shape(shape), _partition_shape(partition_shape)
+    {
+        if (shape[0] <= 0 || shape[1] <= 0) throw std::runtime_error("Array shape must not be empty");
+        if (partition_shape[0] <= 0 || partition_shape[1] <= 0)
+            throw std::runtime_error("Partition shape must not be empty");
+        if (partition_shape[0] > shape[0] || partition_shape[1] > shape[1])
+            throw std::runtime_error("Partition size must be smaller than or equal to array size");
+        Element* p = nullptr;
+        check_cuda(cudaMalloc(&p, nr_elements() * sizeof(Element)), "PartitionedArray");
+        _data.reset(p);
+    }
+
+    PartitionedArray(const PartitionedArray&) = delete;
+    PartitionedArray& operator=(const PartitionedArray&) = delete;
+    PartitionedArray(PartitionedArray&&) = default;
+    PartitionedArray& operator=(PartitionedArray&&) = default;
+
+    static PartitionedArray from_host(const Element* host, Shape shape, Shape partition_shape,
+                                      cudaStream_t stream = nullptr)
+    {
+        PartitionedArray a(shape, partition_shape);
+        check_cuda(cudaMemcpyAsync(a.data(), host, a.nr_elements() * sizeof(Element), cudaMemcpyHostToDevice, stream),
+                   "from_host");
+        check_cuda(cudaStreamSynchronize(stream), "from_host");
+        return a;
+    }
+
+    void to_host(Element* host, cudaStream_t stream = nullptr) const
+    {
+        check_cuda(cudaMemcpyAsync(host, data(), nr_elements() * sizeof(Element), cudaMemcpyDeviceToHost, stream),
+                   "to_host");
+        check_cuda(cudaStreamSynchronize(stream), "to_host");
+    }
+
+    Element* data() const { return _data.get(); }
+    Shape shape() const { return _shape; }
+    Shape partition_shape() const { return _partition_shape; }
+    Shape shape_in_partitions() const
+    {
+        return {_shape[0] / _partition_shape[0], _shape[1] / _partition_shape[1]};
+    }
+    std::int64_t nr_elements() const { return _shape[0] * _shape[1]; }
+
+    // The flow topology of a flow-direction array, built on first use and kept with the array.
+    Topology& topology(cudaStream_t stream = nullptr) const
+    {
+        static_assert(std::is_same_v<Element, std::uint8_t>, "only flow-direction arrays have a topology");
+        if (!_topology) _topology = std::make_shared<Topology>(data(), _shape, _partition_shape, stream);
+        return *_topology;
+    }
+
+   private:
+    struct Free {
+        void operator()(Element* p) const { cudaFree(p); }
+    };
+    std::unique_ptr<Element, Free> _data;
+    Shape _shape{0, 0};
+    Shape _partition_shape{0, 0};
+    mutable std::shared_ptr<Topology> _topology;
+};
+
+template <typename Element>
+struct Scalar {
+    Element value;
+};
+
+namespace detail {
+
+template <typename A, typename B>
+void verify_compatible(const PartitionedArray<A>& a, const PartitionedArray<B>& b)
+{
+    if (a.shape() != b.shape() || a.shape_in_partitions() != b.shape_in_partitions())
+        throw std::runtime_error("Arrays are not compatible: shapes or partitionings differ");
+}
+
+template <typename F>
+struct Arg {
+    const F* ptr;
+    F value;
+};
+
+template <typename F>
+Arg<F> arg(const PartitionedArray<std::uint8_t>& fd, const PartitionedArray<F>& a)
+{
+    verify_compatible(fd, a);
+    return {a.data(), F(0)};
+}
+
+template <typename F>
+Arg<F> arg(const PartitionedArray<std::uint8_t>&, const Scalar<F>& s)
+{
+    return {nullptr, s.value};
+}
+
+template <typename F>
+inline int accu_call(lue_gpu_topology* t, const F* a, F as, F* out, cudaStream_t s);
+template <>
+inline int accu_call<float>(lue_gpu_topology* t, const float* a, float as, float* out, cudaStream_t s)
+{
+    return lue_gpu_accu_f32(t, a, as, out, s);
+}
+template <>
+inline int accu_call<double>(lue_gpu_topology* t, const double* a, double as, double* out, cudaStream_t s)
+{
+    return lue_gpu_accu_f64(t, a, as, out, s);
+}
+
+template <typename F>
+inline int threshold_call(lue_gpu_topology* t, const F* a, F as, const F* b, F bs, F* o1, F* o2, cudaStream_t s);
+template <>
+inline int threshold_call<float>(lue_gpu_topology* t, const float* a, float as, const float* b, float bs, float* o1,
+                                 float* o2, cudaStream_t s)
+{
+    return lue_gpu_accu_threshold_f32(t, a, as, b, bs, o1, o2, s);
+}
+template <>
+inline int threshold_call<double>(lue_gpu_topology* t, const double* a, double as, const double* b, double bs,
+                                  double* o1, double* o2, cudaStream_t s)
+{
+    return lue_gpu_accu_threshold_f64(t, a, as, b, bs, o1, o2, s);
+}
+
+template <typename F>
+inline int fraction_call(lue_gpu_topology* t, const F* a, F as, const F* b, F bs, F* o1, F* o2, cudaStream_t s);
+template <>
+inline int fraction_call<float>(lue_gpu_topology* t, const float* a, float as, const float* b, float bs, float* o1,
+                                float* o2, cudaStream_t s)
+{
+    return lue_gpu_accu_fraction_f32(t, a, as, b, bs, o1, o2, s);
+}
+template <>
+inline int fraction_call<double>(lue_gpu_topology* t, const double* a, double as, const double* b, double bs,
+                                 double* o1, double* o2, cudaStream_t s)
+{
+    return lue_gpu_accu_fraction_f64(t, a, as, b, bs, o1, o2, s);
+}
+
+}  // namespace detail
+
+template <typename Count = std::uint8_t>
+PartitionedArray<Count> inflow_count(const PartitionedArray<std::uint8_t>& flow_direction, cudaStream_t stream = nullptr)
+{
+    static_assert(std::is_same_v<Count, std::uint8_t>, "the count element is uint8 (the reference's BooleanElement)");
+    PartitionedArray<Count> out(flow_direction.shape(), flow_direction.partition_shape());
+    check(lue_gpu_inflow_count_u8(flow_direction.topology(stream).handle(), 1, out.data(), stream), "inflow_count");
+    return out;
+}
+
+namespace value_policies {
+
+// accu(flow_direction, inflow): inflow is a PartitionedArray<F> or a Scalar<F>.
+template <typename F, typename Inflow>
+PartitionedArray<F> accu(const PartitionedArray<std::uint8_t>& flow_direction, const Inflow& inflow,
+                         cudaStream_t stream = nullptr)
+{
+    auto a = detail::arg<F>(flow_direction, inflow);
+    PartitionedArray<F> out(flow_direction.shape(), flow_direction.partition_shape());
+    check(detail::accu_call<F>(flow_direction.topology(stream).handle(), a.ptr, a.value, out.data(), stream), "accu");
+    return out;
+}
+
+template <typename F>
+PartitionedArray<F> accu(const PartitionedArray<std::uint8_t>& fd, const PartitionedArray<F>& inflow)
+{
+    return accu<F, PartitionedArray<F>>(fd, inflow);
+}
+
+template <typename F>
+PartitionedArray<F> accu(const PartitionedArray<std::uint8_t>& fd, const Scalar<F>& inflow)
+{
+    return accu<F, Scalar<F>>(fd, inflow);
+}
+
+// accu_threshold(flow_direction, inflow, threshold) -> (flux, state); raster/scalar in any combination.
+template <typename F, typename Inflow, typename Threshold>
+std::tuple<PartitionedArray<F>, PartitionedArray<F>> accu_threshold(const PartitionedArray<std::uint8_t>& fd,
+                                                                    const Inflow& inflow, const Threshold& threshold,
+                                                                    cudaStream_t stream = nullptr)
+{
+    auto a = detail::arg<F>(fd, inflow);
+    auto b = detail::arg<F>(fd, threshold);
+    PartitionedArray<F> flux(fd.shape(), fd.partition_shape()), state(fd.shape(), fd.partition_shape());
+    check(detail::threshold_call<F>(fd.topology(stream).handle(), a.ptr, a.value, b.ptr, b.value, flux.data(),
+                                    state.data(), stream),
+          "accu_threshold");
+    return {std::move(flux), std::move(state)};
+}
+
+// accu_fraction(flow_direction, inflow, fraction) -> (flux, state).
+template <typename F, typename Inflow, typename Fraction>
+std::tuple<PartitionedArray<F>, PartitionedArray<F>> accu_fraction(const PartitionedArray<std::uint8_t>& fd,
+                                                                   const Inflow& inflow, const Fraction& fraction,
+                                                                   cudaStream_t stream = nullptr)
+{
+    auto a = detail::arg<F>(fd, inflow);
+    auto b = detail::arg<F>(fd, fraction);
+    PartitionedArray<F> flux(fd.shape(), fd.partition_shape()), state(fd.shape(), fd.partition_shape());
+    check(detail::fraction_call<F>(fd.topology(stream).handle(), a.ptr, a.value, b.ptr, b.value, flux.data(),
+                                   state.data(), stream),
+          "accu_fraction");
+    return {std::move(flux), std::move(state)};
+}
+
+// kinematic_wave(flow_direction, current_outflow, inflow, alpha, beta, time_step_duration, channel_length):
+// one time step, double precision (the reference's double instantiation).
+template <typename Alpha, typename Beta, typename ChannelLength>
+PartitionedArray<double> kinematic_wave(const PartitionedArray<std::uint8_t>& fd,
+                                        const PartitionedArray<double>& current_outflow,
+                                        const PartitionedArray<double>& inflow, const Alpha& alpha, const Beta& beta,
+                                        Scalar<double> time_step_duration, const ChannelLength& channel_length,
+                                        cudaStream_t stream = nullptr)
+{
+    auto q = detail::arg<double>(fd, current_outflow);
+    auto l = detail::arg<double>(fd, inflow);
+    auto a = detail::arg<double>(fd, alpha);
+    auto b = detail::arg<double>(fd, beta);
+    auto d = detail::arg<double>(fd, channel_length);
+    PartitionedArray<double> out(fd.shape(), fd.partition_shape());
+    check(lue_gpu_kinematic_wave_f64(fd.topology(stream).handle(), q.ptr, q.value, l.ptr, l.value, a.ptr, a.value,
+                                     b.ptr, b.value, time_step_duration.value, d.ptr, d.value, out.data(), stream),
+          "kinematic_wave");
+    return out;
+}
+
+}  // namespace value_policies
+
+}  // namespace lue_gb300

@@ -103,5 +103,6 @@ extern "C" int lue_gpu_accu_f32_noalloc(const uint8_t* flow_direction, int64_t r
     k_cycle_cells<float><<<grid_for(n, 256), 256, 0, stream>>>(flow_direction, upmask,
                                                                reinterpret_cast<const uint32_t*>(work), n, cols,
                                                                outflow, nullptr, lo);
+    count_launches(3);
     return cuda_status(cudaGetLastError(), "accu_f32_noalloc");
 }

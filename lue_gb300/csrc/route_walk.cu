@@ -30,6 +30,7 @@ static int run(lue_gpu_topology* t, Visitor v, T* out, T* rem, bool use_lo, cuda
     if (rc) return rc;
     WalkGrid g{core->fd, core->count, t->work_count, core->rows, core->cols, n};
     k_walk<<<grid_all(n, 256), 256, 0, stream>>>(g, v);
+    count_launches(core->stats.cycle_cells > 0 ? 2 : 1);
     if (core->stats.cycle_cells > 0) {
         k_cycle_cells<T><<<grid_for(n, 256), 256, 0, stream>>>(core->fd, core->upmask, t->work_count, n, core->cols,
                                                                out, rem, use_lo ? t->lo : nullptr);
@@ -63,14 +64,57 @@ static int route_f64(lue_gpu_topology* t, const double* a, double as, const doub
     return run(t, v, out, rem, false, (cudaStream_t)stream, what);
 }
 
+__global__ void k_copy_words_if(const uint32_t* src, uint32_t* dst, int64_t nwords, const unsigned long long* flag)
+{
+    if (flag[1] == 0) return;
+    for (int64_t i = grid_stride_begin(); i < nwords; i += grid_stride()) dst[i] = src[i];
+}
+
+// Scalar beta as a small rational p/m (beta = 0.6 is 3/5) for the fast kinematic-wave solve;
+// LUE_GB300_KW_SOLVE=reference keeps the reference-faithful float64 solve.
+static BetaRational rational_beta(const double* beta_raster, double beta)
+{
+    const char* e = getenv("LUE_GB300_KW_SOLVE");
+    if (beta_raster || (e && e[0] == 'r') || !(beta > 0.0)) return BetaRational{0, 0, (float)beta};
+    for (int m = 1; m <= 16; ++m) {
+        double p = nearbyint(beta * m);
+        if (p >= 1.0 && p <= 64.0 && fabs(beta - p / m) <= 1e-15 * beta) return BetaRational{(int)p, m, (float)beta};
+    }
+    return BetaRational{0, 0, (float)beta};
+}
+
+static bool walk_engine_forced()
+{
+    const char* e = getenv("LUE_GB300_ENGINE");
+    return e && e[0] == 'w';
+}
+
 }  // namespace lue_gb300
 
 using namespace lue_gb300;
 
+// accu (float32): the tile engine when the topology has one (acyclic rasters), else the walk engine.
+// LUE_GB300_ENGINE=walk forces the walk engine (for comparisons).
 extern "C" int lue_gpu_accu_f32(lue_gpu_topology* t, const float* inflow, float inflow_scalar, float* outflow,
-                                void* stream)
+                                void* stream_)
 {
-    return route_f32<Rule::accu>(t, inflow, inflow_scalar, nullptr, 0.0f, outflow, nullptr, stream, "accu_f32");
+    if (int rc = check_topology(t, "accu_f32")) return rc;
+    if (!outflow) return fail(LUE_GPU_EINVAL, "accu_f32: NULL output");
+    const TopologyCore* core = t->core;
+    if (!core->tiles || walk_engine_forced())
+        return route_f32<Rule::accu>(t, inflow, inflow_scalar, nullptr, 0.0f, outflow, nullptr, stream_, "accu_f32");
+    cudaStream_t stream = (cudaStream_t)stream_;
+    if (int rc = tile_accu_f32(core, &t->tile_scratch, inflow, inflow_scalar, outflow, stream)) return rc;
+    // +inf material or a total beyond the fixed-point range: the walk engine redoes the call
+    const int64_t n = core->n;
+    const unsigned long long* flag = t->tile_scratch.total;
+    k_copy_words_if<<<grid_for(words_for(n), 256), 256, 0, stream>>>(reinterpret_cast<const uint32_t*>(core->count),
+                                                                     t->work_count, words_for(n), flag);
+    WalkGrid g{core->fd, core->count, t->work_count, core->rows, core->cols, n};
+    RouteF32<Rule::accu> v{core->upmask, inflow, inflow_scalar, nullptr, 0.0f, outflow, nullptr, t->lo, core->cols};
+    k_walk_if<<<grid_for(n, 256), 256, 0, stream>>>(g, v, flag);
+    count_launches(2);
+    return cuda_status(cudaGetLastError(), "accu_f32");
 }
 
 extern "C" int lue_gpu_accu_f64(lue_gpu_topology* t, const double* inflow, double inflow_scalar, double* outflow,
@@ -122,7 +166,7 @@ extern "C" int lue_gpu_kinematic_wave_f64(lue_gpu_topology* t, const double* cur
     if (!outflow) return fail(LUE_GPU_EINVAL, "kinematic_wave_f64: NULL output");
     RouteKW<double> v{t->core->upmask, current_outflow, current_outflow_scalar, inflow, inflow_scalar, alpha,
                       alpha_scalar, beta, beta_scalar, time_step_duration, channel_length, channel_length_scalar,
-                      outflow, t->core->cols};
+                      outflow, t->core->cols, rational_beta(beta, beta_scalar)};
     return run(t, v, outflow, (double*)nullptr, false, (cudaStream_t)stream, "kinematic_wave_f64");
 }
 
@@ -136,6 +180,6 @@ extern "C" int lue_gpu_kinematic_wave_f64_f32in(lue_gpu_topology* t, const doubl
     if (!outflow) return fail(LUE_GPU_EINVAL, "kinematic_wave_f64_f32in: NULL output");
     RouteKW<float> v{t->core->upmask, current_outflow, current_outflow_scalar, inflow, inflow_scalar, alpha,
                      alpha_scalar, nullptr, beta, time_step_duration, nullptr, channel_length, outflow,
-                     t->core->cols};
+                     t->core->cols, rational_beta(nullptr, beta)};
     return run(t, v, outflow, (double*)nullptr, false, (cudaStream_t)stream, "kinematic_wave_f64_f32in");
 }

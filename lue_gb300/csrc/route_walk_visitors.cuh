@@ -5,7 +5,7 @@
 
 #include <cfloat>
 
-#include "kinematic_wave.cuh"
+#include "kinematic_wave_fast.cuh"
 #include "walk.cuh"
 
 namespace lue_gb300 {
@@ -190,6 +190,7 @@ struct RouteKW {
     double dx_s;
     double* out;
     int64_t cols;
+    BetaRational br;  // scalar beta as p/m: the fast solve; m == 0: the reference-faithful solve
 
     __device__ void no_data(int64_t c) { out[c] = qnan<double>(); }
 
@@ -215,7 +216,8 @@ struct RouteKW {
             out[c] = qnan<double>();
             return;
         }
-        out[c] = iterate_to_new_discharge(up, qc, q, al, be, dt, len);
+        out[c] = br.m ? iterate_to_new_discharge_fast(up, qc, q, al, be, br, dt, len)
+                      : iterate_to_new_discharge(up, qc, q, al, be, dt, len);
     }
 };
 

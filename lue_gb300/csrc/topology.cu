@@ -17,6 +17,9 @@
 namespace lue_gb300 {
 
 thread_local std::string g_last_error;
+static std::atomic<unsigned long long> g_launches{0};
+
+void count_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
 
 void set_error(const std::string& msg) { g_last_error = msg; }
 
@@ -136,6 +139,11 @@ int allocate_scratch(lue_gpu_topology* t)
         return rc;
     }
     t->scratch_bytes = words_for(n) * 4 + n * (int64_t)sizeof(float);
+    if (t->core->tiles) {
+        rc = tile_scratch_alloc(t->core->tiles, &t->tile_scratch);
+        if (rc) return rc;
+        t->scratch_bytes += t->tile_scratch.bytes;
+    }
     return LUE_GPU_OK;
 }
 
@@ -146,6 +154,7 @@ static void free_core(TopologyCore* core)
     cudaFree(core->count);
     cudaFree(core->upmask);
     cudaFree(core->level);
+    tile_core_free(core->tiles);
     delete core;
 }
 
@@ -154,6 +163,7 @@ static void free_handle(lue_gpu_topology* t)
     if (!t) return;
     cudaFree(t->work_count);
     cudaFree(t->lo);
+    tile_scratch_free(&t->tile_scratch);
     if (t->core && --t->core->refs == 0) free_core(t->core);
     delete t;
 }
@@ -163,6 +173,8 @@ static void free_handle(lue_gpu_topology* t)
 using namespace lue_gb300;
 
 extern "C" int lue_gpu_abi_version(void) { return LUE_GPU_ABI_VERSION; }
+
+extern "C" unsigned long long lue_gpu_kernel_launches(void) { return g_launches.load(); }
 
 extern "C" const char* lue_gpu_last_error(void) { return g_last_error.c_str(); }
 
@@ -203,7 +215,7 @@ extern "C" int lue_gpu_topology_create(const uint8_t* flow_direction, int64_t ro
     if ((rc = cuda_status(cudaMalloc(&core->upmask, padded), "topology upmask"))) goto error;
     if ((rc = cuda_status(cudaMalloc(&core->level, n * sizeof(int32_t)), "topology level"))) goto error;
     core->bytes = 3 * padded + n * (int64_t)sizeof(int32_t);
-    if ((rc = allocate_scratch(t))) goto error;
+    if ((rc = cuda_status(cudaMalloc(&t->work_count, padded), "scratch counters"))) goto error;
     if ((rc = cuda_status(cudaMalloc(&dstats, sizeof hstats), "topology stats"))) goto error;
     if ((rc = cuda_status(cudaMemsetAsync(core->fd, kNoData, padded, stream), "memset"))) goto error;
     if ((rc = cuda_status(cudaMemcpyAsync(core->fd, flow_direction, n, cudaMemcpyDeviceToDevice, stream),
@@ -239,6 +251,20 @@ extern "C" int lue_gpu_topology_create(const uint8_t* flow_direction, int64_t ro
     core->stats.sink_cells = (int64_t)hstats[3];
     core->stats.cycle_cells = (int64_t)hstats[4];
     core->stats.max_level = (int64_t)hstats[5];
+    // the tile engine needs an acyclic network and 32-bit cell indices
+    if (core->stats.cycle_cells == 0 && n < (int64_t(1) << 32)) {
+        rc = tile_core_build(core, stream);
+        if (rc == LUE_GPU_ECUDA || rc == LUE_GPU_ENOMEM) goto error;
+        rc = LUE_GPU_OK;
+    }
+    if (core->tiles) {
+        core->stats.tile_exits = core->tiles->nexit;
+        core->stats.exit_forest_depth = core->tiles->max_depth;
+        core->bytes += core->tiles->bytes;
+    }
+    cudaFree(t->work_count);
+    t->work_count = nullptr;
+    if ((rc = allocate_scratch(t))) goto error;
     *out = t;
     return LUE_GPU_OK;
 error:

@@ -4,6 +4,7 @@
 #include <atomic>
 
 #include "common.cuh"
+#include "tile_accu.cuh"
 
 namespace lue_gb300 {
 
@@ -14,6 +15,7 @@ struct TopologyCore {
     uint8_t* count = nullptr;   // inflow count, 255 where the flow direction is no-data
     uint8_t* upmask = nullptr;  // bit k set: neighbour k (NW, N, NE, W, E, SW, S, SE) drains here
     int32_t* level = nullptr;   // downstream level, -1 for no-data and cycle cells
+    TileCore* tiles = nullptr;  // tiled accu engine (acyclic rasters), else nullptr
     lue_gpu_topology_stats stats{};
     int64_t bytes = 0;
     std::atomic<int> refs{1};
@@ -25,12 +27,17 @@ struct lue_gpu_topology {
     lue_gb300::TopologyCore* core = nullptr;
     uint32_t* work_count = nullptr;  // per-call copy of the counts, 4 cells per word
     float* lo = nullptr;             // per-call float-float residuals of f32 routing
+    lue_gb300::TileScratch tile_scratch;
     int64_t scratch_bytes = 0;
 };
 
 namespace lue_gb300 {
 
 int allocate_scratch(lue_gpu_topology* t);
+
+// accu (float32) on the tile engine; see tile_accu.cuh.
+int tile_accu_f32(const TopologyCore* core, TileScratch* s, const float* ext, float ext_s, float* out,
+                  cudaStream_t stream);
 
 // Launch of the walk engine: one thread per cell; cells without inflow start a downstream walk that
 // continues through a cell once all its upstream neighbours are done (definition/accumulating_router.hpp:

@@ -56,4 +56,22 @@ __global__ void __launch_bounds__(256) k_walk(WalkGrid g, Visitor v)
     }
 }
 
+// The same walk, run only when flag[1] is set (a fallback behind an engine that found inputs it does
+// not handle); grid-stride, so it needs no launch of one thread per cell.
+template <class Visitor>
+__global__ void __launch_bounds__(256) k_walk_if(WalkGrid g, Visitor v, const unsigned long long* flag)
+{
+    if (flag[1] == 0) return;
+    for (int64_t c = grid_stride_begin(); c < g.n; c += grid_stride()) {
+        uint8_t code = __ldg(g.fd + c);
+        if (code == kNoData) {
+            v.no_data(c);
+        } else if (__ldg(g.count + c) == 0) {
+            walk_from(g, v, c);
+        }
+    }
+}
+
+__global__ void k_copy_words_if(const uint32_t* src, uint32_t* dst, int64_t nwords, const unsigned long long* flag);
+
 }  // namespace lue_gb300

@@ -159,6 +159,18 @@ def _empty(flow_direction, dtype):
     return torch.empty(flow_direction.shape, dtype=dtype, device=flow_direction.data.device)
 
 
+def d8_flow_direction(elevation):
+    """value_policies::d8_flow_direction (uint8 D8 codes) from a float32 or float64 elevation array."""
+    if elevation.dtype not in (torch.float32, torch.float64):
+        raise TypeError("elevation must be float32 or float64")
+    out = _empty(elevation, torch.uint8)
+    L = _lib.lib()
+    fn = L.lue_gpu_d8_flow_direction_f32 if elevation.dtype == torch.float32 else L.lue_gpu_d8_flow_direction_f64
+    _lib.check(fn(elevation.data.data_ptr(), elevation.shape[0], elevation.shape[1], out.data_ptr(),
+                  _stream(elevation.data)))
+    return PartitionedArray(out, elevation.partition_shape)
+
+
 def inflow_count(flow_direction, value_policies=True):
     t = flow_direction.topology()
     out = _empty(flow_direction, torch.uint8)

@@ -132,6 +132,7 @@ def rain_blobs(rows, cols, rng, n_blobs=24, max_mm_per_h=20.0):
 WORKLOADS = {
     "accu_1k": dict(rows=1024, cols=1024, partition=(256, 256), amplitude=50.0, seed=1),
     "accu_16k": dict(rows=16384, cols=16384, partition=(2048, 2048), amplitude=200.0, seed=2),
+    "accu_8k": dict(rows=8192, cols=8192, partition=(1024, 1024), amplitude=200.0, seed=4),
     "kw_8k": dict(rows=8192, cols=8192, partition=(1024, 1024), amplitude=200.0, seed=3),
 }
 

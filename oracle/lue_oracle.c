@@ -384,3 +384,31 @@ int lue_oracle_downstream_level(const uint8_t* fd, int64_t rows, int64_t cols, i
     free(queue);
     return 0;
 }
+
+/*
+ * value_policies::d8_flow_direction (ALG/definition/d8_flow_direction.hpp:45-147,
+ * ALG/value_policies/d8_flow_direction.hpp:20-45): steepest unweighted drop, candidates N, W, E, S,
+ * NW, NE, SW, SE with strict '>', sink (5) without a positive drop, 255 for a NaN elevation, NaN
+ * neighbours skipped, DBL_MIN (std::numeric_limits<double>::min()) outside the array.
+ */
+int lue_oracle_d8_flow_direction(const double* z, int64_t rows, int64_t cols, uint8_t* fd)
+{
+    static const int dr[8] = {-1, 0, 0, 1, -1, -1, 1, 1};
+    static const int dc[8] = {0, -1, 1, 0, -1, 1, -1, 1};
+    static const uint8_t code[8] = {8, 4, 6, 2, 7, 9, 1, 3};
+    for (int64_t r = 0; r < rows; ++r)
+        for (int64_t c = 0; c < cols; ++c) {
+            double zc = z[r * cols + c];
+            if (isnan(zc)) { fd[r * cols + c] = U8_NO_DATA; continue; }
+            uint8_t dir = 5;
+            double drop = 0.0;
+            for (int k = 0; k < 8; ++k) {
+                int64_t rn = r + dr[k], cn = c + dc[k];
+                double zn = (rn < 0 || rn >= rows || cn < 0 || cn >= cols) ? DBL_MIN : z[rn * cols + cn];
+                if (isnan(zn)) continue;
+                if (zc - zn > drop) { drop = zc - zn; dir = code[k]; }
+            }
+            fd[r * cols + c] = dir;
+        }
+    return 0;
+}

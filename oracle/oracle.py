@@ -49,6 +49,7 @@ def lib():
             f.argtypes = [p, i64, i64, i64, i64, p, real, p, real, p, real, p, real, real, p, real, p, i32]
         L.lue_oracle_inflow_count.argtypes = [p, i64, i64, i64, i64, i32, p]
         L.lue_oracle_downstream_level.argtypes = [p, i64, i64, p]
+        L.lue_oracle_d8_flow_direction.argtypes = [p, i64, i64, p]
         d = ctypes.c_double
         L.lue_oracle_iterate_to_new_discharge_f64.argtypes = [d] * 7
         L.lue_oracle_iterate_to_new_discharge_f64.restype = d
@@ -96,6 +97,14 @@ def inflow_count(fd, partition_shape=None, value_policies=True):
     out = np.empty(fd.shape, np.uint8)
     _check(lib().lue_oracle_inflow_count(fd.ctypes.data, fd.shape[0], fd.shape[1], pr, pc,
                                          int(value_policies), out.ctypes.data))
+    return out
+
+
+def d8_flow_direction(elevation):
+    """Reference D8 rule on a float64 elevation raster (float32 input is promoted exactly)."""
+    z = np.ascontiguousarray(elevation, dtype=np.float64)
+    out = np.empty(z.shape, np.uint8)
+    _check(lib().lue_oracle_d8_flow_direction(z.ctypes.data, z.shape[0], z.shape[1], out.ctypes.data))
     return out
 
 

@@ -16,6 +16,7 @@ Sources read (paths within the reference project):
 - source/framework/algorithm/test/accu_fraction_test.cpp
 - source/framework/algorithm/test/kinematic_wave_test.cpp
 - source/framework/algorithm/test/inflow_count_test.cpp
+- source/framework/algorithm/test/d8_flow_direction_test.cpp
 
 Each ``create_partitioned_array(shape, partition_shape, {{partition}, ...})`` literal lists its
 partitions in row-major partition order, each partition's cells row-major.  Partition extents follow
@@ -427,6 +428,34 @@ def emit_cases(rel, name, line, env, calls, cases):
                           "compare": "all_positive" if positive and not expected else how})
 
 
+def extract_d8(path, rel, fixtures, cases):
+    """d8_flow_direction_test.cpp: pairs of (elevation, flow_direction_we_want) literals, in source
+    order, for every case that checks them (barnes_2017 only warns, so it pins nothing)."""
+    text = strip_comments(open(path).read())
+    for name, line, body in test_cases(text):
+        if "check_arrays_are_equal" not in body:
+            continue
+        env = Env(base_env())
+        # aliases and shapes declared at the top of the case
+        process_statements([st for st in split_statements(body) if "create_partitioned_array" not in st
+                            and "d8_flow_direction<" not in st and not st.lstrip().startswith("{")],
+                           env, fixtures, lambda st, e: None)
+        env.values.setdefault("y", D8["p"])
+        env.values["x"] = math.nan
+        env.values["u"] = U8_NO_DATA
+        arrays = []
+        for m in re.finditer(r"(elevation|flow_direction_we_want)\s*=\s*lue::test::create_partitioned_array", body):
+            start = m.start(0) + body[m.start(0):].index("lue::test::")
+            close = matching(body, body.index("(", body.index(">", start)), "(", ")")
+            arrays.append((m.group(1), eval_array(body[start:close + 1], env, fixtures)))
+        for (k1, elev), (k2, want) in zip(arrays[0::2], arrays[1::2]):
+            assert k1 == "elevation" and k2 == "flow_direction_we_want"
+            cases.append({"file": rel, "line": line, "name": name, "op": "d8_flow_direction",
+                          "partition_shape": elev["partition_shape"], "elevation": arr(elev),
+                          "expected": {"flow_direction": [[int(v) for v in row] for row in want["data"]]},
+                          "compare": "equal"})
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("LUE_REFERENCE", "/root/reference"))
@@ -438,6 +467,8 @@ def main():
     for f in ("accu_test.cpp", "accu_threshold_test.cpp", "accu_fraction_test.cpp",
               "kinematic_wave_test.cpp", "inflow_count_test.cpp"):
         extract_file(os.path.join(tdir, f), f"{TEST_DIR}/{f}", fixtures, cases)
+    extract_d8(os.path.join(tdir, "d8_flow_direction_test.cpp"), f"{TEST_DIR}/d8_flow_direction_test.cpp",
+               fixtures, cases)
     with open(a.out, "w") as fh:
         json.dump({"generated_by": "tests/golden/extract_reference_cases.py",
                    "source": "computationalgeography/lue " + TEST_DIR, "cases": cases}, fh, indent=None)

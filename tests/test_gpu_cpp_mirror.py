@@ -1,0 +1,27 @@
+"""The C++ mirror of lue::value_policies (lue_gb300/csrc/lue_gb300.hpp) on two of the reference's
+known-answer cases, through a compiled example program (lue_gb300/examples/accu_example.cpp)."""
+import subprocess
+
+import numpy as np
+import pytest
+
+from tests.golden import cases as golden
+
+pytestmark = pytest.mark.gpu
+
+
+def test_cpp_mirror_known_answers():
+    from lue_gb300 import _build
+    exe = _build.cpp_example()
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = r.stdout.strip().splitlines()
+    accu = np.array([float(v) for v in lines[0].split()], np.float32).reshape(6, 5)
+    want = [c for c in golden.load("accu") if c["name"] == "back_and_forth"][0]["expected"]["outflow_we_got"]
+    assert np.array_equal(accu, golden.f32(want))
+    case = [c for c in golden.load("accu_threshold") if c["name"] == "pcraster_manual_example1"][0]
+    flux = np.array([float(v) for v in lines[1].split()], np.float32).reshape(5, 5)
+    state = np.array([float(v) for v in lines[2].split()], np.float32).reshape(5, 5)
+    assert np.array_equal(flux, golden.f32(case["expected"]["outflow_we_got"]))
+    assert np.array_equal(state, golden.f32(case["expected"]["residue_we_got"]))
+    assert lines[3] == "shape mismatch rejected"

@@ -90,3 +90,14 @@ def test_scalar_kw_cases_through_a_one_cell_raster(lfr):
                                               a["beta"], a["time_step_duration"], a["channel_length"]))[0, 0]
         if a["upstream_discharge"] == 0:
             assert boost_close(got, c["expected"])
+
+
+D8_CASES = golden.load("d8_flow_direction")
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+@pytest.mark.parametrize("case", D8_CASES, ids=[f"{golden.case_id(c)}#{i}" for i, c in enumerate(D8_CASES)])
+def test_d8_flow_direction_case(lfr, case, dtype):
+    z = golden.arg({"raster": case["elevation"]}, dtype)
+    got = lfr.to_numpy(lfr.d8_flow_direction(lfr.from_numpy(z)))
+    assert (got == np.array(case["expected"]["flow_direction"], np.uint8)).all(), got

@@ -203,3 +203,85 @@ def test_repeated_calls_are_identical(lfr, c1):
     r1 = lfr.to_numpy(lfr.accu(a, md))
     r2 = lfr.to_numpy(lfr.accu(a, md))
     assert np.array_equal(r1, r2)  # the pull order is fixed: bitwise reproducible
+
+
+def _accu_with_engine(lfr, a, m, engine):
+    import os
+    old = os.environ.get("LUE_GB300_ENGINE")
+    os.environ["LUE_GB300_ENGINE"] = engine
+    try:
+        return lfr.to_numpy(lfr.accu(a, m))
+    finally:
+        if old is None:
+            del os.environ["LUE_GB300_ENGINE"]
+        else:
+            os.environ["LUE_GB300_ENGINE"] = old
+
+
+def test_tile_engine_against_walk_engine_and_oracle(lfr, c1):
+    fd, m, ps = c1["flow_direction"], c1["material"], c1["partition"]
+    a = lfr.from_numpy(fd, ps)
+    s = a.topology().stats()
+    assert s["tile_exits"] > 0 and s["exit_forest_depth"] > 1  # the tile engine is on
+    md = lfr.from_numpy(m, ps)
+    tiles = _accu_with_engine(lfr, a, md, "tiles")
+    walk = _accu_with_engine(lfr, a, md, "walk")
+    want = oracle.accu(fd, m.astype(np.float64), ps, dtype=np.float64)
+    parity.assert_close32(tiles, want, "accu tiles")
+    parity.assert_close32(walk, want, "accu walk")
+    parity.assert_close32(tiles, walk, "tiles vs walk")
+
+
+def test_tile_engine_ragged_with_no_data(lfr):
+    fd, m, rng = ragged(777, 1001, 13)
+    m = m.copy()
+    m[rng.random(fd.shape) < 0.001] = np.nan
+    m[rng.random(fd.shape) < 0.001] = -2.0
+    fd = fd.copy()
+    fd[rng.random(fd.shape) < 0.0005] = 255
+    a = lfr.from_numpy(fd, (256, 300))
+    assert a.topology().stats()["tile_exits"] > 0
+    got = lfr.to_numpy(lfr.accu(a, lfr.from_numpy(m, (256, 300))))
+    want = oracle.accu(fd, m.astype(np.float64), (256, 300), dtype=np.float64)
+    parity.assert_close32(got, want, "accu tiles ragged with no-data")
+    r2 = lfr.to_numpy(lfr.accu(a, lfr.from_numpy(m, (256, 300))))
+    assert np.array_equal(got, r2, equal_nan=True)  # exact integer coarse sums: bitwise reproducible
+
+
+def test_tile_engine_hands_infinite_material_to_the_walk_engine(lfr, c1):
+    fd, m, ps = c1["flow_direction"], c1["material"].copy(), c1["partition"]
+    m[100, 100] = np.inf
+    m[900, 17] = np.inf
+    got = lfr.to_numpy(lfr.accu(lfr.from_numpy(fd, ps), lfr.from_numpy(m, ps)))
+    want = oracle.accu(fd, m.astype(np.float64), ps, dtype=np.float64)
+    assert np.array_equal(np.isinf(got), np.isinf(want))
+    finite = np.isfinite(want)
+    parity.assert_close32(got[finite], want[finite], "accu with +inf material")
+
+
+def test_kinematic_wave_fast_solve_matches_reference_solve(lfr):
+    """The float32-Newton + float64-polish solve against the reference-faithful float64 solve."""
+    import os
+    d = kw_inputs(300, 400, 21)
+    fd = d["flow_direction"]
+    a = lfr.from_numpy(fd)
+    args = (lfr.from_numpy(d["discharge"]), lfr.from_numpy(d["lateral_inflow"]), lfr.from_numpy(d["alpha"]),
+            0.6, 3600.0, 100.0)
+    fast = lfr.to_numpy(lfr.kinematic_wave(a, *args))
+    os.environ["LUE_GB300_KW_SOLVE"] = "reference"
+    try:
+        ref = lfr.to_numpy(lfr.kinematic_wave(a, *args))
+    finally:
+        del os.environ["LUE_GB300_KW_SOLVE"]
+    mx, _ = parity.rel_error(fast, ref, parity.FLOOR64)
+    assert mx <= 1e-11, mx
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+def test_d8_flow_direction_against_oracle(lfr, dtype):
+    """A raw fBm DEM (pits kept, so interior sinks appear) with NaN holes, at a ragged size."""
+    z = synthetic.dem(517, 1031, seed=8, amplitude=40.0, wavelength=200).astype(dtype)
+    rng = np.random.default_rng(8)
+    z[rng.random(z.shape) < 0.002] = np.nan
+    got = lfr.to_numpy(lfr.d8_flow_direction(lfr.from_numpy(z)))
+    assert np.array_equal(got, oracle.d8_flow_direction(z.astype(np.float64) if dtype == np.float64 else z))

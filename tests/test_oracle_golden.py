@@ -119,3 +119,13 @@ def test_threaded_oracle_matches_single_threaded():
     a = oracle.accu(fd, ext, (3, 3), nthreads=1)
     b = oracle.accu(fd, ext, (3, 3), nthreads=4)
     np.testing.assert_allclose(a, b, rtol=1e-6, equal_nan=True)
+
+
+D8_CASES = golden.load("d8_flow_direction")
+
+
+@pytest.mark.parametrize("case", D8_CASES, ids=[f"{golden.case_id(c)}#{i}" for i, c in enumerate(D8_CASES)])
+def test_d8_flow_direction_case(case):
+    z = golden.arg({"raster": case["elevation"]}, np.float32)
+    got = oracle.d8_flow_direction(z)
+    assert (got == np.array(case["expected"]["flow_direction"], np.uint8)).all(), got
