@@ -303,6 +303,10 @@ def bench_ours(args, world, rank, local):
     extra = {}
     if args.kinematic_wave_steps > 0 and rank == 0:
         extra["kinematic_wave"] = bench_kinematic_wave(args, dev)
+    if not args.no_ensemble and rank == 0:
+        extra["ensemble"] = bench_ensemble(args, dev)
+    if args.serve_seconds > 0 and rank == 0:
+        extra["serving"] = bench_serving(args, dev)
 
     if rank != 0:
         return
@@ -343,6 +347,8 @@ def bench_ours(args, world, rank, local):
 
 
 def bench_kinematic_wave(args, dev):
+    """C3: kinematic_wave over the 8192 x 8192 workload, `steps` time steps in one call (time-skewed
+    level waves), next to single-step calls."""
     import torch
 
     from lue_gb300 import framework as lfr
@@ -356,21 +362,88 @@ def bench_kinematic_wave(args, dev):
     lat = lfr.from_numpy(d["lateral_inflow"], ps, device=dev)
     alpha = lfr.from_numpy(d["alpha"], ps, device=dev)
     fd.topology()
-    q = lfr.kinematic_wave(fd, q, lat, alpha, 0.6, 3600.0, 100.0)
-    torch.cuda.synchronize()
+    n = w["rows"] * w["cols"]
     stream = torch.cuda.current_stream(dev)
+    T = args.kinematic_wave_steps
+    lfr.kinematic_wave_steps(fd, q, lat, alpha, 0.6, 3600.0, 100.0, T)  # builds level order + history
+    torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.kinematic_wave_steps):
-        q = lfr.kinematic_wave(fd, q, lat, alpha, 0.6, 3600.0, 100.0)
+    out = lfr.kinematic_wave_steps(fd, q, lat, alpha, 0.6, 3600.0, 100.0, T)
     e1.record(stream)
     torch.cuda.synchronize()
-    s = e0.elapsed_time(e1) / 1000.0
-    n = w["rows"] * w["cols"]
-    return {"workload": "kw_8k", "steps": args.kinematic_wave_steps, "ms_per_step": round(1000 * s / args.kinematic_wave_steps, 3),
-            "value": round(n * args.kinematic_wave_steps / s / 1e6, 3), "unit": "Mcells/s",
-            "roofline_frac": round(KW_BYTES_PER_CELL * n * args.kinematic_wave_steps / s / 1e9 / peaks()[0], 4),
-            "longest_flow_path_cells": fd.topology().stats()["max_level"] + 1}
+    s_multi = e0.elapsed_time(e1) / 1000.0
+    single_steps = 3
+    qq = q
+    e0.record(stream)
+    for _ in range(single_steps):
+        qq = lfr.kinematic_wave(fd, qq, lat, alpha, 0.6, 3600.0, 100.0)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    s_single = e0.elapsed_time(e1) / 1000.0 / single_steps
+    finite = torch.isfinite(out.data)
+    return {"workload": "kw_8k (8192x8192, float64 discharge, float32 rain and alpha, beta 0.6, dt 3600 s, dx 100 m)",
+            "steps": T, "ms_per_step": round(1000 * s_multi / T, 3),
+            "value": round(n * T / s_multi / 1e6, 3), "unit": "Mcells/s",
+            "roofline_frac_hbm": round(KW_BYTES_PER_CELL * n * T / s_multi / 1e9 / peaks()[0], 4),
+            "single_step_call_ms": round(1000 * s_single, 3),
+            "single_step_call_mcells_per_s": round(n / s_single / 1e6, 3),
+            "engine": "time-skewed level waves (lue_gpu_kinematic_wave_steps_f64_f32in)",
+            "longest_flow_path_cells": fd.topology().stats()["max_level"] + 1,
+            "outflow_finite_cells": int(finite.sum())}
+
+
+def bench_ensemble(args, dev):
+    """C4: 256 kinematic-wave instances (64 catchments x 4 rain scenarios), 48 steps, batched in one
+    atlas (one launch per step in a CUDA graph, or all steps as level waves) against one launch per
+    instance and step (timed on a sample of instances)."""
+    from lue_gb300 import ensemble
+    inst = ensemble.ensemble_inputs(n_catchments=64, scenarios=4, lo=512, hi=4096, seed=11)
+    cells = sum(i["flow_direction"].size for i in inst)
+    steps = 48
+    s_graph, atlas, _, stats = ensemble.run_batched(inst, steps, device=dev, graph=True)
+    s_waves, _, _, _ = ensemble.run_batched(inst, steps, device=dev, waves=True)
+    sample = 8
+    s_alone, cells_alone, _ = ensemble.run_unbatched(inst, steps, sample, device=dev)
+    return {"workload": "64 catchments (sides log-uniform 512-4096, depression-filled D8) x 4 rain scenarios, "
+                        "48 kinematic-wave steps", "instances": len(inst), "cells_per_step": cells,
+            "atlas_shape": list(atlas.shape), "longest_flow_path_cells": stats["max_level"] + 1,
+            "batched_graph_mcells_per_s": round(cells * steps / s_graph / 1e6, 3),
+            "batched_graph_s": round(s_graph, 3),
+            "batched_waves_mcells_per_s": round(cells * steps / s_waves / 1e6, 3),
+            "batched_waves_s": round(s_waves, 3),
+            "one_launch_per_instance_mcells_per_s": round(cells_alone * steps / s_alone / 1e6, 3),
+            "one_launch_per_instance_sample": f"first {sample} instances, topology built per instance"}
+
+
+def bench_serving(args, dev):
+    """C5: Poisson stream (200 req/s) of accu and 24-step kinematic_wave requests over a pool of 128
+    resident D8 grids (sides log-uniform 256-8192); p50/p99 latency, and the same requests served one at a
+    time through the plain drop-in path (topology per call) for comparison."""
+    import copy
+
+    from lue_gb300 import serving
+    shapes = serving.pool_shapes(n=128, lo=256, hi=8192, seed=21)
+    pool = serving.build_pool(shapes, seed=21)
+    server = serving.Server(pool, slots=16, device=dev)
+    reqs = serving.make_requests(shapes, rate=200.0, duration=args.serve_seconds, kw_steps=24, seed=5)
+    # warm-up: one request per kind on the smallest grid (clones, history planes)
+    server.run(copy.deepcopy(reqs[:4]), realtime=False, keep_results=False)
+    served = server.run(copy.deepcopy(reqs), realtime=True, keep_results=False)
+    k = min(len(reqs), args.serve_sequential)
+    sub = copy.deepcopy(reqs[:k])
+    for r in sub:
+        r.arrival = 0.0
+    seq = serving.run_sequential_plain(server, sub, keep_results=False)
+    sub2 = copy.deepcopy(reqs[:k])
+    for r in sub2:
+        r.arrival = 0.0
+    batched_sub = server.run(sub2, realtime=False, keep_results=False)
+    return {"workload": "Poisson 200 req/s, 50 % accu (float32) / 50 % 24-step kinematic_wave (float64), "
+                        "128-grid pool, sides log-uniform 256-8192", "seconds_of_arrivals": args.serve_seconds,
+            "served": served,
+            "same_requests_closed_loop": {"first_k": k, "continuous_batching": batched_sub,
+                                          "sequential_plain_calls": seq}}
 
 
 def main():
@@ -380,7 +453,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="accu_16k")
-    ap.add_argument("--kinematic-wave-steps", type=int, default=5)
+    ap.add_argument("--kinematic-wave-steps", type=int, default=100)
+    ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=2.0)
+    ap.add_argument("--serve-sequential", type=int, default=32)
     ap.add_argument("--skip-cpu", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

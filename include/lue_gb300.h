@@ -156,6 +156,16 @@ int lue_gpu_kinematic_wave_f64_f32in(lue_gpu_topology* topology, const double* c
                                      double time_step_duration, double channel_length, double* outflow,
                                      void* stream);
 
+/* `steps` kinematic-wave time steps in one call (the discharge of each step feeds the next, lateral
+ * inflow and alpha constant), equal bit for bit to `steps` calls of lue_gpu_kinematic_wave_f64_f32in.
+ * Replaces the caller's per-step loop (the reference's lue::simulate pattern, source/framework/model/
+ * include/lue/framework/model/simulate.hpp) with time-skewed level waves: max level + steps waves
+ * instead of steps full sweeps.  Needs steps x cells x 8 bytes of scratch (kept by the topology). */
+int lue_gpu_kinematic_wave_steps_f64_f32in(lue_gpu_topology* topology, const double* current_outflow,
+                                           const float* inflow, double inflow_scalar, const float* alpha,
+                                           double alpha_scalar, double beta, double time_step_duration,
+                                           double channel_length, int steps, double* outflow, void* stream);
+
 /* accu (float32) that allocates no device memory.  No counterpart in the reference: it is for callers
  * that must not allocate on their call path (a model step inside a host framework that owns the
  * device memory pool, or a latency-critical loop in which cudaMalloc/cudaFree would synchronise the

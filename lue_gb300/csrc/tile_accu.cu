@@ -317,18 +317,24 @@ __global__ void k_halo_exits(const uint8_t* __restrict__ fd, TileGeom g, const i
 // Per call
 // ---------------------------------------------------------------------------------------------------
 
+constexpr uint16_t kNoCell = 0xFFFFu;
+
 struct __align__(16) TileSmem {
     float hi[kTileCells];
     float lo[kTileCells];
     uint32_t cnt[kTileCells / 4];  // in-tile inflow counters, 4 per word
+    uint16_t dsl[kTileCells];      // downstream cell inside the tile, or kNoCell
+    uint16_t queue[kTileCells];    // cells in the order they become ready (each cell once)
     uint8_t up[kTileCells];        // in-tile upstream mask
     uint8_t fd[kHalo][kHalo + 2];  // flow direction with a one-cell halo (255 outside the array)
+    int round_count[6];            // [0..2]: cells queued for the next rounds (a ring of three counters);
+                                   // [3..5]: head, count and round handed back by the warp phase
 };
 
-// Load the flow direction with halo; fill in-tile upstream masks and counters; returns the thread's
-// bitmask of its 16 cells that have no in-tile inflow (walk starts).
-__device__ __forceinline__ unsigned tile_prepare(TileSmem& sm, const uint8_t* __restrict__ fd, const TileGeom& g,
-                                                 int64_t tr, int64_t tc)
+// Load the flow direction with halo; fill in-tile upstream masks, counters and downstream indices, and
+// queue the cells without in-tile inflow (the first round).  Returns the number of queued cells.
+__device__ __forceinline__ int tile_prepare(TileSmem& sm, const uint8_t* __restrict__ fd, const TileGeom& g,
+                                            int64_t tr, int64_t tc)
 {
     const int t = threadIdx.x;
     for (int i = t; i < kHalo * kHalo; i += kTileThreads) {
@@ -336,15 +342,17 @@ __device__ __forceinline__ unsigned tile_prepare(TileSmem& sm, const uint8_t* __
         int64_t r = tr * kTile + hr - 1, c = tc * kTile + hc - 1;
         sm.fd[hr][hc] = (r >= 0 && r < g.rows && c >= 0 && c < g.cols) ? __ldg(fd + r * g.cols + c) : kNoData;
     }
+    if (t < 3) sm.round_count[t] = 0;
     __syncthreads();
-    unsigned starts = 0;
     uint8_t* cnt8 = reinterpret_cast<uint8_t*>(sm.cnt);
+    const int lane = t & 31;
 #pragma unroll 4
     for (int k = 0; k < kTileCells / kTileThreads; ++k) {
         int i = t + k * kTileThreads;
         int rin = i >> 6, cin = i & 63;
         uint8_t code = sm.fd[rin + 1][cin + 1];
         unsigned mask = 0;
+        uint16_t d = kNoCell;
         if (code != kNoData) {
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
@@ -352,63 +360,138 @@ __device__ __forceinline__ unsigned tile_prepare(TileSmem& sm, const uint8_t* __
                 if (rn >= 0 && rn < kTile && cn >= 0 && cn < kTile && sm.fd[rn + 1][cn + 1] == nb_inflow_code(q))
                     mask |= 1u << q;
             }
-            if (mask == 0) starts |= 1u << k;
+            int dr, dc;
+            if (d8_offset(code, dr, dc)) {
+                int r2 = rin + dr, c2 = cin + dc;
+                if (r2 >= 0 && r2 < kTile && c2 >= 0 && c2 < kTile && sm.fd[r2 + 1][c2 + 1] != kNoData)
+                    d = (uint16_t)(r2 * kTile + c2);
+            }
         }
         sm.up[i] = (uint8_t)mask;
+        sm.dsl[i] = d;
         cnt8[i] = code == kNoData ? kNoData : (uint8_t)__popc(mask);
+        // first round: valid cells without in-tile inflow (warp-aggregated queue appends)
+        bool start = code != kNoData && mask == 0;
+        unsigned ballot = __ballot_sync(0xffffffffu, start);
+        int base = 0;
+        if (lane == 0 && ballot) base = atomicAdd(&sm.round_count[0], __popc(ballot));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (start) sm.queue[base + __popc(ballot & ((1u << lane) - 1u))] = (uint16_t)i;
     }
     __syncthreads();
-    return starts;
+    return sm.round_count[0];
 }
 
-// Walk inside the tile from cell i: value(c) = source(c) + sum of in-tile upstream values, float-float.
-// Before the walk hi[] holds the per-cell source (material, or the inflow entering the tile); NaN or a
-// negative source makes the cell NaN.
-__device__ __forceinline__ void tile_walk(TileSmem& sm, int i)
+// Value of cell i: source(i) (hi/lo before the cell is done) + the sum of its in-tile upstream values,
+// float-float; NaN or a negative source makes the cell NaN.  A sum that is not finite (+inf material)
+// is recomputed plainly so that it keeps IEEE semantics.
+__device__ __forceinline__ void tile_cell(TileSmem& sm, int i)
 {
-    for (;;) {
-        float x = sm.hi[i];
-        FF t{0.0f, 0.0f};
-        bool nan = isnan(x) || !(x >= 0.0f);
-        unsigned m = sm.up[i];
-        while (m) {
-            int q = __ffs(m) - 1;
-            m &= m - 1;
-            int u = i + nb_dr(q) * kTile + nb_dc(q);
-            float h = sm.hi[u];
-            if (isnan(h)) nan = true;
-            else t.add(h, sm.lo[u]);
-        }
-        if (nan) {
-            sm.hi[i] = __int_as_float(0x7fc00000);
-            sm.lo[i] = 0.0f;
-        } else {
-            t.add(x, sm.lo[i]);
-            t.normalise();
-            sm.hi[i] = t.hi;
-            sm.lo[i] = t.lo;
-        }
-        int rin = i >> 6, cin = i & 63, dr, dc;
-        if (!d8_offset(sm.fd[rin + 1][cin + 1], dr, dc)) return;
-        int r2 = rin + dr, c2 = cin + dc;
-        if (r2 < 0 || r2 >= kTile || c2 < 0 || c2 >= kTile) return;
-        if (sm.fd[r2 + 1][c2 + 1] == kNoData) return;
-        int j = r2 * kTile + c2;
-        __threadfence_block();
-        unsigned shift = (unsigned)(j & 3) * 8u;
-        unsigned old = atomicSub(sm.cnt + (j >> 2), 1u << shift);
-        if (((old >> shift) & 0xFFu) != 1u) return;
-        __threadfence_block();
-        i = j;
+    const float x = sm.hi[i];
+    float s = x, e = sm.lo[i];
+    bool nan = isnan(x) || !(x >= 0.0f);
+    unsigned m = sm.up[i];
+    while (m) {
+        int q = __ffs(m) - 1;
+        m &= m - 1;
+        int u = i + nb_dr(q) * kTile + nb_dc(q);
+        float h = sm.hi[u], ts, te;
+        nan |= isnan(h);
+        two_sum(s, h, ts, te);
+        s = ts;
+        e = __fadd_rn(e, __fadd_rn(te, sm.lo[u]));
     }
+    float hi = __fadd_rn(s, e);
+    float lo = __fsub_rn(e, __fsub_rn(hi, s));
+    if (!isfinite(hi)) {  // +inf upstream or material: plain float sum (inf stays inf)
+        float p = x;
+        unsigned mm = sm.up[i];
+        while (mm) {
+            int q = __ffs(mm) - 1;
+            mm &= mm - 1;
+            p += sm.hi[i + nb_dr(q) * kTile + nb_dc(q)];
+        }
+        hi = p;
+        lo = 0.0f;
+    }
+    if (nan) {
+        hi = __int_as_float(0x7fc00000);
+        lo = 0.0f;
+    }
+    sm.hi[i] = hi;
+    sm.lo[i] = lo;
 }
 
-__device__ __forceinline__ void tile_walk_all(TileSmem& sm, unsigned starts)
+// Finish item k of a round (if k < count) and queue its downstream cell when this was its last
+// upstream cell.  All 32 lanes of the warp must call it (warp-aggregated queue appends).
+__device__ __forceinline__ void tile_item(TileSmem& sm, int head, int count, int k, int* next, int next_base)
 {
-    while (starts) {
-        int k = __ffs(starts) - 1;
-        starts &= starts - 1;
-        tile_walk(sm, threadIdx.x + k * kTileThreads);
+    const int lane = threadIdx.x & 31;
+    int d = kNoCell;
+    if (k < count) {
+        int i = sm.queue[head + k];
+        tile_cell(sm, i);
+        d = sm.dsl[i];
+    }
+    bool ready = false;
+    if (d != kNoCell) {
+        unsigned shift = (unsigned)(d & 3) * 8u;
+        unsigned old = atomicSub(sm.cnt + (d >> 2), 1u << shift);
+        ready = ((old >> shift) & 0xFFu) == 1u;
+    }
+    unsigned ballot = __ballot_sync(0xffffffffu, ready);
+    int base = 0;
+    if (lane == 0 && ballot) base = atomicAdd(next, __popc(ballot));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (ready) sm.queue[next_base + base + __popc(ballot & ((1u << lane) - 1u))] = (uint16_t)d;
+}
+
+// Solve the tile in rounds: a round finishes every queued cell of that round (their upstream cells were
+// finished in earlier rounds) and queues each downstream cell whose last upstream cell it finished.
+// Rounds of more than 32 cells use the whole block (one barrier per round); runs of smaller rounds, the
+// long tail of channel cells, are done by warp 0 alone with __syncwarp while the other warps wait at one
+// barrier.  The counts of the next rounds live in a ring of three counters, so the count a round reads is
+// never written during that round.
+__device__ __forceinline__ void tile_solve(TileSmem& sm, int first_round)
+{
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    int head = 0, count = first_round, r = 0;
+    while (count > 0) {
+        if (count > 32) {
+            int* next = &sm.round_count[(r + 1) % 3];
+            const int next_base = head + count;
+            if (t == 0) sm.round_count[(r + 2) % 3] = 0;  // read by everyone two rounds ago
+            for (int k0 = 0; k0 < count; k0 += kTileThreads) tile_item(sm, head, count, k0 + t, next, next_base);
+            __syncthreads();
+            head = next_base;
+            count = *next;
+            ++r;
+        } else {
+            if (warp == 0) {
+                int wh = head, wc = count, wr = r;
+                while (wc > 0 && wc <= 32) {
+                    int* next = &sm.round_count[(wr + 1) % 3];
+                    const int next_base = wh + wc;
+                    if (lane == 0) sm.round_count[(wr + 2) % 3] = 0;
+                    __syncwarp();
+                    tile_item(sm, wh, wc, lane, next, next_base);
+                    __syncwarp();
+                    wh = next_base;
+                    wc = *(volatile int*)next;
+                    ++wr;
+                }
+                if (lane == 0) {
+                    sm.round_count[3] = wh;
+                    sm.round_count[4] = wc;
+                    sm.round_count[5] = wr;
+                }
+            }
+            __syncthreads();
+            head = sm.round_count[3];
+            count = sm.round_count[4];
+            r = sm.round_count[5];
+            __syncthreads();  // everyone has read the hand-over before a later warp phase rewrites it
+        }
     }
 }
 
@@ -438,9 +521,8 @@ __global__ void __launch_bounds__(kTileThreads)
         if (isinf(x) && x > 0.0f) inf = true;
         else if (x > 0.0f) sum.add(x);
     }
-    unsigned starts = tile_prepare(sm, fd, g, tr, tc);
-    tile_walk_all(sm, starts);
-    __syncthreads();
+    int first = tile_prepare(sm, fd, g, tr, tc);
+    tile_solve(sm, first);
 #pragma unroll 4
     for (int k = 0; k < kTileCells / kTileThreads; ++k) {
         int i = t + k * kTileThreads;
@@ -627,7 +709,7 @@ __global__ void __launch_bounds__(kTileThreads)
         sm.hi[t + k * kTileThreads] = 0.0f;
         sm.lo[t + k * kTileThreads] = 0.0f;
     }
-    unsigned starts = tile_prepare(sm, fd, g, tr, tc);
+    int first = tile_prepare(sm, fd, g, tr, tc);
     // sources: border cells gather the exact subtree sums of the halo exits draining into them
     if (t < 4 * kTile - 4) {
         int rin, cin;
@@ -663,8 +745,7 @@ __global__ void __launch_bounds__(kTileThreads)
         }
     }
     __syncthreads();
-    tile_walk_all(sm, starts);
-    __syncthreads();
+    tile_solve(sm, first);
 #pragma unroll 4
     for (int k = 0; k < kTileCells / kTileThreads; ++k) {
         int i = t + k * kTileThreads;

@@ -154,6 +154,7 @@ static void free_core(TopologyCore* core)
     cudaFree(core->count);
     cudaFree(core->upmask);
     cudaFree(core->level);
+    cudaFree(core->order);
     tile_core_free(core->tiles);
     delete core;
 }
@@ -163,6 +164,8 @@ static void free_handle(lue_gpu_topology* t)
     if (!t) return;
     cudaFree(t->work_count);
     cudaFree(t->lo);
+    cudaFree(t->history);
+    cudaFree(t->planes);
     tile_scratch_free(&t->tile_scratch);
     if (t->core && --t->core->refs == 0) free_core(t->core);
     delete t;

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <atomic>
+#include <vector>
 
 #include "common.cuh"
 #include "tile_accu.cuh"
@@ -16,6 +17,8 @@ struct TopologyCore {
     uint8_t* upmask = nullptr;  // bit k set: neighbour k (NW, N, NE, W, E, SW, S, SE) drains here
     int32_t* level = nullptr;   // downstream level, -1 for no-data and cycle cells
     TileCore* tiles = nullptr;  // tiled accu engine (acyclic rasters), else nullptr
+    int32_t* order = nullptr;   // valid cells sorted by downstream level (built on first multi-step call)
+    std::vector<int32_t> level_offsets;  // [levels + 1] start of each level in `order`
     lue_gpu_topology_stats stats{};
     int64_t bytes = 0;
     std::atomic<int> refs{1};
@@ -28,6 +31,10 @@ struct lue_gpu_topology {
     uint32_t* work_count = nullptr;  // per-call copy of the counts, 4 cells per word
     float* lo = nullptr;             // per-call float-float residuals of f32 routing
     lue_gb300::TileScratch tile_scratch;
+    double* history = nullptr;       // discharge planes of multi-step kinematic wave (grown on demand)
+    size_t history_bytes = 0;
+    double** planes = nullptr;       // device array of plane pointers
+    size_t plane_capacity = 0;
     int64_t scratch_bytes = 0;
 };
 

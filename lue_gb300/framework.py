@@ -253,3 +253,24 @@ def kinematic_wave(flow_direction, current_outflow, inflow, alpha, beta, time_st
         del kb, kd
     del kq, kl, ka
     return PartitionedArray(out, flow_direction.partition_shape)
+
+
+def kinematic_wave_steps(flow_direction, current_outflow, inflow, alpha, beta, time_step_duration, channel_length,
+                         steps):
+    """`steps` kinematic_wave time steps in one call (float64 discharge; float32 inflow and alpha rasters or
+    scalars; scalar beta and channel length), equal to calling kinematic_wave `steps` times."""
+    _check_partitioning(flow_direction, current_outflow, inflow, alpha)
+    t = flow_direction.topology()
+    shape = flow_direction.shape
+    out = _empty(flow_direction, torch.float64)
+    pq, sq, kq = _raster_or_scalar(current_outflow, shape, torch.float64, "current_outflow")
+    if pq is None:
+        kq = torch.full(shape, sq, dtype=torch.float64, device=flow_direction.data.device)
+        pq = kq.data_ptr()
+    pl, sl, kl = _raster_or_scalar(inflow, shape, torch.float32, "inflow")
+    pa, sa, ka = _raster_or_scalar(alpha, shape, torch.float32, "alpha")
+    _lib.check(_lib.lib().lue_gpu_kinematic_wave_steps_f64_f32in(
+        t.handle, pq, pl, sl, pa, sa, float(beta), float(time_step_duration), float(channel_length), int(steps),
+        out.data_ptr(), _stream(flow_direction.data)))
+    del kq, kl, ka
+    return PartitionedArray(out, flow_direction.partition_shape)

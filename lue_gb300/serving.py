@@ -1,0 +1,224 @@
+"""Serving: a request loop over a pool of resident flow topologies, with continuous batching.
+
+Requests are accu (float32 material) and multi-step kinematic_wave (float64 discharge) solves on grids
+from a pool whose flow topologies (inflow counts, downstream levels, tile structures) are built once and
+stay on the device.  The loop:
+
+- queues requests as they arrive (a Poisson stream in the benchmark);
+- admits the oldest waiting request as soon as a slot (CUDA stream) is free and its device memory
+  (inputs, outputs, per-request scratch) fits in the free-HBM budget, so requests that arrive while
+  others run start while those are still on the GPU, and their kernels overlap;
+- runs each request on its own stream with its own topology handle (a clone that shares the grid's
+  resident topology and has its own scratch), copies the result back to pinned host memory, and
+  completes it when its event has fired.
+
+Latency is measured from arrival to completion on the host clock.  The same requests can be run one at
+a time through the plain drop-in path (topology built per call, as the reference recomputes inflow
+counts on every call) for comparison, or alone to check that results do not depend on the mix.
+"""
+import collections
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class Request:
+    rid: int
+    kind: str                 # "accu" or "kinematic_wave"
+    grid: int
+    arrival: float            # seconds after the start of the run
+    steps: int = 1
+    inputs: dict = field(default_factory=dict)
+    result: object = None
+    start: float = None
+    done: float = None
+
+    @property
+    def latency(self):
+        return None if self.done is None else self.done - self.arrival
+
+
+def make_requests(pool_shapes, rate, duration, kw_fraction=0.5, kw_steps=24, seed=0):
+    """Poisson arrivals at `rate` per second for `duration` seconds; each request draws a grid uniformly
+    from the pool and is a `kw_steps`-step kinematic_wave solve with probability `kw_fraction`, else an
+    accu.  Each request carries a seed; its input fields are generated on the device from that seed when
+    it is admitted (material lognormal(0, 1) float32; discharge U[0, 1) float64, lateral inflow U[0, 5e-5)
+    m3/s/m float32, alpha U[1, 5) float32), so a request's inputs are the same alone and in any mix."""
+    rng = np.random.default_rng(seed)
+    reqs, t, rid = [], 0.0, 0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > duration:
+            break
+        g = int(rng.integers(len(pool_shapes)))
+        kind = "kinematic_wave" if rng.random() < kw_fraction else "accu"
+        steps = kw_steps if kind == "kinematic_wave" else 1
+        reqs.append(Request(rid, kind, g, t, steps, dict(seed=int(rng.integers(1 << 62)))))
+        rid += 1
+    return reqs
+
+
+def device_inputs(r, shape, device, stream=None):
+    """The request's input fields, generated on `device` (on the current stream) from its seed."""
+    import torch
+    gen = torch.Generator(device=device)
+    gen.manual_seed(r.inputs["seed"])
+    if r.kind == "accu":
+        m = torch.empty(shape, dtype=torch.float32, device=device)
+        m.log_normal_(0.0, 1.0, generator=gen)
+        return {"material": m}
+    q = torch.rand(shape, dtype=torch.float64, device=device, generator=gen)
+    lat = torch.rand(shape, dtype=torch.float32, device=device, generator=gen) * 5e-5
+    al = 1.0 + 4.0 * torch.rand(shape, dtype=torch.float32, device=device, generator=gen)
+    return {"discharge": q, "lateral": lat, "alpha": al}
+
+
+class Server:
+    def __init__(self, pool_fds, slots=8, hbm_fraction=0.8, device="cuda"):
+        import torch
+
+        from . import framework as lfr
+        self.torch, self.lfr, self.device = torch, lfr, torch.device(device)
+        self.grids = [lfr.from_numpy(fd, device=self.device) for fd in pool_fds]
+        self.topologies = [g.topology() for g in self.grids]
+        self.free_clones = collections.defaultdict(list)
+        self.streams = [torch.cuda.Stream(self.device) for _ in range(slots)]
+        free, _ = torch.cuda.mem_get_info(self.device)
+        self.budget = int(free * hbm_fraction)
+        self.in_use = 0
+        torch.cuda.synchronize(self.device)
+
+    def cells(self, r):
+        return int(np.prod(self.grids[r.grid].shape))
+
+    def bytes_needed(self, r):
+        n = self.cells(r)
+        if r.kind == "accu":
+            return n * (4 + 4 + 16)            # material, outflow, scratch
+        return n * (8 + 4 + 4 + 8 + 16 + 8 * max(r.steps - 1, 0))  # discharge in/out, inputs, scratch, history
+
+    def _topology(self, g):
+        lst = self.free_clones[g]
+        return lst.pop() if lst else self.topologies[g].clone()
+
+    def _launch(self, r, stream, keep_results=True):
+        torch = self.torch
+        from . import _lib
+        L = _lib.lib()
+        fd = self.grids[r.grid]
+        topo = self._topology(r.grid)
+        with torch.cuda.stream(stream):
+            x = device_inputs(r, fd.shape, self.device)
+            if r.kind == "accu":
+                out = torch.empty(fd.shape, dtype=torch.float32, device=self.device)
+                _lib.check(L.lue_gpu_accu_f32(topo.handle, x["material"].data_ptr(), 0.0, out.data_ptr(),
+                                              stream.cuda_stream))
+            else:
+                out = torch.empty(fd.shape, dtype=torch.float64, device=self.device)
+                _lib.check(L.lue_gpu_kinematic_wave_steps_f64_f32in(
+                    topo.handle, x["discharge"].data_ptr(), x["lateral"].data_ptr(), 0.0, x["alpha"].data_ptr(), 0.0,
+                    0.6, 3600.0, 100.0, r.steps, out.data_ptr(), stream.cuda_stream))
+            # the result goes back to host memory: part of every request's latency
+            host = torch.empty(out.shape, dtype=out.dtype, pin_memory=True)
+            host.copy_(out, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(stream)
+        return dict(req=r, topo=topo, event=ev, host=host, keep=(x, out), stream=stream)
+
+    def run(self, requests, realtime=True, keep_results=True):
+        """Serve `requests` (sorted by arrival).  With realtime=False every request is available at
+        time zero (a closed-loop stress run).  Returns the summary dict."""
+        torch = self.torch
+        pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
+        waiting, active = collections.deque(), []
+        free_streams = list(self.streams)
+        t0 = time.perf_counter()
+        done = 0
+        self.max_active = 0
+        while done < len(requests):
+            now = time.perf_counter() - t0
+            while pending and (not realtime or pending[0].arrival <= now):
+                waiting.append(pending.popleft())
+            still = []
+            for a in active:
+                if a["event"].query():
+                    r = a["req"]
+                    r.done = time.perf_counter() - t0
+                    if keep_results:
+                        r.result = a["host"].numpy()
+                    self.free_clones[r.grid].append(a["topo"])
+                    self.in_use -= self.bytes_needed(r)
+                    free_streams.append(a["stream"])
+                    done += 1
+                else:
+                    still.append(a)
+            active = still
+            while waiting and free_streams:
+                r = waiting[0]
+                need = self.bytes_needed(r)
+                if active and self.in_use + need > self.budget:
+                    break  # admission by free HBM: wait for running requests to finish
+                waiting.popleft()
+                self.in_use += need
+                r.start = time.perf_counter() - t0
+                active.append(self._launch(r, free_streams.pop(), keep_results))
+                self.max_active = max(self.max_active, len(active))
+            if not active and not waiting and pending and realtime:
+                time.sleep(max(0.0, min(pending[0].arrival - (time.perf_counter() - t0), 0.001)))
+            else:
+                time.sleep(0.0001)
+        wall = time.perf_counter() - t0
+        torch.cuda.synchronize(self.device)
+        return summarize(requests, wall, self)
+
+
+def summarize(requests, wall, server):
+    lat = np.array([r.latency for r in requests])
+    cell_steps = sum(int(np.prod(server.grids[r.grid].shape)) * r.steps for r in requests)
+    return {"requests": len(requests), "max_concurrent": getattr(server, "max_active", 1),
+            "p50_ms": float(np.percentile(lat, 50) * 1e3),
+            "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_ms": float(lat.mean() * 1e3),
+            "wall_s": wall, "mcells_per_s": cell_steps / wall / 1e6,
+            "accu": sum(r.kind == "accu" for r in requests),
+            "kinematic_wave": sum(r.kind == "kinematic_wave" for r in requests)}
+
+
+def run_sequential_plain(server, requests, keep_results=True):
+    """Reference-style: one request at a time, in arrival order, each through the plain drop-in path
+    (the flow topology is built for every call, then one kinematic_wave call per time step; one stream,
+    no overlap).  The result is read back to host memory, as in Server.run."""
+    torch, lfr = server.torch, server.lfr
+    t0 = time.perf_counter()
+    for r in sorted(requests, key=lambda r: r.arrival):
+        now = time.perf_counter() - t0
+        if r.arrival > now:
+            time.sleep(r.arrival - now)
+        r.start = time.perf_counter() - t0
+        fd = lfr.PartitionedArray(server.grids[r.grid].data)  # fresh array: no cached topology
+        x = device_inputs(r, fd.shape, server.device)
+        if r.kind == "accu":
+            out = lfr.accu(fd, lfr.PartitionedArray(x["material"])).data
+        else:
+            q = lfr.PartitionedArray(x["discharge"])
+            lat, al = lfr.PartitionedArray(x["lateral"]), lfr.PartitionedArray(x["alpha"])
+            for _ in range(r.steps):
+                q = lfr.kinematic_wave(fd, q, lat, al, 0.6, 3600.0, 100.0)
+            out = q.data
+        res = out.cpu().numpy()
+        r.done = time.perf_counter() - t0
+        if keep_results:
+            r.result = res
+        fd.topology().close()
+    return summarize(requests, time.perf_counter() - t0, server)
+
+
+def pool_shapes(n=128, lo=256, hi=8192, seed=21):
+    from .ensemble import catchment_sides
+    return [(s, s) for s in catchment_sides(n, lo, hi, seed)]
+
+
+def build_pool(shapes, seed=21, amplitude=200.0):
+    from .ensemble import build_flow_directions
+    return build_flow_directions([s[0] for s in shapes], seed, amplitude)

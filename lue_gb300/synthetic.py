@@ -158,3 +158,49 @@ def kinematic_wave_inputs(rows, cols, seed, amplitude, cached=True, **_):
     alpha = (np.float32(1.0) + np.float32(4.0) * rng.random((rows, cols), dtype=np.float32)).astype(np.float32)
     return dict(flow_direction=fd, discharge=discharge, lateral_inflow=lateral, alpha=alpha, beta=0.6,
                 time_step_duration=3600.0, channel_length=100.0)
+
+
+def dem_device(rows, cols, seed, amplitude, wavelength=None, octaves=8, device="cuda"):
+    """Float32 fBm DEM generated on the GPU with torch (hashed-gradient noise, quintic fade, octaves at
+    halving wavelength and amplitude) on the same south-tilted plane as dem().  It is not bit-identical to
+    dem(); it serves the pools of many grids (ensembles, serving), whose D8 rasters come from
+    lue_gpu_d8_flow_direction without depression filling, so they keep interior sinks (pits)."""
+    import torch
+
+    wl = float(wavelength if wavelength is not None else max(rows, cols) / 4)
+    r = torch.arange(rows, device=device, dtype=torch.float64)[:, None]
+    c = torch.arange(cols, device=device, dtype=torch.float64)[None, :]
+    gx = torch.tensor([np.cos(k * np.pi / 8) for k in range(16)], device=device, dtype=torch.float64)
+    gy = torch.tensor([np.sin(k * np.pi / 8) for k in range(16)], device=device, dtype=torch.float64)
+    m1, m2 = 0x632BE59BD9B4E019, 0x9E3779B97F4A7C15 - (1 << 64)
+
+    def grad(ix, iy, s, dx, dy):
+        h = ix * m1 + iy * m2 + s
+        h = h ^ (h >> 29)
+        h = h * (0xBF58476D1CE4E5B9 - (1 << 64))
+        h = h ^ (h >> 32)
+        k = (h & 15)
+        return gx[k] * dx + gy[k] * dy
+
+    total = torch.zeros((rows, cols), device=device, dtype=torch.float64)
+    amp, norm, lam = 1.0, 0.0, wl
+    for o in range(octaves):
+        x, y = c / lam, r / lam
+        fx, fy = torch.floor(x), torch.floor(y)
+        ix, iy = fx.to(torch.int64), fy.to(torch.int64)
+        dx, dy = x - fx, y - fy
+        s = seed * 1000003 + o * 7919
+        n00 = grad(ix, iy, s, dx, dy)
+        n10 = grad(ix + 1, iy, s, dx - 1, dy)
+        n01 = grad(ix, iy + 1, s, dx, dy - 1)
+        n11 = grad(ix + 1, iy + 1, s, dx - 1, dy - 1)
+        u = dx * dx * dx * (dx * (dx * 6 - 15) + 10)
+        v = dy * dy * dy * (dy * (dy * 6 - 15) + 10)
+        a = n00 + u * (n10 - n00)
+        b = n01 + u * (n11 - n01)
+        total += amp * (a + v * (b - a))
+        norm += amp
+        amp *= 0.5
+        lam *= 0.5
+    base = (rows - 1 - r) * CELL_SIZE * TILT + amplitude + 1.0
+    return (base + amplitude * total / norm).to(torch.float32)

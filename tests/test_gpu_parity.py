@@ -285,3 +285,24 @@ def test_d8_flow_direction_against_oracle(lfr, dtype):
     z[rng.random(z.shape) < 0.002] = np.nan
     got = lfr.to_numpy(lfr.d8_flow_direction(lfr.from_numpy(z)))
     assert np.array_equal(got, oracle.d8_flow_direction(z.astype(np.float64) if dtype == np.float64 else z))
+
+
+@pytest.mark.parametrize("steps", [1, 2, 7])
+def test_kinematic_wave_steps_equal_repeated_single_steps(lfr, steps):
+    d = kw_inputs(400, 333, 17)
+    fd = d["flow_direction"].copy()
+    fd[5, 5] = 255  # a no-data cell
+    a = lfr.from_numpy(fd, (100, 111))
+    lat, alpha = lfr.from_numpy(d["lateral_inflow"], (100, 111)), lfr.from_numpy(d["alpha"], (100, 111))
+    q0 = lfr.from_numpy(d["discharge"], (100, 111))
+    multi = lfr.to_numpy(lfr.kinematic_wave_steps(a, q0, lat, alpha, 0.6, 3600.0, 100.0, steps))
+    q = q0
+    for _ in range(steps):
+        q = lfr.kinematic_wave(a, q, lat, alpha, 0.6, 3600.0, 100.0)
+    single = lfr.to_numpy(q)
+    assert np.array_equal(multi, single, equal_nan=True)
+    q_cpu = d["discharge"]
+    for _ in range(steps):
+        q_cpu = oracle.kinematic_wave(fd, q_cpu, d["lateral_inflow"].astype(np.float64),
+                                      d["alpha"].astype(np.float64), 0.6, 3600.0, 100.0, (100, 111), dtype=np.float64)
+    parity.assert_close64(multi, q_cpu, f"kinematic_wave_steps {steps}")
