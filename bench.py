@@ -301,12 +301,21 @@ def bench_ours(args, world, rank, local):
     traffic = None if tr is None else round(tr[0] / tr[1] * n)
 
     extra = {}
+
+    def leg(name, fn):
+        try:
+            extra[name] = fn(args, dev)
+        except Exception as ex:  # a failing secondary leg must not hide the headline line
+            extra[name] = {"error": f"{type(ex).__name__}: {ex}"}
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+
     if args.kinematic_wave_steps > 0 and rank == 0:
-        extra["kinematic_wave"] = bench_kinematic_wave(args, dev)
+        leg("kinematic_wave", bench_kinematic_wave)
     if not args.no_ensemble and rank == 0:
-        extra["ensemble"] = bench_ensemble(args, dev)
+        leg("ensemble", bench_ensemble)
     if args.serve_seconds > 0 and rank == 0:
-        extra["serving"] = bench_serving(args, dev)
+        leg("serving", bench_serving)
 
     if rank != 0:
         return

@@ -174,12 +174,15 @@ extern "C" int lue_gpu_kinematic_wave_steps_f64_f32in(lue_gpu_topology* t, const
         return LUE_GPU_OK;
     }
     if (int rc = ensure_level_order(core, stream)) return rc;
-    // Steps run in chunks whose history planes fit in 40 % of the free device memory (plus what this
-    // handle already holds); each chunk takes max level + chunk waves.
+    // Steps run in chunks whose history planes fit in a budget: what this handle already holds plus
+    // LUE_GB300_KW_HISTORY_FRACTION (default 0.25) of the free device memory, and at most 64 planes;
+    // each chunk takes max level + chunk waves.
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     const size_t plane = (size_t)n * sizeof(double);
-    int64_t fit = (int64_t)((free_b * 0.4 + (double)t->history_bytes) / (double)plane);
+    double frac = 0.25;
+    if (const char* e = getenv("LUE_GB300_KW_HISTORY_FRACTION")) frac = atof(e);
+    int64_t fit = std::min<int64_t>(64, (int64_t)((free_b * frac + (double)t->history_bytes) / (double)plane));
     int chunk = (int)std::max<int64_t>(1, std::min<int64_t>(steps, fit + 1));
     if (chunk < steps && !single_chunk) {
         const double* src = current_outflow;

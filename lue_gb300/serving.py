@@ -76,7 +76,7 @@ def device_inputs(r, shape, device, stream=None):
 
 
 class Server:
-    def __init__(self, pool_fds, slots=8, hbm_fraction=0.8, device="cuda"):
+    def __init__(self, pool_fds, slots=8, hbm_fraction=0.5, device="cuda"):
         import torch
 
         from . import framework as lfr
@@ -97,7 +97,8 @@ class Server:
         n = self.cells(r)
         if r.kind == "accu":
             return n * (4 + 4 + 16)            # material, outflow, scratch
-        return n * (8 + 4 + 4 + 8 + 16 + 8 * max(r.steps - 1, 0))  # discharge in/out, inputs, scratch, history
+        # discharge in/out, inputs, scratch, history planes (at most 64, see kinematic_wave_steps.cu)
+        return n * (8 + 4 + 4 + 8 + 16 + 8 * min(max(r.steps - 1, 0), 64))
 
     def _topology(self, g):
         lst = self.free_clones[g]
