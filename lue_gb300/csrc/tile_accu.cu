@@ -314,7 +314,7 @@ __global__ void k_halo_exits(const uint8_t* __restrict__ fd, TileGeom g, const i
 }
 
 // ---------------------------------------------------------------------------------------------------
-// Per call
+// Build: per-tile solve schedules
 // ---------------------------------------------------------------------------------------------------
 
 constexpr uint16_t kNoCell = 0xFFFFu;
@@ -327,8 +327,7 @@ struct __align__(16) TileSmem {
     uint16_t queue[kTileCells];    // cells in the order they become ready (each cell once)
     uint8_t up[kTileCells];        // in-tile upstream mask
     uint8_t fd[kHalo][kHalo + 2];  // flow direction with a one-cell halo (255 outside the array)
-    int round_count[6];            // [0..2]: cells queued for the next rounds (a ring of three counters);
-                                   // [3..5]: head, count and round handed back by the warp phase
+    int round_count[3];            // cells queued for the next rounds (a ring of three counters)
 };
 
 // Load the flow direction with halo; fill in-tile upstream masks, counters and downstream indices, and
@@ -382,129 +381,208 @@ __device__ __forceinline__ int tile_prepare(TileSmem& sm, const uint8_t* __restr
     return sm.round_count[0];
 }
 
-// Value of cell i: source(i) (hi/lo before the cell is done) + the sum of its in-tile upstream values,
-// float-float; NaN or a negative source makes the cell NaN.  A sum that is not finite (+inf material)
-// is recomputed plainly so that it keeps IEEE semantics.
-__device__ __forceinline__ void tile_cell(TileSmem& sm, int i)
+// Build: compile the solve schedule of one tile (CTA per tile).  The cells of the tile in the order the
+// round solve finishes them, the round boundaries, the cells downstream of a tile entry ("through"
+// cells) in the same rounds, the valid-cell bits and, per border cell, which outside neighbours drain
+// into it.  Every call then replays the schedule instead of re-deriving it from the flow direction.
+// kCount: first pass, only the number of rounds per tile (it sizes the round offset arrays).
+template <bool kCount>
+__global__ void __launch_bounds__(kTileThreads)
+    k_tile_schedule(const uint8_t* __restrict__ fd, TileGeom g, int32_t* rounds_out, const int32_t* round_base,
+                    uint16_t* sched_order, uint8_t* sched_upm, uint16_t* thr_order, uint8_t* thr_upm,
+                    uint16_t* round_off, uint16_t* thr_round_off, uint32_t* valid_bits, uint8_t* border_in)
 {
-    const float x = sm.hi[i];
-    float s = x, e = sm.lo[i];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TileSmem& sm = *reinterpret_cast<TileSmem*>(smem_raw);
+    const int64_t tile = blockIdx.x;
+    const int64_t tr = tile / g.tcols, tc = tile % g.tcols;
+    const int t = threadIdx.x, lane = t & 31;
+    uint16_t* rstart = reinterpret_cast<uint16_t*>(sm.hi);                        // <= 4097 round starts
+    uint8_t* thr = reinterpret_cast<uint8_t*>(sm.lo);                             // through flag per cell
+    uint16_t* trstart = reinterpret_cast<uint16_t*>(reinterpret_cast<uint8_t*>(sm.lo) + kTileCells);
+    int head = 0, count = tile_prepare(sm, fd, g, tr, tc), r = 0;
+    // the rounds of the round solve (tile_solve without values)
+    while (count > 0) {
+        int* next = &sm.round_count[(r + 1) % 3];
+        const int next_base = head + count;
+        if (t == 0) {
+            if (!kCount) rstart[r] = (uint16_t)head;
+            sm.round_count[(r + 2) % 3] = 0;
+        }
+        for (int k0 = 0; k0 < count; k0 += kTileThreads) {
+            int k = k0 + t, d = kNoCell;
+            if (k < count) d = sm.dsl[sm.queue[head + k]];
+            bool ready = false;
+            if (d != kNoCell) {
+                unsigned shift = (unsigned)(d & 3) * 8u;
+                unsigned old = atomicSub(sm.cnt + (d >> 2), 1u << shift);
+                ready = ((old >> shift) & 0xFFu) == 1u;
+            }
+            unsigned ballot = __ballot_sync(0xffffffffu, ready);
+            int base = 0;
+            if (lane == 0 && ballot) base = atomicAdd(next, __popc(ballot));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (ready) sm.queue[next_base + base + __popc(ballot & ((1u << lane) - 1u))] = (uint16_t)d;
+        }
+        __syncthreads();
+        head = next_base;
+        count = *next;
+        ++r;
+    }
+    const int rounds = r, nvalid = head;
+    if (kCount) {
+        if (t == 0) rounds_out[tile] = rounds;
+        return;
+    }
+    if (t == 0) rstart[rounds] = (uint16_t)nvalid;
+    // entries (valid cells with an outside neighbour draining in), border masks, valid bits
+    for (int i = t; i < kTileCells; i += kTileThreads) {
+        int rin = i >> 6, cin = i & 63;
+        bool valid = sm.fd[rin + 1][cin + 1] != kNoData;
+        bool border = rin == 0 || rin == kTile - 1 || cin == 0 || cin == kTile - 1;
+        unsigned outside = 0;
+        if (valid && border) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                int hr = rin + nb_dr(q), hc = cin + nb_dc(q);
+                if (hr >= 0 && hr < kTile && hc >= 0 && hc < kTile) continue;
+                if (sm.fd[hr + 1][hc + 1] == nb_inflow_code(q)) outside |= 1u << q;
+            }
+        }
+        thr[i] = outside ? 1 : 0;
+        if (border) {
+            int b = rin == 0           ? cin
+                    : rin == kTile - 1 ? kTile + cin
+                    : cin == 0         ? 2 * kTile + rin - 1
+                                       : 3 * kTile - 2 + rin - 1;
+            border_in[tile * kBorderCells + b] = (uint8_t)outside;
+        }
+        unsigned bal = __ballot_sync(0xffffffffu, valid);
+        if (lane == 0) valid_bits[tile * (kTileCells / 32) + (i >> 5)] = bal;
+    }
+    __syncthreads();
+    // through flags, round by round: an entry, or downstream of a through cell
+    for (int q = 0; q < rounds; ++q) {
+        for (int k = rstart[q] + t; k < rstart[q + 1]; k += kTileThreads) {
+            int i = sm.queue[k];
+            if (thr[i]) continue;
+            unsigned m = sm.up[i];
+            while (m) {
+                int b = __ffs(m) - 1;
+                m &= m - 1;
+                if (thr[i + nb_dr(b) * kTile + nb_dc(b)]) {
+                    thr[i] = 1;
+                    break;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    for (int k = t; k < nvalid; k += kTileThreads) {
+        int i = sm.queue[k];
+        sched_order[tile * kTileCells + k] = (uint16_t)i;
+        sched_upm[tile * kTileCells + k] = sm.up[i];
+    }
+    if (t == 0) {
+        int j = 0;
+        for (int q = 0; q < rounds; ++q) {
+            trstart[q] = (uint16_t)j;
+            for (int k = rstart[q]; k < rstart[q + 1]; ++k) {
+                int i = sm.queue[k];
+                if (!thr[i]) continue;
+                unsigned m = sm.up[i], tm = 0;
+                while (m) {
+                    int b = __ffs(m) - 1;
+                    m &= m - 1;
+                    if (thr[i + nb_dr(b) * kTile + nb_dc(b)]) tm |= 1u << b;
+                }
+                thr_order[tile * kTileCells + j] = (uint16_t)i;
+                thr_upm[tile * kTileCells + j] = (uint8_t)tm;
+                ++j;
+            }
+        }
+        trstart[rounds] = (uint16_t)j;
+    }
+    __syncthreads();
+    const int32_t base = round_base[tile];
+    for (int q = t; q <= rounds; q += kTileThreads) {
+        round_off[base + q] = rstart[q];
+        thr_round_off[base + q] = trstart[q];
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Per call
+// ---------------------------------------------------------------------------------------------------
+
+// Cell i of a scheduled round: source (hi/lo before the cell is done) + the float-float sum of the
+// upstream cells in mask m; NaN or a negative source makes the cell NaN; a sum that is not finite
+// (+inf material) is recomputed plainly so that it keeps IEEE semantics.
+__device__ __forceinline__ void sched_cell(float* hi, float* lo, int i, unsigned m)
+{
+    const float x = hi[i];
+    float s = x, e = lo[i];
     bool nan = isnan(x) || !(x >= 0.0f);
-    unsigned m = sm.up[i];
-    while (m) {
-        int q = __ffs(m) - 1;
-        m &= m - 1;
+    unsigned mm = m;
+    while (mm) {
+        int q = __ffs(mm) - 1;
+        mm &= mm - 1;
         int u = i + nb_dr(q) * kTile + nb_dc(q);
-        float h = sm.hi[u], ts, te;
+        float h = hi[u], ts, te;
         nan |= isnan(h);
         two_sum(s, h, ts, te);
         s = ts;
-        e = __fadd_rn(e, __fadd_rn(te, sm.lo[u]));
+        e = __fadd_rn(e, __fadd_rn(te, lo[u]));
     }
-    float hi = __fadd_rn(s, e);
-    float lo = __fsub_rn(e, __fsub_rn(hi, s));
-    if (!isfinite(hi)) {  // +inf upstream or material: plain float sum (inf stays inf)
+    float h = __fadd_rn(s, e);
+    float l = __fsub_rn(e, __fsub_rn(h, s));
+    if (!isfinite(h)) {
         float p = x;
-        unsigned mm = sm.up[i];
-        while (mm) {
-            int q = __ffs(mm) - 1;
-            mm &= mm - 1;
-            p += sm.hi[i + nb_dr(q) * kTile + nb_dc(q)];
+        while (m) {
+            int q = __ffs(m) - 1;
+            m &= m - 1;
+            p += hi[i + nb_dr(q) * kTile + nb_dc(q)];
         }
-        hi = p;
-        lo = 0.0f;
+        h = p;
+        l = 0.0f;
     }
     if (nan) {
-        hi = __int_as_float(0x7fc00000);
-        lo = 0.0f;
+        h = __int_as_float(0x7fc00000);
+        l = 0.0f;
     }
-    sm.hi[i] = hi;
-    sm.lo[i] = lo;
+    hi[i] = h;
+    lo[i] = l;
 }
 
-// Finish item k of a round (if k < count) and queue its downstream cell when this was its last
-// upstream cell.  All 32 lanes of the warp must call it (warp-aggregated queue appends).
-__device__ __forceinline__ void tile_item(TileSmem& sm, int head, int count, int k, int* next, int next_base)
+// Replay a tile's rounds: one barrier per non-empty round.
+__device__ __forceinline__ void sched_replay(float* hi, float* lo, const uint16_t* __restrict__ order,
+                                             const uint8_t* __restrict__ upm, const uint16_t* __restrict__ off,
+                                             int rounds)
 {
-    const int lane = threadIdx.x & 31;
-    int d = kNoCell;
-    if (k < count) {
-        int i = sm.queue[head + k];
-        tile_cell(sm, i);
-        d = sm.dsl[i];
-    }
-    bool ready = false;
-    if (d != kNoCell) {
-        unsigned shift = (unsigned)(d & 3) * 8u;
-        unsigned old = atomicSub(sm.cnt + (d >> 2), 1u << shift);
-        ready = ((old >> shift) & 0xFFu) == 1u;
-    }
-    unsigned ballot = __ballot_sync(0xffffffffu, ready);
-    int base = 0;
-    if (lane == 0 && ballot) base = atomicAdd(next, __popc(ballot));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (ready) sm.queue[next_base + base + __popc(ballot & ((1u << lane) - 1u))] = (uint16_t)d;
-}
-
-// Solve the tile in rounds: a round finishes every queued cell of that round (their upstream cells were
-// finished in earlier rounds) and queues each downstream cell whose last upstream cell it finished.
-// Rounds of more than 32 cells use the whole block (one barrier per round); runs of smaller rounds, the
-// long tail of channel cells, are done by warp 0 alone with __syncwarp while the other warps wait at one
-// barrier.  The counts of the next rounds live in a ring of three counters, so the count a round reads is
-// never written during that round.
-__device__ __forceinline__ void tile_solve(TileSmem& sm, int first_round)
-{
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    int head = 0, count = first_round, r = 0;
-    while (count > 0) {
-        if (count > 32) {
-            int* next = &sm.round_count[(r + 1) % 3];
-            const int next_base = head + count;
-            if (t == 0) sm.round_count[(r + 2) % 3] = 0;  // read by everyone two rounds ago
-            for (int k0 = 0; k0 < count; k0 += kTileThreads) tile_item(sm, head, count, k0 + t, next, next_base);
-            __syncthreads();
-            head = next_base;
-            count = *next;
-            ++r;
-        } else {
-            if (warp == 0) {
-                int wh = head, wc = count, wr = r;
-                while (wc > 0 && wc <= 32) {
-                    int* next = &sm.round_count[(wr + 1) % 3];
-                    const int next_base = wh + wc;
-                    if (lane == 0) sm.round_count[(wr + 2) % 3] = 0;
-                    __syncwarp();
-                    tile_item(sm, wh, wc, lane, next, next_base);
-                    __syncwarp();
-                    wh = next_base;
-                    wc = *(volatile int*)next;
-                    ++wr;
-                }
-                if (lane == 0) {
-                    sm.round_count[3] = wh;
-                    sm.round_count[4] = wc;
-                    sm.round_count[5] = wr;
-                }
-            }
-            __syncthreads();
-            head = sm.round_count[3];
-            count = sm.round_count[4];
-            r = sm.round_count[5];
-            __syncthreads();  // everyone has read the hand-over before a later warp phase rewrites it
-        }
+    const int t = threadIdx.x;
+    int a = off[0];
+    for (int q = 0; q < rounds; ++q) {
+        const int b = off[q + 1];
+        if (b == a) continue;
+        for (int k = a + t; k < b; k += kTileThreads) sched_cell(hi, lo, order[k], upm[k]);
+        __syncthreads();
+        a = b;
     }
 }
 
 // Pass 1: local accu inside each tile; local exit values to P (post-order); material total bound.
 __global__ void __launch_bounds__(kTileThreads)
-    k_tile_local(const uint8_t* __restrict__ fd, TileGeom g, const float* __restrict__ ext, float ext_s,
-                 float* __restrict__ out, const int32_t* __restrict__ exit_base, const uint16_t* __restrict__ exit_local,
-                 const uint32_t* __restrict__ exit_pos, float2* __restrict__ P, unsigned long long* block_total)
+    k_tile_local(TileGeom g, const float* __restrict__ ext, float ext_s, float* __restrict__ out,
+                 const uint16_t* __restrict__ sched_order, const uint8_t* __restrict__ sched_upm,
+                 const int32_t* __restrict__ round_base, const uint16_t* __restrict__ round_off,
+                 const uint32_t* __restrict__ valid_bits, const int32_t* __restrict__ exit_base,
+                 const uint16_t* __restrict__ exit_local, const uint32_t* __restrict__ exit_pos,
+                 float2* __restrict__ P, unsigned long long* block_total)
 {
+    __shared__ float hi[kTileCells];
+    __shared__ float lo[kTileCells];
     __shared__ float warp_sum[kTileThreads / 32];
     __shared__ int warp_inf[kTileThreads / 32];
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    TileSmem& sm = *reinterpret_cast<TileSmem*>(smem_raw);
     const int64_t tile = blockIdx.x;
     const int64_t tr = tile / g.tcols, tc = tile % g.tcols;
     const int t = threadIdx.x;
@@ -516,23 +594,27 @@ __global__ void __launch_bounds__(kTileThreads)
         int64_t r = tr * kTile + (i >> 6), c = tc * kTile + (i & 63);
         float x = 0.0f;
         if (r < g.rows && c < g.cols) x = ext ? __ldg(ext + r * g.cols + c) : ext_s;
-        sm.hi[i] = x;
-        sm.lo[i] = 0.0f;
+        hi[i] = x;
+        lo[i] = 0.0f;
         if (isinf(x) && x > 0.0f) inf = true;
         else if (x > 0.0f) sum.add(x);
     }
-    int first = tile_prepare(sm, fd, g, tr, tc);
-    tile_solve(sm, first);
+    __syncthreads();
+    const int32_t rb = round_base[tile];
+    sched_replay(hi, lo, sched_order + tile * kTileCells, sched_upm + tile * kTileCells, round_off + rb,
+                 round_base[tile + 1] - rb - 1);
 #pragma unroll 4
     for (int k = 0; k < kTileCells / kTileThreads; ++k) {
         int i = t + k * kTileThreads;
         int64_t r = tr * kTile + (i >> 6), c = tc * kTile + (i & 63);
-        if (r < g.rows && c < g.cols)
-            out[r * g.cols + c] = sm.fd[(i >> 6) + 1][(i & 63) + 1] == kNoData ? __int_as_float(0x7fc00000) : sm.hi[i];
+        if (r < g.rows && c < g.cols) {
+            bool valid = (valid_bits[tile * (kTileCells / 32) + (i >> 5)] >> (i & 31)) & 1u;
+            out[r * g.cols + c] = valid ? hi[i] : __int_as_float(0x7fc00000);
+        }
     }
     for (int32_t e = exit_base[tile] + t; e < exit_base[tile + 1]; e += kTileThreads) {
         int loc = exit_local[e];
-        P[exit_pos[e]] = make_float2(sm.hi[loc], sm.lo[loc]);
+        P[exit_pos[e]] = make_float2(hi[loc], lo[loc]);
     }
     // upper bound of this tile's material total, in 2^-16 units; ~0 marks +inf or overflow
     float s = sum.hi + sum.lo;
@@ -693,67 +775,66 @@ __global__ void k_exit_sums(int64_t n, const uint32_t* __restrict__ pos, const u
     A[y] = from_u128(a);
 }
 
-// Pass 3: add the inflow entering each tile to every cell downstream of it.
+// Pass 3: add the inflow entering each tile to every cell downstream of a tile entry.
 __global__ void __launch_bounds__(kTileThreads)
-    k_tile_fixup(const uint8_t* __restrict__ fd, TileGeom g, float* __restrict__ out,
+    k_tile_fixup(TileGeom g, float* __restrict__ out, const uint16_t* __restrict__ thr_order,
+                 const uint8_t* __restrict__ thr_upm, const int32_t* __restrict__ round_base,
+                 const uint16_t* __restrict__ thr_round_off, const uint8_t* __restrict__ border_in,
                  const int32_t* __restrict__ halo_exit, const uint4* __restrict__ A, const unsigned long long* total)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    TileSmem& sm = *reinterpret_cast<TileSmem*>(smem_raw);
+    __shared__ float hi[kTileCells];
+    __shared__ float lo[kTileCells];
     if (total[1]) return;
     const int F = fixed_point_bits(total[0]);
     const int64_t tile = blockIdx.x;
     const int64_t tr = tile / g.tcols, tc = tile % g.tcols;
     const int t = threadIdx.x;
-    for (int k = 0; k < kTileCells / kTileThreads; ++k) {
-        sm.hi[t + k * kTileThreads] = 0.0f;
-        sm.lo[t + k * kTileThreads] = 0.0f;
+    const int32_t rb = round_base[tile];
+    const int rounds = round_base[tile + 1] - rb - 1;
+    const uint16_t* off = thr_round_off + rb;
+    const int nthr = off[rounds];
+    if (nthr == 0) return;  // uniform: nothing enters this tile
+    const uint16_t* order = thr_order + tile * kTileCells;
+    for (int k = t; k < nthr; k += kTileThreads) {
+        int i = order[k];
+        hi[i] = 0.0f;
+        lo[i] = 0.0f;
     }
-    int first = tile_prepare(sm, fd, g, tr, tc);
+    __syncthreads();
     // sources: border cells gather the exact subtree sums of the halo exits draining into them
-    if (t < 4 * kTile - 4) {
-        int rin, cin;
-        if (t < kTile) { rin = 0; cin = t; }
-        else if (t < 2 * kTile) { rin = kTile - 1; cin = t - kTile; }
-        else if (t < 3 * kTile - 2) { rin = t - 2 * kTile + 1; cin = 0; }
-        else { rin = t - (3 * kTile - 2) + 1; cin = kTile - 1; }
-        if (sm.fd[rin + 1][cin + 1] != kNoData) {
+    if (t < kBorderCells) {
+        unsigned mask = border_in[tile * kBorderCells + t];
+        if (mask) {
+            int rin, cin;
+            if (t < kTile) { rin = 0; cin = t; }
+            else if (t < 2 * kTile) { rin = kTile - 1; cin = t - kTile; }
+            else if (t < 3 * kTile - 2) { rin = t - 2 * kTile + 1; cin = 0; }
+            else { rin = t - (3 * kTile - 2) + 1; cin = kTile - 1; }
             u128 s = 0;
-            bool any = false;
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                int hr = rin + nb_dr(q), hc = cin + nb_dc(q);
-                if (hr >= 0 && hr < kTile && hc >= 0 && hc < kTile) continue;  // in-tile neighbour
-                if (sm.fd[hr + 1][hc + 1] != nb_inflow_code(q)) continue;
-                int32_t id = halo_exit[tile * kHaloSlots + halo_slot_of(hr, hc)];
-                if (id >= 0) {
-                    s += to_u128(A[id]);
-                    any = true;
-                }
+            while (mask) {
+                int q = __ffs(mask) - 1;
+                mask &= mask - 1;
+                int32_t id = halo_exit[tile * kHaloSlots + halo_slot_of(rin + nb_dr(q), cin + nb_dc(q))];
+                if (id >= 0) s += to_u128(A[id]);
             }
-            if (any) {
-                int i = rin * kTile + cin;
-                if ((s >> 96) != 0) {
-                    sm.hi[i] = __int_as_float(0x7fc00000);
-                } else {
-                    double d = fixed_to_double(s, F);
-                    float h = __double2float_rn(d);
-                    sm.hi[i] = h;
-                    sm.lo[i] = __double2float_rn(d - (double)h);
-                }
+            int i = rin * kTile + cin;
+            if ((s >> 96) != 0) {
+                hi[i] = __int_as_float(0x7fc00000);
+            } else {
+                double d = fixed_to_double(s, F);
+                float h = __double2float_rn(d);
+                hi[i] = h;
+                lo[i] = __double2float_rn(d - (double)h);
             }
         }
     }
     __syncthreads();
-    tile_solve(sm, first);
-#pragma unroll 4
-    for (int k = 0; k < kTileCells / kTileThreads; ++k) {
-        int i = t + k * kTileThreads;
-        float h = sm.hi[i], l = sm.lo[i];
+    sched_replay(hi, lo, order, thr_upm + tile * kTileCells, off, rounds);
+    for (int k = t; k < nthr; k += kTileThreads) {
+        int i = order[k];
+        float h = hi[i], l = lo[i];
         if (h == 0.0f && l == 0.0f) continue;
-        int64_t r = tr * kTile + (i >> 6), c = tc * kTile + (i & 63);
-        if (r >= g.rows || c >= g.cols || sm.fd[(i >> 6) + 1][(i & 63) + 1] == kNoData) continue;
-        float* o = out + r * g.cols + c;
+        float* o = out + (tr * kTile + (i >> 6)) * g.cols + tc * kTile + (i & 63);
         if (isnan(h)) {
             *o = __int_as_float(0x7fc00000);
         } else {
@@ -889,6 +970,48 @@ int tile_core_build(TopologyCore* core, cudaStream_t stream)
         rc = fail(LUE_GPU_EINVAL, "tile topology: cycle inside a tile or inconsistent exit forest");
         goto error;
     }
+    // solve schedules: rounds per tile, then the schedules themselves
+    {
+        const size_t smem = sizeof(TileSmem);
+        TRY(cudaFuncSetAttribute(k_tile_schedule<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+            "tile schedule");
+        TRY(cudaFuncSetAttribute(k_tile_schedule<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+            "tile schedule");
+        TRY(cudaMalloc(&tc->round_base, (nt + 1) * sizeof(int32_t)), "tile round base");
+        k_tile_schedule<true><<<(unsigned)nt, kTileThreads, smem, stream>>>(
+            core->fd, g, count, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+        TRY(cudaGetLastError(), "tile schedule");
+        TRY(cudaMemcpyAsync(hcount.data(), count, nt * sizeof(int32_t), cudaMemcpyDeviceToHost, stream),
+            "tile rounds");
+        TRY(cudaStreamSynchronize(stream), "tile rounds");
+        int64_t total = 0;
+        for (int64_t i = 0; i < nt; ++i) {
+            hbase[i] = (int32_t)total;
+            total += hcount[i] + 1;
+            if (total > INT32_MAX) {
+                rc = fail(LUE_GPU_ERANGE, "tile topology: too many solve rounds");
+                goto error;
+            }
+        }
+        hbase[nt] = (int32_t)total;
+        TRY(cudaMemcpyAsync(tc->round_base, hbase.data(), (nt + 1) * sizeof(int32_t), cudaMemcpyHostToDevice,
+                            stream),
+            "tile round base");
+        TRY(cudaMalloc(&tc->round_off, total * sizeof(uint16_t)), "tile round offsets");
+        TRY(cudaMalloc(&tc->thr_round_off, total * sizeof(uint16_t)), "tile round offsets");
+        TRY(cudaMalloc(&tc->sched_order, nt * kTileCells * sizeof(uint16_t)), "tile schedule");
+        TRY(cudaMalloc(&tc->sched_upm, nt * kTileCells), "tile schedule");
+        TRY(cudaMalloc(&tc->thr_order, nt * kTileCells * sizeof(uint16_t)), "tile schedule");
+        TRY(cudaMalloc(&tc->thr_upm, nt * kTileCells), "tile schedule");
+        TRY(cudaMalloc(&tc->valid_bits, nt * (kTileCells / 32) * sizeof(uint32_t)), "tile valid bits");
+        TRY(cudaMalloc(&tc->border_in, nt * kBorderCells), "tile border masks");
+        k_tile_schedule<false><<<(unsigned)nt, kTileThreads, smem, stream>>>(
+            core->fd, g, nullptr, tc->round_base, tc->sched_order, tc->sched_upm, tc->thr_order, tc->thr_upm,
+            tc->round_off, tc->thr_round_off, tc->valid_bits, tc->border_in);
+        TRY(cudaGetLastError(), "tile schedule");
+        TRY(cudaStreamSynchronize(stream), "tile schedule");  // hbase must outlive its copy
+        tc->bytes += (nt + 1) * 4 + total * 4 + nt * kTileCells * 6 + nt * (kTileCells / 8) + nt * kBorderCells;
+    }
     cudaFree(bitmap);
     cudaFree(rowpref);
     cudaFree(count);
@@ -937,6 +1060,15 @@ void tile_core_free(TileCore* tc)
     cudaFree(tc->exit_pos);
     cudaFree(tc->exit_start);
     cudaFree(tc->halo_exit);
+    cudaFree(tc->sched_order);
+    cudaFree(tc->sched_upm);
+    cudaFree(tc->thr_order);
+    cudaFree(tc->thr_upm);
+    cudaFree(tc->round_base);
+    cudaFree(tc->round_off);
+    cudaFree(tc->thr_round_off);
+    cudaFree(tc->valid_bits);
+    cudaFree(tc->border_in);
     delete tc;
 }
 
@@ -975,16 +1107,9 @@ int tile_accu_f32(const TopologyCore* core, TileScratch* s, const float* ext, fl
 {
     const TileCore* tc = core->tiles;
     TileGeom g{core->rows, core->cols, tc->trows, tc->tcols};
-    const size_t smem = sizeof(TileSmem);
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(k_tile_local, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(k_tile_fixup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        configured = true;
-    }
-    k_tile_local<<<(unsigned)tc->ntiles, kTileThreads, smem, stream>>>(core->fd, g, ext, ext_s, out, tc->exit_base,
-                                                                      tc->exit_local, tc->exit_pos, s->P,
-                                                                      s->block_total);
+    k_tile_local<<<(unsigned)tc->ntiles, kTileThreads, 0, stream>>>(
+        g, ext, ext_s, out, tc->sched_order, tc->sched_upm, tc->round_base, tc->round_off, tc->valid_bits,
+        tc->exit_base, tc->exit_local, tc->exit_pos, s->P, s->block_total);
     k_total<<<1, 1024, 0, stream>>>(s->block_total, tc->ntiles, s->total);
     count_launches(2);
     const int64_t E = tc->nexit;
@@ -994,8 +1119,9 @@ int tile_accu_f32(const TopologyCore* core, TileScratch* s, const float* ext, fl
         k_scan_blocks<<<1, kTileThreads, 0, stream>>>(s->block_sums, nb, s->total);
         k_scan_final<<<(unsigned)nb, kTileThreads, 0, stream>>>(s->P, E, s->total, s->block_sums, s->S);
         k_exit_sums<<<blocks_for(E, 256), 256, 0, stream>>>(E, tc->exit_pos, tc->exit_start, s->S, s->A, s->total);
-        k_tile_fixup<<<(unsigned)tc->ntiles, kTileThreads, smem, stream>>>(core->fd, g, out, tc->halo_exit, s->A,
-                                                                           s->total);
+        k_tile_fixup<<<(unsigned)tc->ntiles, kTileThreads, 0, stream>>>(g, out, tc->thr_order, tc->thr_upm,
+                                                                        tc->round_base, tc->thr_round_off,
+                                                                        tc->border_in, tc->halo_exit, s->A, s->total);
         count_launches(5);
     }
     return cuda_status(cudaGetLastError(), "accu_f32 (tiles)");
