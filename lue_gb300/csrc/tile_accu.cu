@@ -390,24 +390,25 @@ template <bool kCount>
 __global__ void __launch_bounds__(kTileThreads)
     k_tile_schedule(const uint8_t* __restrict__ fd, TileGeom g, int32_t* rounds_out, const int32_t* round_base,
                     uint16_t* sched_order, uint8_t* sched_upm, uint16_t* thr_order, uint8_t* thr_upm,
-                    uint16_t* round_off, uint16_t* thr_round_off, uint32_t* valid_bits, uint8_t* border_in)
+                    uint16_t* round_off, uint16_t* thr_round_off, uint16_t* tails, uint32_t* valid_bits,
+                    uint8_t* border_in)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TileSmem& sm = *reinterpret_cast<TileSmem*>(smem_raw);
     const int64_t tile = blockIdx.x;
     const int64_t tr = tile / g.tcols, tc = tile % g.tcols;
-    const int t = threadIdx.x, lane = t & 31;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     uint16_t* rstart = reinterpret_cast<uint16_t*>(sm.hi);                        // <= 4097 round starts
     uint8_t* thr = reinterpret_cast<uint8_t*>(sm.lo);                             // through flag per cell
     uint16_t* trstart = reinterpret_cast<uint16_t*>(reinterpret_cast<uint8_t*>(sm.lo) + kTileCells);
     int head = 0, count = tile_prepare(sm, fd, g, tr, tc), r = 0;
-    // the rounds of the round solve (tile_solve without values)
+    // the rounds: a round holds the cells whose in-tile upstream cells are all in earlier rounds
     while (count > 0) {
         int* next = &sm.round_count[(r + 1) % 3];
         const int next_base = head + count;
         if (t == 0) {
             if (!kCount) rstart[r] = (uint16_t)head;
-            sm.round_count[(r + 2) % 3] = 0;
+            sm.round_count[(r + 2) % 3] = 0;  // read by everyone two rounds ago
         }
         for (int k0 = 0; k0 < count; k0 += kTileThreads) {
             int k = k0 + t, d = kNoCell;
@@ -461,10 +462,40 @@ __global__ void __launch_bounds__(kTileThreads)
         if (lane == 0) valid_bits[tile * (kTileCells / 32) + (i >> 5)] = bal;
     }
     __syncthreads();
+    // Inside each round, order the cells by decreasing number of in-tile upstream cells, so that the
+    // lanes of a warp loop over the same number of neighbours.  The downstream indices (dsl) and the
+    // counters (cnt) are no longer needed: they hold the sorted order and the bucket counts.
+    uint16_t* ord = sm.dsl;
+    int* bucket = reinterpret_cast<int*>(sm.cnt);  // [0..8] counts, then fill positions
+    for (int q = 0; q < rounds; ++q) {
+        const int a = rstart[q], b = rstart[q + 1];
+        if (b - a == 1) {
+            if (t == 0) ord[a] = sm.queue[a];
+            continue;
+        }
+        if (t < 9) bucket[t] = 0;
+        __syncthreads();
+        for (int k = a + t; k < b; k += kTileThreads) atomicAdd(&bucket[8 - __popc(sm.up[sm.queue[k]])], 1);
+        __syncthreads();
+        if (t == 0) {
+            int acc = 0;
+            for (int j = 0; j < 9; ++j) {
+                int c = bucket[j];
+                bucket[j] = acc;
+                acc += c;
+            }
+        }
+        __syncthreads();
+        for (int k = a + t; k < b; k += kTileThreads) {
+            int i = sm.queue[k];
+            ord[a + atomicAdd(&bucket[8 - __popc(sm.up[i])], 1)] = (uint16_t)i;
+        }
+        __syncthreads();
+    }
     // through flags, round by round: an entry, or downstream of a through cell
     for (int q = 0; q < rounds; ++q) {
         for (int k = rstart[q] + t; k < rstart[q + 1]; k += kTileThreads) {
-            int i = sm.queue[k];
+            int i = ord[k];
             if (thr[i]) continue;
             unsigned m = sm.up[i];
             while (m) {
@@ -479,35 +510,55 @@ __global__ void __launch_bounds__(kTileThreads)
         __syncthreads();
     }
     for (int k = t; k < nvalid; k += kTileThreads) {
-        int i = sm.queue[k];
+        int i = ord[k];
         sched_order[tile * kTileCells + k] = (uint16_t)i;
         sched_upm[tile * kTileCells + k] = sm.up[i];
     }
-    if (t == 0) {
-        int j = 0;
-        for (int q = 0; q < rounds; ++q) {
-            trstart[q] = (uint16_t)j;
-            for (int k = rstart[q]; k < rstart[q + 1]; ++k) {
-                int i = sm.queue[k];
-                if (!thr[i]) continue;
+    // the through cells of each round, in the same order, with upstream masks restricted to through cells
+    int* wcount = bucket + 16;
+    int j = 0;
+    for (int q = 0; q < rounds; ++q) {
+        if (t == 0) trstart[q] = (uint16_t)j;
+        for (int k0 = rstart[q]; k0 < rstart[q + 1]; k0 += kTileThreads) {
+            const int k = k0 + t;
+            const int i = k < rstart[q + 1] ? ord[k] : 0;
+            const bool f = k < rstart[q + 1] && thr[i];
+            const unsigned bal = __ballot_sync(0xffffffffu, f);
+            if (lane == 0) wcount[warp] = __popc(bal);
+            __syncthreads();
+            int before = 0, all = 0;
+            for (int w = 0; w < kTileThreads / 32; ++w) {
+                before += w < warp ? wcount[w] : 0;
+                all += wcount[w];
+            }
+            if (f) {
                 unsigned m = sm.up[i], tm = 0;
                 while (m) {
                     int b = __ffs(m) - 1;
                     m &= m - 1;
                     if (thr[i + nb_dr(b) * kTile + nb_dc(b)]) tm |= 1u << b;
                 }
-                thr_order[tile * kTileCells + j] = (uint16_t)i;
-                thr_upm[tile * kTileCells + j] = (uint8_t)tm;
-                ++j;
+                const int pos = j + before + __popc(bal & ((1u << lane) - 1u));
+                thr_order[tile * kTileCells + pos] = (uint16_t)i;
+                thr_upm[tile * kTileCells + pos] = (uint8_t)tm;
             }
+            j += all;
+            __syncthreads();  // wcount is rewritten by the next chunk
         }
-        trstart[rounds] = (uint16_t)j;
     }
+    if (t == 0) trstart[rounds] = (uint16_t)j;
     __syncthreads();
     const int32_t base = round_base[tile];
     for (int q = t; q <= rounds; q += kTileThreads) {
         round_off[base + q] = rstart[q];
         thr_round_off[base + q] = trstart[q];
+    }
+    // first round of the warp phase: every later round holds at most 32 cells
+    if (t < 2) {
+        const uint16_t* st = t == 0 ? rstart : trstart;
+        int q = rounds;
+        while (q > 0 && st[q] - st[q - 1] <= 32) --q;
+        tails[tile * 2 + t] = (uint16_t)q;
     }
 }
 
@@ -518,6 +569,13 @@ __global__ void __launch_bounds__(kTileThreads)
 // Cell i of a scheduled round: source (hi/lo before the cell is done) + the float-float sum of the
 // upstream cells in mask m; NaN or a negative source makes the cell NaN; a sum that is not finite
 // (+inf material) is recomputed plainly so that it keeps IEEE semantics.
+__device__ __forceinline__ int tile_nb_offset(int q)
+{
+    static_assert(kTile == 64, "neighbour offsets are packed for 64-cell rows");
+    // -65 -64 -63 -1 +1 +63 +64 +65 (NW N NE W E SW S SE) as signed bytes
+    return (int)(signed char)(unsigned)(0x41403F01FFC1C0BFull >> (8 * q));
+}
+
 __device__ __forceinline__ void sched_cell(float* hi, float* lo, int i, unsigned m)
 {
     const float x = hi[i];
@@ -525,9 +583,8 @@ __device__ __forceinline__ void sched_cell(float* hi, float* lo, int i, unsigned
     bool nan = isnan(x) || !(x >= 0.0f);
     unsigned mm = m;
     while (mm) {
-        int q = __ffs(mm) - 1;
+        int u = i + tile_nb_offset(__ffs(mm) - 1);
         mm &= mm - 1;
-        int u = i + nb_dr(q) * kTile + nb_dc(q);
         float h = hi[u], ts, te;
         nan |= isnan(h);
         two_sum(s, h, ts, te);
@@ -539,9 +596,8 @@ __device__ __forceinline__ void sched_cell(float* hi, float* lo, int i, unsigned
     if (!isfinite(h)) {
         float p = x;
         while (m) {
-            int q = __ffs(m) - 1;
+            p += hi[i + tile_nb_offset(__ffs(m) - 1)];
             m &= m - 1;
-            p += hi[i + nb_dr(q) * kTile + nb_dc(q)];
         }
         h = p;
         l = 0.0f;
@@ -554,74 +610,173 @@ __device__ __forceinline__ void sched_cell(float* hi, float* lo, int i, unsigned
     lo[i] = l;
 }
 
-// Replay a tile's rounds: one barrier per non-empty round.
-__device__ __forceinline__ void sched_replay(float* hi, float* lo, const uint16_t* __restrict__ order,
+constexpr int kStagedRounds = 1023;  // round offsets held in shared memory; later ones are read from global
+
+// The tile's values and one of its schedules, in shared memory (47 KB).
+struct __align__(16) ReplaySmem {
+    float hi[kTileCells];
+    float lo[kTileCells];
+    uint16_t order[kTileCells];
+    uint8_t upm[kTileCells];
+    uint16_t off[kStagedRounds + 1];
+};
+
+// Stage a schedule (order, masks: always the full 12 KB, so that the loads depend only on the tile
+// index; round offsets) in shared memory.  Loads first, then stores, so that all are in flight at once.
+__device__ __forceinline__ void replay_stage(ReplaySmem& sm, const uint16_t* __restrict__ order,
                                              const uint8_t* __restrict__ upm, const uint16_t* __restrict__ off,
                                              int rounds)
 {
     const int t = threadIdx.x;
-    int a = off[0];
-    for (int q = 0; q < rounds; ++q) {
-        const int b = off[q + 1];
+    const uint4* o4 = reinterpret_cast<const uint4*>(order);
+    const uint4 a = __ldg(o4 + t), b = __ldg(o4 + t + kTileThreads);
+    const uint4 c = __ldg(reinterpret_cast<const uint4*>(upm) + t);
+    const int staged = min(rounds, kStagedRounds) + 1;
+    uint16_t r0 = t < staged ? __ldg(off + t) : 0;
+    reinterpret_cast<uint4*>(sm.order)[t] = a;
+    reinterpret_cast<uint4*>(sm.order)[t + kTileThreads] = b;
+    reinterpret_cast<uint4*>(sm.upm)[t] = c;
+    if (t < staged) sm.off[t] = r0;
+    for (int q = t + kTileThreads; q < staged; q += kTileThreads) sm.off[q] = __ldg(off + q);
+}
+
+// Replay `rounds` rounds: rounds before `tail` by the whole block (a barrier after each non-empty one),
+// the rest (at most 32 cells each) by warp 0 alone.  Ends with a block barrier.
+__device__ __forceinline__ void replay(ReplaySmem& sm, const uint16_t* __restrict__ off_g, int rounds, int tail)
+{
+    const int t = threadIdx.x;
+    auto off = [&](int q) -> int { return q <= kStagedRounds ? sm.off[q] : __ldg(off_g + q); };
+    int a = off(0);
+    for (int q = 0; q < tail; ++q) {
+        const int b = off(q + 1);
         if (b == a) continue;
-        for (int k = a + t; k < b; k += kTileThreads) sched_cell(hi, lo, order[k], upm[k]);
+        for (int k = a + t; k < b; k += kTileThreads) sched_cell(sm.hi, sm.lo, sm.order[k], sm.upm[k]);
         __syncthreads();
         a = b;
     }
+    if (t < 32) {
+        for (int q = tail; q < rounds; ++q) {
+            const int b = off(q + 1);
+            if (a + t < b) sched_cell(sm.hi, sm.lo, sm.order[a + t], sm.upm[a + t]);
+            __syncwarp();
+            a = b;
+        }
+    }
+    __syncthreads();
 }
 
-// Pass 1: local accu inside each tile; local exit values to P (post-order); material total bound.
-__global__ void __launch_bounds__(kTileThreads)
-    k_tile_local(TileGeom g, const float* __restrict__ ext, float ext_s, float* __restrict__ out,
-                 const uint16_t* __restrict__ sched_order, const uint8_t* __restrict__ sched_upm,
-                 const int32_t* __restrict__ round_base, const uint16_t* __restrict__ round_off,
-                 const uint32_t* __restrict__ valid_bits, const int32_t* __restrict__ exit_base,
-                 const uint16_t* __restrict__ exit_local, const uint32_t* __restrict__ exit_pos,
-                 float2* __restrict__ P, unsigned long long* block_total)
+// Cells of a tile by thread: thread t holds the 4 x 4 cells (row (t + 256 j) / 16, columns 4 ((t + 256 j)
+// % 16) .. + 3), j = 0..3, so that a row of the tile is 16 float4.
+__device__ __forceinline__ int quad_cell(int j) { return ((threadIdx.x + kTileThreads * j) >> 4) * kTile + ((threadIdx.x + kTileThreads * j) & 15) * 4; }
+
+__device__ __forceinline__ float4 load_quad(const float* __restrict__ p, const TileGeom& g, int64_t r, int64_t c,
+                                            bool vec, float fill)
 {
-    __shared__ float hi[kTileCells];
-    __shared__ float lo[kTileCells];
+    if (vec) {
+        if (r < g.rows && c < g.cols) return __ldg(reinterpret_cast<const float4*>(p + r * g.cols + c));
+        return make_float4(fill, fill, fill, fill);
+    }
+    float v[4];
+#pragma unroll
+    for (int x = 0; x < 4; ++x) v[x] = (r < g.rows && c + x < g.cols) ? __ldg(p + r * g.cols + c + x) : fill;
+    return make_float4(v[0], v[1], v[2], v[3]);
+}
+
+__device__ __forceinline__ void store_quad(float* __restrict__ p, const TileGeom& g, int64_t r, int64_t c, bool vec,
+                                           float4 v)
+{
+    if (r >= g.rows) return;
+    if (vec) {
+        if (c < g.cols) *reinterpret_cast<float4*>(p + r * g.cols + c) = v;
+        return;
+    }
+    const float w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int x = 0; x < 4; ++x)
+        if (c + x < g.cols) p[r * g.cols + c + x] = w[x];
+}
+
+struct TileSched {
+    const int32_t* round_base;
+    const uint16_t* order;
+    const uint8_t* upm;
+    const uint16_t* off;
+    const uint16_t* thr_order;
+    const uint8_t* thr_upm;
+    const uint16_t* thr_off;
+    const uint16_t* tails;
+    const uint32_t* valid_bits;
+    const uint8_t* border_in;
+    const int32_t* halo_exit;
+};
+
+// Pass 1: local accu inside each tile; local exit values to P (post-order); material total bound.
+// vec: material and result rows can be moved as float4 (16-byte aligned, columns a multiple of 4).
+__global__ void __launch_bounds__(kTileThreads)
+    k_tile_local(TileGeom g, const float* __restrict__ ext, float ext_s, bool vec, float* __restrict__ out,
+                 TileSched sc, const int32_t* __restrict__ exit_base, const uint16_t* __restrict__ exit_local,
+                 const uint32_t* __restrict__ exit_pos, float2* __restrict__ P, unsigned long long* block_total)
+{
+    __shared__ ReplaySmem sm;
     __shared__ float warp_sum[kTileThreads / 32];
     __shared__ int warp_inf[kTileThreads / 32];
     const int64_t tile = blockIdx.x;
     const int64_t tr = tile / g.tcols, tc = tile % g.tcols;
     const int t = threadIdx.x;
-    FF sum{0.0f, 0.0f};
+    const int32_t rb = __ldg(sc.round_base + tile);
+    const int rounds = __ldg(sc.round_base + tile + 1) - rb - 1;
+    const int tail = __ldg(sc.tails + 2 * tile);
+    const int32_t e0 = __ldg(exit_base + tile), ne = __ldg(exit_base + tile + 1) - e0;
+    // material and valid bits of this thread's 16 cells
+    float4 x[4];
+    uint32_t vbits[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int cell = quad_cell(j);
+        const int64_t r = tr * kTile + (cell >> 6), c = tc * kTile + (cell & 63);
+        x[j] = ext ? load_quad(ext, g, r, c, vec, 0.0f) : make_float4(ext_s, ext_s, ext_s, ext_s);
+        vbits[j] = __ldg(sc.valid_bits + tile * (kTileCells / 32) + (cell >> 5)) >> (cell & 31);
+    }
+    replay_stage(sm, sc.order + tile * kTileCells, sc.upm + tile * kTileCells, sc.off + rb, rounds);
+    int my_loc = -1;
+    uint32_t my_pos = 0;
+    if (t < ne) {  // a tile has at most 252 exits (its border cells)
+        my_loc = __ldg(exit_local + e0 + t);
+        my_pos = __ldg(exit_pos + e0 + t);
+    }
+    float sum = 0.0f;
     bool inf = false;
-#pragma unroll 4
-    for (int k = 0; k < kTileCells / kTileThreads; ++k) {
-        int i = t + k * kTileThreads;
-        int64_t r = tr * kTile + (i >> 6), c = tc * kTile + (i & 63);
-        float x = 0.0f;
-        if (r < g.rows && c < g.cols) x = ext ? __ldg(ext + r * g.cols + c) : ext_s;
-        hi[i] = x;
-        lo[i] = 0.0f;
-        if (isinf(x) && x > 0.0f) inf = true;
-        else if (x > 0.0f) sum.add(x);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int cell = quad_cell(j);
+        float v[4] = {x[j].x, x[j].y, x[j].z, x[j].w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if ((vbits[j] >> k) & 1u) {
+                if (isinf(v[k]) && v[k] > 0.0f) inf = true;
+                else if (v[k] > 0.0f) sum += v[k];
+            } else {
+                v[k] = __int_as_float(0x7fc00000);  // no-data flow direction: never read, result NaN
+            }
+        }
+        *reinterpret_cast<float4*>(sm.hi + cell) = make_float4(v[0], v[1], v[2], v[3]);
+        *reinterpret_cast<float4*>(sm.lo + cell) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
     __syncthreads();
-    const int32_t rb = round_base[tile];
-    sched_replay(hi, lo, sched_order + tile * kTileCells, sched_upm + tile * kTileCells, round_off + rb,
-                 round_base[tile + 1] - rb - 1);
-#pragma unroll 4
-    for (int k = 0; k < kTileCells / kTileThreads; ++k) {
-        int i = t + k * kTileThreads;
-        int64_t r = tr * kTile + (i >> 6), c = tc * kTile + (i & 63);
-        if (r < g.rows && c < g.cols) {
-            bool valid = (valid_bits[tile * (kTileCells / 32) + (i >> 5)] >> (i & 31)) & 1u;
-            out[r * g.cols + c] = valid ? hi[i] : __int_as_float(0x7fc00000);
-        }
+    replay(sm, sc.off + rb, rounds, tail);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int cell = quad_cell(j);
+        store_quad(out, g, tr * kTile + (cell >> 6), tc * kTile + (cell & 63), vec,
+                   *reinterpret_cast<const float4*>(sm.hi + cell));
     }
-    for (int32_t e = exit_base[tile] + t; e < exit_base[tile + 1]; e += kTileThreads) {
-        int loc = exit_local[e];
-        P[exit_pos[e]] = make_float2(hi[loc], lo[loc]);
-    }
-    // upper bound of this tile's material total, in 2^-16 units; ~0 marks +inf or overflow
-    float s = sum.hi + sum.lo;
-    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    if (my_loc >= 0) P[my_pos] = make_float2(sm.hi[my_loc], sm.lo[my_loc]);
+    // upper bound of this tile's material total, in 2^-16 units; ~0 marks +inf or overflow.  A float
+    // sum of <= 4096 non-negative terms is within 4096 * 2^-24 of the exact sum, inside the 1e-4 margin.
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
     unsigned any_inf = __any_sync(0xffffffffu, inf);
     if ((t & 31) == 0) {
-        warp_sum[t >> 5] = s;
+        warp_sum[t >> 5] = sum;
         warp_inf[t >> 5] = any_inf ? 1 : 0;
     }
     __syncthreads();
@@ -777,72 +932,83 @@ __global__ void k_exit_sums(int64_t n, const uint32_t* __restrict__ pos, const u
 
 // Pass 3: add the inflow entering each tile to every cell downstream of a tile entry.
 __global__ void __launch_bounds__(kTileThreads)
-    k_tile_fixup(TileGeom g, float* __restrict__ out, const uint16_t* __restrict__ thr_order,
-                 const uint8_t* __restrict__ thr_upm, const int32_t* __restrict__ round_base,
-                 const uint16_t* __restrict__ thr_round_off, const uint8_t* __restrict__ border_in,
-                 const int32_t* __restrict__ halo_exit, const uint4* __restrict__ A, const unsigned long long* total)
+    k_tile_fixup(TileGeom g, float* __restrict__ out, bool vec, TileSched sc, const uint4* __restrict__ A,
+                 const unsigned long long* total)
 {
-    __shared__ float hi[kTileCells];
-    __shared__ float lo[kTileCells];
+    __shared__ ReplaySmem sm;
     if (total[1]) return;
     const int F = fixed_point_bits(total[0]);
     const int64_t tile = blockIdx.x;
     const int64_t tr = tile / g.tcols, tc = tile % g.tcols;
     const int t = threadIdx.x;
-    const int32_t rb = round_base[tile];
-    const int rounds = round_base[tile + 1] - rb - 1;
-    const uint16_t* off = thr_round_off + rb;
-    const int nthr = off[rounds];
-    if (nthr == 0) return;  // uniform: nothing enters this tile
-    const uint16_t* order = thr_order + tile * kTileCells;
-    for (int k = t; k < nthr; k += kTileThreads) {
-        int i = order[k];
-        hi[i] = 0.0f;
-        lo[i] = 0.0f;
+    const int32_t rb = __ldg(sc.round_base + tile);
+    const int rounds = __ldg(sc.round_base + tile + 1) - rb - 1;
+    const int tail = __ldg(sc.tails + 2 * tile + 1);
+    const unsigned in_mask = t < kBorderCells ? __ldg(sc.border_in + tile * kBorderCells + t) : 0u;
+    replay_stage(sm, sc.thr_order + tile * kTileCells, sc.thr_upm + tile * kTileCells, sc.thr_off + rb, rounds);
+    float4 o[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int cell = quad_cell(j);
+        o[j] = load_quad(out, g, tr * kTile + (cell >> 6), tc * kTile + (cell & 63), vec, 0.0f);
+        *reinterpret_cast<float4*>(sm.hi + cell) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        *reinterpret_cast<float4*>(sm.lo + cell) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
-    __syncthreads();
     // sources: border cells gather the exact subtree sums of the halo exits draining into them
-    if (t < kBorderCells) {
-        unsigned mask = border_in[tile * kBorderCells + t];
-        if (mask) {
-            int rin, cin;
-            if (t < kTile) { rin = 0; cin = t; }
-            else if (t < 2 * kTile) { rin = kTile - 1; cin = t - kTile; }
-            else if (t < 3 * kTile - 2) { rin = t - 2 * kTile + 1; cin = 0; }
-            else { rin = t - (3 * kTile - 2) + 1; cin = kTile - 1; }
-            u128 s = 0;
-            while (mask) {
-                int q = __ffs(mask) - 1;
-                mask &= mask - 1;
-                int32_t id = halo_exit[tile * kHaloSlots + halo_slot_of(rin + nb_dr(q), cin + nb_dc(q))];
-                if (id >= 0) s += to_u128(A[id]);
-            }
-            int i = rin * kTile + cin;
-            if ((s >> 96) != 0) {
-                hi[i] = __int_as_float(0x7fc00000);
-            } else {
-                double d = fixed_to_double(s, F);
-                float h = __double2float_rn(d);
-                hi[i] = h;
-                lo[i] = __double2float_rn(d - (double)h);
-            }
+    u128 src = 0;
+    int src_cell = -1;
+    if (in_mask) {
+        int rin, cin;
+        if (t < kTile) { rin = 0; cin = t; }
+        else if (t < 2 * kTile) { rin = kTile - 1; cin = t - kTile; }
+        else if (t < 3 * kTile - 2) { rin = t - 2 * kTile + 1; cin = 0; }
+        else { rin = t - (3 * kTile - 2) + 1; cin = kTile - 1; }
+        unsigned m = in_mask;
+        while (m) {
+            int q = __ffs(m) - 1;
+            m &= m - 1;
+            int32_t id = __ldg(sc.halo_exit + tile * kHaloSlots + halo_slot_of(rin + nb_dr(q), cin + nb_dc(q)));
+            if (id >= 0) src += to_u128(A[id]);
+        }
+        src_cell = rin * kTile + cin;
+    }
+    __syncthreads();  // the zeroing is done before the sources are written
+    if (src_cell >= 0) {
+        if ((src >> 96) != 0) {
+            sm.hi[src_cell] = __int_as_float(0x7fc00000);
+        } else {
+            double d = fixed_to_double(src, F);
+            float h = __double2float_rn(d);
+            sm.hi[src_cell] = h;
+            sm.lo[src_cell] = __double2float_rn(d - (double)h);
         }
     }
     __syncthreads();
-    sched_replay(hi, lo, order, thr_upm + tile * kTileCells, off, rounds);
-    for (int k = t; k < nthr; k += kTileThreads) {
-        int i = order[k];
-        float h = hi[i], l = lo[i];
-        if (h == 0.0f && l == 0.0f) continue;
-        float* o = out + (tr * kTile + (i >> 6)) * g.cols + tc * kTile + (i & 63);
-        if (isnan(h)) {
-            *o = __int_as_float(0x7fc00000);
-        } else {
-            FF v{*o, 0.0f};
-            v.add(h, l);
-            v.normalise();
-            *o = v.hi;
+    replay(sm, sc.thr_off + rb, rounds, tail);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int cell = quad_cell(j);
+        const float4 h4 = *reinterpret_cast<const float4*>(sm.hi + cell);
+        const float4 l4 = *reinterpret_cast<const float4*>(sm.lo + cell);
+        const float hv[4] = {h4.x, h4.y, h4.z, h4.w}, lv[4] = {l4.x, l4.y, l4.z, l4.w};
+        float v[4] = {o[j].x, o[j].y, o[j].z, o[j].w};
+        bool changed = false;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (hv[k] == 0.0f && lv[k] == 0.0f) continue;
+            changed = true;
+            if (isnan(hv[k])) {
+                v[k] = __int_as_float(0x7fc00000);
+            } else {
+                FF f{v[k], 0.0f};
+                f.add(hv[k], lv[k]);
+                f.normalise();
+                v[k] = f.hi;
+            }
         }
+        if (changed)
+            store_quad(out, g, tr * kTile + (cell >> 6), tc * kTile + (cell & 63), vec,
+                       make_float4(v[0], v[1], v[2], v[3]));
     }
 }
 
@@ -979,7 +1145,8 @@ int tile_core_build(TopologyCore* core, cudaStream_t stream)
             "tile schedule");
         TRY(cudaMalloc(&tc->round_base, (nt + 1) * sizeof(int32_t)), "tile round base");
         k_tile_schedule<true><<<(unsigned)nt, kTileThreads, smem, stream>>>(
-            core->fd, g, count, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+            core->fd, g, count, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+            nullptr);
         TRY(cudaGetLastError(), "tile schedule");
         TRY(cudaMemcpyAsync(hcount.data(), count, nt * sizeof(int32_t), cudaMemcpyDeviceToHost, stream),
             "tile rounds");
@@ -1005,12 +1172,14 @@ int tile_core_build(TopologyCore* core, cudaStream_t stream)
         TRY(cudaMalloc(&tc->thr_upm, nt * kTileCells), "tile schedule");
         TRY(cudaMalloc(&tc->valid_bits, nt * (kTileCells / 32) * sizeof(uint32_t)), "tile valid bits");
         TRY(cudaMalloc(&tc->border_in, nt * kBorderCells), "tile border masks");
+        TRY(cudaMalloc(&tc->tails, nt * 2 * sizeof(uint16_t)), "tile warp-phase rounds");
         k_tile_schedule<false><<<(unsigned)nt, kTileThreads, smem, stream>>>(
             core->fd, g, nullptr, tc->round_base, tc->sched_order, tc->sched_upm, tc->thr_order, tc->thr_upm,
-            tc->round_off, tc->thr_round_off, tc->valid_bits, tc->border_in);
+            tc->round_off, tc->thr_round_off, tc->tails, tc->valid_bits, tc->border_in);
         TRY(cudaGetLastError(), "tile schedule");
         TRY(cudaStreamSynchronize(stream), "tile schedule");  // hbase must outlive its copy
-        tc->bytes += (nt + 1) * 4 + total * 4 + nt * kTileCells * 6 + nt * (kTileCells / 8) + nt * kBorderCells;
+        tc->bytes += (nt + 1) * 4 + total * 4 + nt * kTileCells * 6 + nt * (kTileCells / 8) + nt * kBorderCells +
+                     nt * 4;
     }
     cudaFree(bitmap);
     cudaFree(rowpref);
@@ -1069,6 +1238,7 @@ void tile_core_free(TileCore* tc)
     cudaFree(tc->thr_round_off);
     cudaFree(tc->valid_bits);
     cudaFree(tc->border_in);
+    cudaFree(tc->tails);
     delete tc;
 }
 
@@ -1107,9 +1277,14 @@ int tile_accu_f32(const TopologyCore* core, TileScratch* s, const float* ext, fl
 {
     const TileCore* tc = core->tiles;
     TileGeom g{core->rows, core->cols, tc->trows, tc->tcols};
-    k_tile_local<<<(unsigned)tc->ntiles, kTileThreads, 0, stream>>>(
-        g, ext, ext_s, out, tc->sched_order, tc->sched_upm, tc->round_base, tc->round_off, tc->valid_bits,
-        tc->exit_base, tc->exit_local, tc->exit_pos, s->P, s->block_total);
+    const TileSched sc{tc->round_base, tc->sched_order, tc->sched_upm, tc->round_off, tc->thr_order,
+                       tc->thr_upm,    tc->thr_round_off, tc->tails,     tc->valid_bits, tc->border_in,
+                       tc->halo_exit};
+    const bool vec_out = (reinterpret_cast<uintptr_t>(out) & 15) == 0 && (core->cols & 3) == 0;
+    const bool vec = vec_out && (!ext || (reinterpret_cast<uintptr_t>(ext) & 15) == 0);
+    k_tile_local<<<(unsigned)tc->ntiles, kTileThreads, 0, stream>>>(g, ext, ext_s, vec, out, sc, tc->exit_base,
+                                                                    tc->exit_local, tc->exit_pos, s->P,
+                                                                    s->block_total);
     k_total<<<1, 1024, 0, stream>>>(s->block_total, tc->ntiles, s->total);
     count_launches(2);
     const int64_t E = tc->nexit;
@@ -1119,9 +1294,7 @@ int tile_accu_f32(const TopologyCore* core, TileScratch* s, const float* ext, fl
         k_scan_blocks<<<1, kTileThreads, 0, stream>>>(s->block_sums, nb, s->total);
         k_scan_final<<<(unsigned)nb, kTileThreads, 0, stream>>>(s->P, E, s->total, s->block_sums, s->S);
         k_exit_sums<<<blocks_for(E, 256), 256, 0, stream>>>(E, tc->exit_pos, tc->exit_start, s->S, s->A, s->total);
-        k_tile_fixup<<<(unsigned)tc->ntiles, kTileThreads, 0, stream>>>(g, out, tc->thr_order, tc->thr_upm,
-                                                                        tc->round_base, tc->thr_round_off,
-                                                                        tc->border_in, tc->halo_exit, s->A, s->total);
+        k_tile_fixup<<<(unsigned)tc->ntiles, kTileThreads, 0, stream>>>(g, out, vec_out, sc, s->A, s->total);
         count_launches(5);
     }
     return cuda_status(cudaGetLastError(), "accu_f32 (tiles)");

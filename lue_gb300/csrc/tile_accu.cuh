@@ -50,6 +50,7 @@ struct TileCore {
     int32_t* round_base = nullptr;             // [ntiles + 1] first entry of each tile in round_off
     uint16_t* round_off = nullptr;             // per tile: rounds + 1 offsets into sched_order
     uint16_t* thr_round_off = nullptr;         // per tile: the same rounds' offsets into thr_order
+    uint16_t* tails = nullptr;                 // [ntiles * 2] first round of the warp phase (all, through)
     uint32_t* valid_bits = nullptr;            // [ntiles * 128] bit per cell: inside the array, not no-data
     uint8_t* border_in = nullptr;              // [ntiles * kBorderCells] per border cell: outside neighbours draining in
     int64_t bytes = 0;
