@@ -314,10 +314,11 @@ __global__ void k_halo_exits(const uint8_t* __restrict__ fd, TileGeom g, const i
 }
 
 // ---------------------------------------------------------------------------------------------------
-// Build: per-tile solve schedules
+// Build: per-tile flow forests in post-order
 // ---------------------------------------------------------------------------------------------------
 
 constexpr uint16_t kNoCell = 0xFFFFu;
+constexpr int kInvalidPos = 0x8000;  // tile_pos flag: no-data flow direction, or outside the array
 
 struct __align__(16) TileSmem {
     float hi[kTileCells];
@@ -381,33 +382,78 @@ __device__ __forceinline__ int tile_prepare(TileSmem& sm, const uint8_t* __restr
     return sm.round_count[0];
 }
 
-// Build: compile the solve schedule of one tile (CTA per tile).  The cells of the tile in the order the
-// round solve finishes them, the round boundaries, the cells downstream of a tile entry ("through"
-// cells) in the same rounds, the valid-cell bits and, per border cell, which outside neighbours drain
-// into it.  Every call then replays the schedule instead of re-deriving it from the flow direction.
-// kCount: first pass, only the number of rounds per tile (it sizes the round offset arrays).
-template <bool kCount>
+// In-tile linear offset of neighbour q (NW N NE W E SW S SE).
+__device__ __forceinline__ int tile_nb_offset(int q)
+{
+    static_assert(kTile == 64, "neighbour offsets are packed for 64-cell rows");
+    // -65 -64 -63 -1 +1 +63 +64 +65 as signed bytes
+    return (int)(signed char)(unsigned)(0x41403F01FFC1C0BFull >> (8 * q));
+}
+
+// Neighbour index (0..7, NW N NE W E SW S SE) of in-tile cell c as seen from its downstream cell d.
+__device__ __forceinline__ int nb_index_from(int d, int c)
+{
+    const int idx = ((c >> 6) - (d >> 6) + 1) * 3 + ((c & 63) - (d & 63) + 1);
+    return idx < 4 ? idx : idx - 1;
+}
+
+// Border cell b (0..251: N row, S row, W column, E column without corners) of a tile.
+__device__ __forceinline__ void border_cell(int b, int& rin, int& cin)
+{
+    if (b < kTile) { rin = 0; cin = b; }
+    else if (b < 2 * kTile) { rin = kTile - 1; cin = b - kTile; }
+    else if (b < 3 * kTile - 2) { rin = b - 2 * kTile + 1; cin = 0; }
+    else { rin = b - (3 * kTile - 2) + 1; cin = kTile - 1; }
+}
+
+// Exclusive prefix of one int per thread over the block; `total` gets the block sum.
+__device__ __forceinline__ int block_exclusive_int(int v, int* warp_tot, int& total)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    int before = 0;
+    total = 0;
+    for (int w = 0; w < kTileThreads / 32; ++w) {
+        const int s = warp_tot[w];
+        before += w < warp ? s : 0;
+        total += s;
+    }
+    __syncthreads();  // warp_tot may be reused
+    return before + x - v;
+}
+
+// Build: the flow forest of one tile (CTA per tile), in post-order.  A cell's in-tile upstream cells
+// (its subtree) get the positions start .. pos - 1 and the cell itself pos, so that the accu of any cell
+// is the difference of two prefix sums over the material laid out in post-order.  Cells with a no-data
+// flow direction (or outside the array) take the positions after the valid cells, flagged kInvalidPos.
+// Also: each exit's (pos, start) and, per border cell, which outside neighbours drain into it.
 __global__ void __launch_bounds__(kTileThreads)
-    k_tile_schedule(const uint8_t* __restrict__ fd, TileGeom g, int32_t* rounds_out, const int32_t* round_base,
-                    uint16_t* sched_order, uint8_t* sched_upm, uint16_t* thr_order, uint8_t* thr_upm,
-                    uint16_t* round_off, uint16_t* thr_round_off, uint16_t* tails, uint32_t* valid_bits,
-                    uint8_t* border_in)
+    k_tile_forest(const uint8_t* __restrict__ fd, TileGeom g, const int32_t* __restrict__ exit_base,
+                  const uint16_t* __restrict__ exit_local, uint16_t* tile_pos, uint16_t* tile_start,
+                  uint32_t* exit_span, uint8_t* border_in, int* error)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TileSmem& sm = *reinterpret_cast<TileSmem*>(smem_raw);
     const int64_t tile = blockIdx.x;
     const int64_t tr = tile / g.tcols, tc = tile % g.tcols;
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    uint16_t* rstart = reinterpret_cast<uint16_t*>(sm.hi);                        // <= 4097 round starts
-    uint8_t* thr = reinterpret_cast<uint8_t*>(sm.lo);                             // through flag per cell
-    uint16_t* trstart = reinterpret_cast<uint16_t*>(reinterpret_cast<uint8_t*>(sm.lo) + kTileCells);
+    const int t = threadIdx.x, lane = t & 31;
+    uint16_t* rstart = reinterpret_cast<uint16_t*>(sm.hi);  // <= 4097 round starts
+    uint16_t* sz = reinterpret_cast<uint16_t*>(sm.lo);      // subtree size
+    uint16_t* st = sz + kTileCells;                         // first position of the subtree
     int head = 0, count = tile_prepare(sm, fd, g, tr, tc), r = 0;
-    // the rounds: a round holds the cells whose in-tile upstream cells are all in earlier rounds
+    // rounds: a round holds the cells whose in-tile upstream cells are all in earlier rounds
     while (count > 0) {
         int* next = &sm.round_count[(r + 1) % 3];
         const int next_base = head + count;
         if (t == 0) {
-            if (!kCount) rstart[r] = (uint16_t)head;
+            rstart[r] = (uint16_t)head;
             sm.round_count[(r + 2) % 3] = 0;  // read by everyone two rounds ago
         }
         for (int k0 = 0; k0 < count; k0 += kTileThreads) {
@@ -431,243 +477,188 @@ __global__ void __launch_bounds__(kTileThreads)
         ++r;
     }
     const int rounds = r, nvalid = head;
-    if (kCount) {
-        if (t == 0) rounds_out[tile] = rounds;
-        return;
-    }
     if (t == 0) rstart[rounds] = (uint16_t)nvalid;
-    // entries (valid cells with an outside neighbour draining in), border masks, valid bits
+    __syncthreads();
+    // subtree sizes, upstream first
+    for (int q = 0; q < rounds; ++q) {
+        for (int k = rstart[q] + t; k < rstart[q + 1]; k += kTileThreads) {
+            const int i = sm.queue[k];
+            unsigned m = sm.up[i];
+            int size = 1;
+            while (m) {
+                size += sz[i + tile_nb_offset(__ffs(m) - 1)];
+                m &= m - 1;
+            }
+            sz[i] = (uint16_t)size;
+        }
+        __syncthreads();
+    }
+    // roots (valid cells without an in-tile downstream cell) and invalid cells, in cell order: thread t
+    // owns cells 16 t .. 16 t + 15
+    int* wt = reinterpret_cast<int*>(sm.cnt);  // the counters are free after the rounds
+    int root_sum = 0, invalid = 0;
+    for (int j = 0; j < 16; ++j) {
+        const int i = 16 * t + j;
+        if (sm.fd[(i >> 6) + 1][(i & 63) + 1] == kNoData) ++invalid;
+        else if (sm.dsl[i] == kNoCell) root_sum += sz[i];
+    }
+    int root_total, invalid_total;
+    int root_base = block_exclusive_int(root_sum, wt, root_total);
+    int invalid_base = nvalid + block_exclusive_int(invalid, wt, invalid_total);
+    for (int j = 0; j < 16; ++j) {
+        const int i = 16 * t + j;
+        if (sm.fd[(i >> 6) + 1][(i & 63) + 1] == kNoData) {
+            st[i] = (uint16_t)invalid_base++;
+            sz[i] = 1;
+        } else if (sm.dsl[i] == kNoCell) {
+            st[i] = (uint16_t)root_base;
+            root_base += sz[i];
+        }
+    }
+    __syncthreads();
+    // the other cells, downstream first: after the siblings that come before them
+    for (int q = rounds - 1; q >= 0; --q) {
+        for (int k = rstart[q] + t; k < rstart[q + 1]; k += kTileThreads) {
+            const int i = sm.queue[k], d = sm.dsl[i];
+            if (d == kNoCell) continue;
+            unsigned m = sm.up[d] & ((1u << nb_index_from(d, i)) - 1u);
+            int o = st[d];
+            while (m) {
+                o += sz[d + tile_nb_offset(__ffs(m) - 1)];
+                m &= m - 1;
+            }
+            st[i] = (uint16_t)o;
+        }
+        __syncthreads();
+    }
+    // positions, checked to be a permutation of 0 .. 4095
+    uint32_t* seen = reinterpret_cast<uint32_t*>(sm.queue);  // the queue is no longer read
+    if (t < kTileCells / 32) seen[t] = 0;
+    __syncthreads();
     for (int i = t; i < kTileCells; i += kTileThreads) {
-        int rin = i >> 6, cin = i & 63;
-        bool valid = sm.fd[rin + 1][cin + 1] != kNoData;
-        bool border = rin == 0 || rin == kTile - 1 || cin == 0 || cin == kTile - 1;
+        const bool valid = sm.fd[(i >> 6) + 1][(i & 63) + 1] != kNoData;
+        const int s0 = st[i], p = s0 + sz[i] - 1;
+        bool bad = p >= kTileCells || s0 > p;
+        if (!bad) bad = (atomicOr(&seen[p >> 5], 1u << (p & 31)) >> (p & 31)) & 1u;
+        if (bad) *error = 1;
+        tile_pos[tile * kTileCells + i] = (uint16_t)((p & (kTileCells - 1)) | (valid ? 0 : kInvalidPos));
+        tile_start[tile * kTileCells + i] = (uint16_t)(s0 & (kTileCells - 1));
+    }
+    const int32_t e0 = exit_base[tile], ne = exit_base[tile + 1] - e0;
+    for (int e = t; e < ne; e += kTileThreads) {
+        const int loc = exit_local[e0 + e];
+        exit_span[e0 + e] = (uint32_t)(st[loc] + sz[loc] - 1) | ((uint32_t)st[loc] << 16);
+    }
+    for (int b = t; b < kBorderCells; b += kTileThreads) {
+        int rin, cin;
+        border_cell(b, rin, cin);
         unsigned outside = 0;
-        if (valid && border) {
+        if (sm.fd[rin + 1][cin + 1] != kNoData) {
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-                int hr = rin + nb_dr(q), hc = cin + nb_dc(q);
+                const int hr = rin + nb_dr(q), hc = cin + nb_dc(q);
                 if (hr >= 0 && hr < kTile && hc >= 0 && hc < kTile) continue;
                 if (sm.fd[hr + 1][hc + 1] == nb_inflow_code(q)) outside |= 1u << q;
             }
         }
-        thr[i] = outside ? 1 : 0;
-        if (border) {
-            int b = rin == 0           ? cin
-                    : rin == kTile - 1 ? kTile + cin
-                    : cin == 0         ? 2 * kTile + rin - 1
-                                       : 3 * kTile - 2 + rin - 1;
-            border_in[tile * kBorderCells + b] = (uint8_t)outside;
-        }
-        unsigned bal = __ballot_sync(0xffffffffu, valid);
-        if (lane == 0) valid_bits[tile * (kTileCells / 32) + (i >> 5)] = bal;
-    }
-    __syncthreads();
-    // Inside each round, order the cells by decreasing number of in-tile upstream cells, so that the
-    // lanes of a warp loop over the same number of neighbours.  The downstream indices (dsl) and the
-    // counters (cnt) are no longer needed: they hold the sorted order and the bucket counts.
-    uint16_t* ord = sm.dsl;
-    int* bucket = reinterpret_cast<int*>(sm.cnt);  // [0..8] counts, then fill positions
-    for (int q = 0; q < rounds; ++q) {
-        const int a = rstart[q], b = rstart[q + 1];
-        if (b - a == 1) {
-            if (t == 0) ord[a] = sm.queue[a];
-            continue;
-        }
-        if (t < 9) bucket[t] = 0;
-        __syncthreads();
-        for (int k = a + t; k < b; k += kTileThreads) atomicAdd(&bucket[8 - __popc(sm.up[sm.queue[k]])], 1);
-        __syncthreads();
-        if (t == 0) {
-            int acc = 0;
-            for (int j = 0; j < 9; ++j) {
-                int c = bucket[j];
-                bucket[j] = acc;
-                acc += c;
-            }
-        }
-        __syncthreads();
-        for (int k = a + t; k < b; k += kTileThreads) {
-            int i = sm.queue[k];
-            ord[a + atomicAdd(&bucket[8 - __popc(sm.up[i])], 1)] = (uint16_t)i;
-        }
-        __syncthreads();
-    }
-    // through flags, round by round: an entry, or downstream of a through cell
-    for (int q = 0; q < rounds; ++q) {
-        for (int k = rstart[q] + t; k < rstart[q + 1]; k += kTileThreads) {
-            int i = ord[k];
-            if (thr[i]) continue;
-            unsigned m = sm.up[i];
-            while (m) {
-                int b = __ffs(m) - 1;
-                m &= m - 1;
-                if (thr[i + nb_dr(b) * kTile + nb_dc(b)]) {
-                    thr[i] = 1;
-                    break;
-                }
-            }
-        }
-        __syncthreads();
-    }
-    for (int k = t; k < nvalid; k += kTileThreads) {
-        int i = ord[k];
-        sched_order[tile * kTileCells + k] = (uint16_t)i;
-        sched_upm[tile * kTileCells + k] = sm.up[i];
-    }
-    // the through cells of each round, in the same order, with upstream masks restricted to through cells
-    int* wcount = bucket + 16;
-    int j = 0;
-    for (int q = 0; q < rounds; ++q) {
-        if (t == 0) trstart[q] = (uint16_t)j;
-        for (int k0 = rstart[q]; k0 < rstart[q + 1]; k0 += kTileThreads) {
-            const int k = k0 + t;
-            const int i = k < rstart[q + 1] ? ord[k] : 0;
-            const bool f = k < rstart[q + 1] && thr[i];
-            const unsigned bal = __ballot_sync(0xffffffffu, f);
-            if (lane == 0) wcount[warp] = __popc(bal);
-            __syncthreads();
-            int before = 0, all = 0;
-            for (int w = 0; w < kTileThreads / 32; ++w) {
-                before += w < warp ? wcount[w] : 0;
-                all += wcount[w];
-            }
-            if (f) {
-                unsigned m = sm.up[i], tm = 0;
-                while (m) {
-                    int b = __ffs(m) - 1;
-                    m &= m - 1;
-                    if (thr[i + nb_dr(b) * kTile + nb_dc(b)]) tm |= 1u << b;
-                }
-                const int pos = j + before + __popc(bal & ((1u << lane) - 1u));
-                thr_order[tile * kTileCells + pos] = (uint16_t)i;
-                thr_upm[tile * kTileCells + pos] = (uint8_t)tm;
-            }
-            j += all;
-            __syncthreads();  // wcount is rewritten by the next chunk
-        }
-    }
-    if (t == 0) trstart[rounds] = (uint16_t)j;
-    __syncthreads();
-    const int32_t base = round_base[tile];
-    for (int q = t; q <= rounds; q += kTileThreads) {
-        round_off[base + q] = rstart[q];
-        thr_round_off[base + q] = trstart[q];
-    }
-    // first round of the warp phase: every later round holds at most 32 cells
-    if (t < 2) {
-        const uint16_t* st = t == 0 ? rstart : trstart;
-        int q = rounds;
-        while (q > 0 && st[q] - st[q - 1] <= 32) --q;
-        tails[tile * 2 + t] = (uint16_t)q;
+        border_in[tile * kBorderCells + b] = (uint8_t)outside;
     }
 }
 
 // ---------------------------------------------------------------------------------------------------
 // Per call
 // ---------------------------------------------------------------------------------------------------
+//
+// Inside a tile the material is summed in 64-bit fixed point, round(x * 2^F) with F chosen per tile so
+// that the tile's total stays below 2^62: prefix sums over the post-order are then exact, and so is every
+// subtree sum taken as their difference (modulo 2^64, which is exact because the true sum is < 2^64).
+// A term x > 0 is represented to within 2^-(F+1) absolute; a tile whose smallest positive term would
+// carry fewer than 19 bits (x * 2^F < 2^19: a range of more than 2^43 between the tile total and its
+// smallest term) or that holds +inf asks for the walk engine instead.
 
-// Cell i of a scheduled round: source (hi/lo before the cell is done) + the float-float sum of the
-// upstream cells in mask m; NaN or a negative source makes the cell NaN; a sum that is not finite
-// (+inf material) is recomputed plainly so that it keeps IEEE semantics.
-__device__ __forceinline__ int tile_nb_offset(int q)
+constexpr int kScanSlots = kTileCells + kTileCells / 16;  // one padding slot per 16 positions
+constexpr float kMinQuantum = 524288.0f;                  // 2^19
+
+__device__ __forceinline__ int scan_slot(int k) { return k + (k >> 4); }
+
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }  // -126 <= e <= 127
+
+// Largest F <= 126 with bound * 2^F < 2^62 (0 for bound 0).
+__device__ __forceinline__ int tile_scale(float bound)
 {
-    static_assert(kTile == 64, "neighbour offsets are packed for 64-cell rows");
-    // -65 -64 -63 -1 +1 +63 +64 +65 (NW N NE W E SW S SE) as signed bytes
-    return (int)(signed char)(unsigned)(0x41403F01FFC1C0BFull >> (8 * q));
+    if (!(bound > 0.0f)) return 0;
+    const int e = (int)((__float_as_uint(bound) >> 23) & 0xFFu) - 126;  // bound < 2^e
+    return min(62 - e, 126);
 }
 
-__device__ __forceinline__ void sched_cell(float* hi, float* lo, int i, unsigned m)
+// In-place inclusive prefix sums (modulo 2^64) of the 4096 post-order positions of a tile.  Thread t
+// owns positions 16 t .. 16 t + 15 (slots 17 t ..: the padding puts the lanes of a warp on distinct
+// banks).  Ends with a block barrier.
+__device__ __forceinline__ void tile_scan(unsigned long long* S, unsigned long long* warp_tot)
 {
-    const float x = hi[i];
-    float s = x, e = lo[i];
-    bool nan = isnan(x) || !(x >= 0.0f);
-    unsigned mm = m;
-    while (mm) {
-        int u = i + tile_nb_offset(__ffs(mm) - 1);
-        mm &= mm - 1;
-        float h = hi[u], ts, te;
-        nan |= isnan(h);
-        two_sum(s, h, ts, te);
-        s = ts;
-        e = __fadd_rn(e, __fadd_rn(te, lo[u]));
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    unsigned long long* mine = S + 17 * t;
+    unsigned long long tot = 0;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) tot += mine[j];
+    unsigned long long x = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
     }
-    float h = __fadd_rn(s, e);
-    float l = __fsub_rn(e, __fsub_rn(h, s));
-    if (!isfinite(h)) {
-        float p = x;
-        while (m) {
-            p += hi[i + tile_nb_offset(__ffs(m) - 1)];
-            m &= m - 1;
-        }
-        h = p;
-        l = 0.0f;
-    }
-    if (nan) {
-        h = __int_as_float(0x7fc00000);
-        l = 0.0f;
-    }
-    hi[i] = h;
-    lo[i] = l;
-}
-
-constexpr int kStagedRounds = 1023;  // round offsets held in shared memory; later ones are read from global
-
-// The tile's values and one of its schedules, in shared memory (47 KB).
-struct __align__(16) ReplaySmem {
-    float hi[kTileCells];
-    float lo[kTileCells];
-    uint16_t order[kTileCells];
-    uint8_t upm[kTileCells];
-    uint16_t off[kStagedRounds + 1];
-};
-
-// Stage a schedule (order, masks: always the full 12 KB, so that the loads depend only on the tile
-// index; round offsets) in shared memory.  Loads first, then stores, so that all are in flight at once.
-__device__ __forceinline__ void replay_stage(ReplaySmem& sm, const uint16_t* __restrict__ order,
-                                             const uint8_t* __restrict__ upm, const uint16_t* __restrict__ off,
-                                             int rounds)
-{
-    const int t = threadIdx.x;
-    const uint4* o4 = reinterpret_cast<const uint4*>(order);
-    const uint4 a = __ldg(o4 + t), b = __ldg(o4 + t + kTileThreads);
-    const uint4 c = __ldg(reinterpret_cast<const uint4*>(upm) + t);
-    const int staged = min(rounds, kStagedRounds) + 1;
-    uint16_t r0 = t < staged ? __ldg(off + t) : 0;
-    reinterpret_cast<uint4*>(sm.order)[t] = a;
-    reinterpret_cast<uint4*>(sm.order)[t + kTileThreads] = b;
-    reinterpret_cast<uint4*>(sm.upm)[t] = c;
-    if (t < staged) sm.off[t] = r0;
-    for (int q = t + kTileThreads; q < staged; q += kTileThreads) sm.off[q] = __ldg(off + q);
-}
-
-// Replay `rounds` rounds: rounds before `tail` by the whole block (a barrier after each non-empty one),
-// the rest (at most 32 cells each) by warp 0 alone.  Ends with a block barrier.
-__device__ __forceinline__ void replay(ReplaySmem& sm, const uint16_t* __restrict__ off_g, int rounds, int tail)
-{
-    const int t = threadIdx.x;
-    auto off = [&](int q) -> int { return q <= kStagedRounds ? sm.off[q] : __ldg(off_g + q); };
-    int a = off(0);
-    for (int q = 0; q < tail; ++q) {
-        const int b = off(q + 1);
-        if (b == a) continue;
-        for (int k = a + t; k < b; k += kTileThreads) sched_cell(sm.hi, sm.lo, sm.order[k], sm.upm[k]);
-        __syncthreads();
-        a = b;
-    }
-    if (t < 32) {
-        for (int q = tail; q < rounds; ++q) {
-            const int b = off(q + 1);
-            if (a + t < b) sched_cell(sm.hi, sm.lo, sm.order[a + t], sm.upm[a + t]);
-            __syncwarp();
-            a = b;
-        }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    unsigned long long run = x - tot;
+    for (int w = 0; w < warp; ++w) run += warp_tot[w];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        run += mine[j];
+        mine[j] = run;
     }
     __syncthreads();
 }
 
+__device__ __forceinline__ unsigned long long subtree_sum(const unsigned long long* S, int pos, int start)
+{
+    unsigned long long v = S[scan_slot(pos)];
+    if (start > 0) v -= S[scan_slot(start - 1)];
+    return v;
+}
+
+// A fixed-point value V * 2^-F as float-float (hi, lo).
+__device__ __forceinline__ float2 fixed64_to_ff(unsigned long long V, int F)
+{
+    const float h = __ull2float_rn(V);
+    const long long r = (long long)(V - __float2ull_rn(h));
+    const float s = pow2f(-F);
+    return make_float2(h * s, __ll2float_rn(r) * s);
+}
+
+// A 96-bit fixed-point value v * 2^-F, rounded to float (the bits below the top 64 are dropped).
+__device__ __forceinline__ float fixed128_to_float(u128 v, int F)
+{
+    const unsigned long long hi = (unsigned long long)(v >> 64);
+    if (hi == 0) return ldexpf(__ull2float_rn((unsigned long long)v), -F);
+    const int shift = 64 - __clzll((long long)hi);
+    return ldexpf(__ull2float_rn((unsigned long long)(v >> shift)), shift - F);
+}
+
+// v * 2^d rounded to the nearest integer (v < 2^96; the result is known to be < 2^62).
+__device__ __forceinline__ unsigned long long rescale_fixed(u128 v, int d)
+{
+    if (d >= 0) return d >= 64 ? 0ull : (unsigned long long)(v << d);  // d >= 62 leaves room only for v == 0
+    if (d <= -97) return 0;
+    return (unsigned long long)((v + ((u128)1 << (-d - 1))) >> (-d));
+}
+
 // Cells of a tile by thread: thread t holds the 4 x 4 cells (row (t + 256 j) / 16, columns 4 ((t + 256 j)
 // % 16) .. + 3), j = 0..3, so that a row of the tile is 16 float4.
-__device__ __forceinline__ int quad_cell(int j) { return ((threadIdx.x + kTileThreads * j) >> 4) * kTile + ((threadIdx.x + kTileThreads * j) & 15) * 4; }
+__device__ __forceinline__ int quad_cell(int j)
+{
+    const int k = threadIdx.x + kTileThreads * j;
+    return (k >> 4) * kTile + (k & 15) * 4;
+}
 
 __device__ __forceinline__ float4 load_quad(const float* __restrict__ p, const TileGeom& g, int64_t r, int64_t c,
                                             bool vec, float fill)
@@ -696,99 +687,139 @@ __device__ __forceinline__ void store_quad(float* __restrict__ p, const TileGeom
         if (c + x < g.cols) p[r * g.cols + c + x] = w[x];
 }
 
-struct TileSched {
-    const int32_t* round_base;
-    const uint16_t* order;
-    const uint8_t* upm;
-    const uint16_t* off;
-    const uint16_t* thr_order;
-    const uint8_t* thr_upm;
-    const uint16_t* thr_off;
-    const uint16_t* tails;
-    const uint32_t* valid_bits;
+__device__ __forceinline__ float quad_at(const float4& q, int k) { return k == 0 ? q.x : k == 1 ? q.y : k == 2 ? q.z : q.w; }
+__device__ __forceinline__ int half_at(const uint2& q, int k)
+{
+    return (int)(((k < 2 ? q.x : q.y) >> (16 * (k & 1))) & 0xFFFFu);
+}
+
+struct TileForest {
+    const uint16_t* pos;
+    const uint16_t* start;
     const uint8_t* border_in;
     const int32_t* halo_exit;
 };
 
-// Pass 1: local accu inside each tile; local exit values to P (post-order); material total bound.
-// vec: material and result rows can be moved as float4 (16-byte aligned, columns a multiple of 4).
-__global__ void __launch_bounds__(kTileThreads)
-    k_tile_local(TileGeom g, const float* __restrict__ ext, float ext_s, bool vec, float* __restrict__ out,
-                 TileSched sc, const int32_t* __restrict__ exit_base, const uint16_t* __restrict__ exit_local,
+// Tile reductions: sum and minimum of the positive finite terms, flags (1: +inf, 2: NaN or negative).
+struct TileReduce {
+    float sum[kTileThreads / 32];
+    float min[kTileThreads / 32];
+    int flags[kTileThreads / 32];
+};
+
+__device__ __forceinline__ void tile_reduce(TileReduce& red, float sum, float mn, int flags, float& tot, float& tmin,
+                                            int& tflags)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        flags |= __shfl_xor_sync(0xffffffffu, flags, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        red.sum[threadIdx.x >> 5] = sum;
+        red.min[threadIdx.x >> 5] = mn;
+        red.flags[threadIdx.x >> 5] = flags;
+    }
+    __syncthreads();
+    tot = 0.0f;
+    tmin = INFINITY;
+    tflags = 0;
+    for (int w = 0; w < kTileThreads / 32; ++w) {  // the same order in every thread
+        tot += red.sum[w];
+        tmin = fminf(tmin, red.min[w]);
+        tflags |= red.flags[w];
+    }
+}
+
+// Pass 1: the local value of every exit (the accu of its in-tile subtree) to P, in the exit forest's
+// post-order, and an upper bound of the tile's material total.  ~0 as the bound asks for the walk engine.
+// vec: material rows can be read as float4 (16-byte aligned, columns a multiple of 4).
+__global__ void __launch_bounds__(kTileThreads, 4)
+    k_tile_exits(TileGeom g, const float* __restrict__ ext, float ext_s, bool vec, TileForest f,
+                 const int32_t* __restrict__ exit_base, const uint32_t* __restrict__ exit_span,
                  const uint32_t* __restrict__ exit_pos, float2* __restrict__ P, unsigned long long* block_total)
 {
-    __shared__ ReplaySmem sm;
-    __shared__ float warp_sum[kTileThreads / 32];
-    __shared__ int warp_inf[kTileThreads / 32];
+    __shared__ unsigned long long S[kScanSlots];
+    __shared__ unsigned long long warp_tot[kTileThreads / 32];
+    __shared__ TileReduce red;
     const int64_t tile = blockIdx.x;
     const int64_t tr = tile / g.tcols, tc = tile % g.tcols;
     const int t = threadIdx.x;
-    const int32_t rb = __ldg(sc.round_base + tile);
-    const int rounds = __ldg(sc.round_base + tile + 1) - rb - 1;
-    const int tail = __ldg(sc.tails + 2 * tile);
-    const int32_t e0 = __ldg(exit_base + tile), ne = __ldg(exit_base + tile + 1) - e0;
-    // material and valid bits of this thread's 16 cells
     float4 x[4];
-    uint32_t vbits[4];
+    uint2 pq[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         const int cell = quad_cell(j);
         const int64_t r = tr * kTile + (cell >> 6), c = tc * kTile + (cell & 63);
         x[j] = ext ? load_quad(ext, g, r, c, vec, 0.0f) : make_float4(ext_s, ext_s, ext_s, ext_s);
-        vbits[j] = __ldg(sc.valid_bits + tile * (kTileCells / 32) + (cell >> 5)) >> (cell & 31);
+        pq[j] = __ldg(reinterpret_cast<const uint2*>(f.pos + tile * kTileCells + cell));
     }
-    replay_stage(sm, sc.order + tile * kTileCells, sc.upm + tile * kTileCells, sc.off + rb, rounds);
-    int my_loc = -1;
-    uint32_t my_pos = 0;
+    const int32_t e0 = __ldg(exit_base + tile), ne = __ldg(exit_base + tile + 1) - e0;
+    uint32_t span = 0, epos = 0;
     if (t < ne) {  // a tile has at most 252 exits (its border cells)
-        my_loc = __ldg(exit_local + e0 + t);
-        my_pos = __ldg(exit_pos + e0 + t);
+        span = __ldg(exit_span + e0 + t);
+        epos = __ldg(exit_pos + e0 + t);
     }
-    float sum = 0.0f;
-    bool inf = false;
+    float sum = 0.0f, mn = INFINITY;
+    int flags = 0;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const int cell = quad_cell(j);
-        float v[4] = {x[j].x, x[j].y, x[j].z, x[j].w};
+    for (int j = 0; j < 4; ++j)
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            if ((vbits[j] >> k) & 1u) {
-                if (isinf(v[k]) && v[k] > 0.0f) inf = true;
-                else if (v[k] > 0.0f) sum += v[k];
-            } else {
-                v[k] = __int_as_float(0x7fc00000);  // no-data flow direction: never read, result NaN
+            if (half_at(pq[j], k) & kInvalidPos) continue;
+            const float v = quad_at(x[j], k);
+            if (v > 0.0f) {
+                if (isinf(v)) flags |= 1;
+                else {
+                    sum += v;
+                    mn = fminf(mn, v);
+                }
+            } else if (!(v == 0.0f)) {
+                flags |= 2;
             }
         }
-        *reinterpret_cast<float4*>(sm.hi + cell) = make_float4(v[0], v[1], v[2], v[3]);
-        *reinterpret_cast<float4*>(sm.lo + cell) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float tot, tmin;
+    int tflags;
+    tile_reduce(red, sum, mn, flags, tot, tmin, tflags);
+    const float bound = tot * 1.0009765625f;
+    const int F = tile_scale(bound);
+    if ((tflags & 1) || !(bound < 1.0e38f) || (tmin < INFINITY && tmin * pow2f(F) < kMinQuantum)) {
+        if (t == 0) block_total[tile] = ~0ull;
+        return;  // uniform: every thread has the same reductions
     }
-    __syncthreads();
-    replay(sm, sc.off + rb, rounds, tail);
+    const float scale = pow2f(F);
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const int cell = quad_cell(j);
-        store_quad(out, g, tr * kTile + (cell >> 6), tc * kTile + (cell & 63), vec,
-                   *reinterpret_cast<const float4*>(sm.hi + cell));
-    }
-    if (my_loc >= 0) P[my_pos] = make_float2(sm.hi[my_loc], sm.lo[my_loc]);
-    // upper bound of this tile's material total, in 2^-16 units; ~0 marks +inf or overflow.  A float
-    // sum of <= 4096 non-negative terms is within 4096 * 2^-24 of the exact sum, inside the 1e-4 margin.
-    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
-    unsigned any_inf = __any_sync(0xffffffffu, inf);
-    if ((t & 31) == 0) {
-        warp_sum[t >> 5] = sum;
-        warp_inf[t >> 5] = any_inf ? 1 : 0;
-    }
-    __syncthreads();
-    if (t == 0) {
-        double tot = 0.0;
-        int bad = 0;
-        for (int w = 0; w < kTileThreads / 32; ++w) {
-            tot += (double)warp_sum[w];
-            bad |= warp_inf[w];
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int p = half_at(pq[j], k);
+            const float v = quad_at(x[j], k);
+            S[scan_slot(p & (kTileCells - 1))] =
+                (!(p & kInvalidPos) && v > 0.0f) ? __float2ull_rn(v * scale) : 0ull;
         }
-        double units = tot * 1.0001 * 65536.0 + 64.0;
-        block_total[tile] = (bad || !(units < 1.0e18)) ? ~0ull : (unsigned long long)units;
+    __syncthreads();
+    tile_scan(S, warp_tot);
+    const int epos_t = (int)(span & 0xFFFFu), estart = (int)(span >> 16);
+    float2 value = make_float2(0.0f, 0.0f);
+    if (t < ne) value = fixed64_to_ff(subtree_sum(S, epos_t, estart), F);
+    if (tflags & 2) {  // NaN or negative material: count it along the same post-order
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int p = half_at(pq[j], k);
+                S[scan_slot(p & (kTileCells - 1))] = (!(p & kInvalidPos) && !(quad_at(x[j], k) >= 0.0f)) ? 1ull : 0ull;
+            }
+        __syncthreads();
+        tile_scan(S, warp_tot);
+        if (t < ne && subtree_sum(S, epos_t, estart) != 0) value.x = __int_as_float(0x7fc00000);
+    }
+    if (t < ne) P[epos] = value;
+    if (t == 0) {
+        const double units = (double)bound * 65536.0 + 64.0;
+        block_total[tile] = units < 1.0e18 ? (unsigned long long)units : ~0ull;
     }
 }
 
@@ -930,85 +961,130 @@ __global__ void k_exit_sums(int64_t n, const uint32_t* __restrict__ pos, const u
     A[y] = from_u128(a);
 }
 
-// Pass 3: add the inflow entering each tile to every cell downstream of a tile entry.
-__global__ void __launch_bounds__(kTileThreads)
-    k_tile_fixup(TileGeom g, float* __restrict__ out, bool vec, TileSched sc, const uint4* __restrict__ A,
-                 const unsigned long long* total)
+// Pass 3: the result of every cell: the accu of its in-tile subtree plus what enters the tile upstream of
+// it (the exact subtree sums of the exits draining into the tile's border cells), in one fixed-point scan
+// per tile.  A tile that cannot be scaled sets the fallback flag total[1]: the walk engine redoes the call.
+__global__ void __launch_bounds__(kTileThreads, 4)
+    k_tile_accu(TileGeom g, const float* __restrict__ ext, float ext_s, bool vec, float* __restrict__ out,
+                TileForest f, const uint4* __restrict__ A, unsigned long long* total)
 {
-    __shared__ ReplaySmem sm;
+    __shared__ unsigned long long S[kScanSlots];
+    __shared__ unsigned long long warp_tot[kTileThreads / 32];
+    __shared__ TileReduce red;
     if (total[1]) return;
-    const int F = fixed_point_bits(total[0]);
+    const int Fg = fixed_point_bits(total[0]);
     const int64_t tile = blockIdx.x;
     const int64_t tr = tile / g.tcols, tc = tile % g.tcols;
     const int t = threadIdx.x;
-    const int32_t rb = __ldg(sc.round_base + tile);
-    const int rounds = __ldg(sc.round_base + tile + 1) - rb - 1;
-    const int tail = __ldg(sc.tails + 2 * tile + 1);
-    const unsigned in_mask = t < kBorderCells ? __ldg(sc.border_in + tile * kBorderCells + t) : 0u;
-    replay_stage(sm, sc.thr_order + tile * kTileCells, sc.thr_upm + tile * kTileCells, sc.thr_off + rb, rounds);
-    float4 o[4];
+    float4 x[4];
+    uint2 pq[4], sq[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         const int cell = quad_cell(j);
-        o[j] = load_quad(out, g, tr * kTile + (cell >> 6), tc * kTile + (cell & 63), vec, 0.0f);
-        *reinterpret_cast<float4*>(sm.hi + cell) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        *reinterpret_cast<float4*>(sm.lo + cell) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const int64_t r = tr * kTile + (cell >> 6), c = tc * kTile + (cell & 63);
+        x[j] = ext ? load_quad(ext, g, r, c, vec, 0.0f) : make_float4(ext_s, ext_s, ext_s, ext_s);
+        pq[j] = __ldg(reinterpret_cast<const uint2*>(f.pos + tile * kTileCells + cell));
+        sq[j] = __ldg(reinterpret_cast<const uint2*>(f.start + tile * kTileCells + cell));
     }
-    // sources: border cells gather the exact subtree sums of the halo exits draining into them
+    // sources entering through the border: the exits of the neighbouring tiles draining into it
+    const unsigned in_mask = t < kBorderCells ? __ldg(f.border_in + tile * kBorderCells + t) : 0u;
     u128 src = 0;
-    int src_cell = -1;
+    int src_pos = -1;
     if (in_mask) {
         int rin, cin;
-        if (t < kTile) { rin = 0; cin = t; }
-        else if (t < 2 * kTile) { rin = kTile - 1; cin = t - kTile; }
-        else if (t < 3 * kTile - 2) { rin = t - 2 * kTile + 1; cin = 0; }
-        else { rin = t - (3 * kTile - 2) + 1; cin = kTile - 1; }
+        border_cell(t, rin, cin);
         unsigned m = in_mask;
         while (m) {
-            int q = __ffs(m) - 1;
+            const int q = __ffs(m) - 1;
             m &= m - 1;
-            int32_t id = __ldg(sc.halo_exit + tile * kHaloSlots + halo_slot_of(rin + nb_dr(q), cin + nb_dc(q)));
+            const int32_t id = __ldg(f.halo_exit + tile * kHaloSlots + halo_slot_of(rin + nb_dr(q), cin + nb_dc(q)));
             if (id >= 0) src += to_u128(A[id]);
         }
-        src_cell = rin * kTile + cin;
+        src_pos = __ldg(f.pos + tile * kTileCells + rin * kTile + cin) & (kTileCells - 1);
     }
-    __syncthreads();  // the zeroing is done before the sources are written
-    if (src_cell >= 0) {
-        if ((src >> 96) != 0) {
-            sm.hi[src_cell] = __int_as_float(0x7fc00000);
-        } else {
-            double d = fixed_to_double(src, F);
-            float h = __double2float_rn(d);
-            sm.hi[src_cell] = h;
-            sm.lo[src_cell] = __double2float_rn(d - (double)h);
-        }
+    const bool src_poison = (src >> 96) != 0;
+    const float src_value = src_pos >= 0 ? fixed128_to_float(src & kValueMask, Fg) : 0.0f;
+    float sum = 0.0f, mn = INFINITY;
+    int flags = src_poison ? 2 : 0;
+    if (src_value > 0.0f) {
+        sum = src_value;
+        mn = src_value;
     }
-    __syncthreads();
-    replay(sm, sc.thr_off + rb, rounds, tail);
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const int cell = quad_cell(j);
-        const float4 h4 = *reinterpret_cast<const float4*>(sm.hi + cell);
-        const float4 l4 = *reinterpret_cast<const float4*>(sm.lo + cell);
-        const float hv[4] = {h4.x, h4.y, h4.z, h4.w}, lv[4] = {l4.x, l4.y, l4.z, l4.w};
-        float v[4] = {o[j].x, o[j].y, o[j].z, o[j].w};
-        bool changed = false;
+    for (int j = 0; j < 4; ++j)
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            if (hv[k] == 0.0f && lv[k] == 0.0f) continue;
-            changed = true;
-            if (isnan(hv[k])) {
-                v[k] = __int_as_float(0x7fc00000);
-            } else {
-                FF f{v[k], 0.0f};
-                f.add(hv[k], lv[k]);
-                f.normalise();
-                v[k] = f.hi;
+            if (half_at(pq[j], k) & kInvalidPos) continue;
+            const float v = quad_at(x[j], k);
+            if (v > 0.0f) {
+                if (isinf(v)) flags |= 1;
+                else {
+                    sum += v;
+                    mn = fminf(mn, v);
+                }
+            } else if (!(v == 0.0f)) {
+                flags |= 2;
             }
         }
-        if (changed)
-            store_quad(out, g, tr * kTile + (cell >> 6), tc * kTile + (cell & 63), vec,
-                       make_float4(v[0], v[1], v[2], v[3]));
+    float tot, tmin;
+    int tflags;
+    tile_reduce(red, sum, mn, flags, tot, tmin, tflags);
+    const float bound = tot * 1.0009765625f;
+    const int F = tile_scale(bound);
+    if ((tflags & 1) || !(bound < 1.0e38f) || (tmin < INFINITY && tmin * pow2f(F) < kMinQuantum)) {
+        if (t == 0) total[1] = 1ull;  // the walk engine redoes the call
+        return;
+    }
+    // NaN or negative material, or a no-data exit upstream: count them along the post-order first
+    unsigned poisoned = 0;  // bit 4 j + k: cell k of quad j has such a cell in its subtree
+    if (tflags & 2) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int p = half_at(pq[j], k);
+                S[scan_slot(p & (kTileCells - 1))] = (!(p & kInvalidPos) && !(quad_at(x[j], k) >= 0.0f)) ? 1ull : 0ull;
+            }
+        __syncthreads();
+        if (src_poison) atomicAdd(&S[scan_slot(src_pos)], 1ull);
+        __syncthreads();
+        tile_scan(S, warp_tot);
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int p = half_at(pq[j], k);
+                if (!(p & kInvalidPos) && subtree_sum(S, p, half_at(sq[j], k)) != 0) poisoned |= 1u << (4 * j + k);
+            }
+        __syncthreads();  // S is rewritten below
+    }
+    const float scale = pow2f(F);
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int p = half_at(pq[j], k);
+            const float v = quad_at(x[j], k);
+            S[scan_slot(p & (kTileCells - 1))] =
+                (!(p & kInvalidPos) && v > 0.0f) ? __float2ull_rn(v * scale) : 0ull;
+        }
+    __syncthreads();
+    if (src_pos >= 0 && !src_poison) atomicAdd(&S[scan_slot(src_pos)], rescale_fixed(src & kValueMask, F - Fg));
+    __syncthreads();
+    tile_scan(S, warp_tot);
+    const float unscale = pow2f(-F);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        float v[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int p = half_at(pq[j], k);
+            v[k] = ((p & kInvalidPos) || ((poisoned >> (4 * j + k)) & 1u))
+                       ? __int_as_float(0x7fc00000)
+                       : __ull2float_rn(subtree_sum(S, p, half_at(sq[j], k))) * unscale;
+        }
+        const int cell = quad_cell(j);
+        store_quad(out, g, tr * kTile + (cell >> 6), tc * kTile + (cell & 63), vec, make_float4(v[0], v[1], v[2], v[3]));
     }
 }
 
@@ -1129,57 +1205,22 @@ int tile_core_build(TopologyCore* core, cudaStream_t stream)
     }
     k_halo_exits<<<blocks_for(nt * kHaloSlots, 256), 256, 0, stream>>>(core->fd, g, tc->exit_base, bitmap, rowpref,
                                                                       tc->halo_exit);
+    // per-tile flow forests in post-order
+    TRY(cudaMalloc(&tc->tile_pos, nt * kTileCells * sizeof(uint16_t)), "tile forest");
+    TRY(cudaMalloc(&tc->tile_start, nt * kTileCells * sizeof(uint16_t)), "tile forest");
+    TRY(cudaMalloc(&tc->exit_span, std::max<int64_t>(E, 1) * sizeof(uint32_t)), "exit span");
+    TRY(cudaMalloc(&tc->border_in, nt * kBorderCells), "tile border masks");
+    TRY(cudaFuncSetAttribute(k_tile_forest, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TileSmem)),
+        "tile forest");
+    k_tile_forest<<<(unsigned)nt, kTileThreads, sizeof(TileSmem), stream>>>(
+        core->fd, g, tc->exit_base, tc->exit_local, tc->tile_pos, tc->tile_start, tc->exit_span, tc->border_in, flag);
+    tc->bytes += nt * kTileCells * 4 + E * 4 + nt * kBorderCells;
     TRY(cudaGetLastError(), "tile build");
     TRY(cudaMemcpyAsync(&herr, flag, sizeof(int), cudaMemcpyDeviceToHost, stream), "tile flag");
     TRY(cudaStreamSynchronize(stream), "tile build");
     if (herr) {
         rc = fail(LUE_GPU_EINVAL, "tile topology: cycle inside a tile or inconsistent exit forest");
         goto error;
-    }
-    // solve schedules: rounds per tile, then the schedules themselves
-    {
-        const size_t smem = sizeof(TileSmem);
-        TRY(cudaFuncSetAttribute(k_tile_schedule<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-            "tile schedule");
-        TRY(cudaFuncSetAttribute(k_tile_schedule<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-            "tile schedule");
-        TRY(cudaMalloc(&tc->round_base, (nt + 1) * sizeof(int32_t)), "tile round base");
-        k_tile_schedule<true><<<(unsigned)nt, kTileThreads, smem, stream>>>(
-            core->fd, g, count, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
-            nullptr);
-        TRY(cudaGetLastError(), "tile schedule");
-        TRY(cudaMemcpyAsync(hcount.data(), count, nt * sizeof(int32_t), cudaMemcpyDeviceToHost, stream),
-            "tile rounds");
-        TRY(cudaStreamSynchronize(stream), "tile rounds");
-        int64_t total = 0;
-        for (int64_t i = 0; i < nt; ++i) {
-            hbase[i] = (int32_t)total;
-            total += hcount[i] + 1;
-            if (total > INT32_MAX) {
-                rc = fail(LUE_GPU_ERANGE, "tile topology: too many solve rounds");
-                goto error;
-            }
-        }
-        hbase[nt] = (int32_t)total;
-        TRY(cudaMemcpyAsync(tc->round_base, hbase.data(), (nt + 1) * sizeof(int32_t), cudaMemcpyHostToDevice,
-                            stream),
-            "tile round base");
-        TRY(cudaMalloc(&tc->round_off, total * sizeof(uint16_t)), "tile round offsets");
-        TRY(cudaMalloc(&tc->thr_round_off, total * sizeof(uint16_t)), "tile round offsets");
-        TRY(cudaMalloc(&tc->sched_order, nt * kTileCells * sizeof(uint16_t)), "tile schedule");
-        TRY(cudaMalloc(&tc->sched_upm, nt * kTileCells), "tile schedule");
-        TRY(cudaMalloc(&tc->thr_order, nt * kTileCells * sizeof(uint16_t)), "tile schedule");
-        TRY(cudaMalloc(&tc->thr_upm, nt * kTileCells), "tile schedule");
-        TRY(cudaMalloc(&tc->valid_bits, nt * (kTileCells / 32) * sizeof(uint32_t)), "tile valid bits");
-        TRY(cudaMalloc(&tc->border_in, nt * kBorderCells), "tile border masks");
-        TRY(cudaMalloc(&tc->tails, nt * 2 * sizeof(uint16_t)), "tile warp-phase rounds");
-        k_tile_schedule<false><<<(unsigned)nt, kTileThreads, smem, stream>>>(
-            core->fd, g, nullptr, tc->round_base, tc->sched_order, tc->sched_upm, tc->thr_order, tc->thr_upm,
-            tc->round_off, tc->thr_round_off, tc->tails, tc->valid_bits, tc->border_in);
-        TRY(cudaGetLastError(), "tile schedule");
-        TRY(cudaStreamSynchronize(stream), "tile schedule");  // hbase must outlive its copy
-        tc->bytes += (nt + 1) * 4 + total * 4 + nt * kTileCells * 6 + nt * (kTileCells / 8) + nt * kBorderCells +
-                     nt * 4;
     }
     cudaFree(bitmap);
     cudaFree(rowpref);
@@ -1229,16 +1270,10 @@ void tile_core_free(TileCore* tc)
     cudaFree(tc->exit_pos);
     cudaFree(tc->exit_start);
     cudaFree(tc->halo_exit);
-    cudaFree(tc->sched_order);
-    cudaFree(tc->sched_upm);
-    cudaFree(tc->thr_order);
-    cudaFree(tc->thr_upm);
-    cudaFree(tc->round_base);
-    cudaFree(tc->round_off);
-    cudaFree(tc->thr_round_off);
-    cudaFree(tc->valid_bits);
+    cudaFree(tc->tile_pos);
+    cudaFree(tc->tile_start);
+    cudaFree(tc->exit_span);
     cudaFree(tc->border_in);
-    cudaFree(tc->tails);
     delete tc;
 }
 
@@ -1277,13 +1312,13 @@ int tile_accu_f32(const TopologyCore* core, TileScratch* s, const float* ext, fl
 {
     const TileCore* tc = core->tiles;
     TileGeom g{core->rows, core->cols, tc->trows, tc->tcols};
-    const TileSched sc{tc->round_base, tc->sched_order, tc->sched_upm, tc->round_off, tc->thr_order,
-                       tc->thr_upm,    tc->thr_round_off, tc->tails,     tc->valid_bits, tc->border_in,
-                       tc->halo_exit};
-    const bool vec_out = (reinterpret_cast<uintptr_t>(out) & 15) == 0 && (core->cols & 3) == 0;
-    const bool vec = vec_out && (!ext || (reinterpret_cast<uintptr_t>(ext) & 15) == 0);
-    k_tile_local<<<(unsigned)tc->ntiles, kTileThreads, 0, stream>>>(g, ext, ext_s, vec, out, sc, tc->exit_base,
-                                                                    tc->exit_local, tc->exit_pos, s->P,
+    const TileForest f{tc->tile_pos, tc->tile_start, tc->border_in, tc->halo_exit};
+    // rows move as float4 when the columns are a multiple of 4 and the arrays 16-byte aligned
+    const bool cols4 = (core->cols & 3) == 0;
+    const bool vec_in = cols4 && (!ext || (reinterpret_cast<uintptr_t>(ext) & 15) == 0);
+    const bool vec_out = cols4 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
+    k_tile_exits<<<(unsigned)tc->ntiles, kTileThreads, 0, stream>>>(g, ext, ext_s, vec_in, f, tc->exit_base,
+                                                                    tc->exit_span, tc->exit_pos, s->P,
                                                                     s->block_total);
     k_total<<<1, 1024, 0, stream>>>(s->block_total, tc->ntiles, s->total);
     count_launches(2);
@@ -1294,9 +1329,11 @@ int tile_accu_f32(const TopologyCore* core, TileScratch* s, const float* ext, fl
         k_scan_blocks<<<1, kTileThreads, 0, stream>>>(s->block_sums, nb, s->total);
         k_scan_final<<<(unsigned)nb, kTileThreads, 0, stream>>>(s->P, E, s->total, s->block_sums, s->S);
         k_exit_sums<<<blocks_for(E, 256), 256, 0, stream>>>(E, tc->exit_pos, tc->exit_start, s->S, s->A, s->total);
-        k_tile_fixup<<<(unsigned)tc->ntiles, kTileThreads, 0, stream>>>(g, out, vec_out, sc, s->A, s->total);
-        count_launches(5);
+        count_launches(4);
     }
+    k_tile_accu<<<(unsigned)tc->ntiles, kTileThreads, 0, stream>>>(g, ext, ext_s, vec_in && vec_out, out, f, s->A,
+                                                                   s->total);
+    count_launches(1);
     return cuda_status(cudaGetLastError(), "accu_f32 (tiles)");
 }
 

@@ -1,21 +1,21 @@
 // tile_accu.cuh — the tiled accu engine: resident tile topology and per-call scratch.
 //
-// The raster is cut into 64 x 64 tiles (the GPU's partitions).  Once, when the topology is built, each
-// tile's solve is compiled into a schedule: its valid cells grouped in rounds (a round's cells depend
-// only on cells of earlier rounds), each cell with its in-tile upstream mask; the same for the cells
-// downstream of a tile entry.  Per call, a tile's solve replays its schedule (one barrier per round,
-// 3 bytes of schedule read per cell) instead of re-deriving it from the flow direction:
-//   1. k_tile_local: one CTA per tile solves accu inside the tile in shared memory, ignoring flow that
-//      enters from other tiles, and writes that local result for every cell.  The local result of each
-//      exit cell (a cell whose flow leaves its tile but not the array) goes to P, in the post-order of
-//      the exit forest.
+// The raster is cut into 64 x 64 tiles (the GPU's partitions).  Inside a tile, the flow paths form a
+// forest; once, when the topology is built, it is laid out in post-order, so that the accu of a cell
+// (the material of its in-tile subtree) is the difference of two prefix sums of the material taken in
+// that order.  Per call:
+//   1. k_tile_exits: one CTA per tile scatters its material into post-order in shared memory, takes one
+//      exact 64-bit fixed-point prefix sum, and writes the local value of each exit cell (a cell whose
+//      flow leaves its tile but not the array) to P, in the post-order of the exit forest.
 //   2. Exit forest: exit y's parent is the exit reached by following the flow from y's downstream
 //      cell through that cell's tile.  The final value of exit y is the sum of the local values over
 //      y's subtree of this forest, so an inclusive prefix sum over P in post-order gives every subtree
 //      sum as a difference of two prefix sums.  The sums are exact: 128-bit fixed point (96 value bits,
 //      32 bits counting no-data exits), so summation order cannot change the result.
-//   3. k_tile_fixup: one CTA per tile adds, to every cell downstream of a tile entry, the exact sum of
-//      what enters the tile upstream of it.
+//   3. k_tile_accu: one CTA per tile adds, at each border cell, the subtree sums of the exits draining
+//      into it to the material, takes the same prefix sum again and writes every cell's result.
+// Both tile passes read the material once (coalesced float4 rows) and 2-4 bytes of forest per cell; the
+// prefix sums stay in shared memory.
 // Reference counterpart: the per-partition intra/inter split of ALG/definition/accumulating_router.hpp
 // (intra :789-899, inter :902-1209), with the inter-partition channel hand-off replaced by the exit-forest
 // prefix sum.
@@ -42,16 +42,11 @@ struct TileCore {
     uint32_t* exit_start = nullptr;            // [nexit] post-order position of the first node of the subtree
     int32_t* halo_exit = nullptr;              // [ntiles * kHaloSlots] exit id of the halo cell draining into
                                                // the tile, or -1
-    // Per-tile solve schedules, compiled once from the flow direction (so no call re-derives them):
-    uint16_t* sched_order = nullptr;           // [ntiles * 4096] valid cells, grouped by in-tile round
-    uint8_t* sched_upm = nullptr;              // [ntiles * 4096] in-tile upstream mask of sched_order[k]
-    uint16_t* thr_order = nullptr;             // [ntiles * 4096] cells downstream of a tile entry, by round
-    uint8_t* thr_upm = nullptr;                // [ntiles * 4096] their upstream mask, restricted to such cells
-    int32_t* round_base = nullptr;             // [ntiles + 1] first entry of each tile in round_off
-    uint16_t* round_off = nullptr;             // per tile: rounds + 1 offsets into sched_order
-    uint16_t* thr_round_off = nullptr;         // per tile: the same rounds' offsets into thr_order
-    uint16_t* tails = nullptr;                 // [ntiles * 2] first round of the warp phase (all, through)
-    uint32_t* valid_bits = nullptr;            // [ntiles * 128] bit per cell: inside the array, not no-data
+    // Per-tile flow forests in post-order (built once from the flow direction):
+    uint16_t* tile_pos = nullptr;              // [ntiles * 4096] post-order position of each cell in its tile;
+                                               // 0x8000 set for no-data cells (after the valid ones)
+    uint16_t* tile_start = nullptr;            // [ntiles * 4096] first position of the cell's in-tile subtree
+    uint32_t* exit_span = nullptr;             // [nexit] position | start << 16 of each exit cell
     uint8_t* border_in = nullptr;              // [ntiles * kBorderCells] per border cell: outside neighbours draining in
     int64_t bytes = 0;
 };

@@ -259,6 +259,23 @@ def test_tile_engine_hands_infinite_material_to_the_walk_engine(lfr, c1):
     parity.assert_close32(got[finite], want[finite], "accu with +inf material")
 
 
+@pytest.mark.parametrize("tiny", [1e-6, 1e-14])
+def test_tile_engine_wide_material_range(lfr, c1, tiny):
+    """1 % of the cells carry material ~tiny next to U[0, 1) material: 1e-6 stays on the tile engine's
+    64-bit fixed point, 1e-14 (a range beyond 2^43 inside a tile) is handed to the walk engine.  Either
+    way the small values keep float32 precision."""
+    fd, ps = c1["flow_direction"], c1["partition"]
+    rng = np.random.default_rng(5)
+    m = c1["material"].copy()
+    small = rng.random(fd.shape) < 0.01
+    m[small] = (tiny * (1.0 + rng.random(int(small.sum())))).astype(np.float32)
+    got = lfr.to_numpy(lfr.accu(lfr.from_numpy(fd, ps), lfr.from_numpy(m, ps)))
+    want = oracle.accu(fd, m.astype(np.float64), ps, dtype=np.float64)
+    parity.assert_close32(got, want, f"accu with material down to {tiny}")
+    rel = np.abs(got[small].astype(np.float64) - want[small]) / want[small]
+    assert rel.max() <= parity.RTOL32, rel.max()
+
+
 def test_kinematic_wave_fast_solve_matches_reference_solve(lfr):
     """The float32-Newton + float64-polish solve against the reference-faithful float64 solve."""
     import os
