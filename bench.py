@@ -43,6 +43,7 @@ sys.path.insert(0, ROOT)
 ACCU_BYTES_PER_CELL = 9      # fd 1 + material 4 + outflow 4
 KW_BYTES_PER_CELL = 25       # fd 1 + Q_cur 8 + lateral 4 + alpha 4 + Q_new 8
 REF_SAMPLE_ROWS = 4096       # reference-arm / cpu_baseline sample: the top 4096 rows, all columns
+METRIC = "accu Mcells/s (16384^2 D8 raster, float32 material)"  # the headline metric, on accu_16k
 
 
 def peaks():
@@ -204,7 +205,7 @@ def bench_reference(args, world, rank):
     sample = (f"accu over rows 0-{fd.shape[0] - 1} of the {w['rows']}x{w['cols']} raster "
               f"({fd.shape[0]}x{fd.shape[1]} cells, partitions {ps[0]}x{ps[1]}) per step")
     line = {
-        "impl": "reference", "metric": "accu Mcells/s (16384^2 D8 raster, float32 material)", "value": round(value, 3),
+        "impl": "reference", "metric": METRIC, "value": round(value, 3),
         "unit": "Mcells/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1000 * total / args.steps, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fBm DEM, lognormal material)",
@@ -293,7 +294,7 @@ def bench_ours(args, world, rank, local):
     e2e_s = max_over_ranks(e0.elapsed_time(e1) / 1000.0, world)
     e2e_value = world * n * e2e_steps / e2e_s / 1e6
 
-    # roofline of the dominant kernel (the routing walk; one launch per step)
+    # roofline of the accu call (its kernels together; one call per step)
     peak, peak_kind = peaks()
     mean_step_s = statistics.mean(step_ms) / 1000.0
     achieved = ACCU_BYTES_PER_CELL * n / mean_step_s / 1e9
@@ -328,7 +329,7 @@ def bench_ours(args, world, rank, local):
                "sample": f"accu over rows 0-{fd_s.shape[0] - 1} of the raster ({fd_s.shape[0]}x{fd_s.shape[1]} "
                          f"cells, partitions {ps_s[0]}x{ps_s[1]}), one pass, oracle/lue_oracle.c threaded"}
     line = {
-        "metric": "accu Mcells/s (16384^2 D8 raster, float32 material)", "value": round(value, 3),
+        "metric": METRIC, "value": round(value, 3),
         "unit": "Mcells/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1000 * total_s / args.steps, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fBm DEM, lognormal material)",
@@ -341,7 +342,7 @@ def bench_ours(args, world, rank, local):
                 "d2h_bytes_per_step": 4 * n},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "kernel": ("accu_f32 call: k_tile_local + exit-forest scan + k_tile_fixup" if engine == "tiles"
+                     "kernel": ("accu_f32 call: k_tile_exits + exit-forest scan + k_tile_accu" if engine == "tiles"
                                 else "k_walk<RouteF32<accu>>"),
                      "timed": "whole call per step (all its kernels), CUDA events on the launching stream",
                      "peak_kind": peak_kind, "bytes_per_cell": ACCU_BYTES_PER_CELL},
