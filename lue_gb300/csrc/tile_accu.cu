@@ -318,7 +318,6 @@ __global__ void k_halo_exits(const uint8_t* __restrict__ fd, TileGeom g, const i
 // ---------------------------------------------------------------------------------------------------
 
 constexpr uint16_t kNoCell = 0xFFFFu;
-constexpr int kInvalidPos = 0x8000;  // tile_pos flag: no-data flow direction, or outside the array
 
 struct __align__(16) TileSmem {
     float hi[kTileCells];
@@ -328,6 +327,7 @@ struct __align__(16) TileSmem {
     uint16_t queue[kTileCells];    // cells in the order they become ready (each cell once)
     uint8_t up[kTileCells];        // in-tile upstream mask
     uint8_t fd[kHalo][kHalo + 2];  // flow direction with a one-cell halo (255 outside the array)
+    uint8_t border[kBorderCells];  // per border cell: outside neighbours draining into it
     int round_count[3];            // cells queued for the next rounds (a ring of three counters)
 };
 
@@ -406,6 +406,22 @@ __device__ __forceinline__ void border_cell(int b, int& rin, int& cin)
     else { rin = b - (3 * kTile - 2) + 1; cin = kTile - 1; }
 }
 
+// Border index (0..251, see border_cell) of a border cell of the tile.
+__device__ __forceinline__ int border_index(int rin, int cin)
+{
+    if (rin == 0) return cin;
+    if (rin == kTile - 1) return kTile + cin;
+    return cin == 0 ? 2 * kTile + rin - 1 : 3 * kTile - 2 + rin - 1;
+}
+
+// 1 when in-tile cell i is a border cell with inflow from outside the tile (sm.border filled).
+__device__ __forceinline__ int entry_of(const TileSmem& sm, int i)
+{
+    const int rin = i >> 6, cin = i & 63;
+    if (!(rin == 0 || rin == kTile - 1 || cin == 0 || cin == kTile - 1)) return 0;
+    return sm.border[border_index(rin, cin)] != 0;
+}
+
 // Exclusive prefix of one int per thread over the block; `total` gets the block sum.
 __device__ __forceinline__ int block_exclusive_int(int v, int* warp_tot, int& total)
 {
@@ -436,13 +452,13 @@ __device__ __forceinline__ int block_exclusive_int(int v, int* warp_tot, int& to
 // Also: each exit's (pos, start) and, per border cell, which outside neighbours drain into it.
 __global__ void __launch_bounds__(kTileThreads)
     k_tile_forest(const uint8_t* __restrict__ fd, TileGeom g, const int32_t* __restrict__ exit_base,
-                  const uint16_t* __restrict__ exit_local, uint16_t* tile_pos, uint16_t* tile_start,
+                  const uint16_t* __restrict__ exit_local, uint16_t* cell_at, uint16_t* prev_at,
                   uint32_t* exit_span, uint8_t* border_in, int* error)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TileSmem& sm = *reinterpret_cast<TileSmem*>(smem_raw);
-    const int64_t tile = blockIdx.x;
-    const int64_t tr = tile / g.tcols, tc = tile % g.tcols;
+    const int64_t tr = blockIdx.y, tc = blockIdx.x;  // grid = (tile columns, tile rows)
+    const int64_t tile = tr * g.tcols + tc;
     const int t = threadIdx.x, lane = t & 31;
     uint16_t* rstart = reinterpret_cast<uint16_t*>(sm.hi);  // <= 4097 round starts
     uint16_t* sz = reinterpret_cast<uint16_t*>(sm.lo);      // subtree size
@@ -479,12 +495,29 @@ __global__ void __launch_bounds__(kTileThreads)
     const int rounds = r, nvalid = head;
     if (t == 0) rstart[rounds] = (uint16_t)nvalid;
     __syncthreads();
-    // subtree sizes, upstream first
+    // per border cell, the neighbours outside the tile that drain into it (the cell then gets an entry node)
+    for (int b = t; b < kBorderCells; b += kTileThreads) {
+        int rin, cin;
+        border_cell(b, rin, cin);
+        unsigned outside = 0;
+        if (sm.fd[rin + 1][cin + 1] != kNoData) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int hr = rin + nb_dr(q), hc = cin + nb_dc(q);
+                if (hr >= 0 && hr < kTile && hc >= 0 && hc < kTile) continue;
+                if (sm.fd[hr + 1][hc + 1] == nb_inflow_code(q)) outside |= 1u << q;
+            }
+        }
+        sm.border[b] = (uint8_t)outside;
+        border_in[tile * kBorderCells + b] = (uint8_t)outside;
+    }
+    __syncthreads();
+    // subtree sizes (entry nodes included), upstream first
     for (int q = 0; q < rounds; ++q) {
         for (int k = rstart[q] + t; k < rstart[q + 1]; k += kTileThreads) {
             const int i = sm.queue[k];
             unsigned m = sm.up[i];
-            int size = 1;
+            int size = 1 + entry_of(sm, i);
             while (m) {
                 size += sz[i + tile_nb_offset(__ffs(m) - 1)];
                 m &= m - 1;
@@ -504,7 +537,7 @@ __global__ void __launch_bounds__(kTileThreads)
     }
     int root_total, invalid_total;
     int root_base = block_exclusive_int(root_sum, wt, root_total);
-    int invalid_base = nvalid + block_exclusive_int(invalid, wt, invalid_total);
+    int invalid_base = root_total + block_exclusive_int(invalid, wt, invalid_total);
     for (int j = 0; j < 16; ++j) {
         const int i = 16 * t + j;
         if (sm.fd[(i >> 6) + 1][(i & 63) + 1] == kNoData) {
@@ -522,7 +555,7 @@ __global__ void __launch_bounds__(kTileThreads)
             const int i = sm.queue[k], d = sm.dsl[i];
             if (d == kNoCell) continue;
             unsigned m = sm.up[d] & ((1u << nb_index_from(d, i)) - 1u);
-            int o = st[d];
+            int o = st[d] + entry_of(sm, d);  // after d's entry node and the siblings before i
             while (m) {
                 o += sz[d + tile_nb_offset(__ffs(m) - 1)];
                 m &= m - 1;
@@ -531,37 +564,41 @@ __global__ void __launch_bounds__(kTileThreads)
         }
         __syncthreads();
     }
-    // positions, checked to be a permutation of 0 .. 4095
+    // positions, checked distinct, and the tables by position: cells, entry nodes, then padding
+    const int64_t T = tile * kRunPositions;
     uint32_t* seen = reinterpret_cast<uint32_t*>(sm.queue);  // the queue is no longer read
-    if (t < kTileCells / 32) seen[t] = 0;
+    for (int w = t; w < kRunPositions / 32; w += kTileThreads) seen[w] = 0;
     __syncthreads();
     for (int i = t; i < kTileCells; i += kTileThreads) {
-        const bool valid = sm.fd[(i >> 6) + 1][(i & 63) + 1] != kNoData;
+        const int rin = i >> 6, cin = i & 63;
+        const bool valid = sm.fd[rin + 1][cin + 1] != kNoData;
+        const bool entry = valid && entry_of(sm, i);
         const int s0 = st[i], p = s0 + sz[i] - 1;
-        bool bad = p >= kTileCells || s0 > p;
+        bool bad = p >= kRunPositions || s0 > p;
         if (!bad) bad = (atomicOr(&seen[p >> 5], 1u << (p & 31)) >> (p & 31)) & 1u;
-        if (bad) *error = 1;
-        tile_pos[tile * kTileCells + i] = (uint16_t)((p & (kTileCells - 1)) | (valid ? 0 : kInvalidPos));
-        tile_start[tile * kTileCells + i] = (uint16_t)(s0 & (kTileCells - 1));
+        if (!bad && entry) bad = (atomicOr(&seen[s0 >> 5], 1u << (s0 & 31)) >> (s0 & 31)) & 1u;
+        if (bad) {
+            *error = 1;
+            continue;
+        }
+        cell_at[T + run_table_index(p)] = (uint16_t)(i | (valid ? 0u : kNoValue));
+        prev_at[T + run_table_index(p)] = (uint16_t)((s0 > 0 ? s0 - 1 : kZeroSlot) | (s0 == p ? kPrevRidge : 0u));
+        if (entry) {
+            cell_at[T + run_table_index(s0)] = (uint16_t)((kEntryBase + border_index(rin, cin)) | kNoOutput);
+            prev_at[T + run_table_index(s0)] = (uint16_t)kZeroSlot;
+        }
+    }
+    __syncthreads();
+    for (int p = t; p < kRunPositions; p += kTileThreads) {
+        if ((seen[p >> 5] >> (p & 31)) & 1u) continue;
+        cell_at[T + run_table_index(p)] = (uint16_t)(kNoValue | kNoOutput);
+        prev_at[T + run_table_index(p)] = (uint16_t)kZeroSlot;
     }
     const int32_t e0 = exit_base[tile], ne = exit_base[tile + 1] - e0;
     for (int e = t; e < ne; e += kTileThreads) {
         const int loc = exit_local[e0 + e];
-        exit_span[e0 + e] = (uint32_t)(st[loc] + sz[loc] - 1) | ((uint32_t)st[loc] << 16);
-    }
-    for (int b = t; b < kBorderCells; b += kTileThreads) {
-        int rin, cin;
-        border_cell(b, rin, cin);
-        unsigned outside = 0;
-        if (sm.fd[rin + 1][cin + 1] != kNoData) {
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const int hr = rin + nb_dr(q), hc = cin + nb_dc(q);
-                if (hr >= 0 && hr < kTile && hc >= 0 && hc < kTile) continue;
-                if (sm.fd[hr + 1][hc + 1] == nb_inflow_code(q)) outside |= 1u << q;
-            }
-        }
-        border_in[tile * kBorderCells + b] = (uint8_t)outside;
+        const int s0 = st[loc], p = s0 + sz[loc] - 1;
+        exit_span[e0 + e] = (uint32_t)p | ((uint32_t)(s0 > 0 ? s0 - 1 : kZeroSlot) << 16);
     }
 }
 
@@ -569,17 +606,21 @@ __global__ void __launch_bounds__(kTileThreads)
 // Per call
 // ---------------------------------------------------------------------------------------------------
 //
-// Inside a tile the material is summed in 64-bit fixed point, round(x * 2^F) with F chosen per tile so
-// that the tile's total stays below 2^62: prefix sums over the post-order are then exact, and so is every
-// subtree sum taken as their difference (modulo 2^64, which is exact because the true sum is < 2^64).
-// A term x > 0 is represented to within 2^-(F+1) absolute; a tile whose smallest positive term would
-// carry fewer than 19 bits (x * 2^F < 2^19: a range of more than 2^43 between the tile total and its
-// smallest term) or that holds +inf asks for the walk engine instead.
+// A tile CTA works in two orders.  Material and results move between HBM and shared memory in cell
+// order (row-major float4 rows, coalesced).  Thread t owns the post-order positions 16 t .. 16 t + 15:
+// it gathers their material from shared memory through cell_at (one 4-byte read per cell), converts it
+// to fixed point and takes the prefix sum of its run in registers; a warp scan and the warp totals give
+// the run's offset, and each inclusive prefix is written to shared memory once.  The accu of a cell is
+// then its own prefix minus the prefix just before its subtree (prev_at).
+//
+// Inside a tile the material is summed in 64-bit fixed point, round(x * 2^F), with F chosen per tile
+// from a bound on the tile's total (4096 times its largest term, plus what enters through its border)
+// so that the total stays below 2^62: prefix sums over the post-order are then exact, and so is every
+// subtree sum taken as their difference (modulo 2^64, exact because the true sum is < 2^64).  A term
+// x > 0 is represented to within 2^-(F+1) absolute; a tile whose smallest positive term would carry
+// fewer than 19 bits (x * 2^F < 2^19) or that holds +inf asks for the walk engine instead.
 
-constexpr int kScanSlots = kTileCells + kTileCells / 16;  // one padding slot per 16 positions
-constexpr float kMinQuantum = 524288.0f;                  // 2^19
-
-__device__ __forceinline__ int scan_slot(int k) { return k + (k >> 4); }
+constexpr float kMinQuantum = 524288.0f;  // 2^19
 
 __device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }  // -126 <= e <= 127
 
@@ -591,48 +632,63 @@ __device__ __forceinline__ int tile_scale(float bound)
     return min(62 - e, 126);
 }
 
-// In-place inclusive prefix sums (modulo 2^64) of the 4096 post-order positions of a tile.  Thread t
-// owns positions 16 t .. 16 t + 15 (slots 17 t ..: the padding puts the lanes of a warp on distinct
-// banks).  Ends with a block barrier.
-__device__ __forceinline__ void tile_scan(unsigned long long* S, unsigned long long* warp_tot)
+// Bound on a tile's total from the bits of its largest term (4096 terms below 2^(e - 126)) and of the
+// largest sum entering through its border (at most 252 of them); +inf when beyond float range.
+__device__ __forceinline__ float tile_bound(unsigned max_bits, unsigned src_bits)
 {
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    unsigned long long* mine = S + 17 * t;
-    unsigned long long tot = 0;
-#pragma unroll
-    for (int j = 0; j < 16; ++j) tot += mine[j];
-    unsigned long long x = tot;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) warp_tot[warp] = x;
-    __syncthreads();
-    unsigned long long run = x - tot;
-    for (int w = 0; w < warp; ++w) run += warp_tot[w];
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-        run += mine[j];
-        mine[j] = run;
-    }
-    __syncthreads();
+    const int e = (int)(max_bits >> 23);
+    const float local = e > 240 ? INFINITY : pow2f(e - 114);
+    return (local + 256.0f * __uint_as_float(src_bits)) * 1.0009765625f;
 }
 
-__device__ __forceinline__ unsigned long long subtree_sum(const unsigned long long* S, int pos, int start)
+// Conversions between float and 64-bit fixed point in integer arithmetic.  GB300 executes the 64-bit
+// float <-> integer conversion instructions on its float64 pipe, which runs at a small fraction of the
+// integer rate; these run on the integer pipes.
+
+// round(x * 2^F) for finite x >= 0 with x * 2^F < 2^63 (ties away from zero).
+__device__ __forceinline__ unsigned long long float_to_fixed64(float x, int F)
 {
-    unsigned long long v = S[scan_slot(pos)];
-    if (start > 0) v -= S[scan_slot(start - 1)];
-    return v;
+    const unsigned b = __float_as_uint(x);
+    const unsigned e = b >> 23;
+    const unsigned m = (b & 0x7FFFFFu) | (e ? 0x800000u : 0u);
+    const int s = (int)(e ? e : 1u) - 150 + F;  // x * 2^F = m * 2^s
+    const unsigned rs = s < 0 ? (unsigned)min(-s, 31) : 0u;
+    const unsigned r = rs ? (m + (1u << (rs - 1))) >> rs : m;
+    return (unsigned long long)r << (s > 0 ? s : 0);
 }
 
-// A fixed-point value V * 2^-F as float-float (hi, lo).
+// x * 2^F exactly, for x == 0 or a normal x >= 0 with x * 2^F >= 2^23 (no bit is shifted out).
+__device__ __forceinline__ unsigned long long float_to_fixed64_exact(float x, int F)
+{
+    const unsigned b = __float_as_uint(x);
+    const unsigned m = (b & 0x7FFFFFu) | 0x800000u;
+    const int s = b ? (int)(b >> 23) - 150 + F : 0;
+    return b ? (unsigned long long)m << s : 0ull;
+}
+
+// v * 2^-F rounded to float (to nearest, ties to even), for v * 2^-F in the normal float range.
+__device__ __forceinline__ float u64_to_float_scaled(unsigned long long v, int F)
+{
+    if (v == 0) return 0.0f;
+    const int lz = __clzll((long long)v);
+    const unsigned long long n = v << lz;  // leading bit at 63
+    const unsigned hi = (unsigned)(n >> 32), lo = (unsigned)n;
+    unsigned mant = hi >> 8;  // 24 bits with the implicit one
+    const unsigned round = (hi >> 7) & 1u, sticky = ((hi & 0x7Fu) | lo) != 0u;
+    mant += round & (sticky | (mant & 1u));
+    // biased exponent 63 - lz - F + 127; a mantissa that rounds up to 2^24 carries into it
+    return __uint_as_float((unsigned)(63 - lz + 126 - F) * 0x800000u + mant);
+}
+__device__ __forceinline__ float u64_to_float(unsigned long long v) { return u64_to_float_scaled(v, 0); }
+
+// A fixed-point value V * 2^-F as float-float (hi, lo): hi holds the top 24 bits of V, lo the rest.
 __device__ __forceinline__ float2 fixed64_to_ff(unsigned long long V, int F)
 {
-    const float h = __ull2float_rn(V);
-    const long long r = (long long)(V - __float2ull_rn(h));
+    if (V == 0) return make_float2(0.0f, 0.0f);
+    const int lz = __clzll((long long)V);
+    const unsigned long long keep = lz >= 40 ? ~0ull : ~((1ull << (40 - lz)) - 1ull);
     const float s = pow2f(-F);
-    return make_float2(h * s, __ll2float_rn(r) * s);
+    return make_float2(u64_to_float(V & keep) * s, u64_to_float(V & ~keep) * s);
 }
 
 // A 96-bit fixed-point value v * 2^-F, rounded to float (the bits below the top 64 are dropped).
@@ -652,8 +708,8 @@ __device__ __forceinline__ unsigned long long rescale_fixed(u128 v, int d)
     return (unsigned long long)((v + ((u128)1 << (-d - 1))) >> (-d));
 }
 
-// Cells of a tile by thread: thread t holds the 4 x 4 cells (row (t + 256 j) / 16, columns 4 ((t + 256 j)
-// % 16) .. + 3), j = 0..3, so that a row of the tile is 16 float4.
+// Cells of a tile by thread in cell order: thread t holds the 4 x 4 cells (row (t + 256 j) / 16,
+// columns 4 ((t + 256 j) % 16) .. + 3), j = 0..3, so that a row of the tile is 16 float4.
 __device__ __forceinline__ int quad_cell(int j)
 {
     const int k = threadIdx.x + kTileThreads * j;
@@ -687,138 +743,253 @@ __device__ __forceinline__ void store_quad(float* __restrict__ p, const TileGeom
         if (c + x < g.cols) p[r * g.cols + c + x] = w[x];
 }
 
-__device__ __forceinline__ float quad_at(const float4& q, int k) { return k == 0 ? q.x : k == 1 ? q.y : k == 2 ? q.z : q.w; }
-__device__ __forceinline__ int half_at(const uint2& q, int k)
-{
-    return (int)(((k < 2 ? q.x : q.y) >> (16 * (k & 1))) & 0xFFFFu);
-}
-
 struct TileForest {
-    const uint16_t* pos;
-    const uint16_t* start;
+    const uint16_t* cell_at;
+    const uint16_t* prev_at;
     const uint8_t* border_in;
     const int32_t* halo_exit;
 };
 
-// Tile reductions: sum and minimum of the positive finite terms, flags (1: +inf, 2: NaN or negative).
-struct TileReduce {
-    float sum[kTileThreads / 32];
-    float min[kTileThreads / 32];
-    int flags[kTileThreads / 32];
+// Shared memory of a tile CTA (dynamic: 54 KB, four CTAs per SM).
+struct __align__(16) TileCallSmem {
+    unsigned long long S[kScanSlotCount];  // inclusive prefix sums by position; S[kZeroSlot] = 0
+    float M[kTileCells + kTileThreads];    // material in cell order, then the entry sums (kEntryBase + b);
+                                           // pass 3 then puts the results there in cell order
+    float warp_sum[kTileThreads / 32];
+    unsigned long long warp_tot[kTileThreads / 32];
+    unsigned red[2][kTileThreads / 32];
 };
 
-__device__ __forceinline__ void tile_reduce(TileReduce& red, float sum, float mn, int flags, float& tot, float& tmin,
-                                            int& tflags)
+// The thread's run of a per-position table (cell_at or prev_at): nine coalesced 4-byte loads.
+__device__ __forceinline__ void load_run(const uint16_t* __restrict__ table, uint32_t (&w)[kRunWords])
+{
+    const uint32_t* p = reinterpret_cast<const uint32_t*>(table) + threadIdx.x;
+#pragma unroll
+    for (int i = 0; i < kRunWords; ++i) w[i] = __ldg(p + i * kTileThreads);
+}
+__device__ __forceinline__ unsigned run_at(const uint32_t (&w)[kRunWords], int j)
+{
+    return (w[j >> 1] >> (16 * (j & 1))) & 0xFFFFu;
+}
+
+// Material of the tile in cell order (0 outside the array): the loads, then the stores to M.
+__device__ __forceinline__ void load_material(float4 (&x)[4], const float* __restrict__ ext, float ext_s,
+                                              const TileGeom& g, int64_t tr, int64_t tc, bool vec)
 {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        sum += __shfl_xor_sync(0xffffffffu, sum, o);
-        mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-        flags |= __shfl_xor_sync(0xffffffffu, flags, o);
+    for (int j = 0; j < 4; ++j) {
+        const int cell = quad_cell(j);
+        x[j] = ext ? load_quad(ext, g, tr * kTile + (cell >> 6), tc * kTile + (cell & 63), vec, 0.0f)
+                   : make_float4(ext_s, ext_s, ext_s, ext_s);
     }
-    if ((threadIdx.x & 31) == 0) {
-        red.sum[threadIdx.x >> 5] = sum;
-        red.min[threadIdx.x >> 5] = mn;
-        red.flags[threadIdx.x >> 5] = flags;
+}
+__device__ __forceinline__ void store_material(TileCallSmem& sm, const float4 (&x)[4])
+{
+#pragma unroll
+    for (int j = 0; j < 4; ++j) *reinterpret_cast<float4*>(sm.M + quad_cell(j)) = x[j];
+}
+
+// Block reductions: the largest bits, the smallest bits, and the float sum of one value per thread.
+__device__ __forceinline__ void tile_reduce(TileCallSmem& sm, unsigned& mx, unsigned& mn, float& sum)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    mn = __reduce_min_sync(0xffffffffu, mn);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if (lane == 0) {
+        sm.red[0][warp] = mx;
+        sm.red[1][warp] = mn;
+        sm.warp_sum[warp] = sum;
     }
     __syncthreads();
-    tot = 0.0f;
-    tmin = INFINITY;
-    tflags = 0;
+    sum = 0.0f;
+#pragma unroll
     for (int w = 0; w < kTileThreads / 32; ++w) {  // the same order in every thread
-        tot += red.sum[w];
-        tmin = fminf(tmin, red.min[w]);
-        tflags |= red.flags[w];
+        mx = max(mx, sm.red[0][w]);
+        mn = min(mn, sm.red[1][w]);
+        sum += sm.warp_sum[w];
     }
 }
 
+// The thread's terms in post-order (0 where flagged kNoValue), with the bits of its largest term, of its
+// smallest positive term minus one, and its float sum.
+__device__ __forceinline__ void gather_run(const TileCallSmem& sm, const uint32_t (&ca)[kRunWords], float (&x)[kRun],
+                                           unsigned& mx, unsigned& mn, float& sum)
+{
+    mx = 0;
+    mn = 0xFFFFFFFFu;
+    sum = 0.0f;
+#pragma unroll
+    for (int j = 0; j < kRun; ++j) {
+        const unsigned w = run_at(ca, j);
+        const float v = (w & kNoValue) ? 0.0f : sm.M[w & kIndexMask];
+        x[j] = v;
+        const unsigned b = __float_as_uint(v);
+        mx = max(mx, b);
+        mn = min(mn, b - 1u);
+        sum += v;
+    }
+}
+
+// NaN or negative terms (material, or a no-data exit upstream entering the tile): they become 0 and
+// are flagged in the returned mask; the reductions are redone on the cleaned run.
+__device__ __forceinline__ unsigned clean_run(const uint32_t (&ca)[kRunWords], float (&x)[kRun], unsigned& mx,
+                                              unsigned& mn, float& sum)
+{
+    unsigned bad = 0;
+    mx = 0;
+    mn = 0xFFFFFFFFu;
+    sum = 0.0f;
+#pragma unroll
+    for (int j = 0; j < kRun; ++j) {
+        const bool valid = !(run_at(ca, j) & kNoValue);
+        const float v = x[j];
+        if (valid && !(v >= 0.0f)) bad |= 1u << j;
+        x[j] = (valid && v >= 0.0f) ? fabsf(v) : 0.0f;  // fabsf: -0 counts as 0
+        const unsigned b = __float_as_uint(x[j]);
+        mx = max(mx, b);
+        mn = min(mn, b - 1u);
+        sum += x[j];
+    }
+    return bad;
+}
+
+// Poison counts: inclusive prefix sums over the post-order of the flagged terms, written as 32-bit
+// counts by position over S (free until the value scan).  Ends with a block barrier.
+__device__ __forceinline__ void poison_counts(TileCallSmem& sm, unsigned bad)
+{
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    unsigned c[kRun];
+    unsigned run = 0;
+#pragma unroll
+    for (int j = 0; j < kRun; ++j) {
+        run += (bad >> j) & 1u;
+        c[j] = run;
+    }
+    unsigned x = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    __syncthreads();  // warp_tot is free
+    if (lane == 31) sm.warp_tot[warp] = x;
+    __syncthreads();
+    unsigned off = x - run;
+    for (int w = 0; w < warp; ++w) off += (unsigned)sm.warp_tot[w];
+    unsigned* C = reinterpret_cast<unsigned*>(sm.S);
+#pragma unroll
+    for (int j = 0; j < kRun; ++j) C[kRun * t + j] = c[j] + off;
+    __syncthreads();
+}
+
+// The poison count up to a scan slot (0 for the zero slot).
+__device__ __forceinline__ unsigned count_at(const TileCallSmem& sm, int slot)
+{
+    return slot == kZeroSlot ? 0u : reinterpret_cast<const unsigned*>(sm.S)[slot];
+}
+
+// Inclusive prefix sums (modulo 2^64) of the thread runs a[0..17] over the whole tile, written to S.
+// Ends with a block barrier.
+__device__ __forceinline__ void tile_prefix(TileCallSmem& sm, unsigned long long (&a)[kRun])
+{
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+#pragma unroll
+    for (int j = 1; j < kRun; ++j) a[j] += a[j - 1];
+    unsigned long long x = a[kRun - 1];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sm.warp_tot[warp] = x;
+    __syncthreads();
+    unsigned long long off = x - a[kRun - 1];
+    for (int w = 0; w < warp; ++w) off += sm.warp_tot[w];
+    // 144-byte runs: 16-byte aligned, and the 16-byte stores of a quarter-warp fall on distinct banks
+    ulonglong2* run = reinterpret_cast<ulonglong2*>(sm.S + kRun * t);
+#pragma unroll
+    for (int i = 0; i < kRunWords; ++i) {
+        a[2 * i] += off;
+        a[2 * i + 1] += off;
+        run[i] = make_ulonglong2(a[2 * i], a[2 * i + 1]);
+    }
+    if (t == 0) sm.S[kZeroSlot] = 0ull;
+    __syncthreads();
+}
+
+// F for a tile from its float sum, and whether the tile must go to the walk engine: +inf, a total
+// beyond float range, or a smallest positive term with fewer than 19 bits at that scale.
+__device__ __forceinline__ bool tile_fixed_scale(unsigned mx, unsigned mn, float sum, int& F)
+{
+    const float bound = sum * 1.0009765625f;
+    F = tile_scale(bound);
+    return mx == 0x7F800000u || !(bound < 1.0e38f) ||
+           (mn != 0xFFFFFFFFu && __uint_as_float(mn + 1u) * pow2f(F) < kMinQuantum);
+}
+
 // Pass 1: the local value of every exit (the accu of its in-tile subtree) to P, in the exit forest's
-// post-order, and an upper bound of the tile's material total.  ~0 as the bound asks for the walk engine.
+// post-order, and an upper bound of the tile's material total in 2^-16 units (from its exact fixed-point
+// total).  ~0 as the bound asks for the walk engine.
 // vec: material rows can be read as float4 (16-byte aligned, columns a multiple of 4).
 __global__ void __launch_bounds__(kTileThreads, 4)
     k_tile_exits(TileGeom g, const float* __restrict__ ext, float ext_s, bool vec, TileForest f,
                  const int32_t* __restrict__ exit_base, const uint32_t* __restrict__ exit_span,
                  const uint32_t* __restrict__ exit_pos, float2* __restrict__ P, unsigned long long* block_total)
 {
-    __shared__ unsigned long long S[kScanSlots];
-    __shared__ unsigned long long warp_tot[kTileThreads / 32];
-    __shared__ TileReduce red;
-    const int64_t tile = blockIdx.x;
-    const int64_t tr = tile / g.tcols, tc = tile % g.tcols;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TileCallSmem& sm = *reinterpret_cast<TileCallSmem*>(smem_raw);
+    const int64_t tr = blockIdx.y, tc = blockIdx.x;  // grid = (tile columns, tile rows)
+    const int64_t tile = tr * g.tcols + tc;
     const int t = threadIdx.x;
-    float4 x[4];
-    uint2 pq[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const int cell = quad_cell(j);
-        const int64_t r = tr * kTile + (cell >> 6), c = tc * kTile + (cell & 63);
-        x[j] = ext ? load_quad(ext, g, r, c, vec, 0.0f) : make_float4(ext_s, ext_s, ext_s, ext_s);
-        pq[j] = __ldg(reinterpret_cast<const uint2*>(f.pos + tile * kTileCells + cell));
-    }
+    float4 xm[4];
+    load_material(xm, ext, ext_s, g, tr, tc, vec);
+    uint32_t ca[kRunWords];
+    load_run(f.cell_at + tile * kRunPositions, ca);
     const int32_t e0 = __ldg(exit_base + tile), ne = __ldg(exit_base + tile + 1) - e0;
     uint32_t span = 0, epos = 0;
     if (t < ne) {  // a tile has at most 252 exits (its border cells)
         span = __ldg(exit_span + e0 + t);
         epos = __ldg(exit_pos + e0 + t);
     }
-    float sum = 0.0f, mn = INFINITY;
-    int flags = 0;
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            if (half_at(pq[j], k) & kInvalidPos) continue;
-            const float v = quad_at(x[j], k);
-            if (v > 0.0f) {
-                if (isinf(v)) flags |= 1;
-                else {
-                    sum += v;
-                    mn = fminf(mn, v);
-                }
-            } else if (!(v == 0.0f)) {
-                flags |= 2;
-            }
-        }
-    float tot, tmin;
-    int tflags;
-    tile_reduce(red, sum, mn, flags, tot, tmin, tflags);
-    const float bound = tot * 1.0009765625f;
-    const int F = tile_scale(bound);
-    if ((tflags & 1) || !(bound < 1.0e38f) || (tmin < INFINITY && tmin * pow2f(F) < kMinQuantum)) {
+    store_material(sm, xm);
+    sm.M[kEntryBase + t] = 0.0f;  // nothing enters the tile in this pass
+    __syncthreads();
+    float x[kRun], sum;
+    unsigned mx, mn;
+    gather_run(sm, ca, x, mx, mn, sum);
+    tile_reduce(sm, mx, mn, sum);
+    unsigned poisoned_exit = 0;
+    if (mx > 0x7F800000u) {  // NaN or negative material (or -0): clean the run and count
+        const unsigned bad = clean_run(ca, x, mx, mn, sum);
+        __syncthreads();  // red is reused
+        tile_reduce(sm, mx, mn, sum);
+        poison_counts(sm, bad);
+        if (t < ne) poisoned_exit = count_at(sm, (int)(span & 0xFFFFu)) != count_at(sm, (int)(span >> 16));
+        __syncthreads();  // S and warp_tot are free for the value scan
+    }
+    int F;
+    if (tile_fixed_scale(mx, mn, sum, F)) {
         if (t == 0) block_total[tile] = ~0ull;
         return;  // uniform: every thread has the same reductions
     }
-    const float scale = pow2f(F);
+    unsigned long long a[kRun];
+    if (mn == 0xFFFFFFFFu || __uint_as_float(mn + 1u) * pow2f(F) >= 8388608.0f) {  // every term exact
 #pragma unroll
-    for (int j = 0; j < 4; ++j)
+        for (int j = 0; j < kRun; ++j) a[j] = float_to_fixed64_exact(x[j], F);
+    } else {
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const int p = half_at(pq[j], k);
-            const float v = quad_at(x[j], k);
-            S[scan_slot(p & (kTileCells - 1))] =
-                (!(p & kInvalidPos) && v > 0.0f) ? __float2ull_rn(v * scale) : 0ull;
-        }
-    __syncthreads();
-    tile_scan(S, warp_tot);
-    const int epos_t = (int)(span & 0xFFFFu), estart = (int)(span >> 16);
-    float2 value = make_float2(0.0f, 0.0f);
-    if (t < ne) value = fixed64_to_ff(subtree_sum(S, epos_t, estart), F);
-    if (tflags & 2) {  // NaN or negative material: count it along the same post-order
-        __syncthreads();
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int p = half_at(pq[j], k);
-                S[scan_slot(p & (kTileCells - 1))] = (!(p & kInvalidPos) && !(quad_at(x[j], k) >= 0.0f)) ? 1ull : 0ull;
-            }
-        __syncthreads();
-        tile_scan(S, warp_tot);
-        if (t < ne && subtree_sum(S, epos_t, estart) != 0) value.x = __int_as_float(0x7fc00000);
+        for (int j = 0; j < kRun; ++j) a[j] = float_to_fixed64(x[j], F);
     }
-    if (t < ne) P[epos] = value;
-    if (t == 0) {
-        const double units = (double)bound * 65536.0 + 64.0;
+    tile_prefix(sm, a);
+    if (t < ne) {
+        float2 value = fixed64_to_ff(sm.S[span & 0xFFFFu] - sm.S[span >> 16], F);
+        if (poisoned_exit) value.x = __int_as_float(0x7fc00000);
+        P[epos] = value;
+    }
+    if (t == kTileThreads - 1) {  // a[17] of the last thread: the tile's fixed-point total, exact
+        const double units = ldexp(((double)a[kRun - 1] + 8192.0) * (1.0 + 1e-12), 16 - F) + 64.0;
         block_total[tile] = units < 1.0e18 ? (unsigned long long)units : ~0ull;
     }
 }
@@ -961,130 +1132,113 @@ __global__ void k_exit_sums(int64_t n, const uint32_t* __restrict__ pos, const u
     A[y] = from_u128(a);
 }
 
-// Pass 3: the result of every cell: the accu of its in-tile subtree plus what enters the tile upstream of
-// it (the exact subtree sums of the exits draining into the tile's border cells), in one fixed-point scan
-// per tile.  A tile that cannot be scaled sets the fallback flag total[1]: the walk engine redoes the call.
+// Pass 3: the result of every cell: the accu of its in-tile subtree, where the entry node of each border
+// cell carries the exact subtree sums of the exits draining into it (rounded to float), in one
+// fixed-point scan per tile.  A tile that cannot be scaled sets the fallback flag total[1]: the walk
+// engine redoes the call.
 __global__ void __launch_bounds__(kTileThreads, 4)
     k_tile_accu(TileGeom g, const float* __restrict__ ext, float ext_s, bool vec, float* __restrict__ out,
                 TileForest f, const uint4* __restrict__ A, unsigned long long* total)
 {
-    __shared__ unsigned long long S[kScanSlots];
-    __shared__ unsigned long long warp_tot[kTileThreads / 32];
-    __shared__ TileReduce red;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TileCallSmem& sm = *reinterpret_cast<TileCallSmem*>(smem_raw);
     if (total[1]) return;
     const int Fg = fixed_point_bits(total[0]);
-    const int64_t tile = blockIdx.x;
-    const int64_t tr = tile / g.tcols, tc = tile % g.tcols;
+    const int64_t tr = blockIdx.y, tc = blockIdx.x;  // grid = (tile columns, tile rows)
+    const int64_t tile = tr * g.tcols + tc;
     const int t = threadIdx.x;
-    float4 x[4];
-    uint2 pq[4], sq[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const int cell = quad_cell(j);
-        const int64_t r = tr * kTile + (cell >> 6), c = tc * kTile + (cell & 63);
-        x[j] = ext ? load_quad(ext, g, r, c, vec, 0.0f) : make_float4(ext_s, ext_s, ext_s, ext_s);
-        pq[j] = __ldg(reinterpret_cast<const uint2*>(f.pos + tile * kTileCells + cell));
-        sq[j] = __ldg(reinterpret_cast<const uint2*>(f.start + tile * kTileCells + cell));
-    }
-    // sources entering through the border: the exits of the neighbouring tiles draining into it
-    const unsigned in_mask = t < kBorderCells ? __ldg(f.border_in + tile * kBorderCells + t) : 0u;
-    u128 src = 0;
-    int src_pos = -1;
-    if (in_mask) {
-        int rin, cin;
-        border_cell(t, rin, cin);
-        unsigned m = in_mask;
-        while (m) {
-            const int q = __ffs(m) - 1;
-            m &= m - 1;
-            const int32_t id = __ldg(f.halo_exit + tile * kHaloSlots + halo_slot_of(rin + nb_dr(q), cin + nb_dc(q)));
-            if (id >= 0) src += to_u128(A[id]);
-        }
-        src_pos = __ldg(f.pos + tile * kTileCells + rin * kTile + cin) & (kTileCells - 1);
-    }
-    const bool src_poison = (src >> 96) != 0;
-    const float src_value = src_pos >= 0 ? fixed128_to_float(src & kValueMask, Fg) : 0.0f;
-    float sum = 0.0f, mn = INFINITY;
-    int flags = src_poison ? 2 : 0;
-    if (src_value > 0.0f) {
-        sum = src_value;
-        mn = src_value;
-    }
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            if (half_at(pq[j], k) & kInvalidPos) continue;
-            const float v = quad_at(x[j], k);
-            if (v > 0.0f) {
-                if (isinf(v)) flags |= 1;
-                else {
-                    sum += v;
-                    mn = fminf(mn, v);
-                }
-            } else if (!(v == 0.0f)) {
-                flags |= 2;
+    const uint16_t* pv_table = f.prev_at + tile * kRunPositions;
+    if (t < kRunPositions * 2 / 128)  // the run tables read at the end: into L2 now
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(reinterpret_cast<const char*>(pv_table) + 128 * t));
+    float4 xm[4];
+    load_material(xm, ext, ext_s, g, tr, tc, vec);
+    uint32_t ca[kRunWords];
+    load_run(f.cell_at + tile * kRunPositions, ca);
+    // what enters through border cell t: the exact subtree sums of the exits draining into it, as float
+    // (NaN when one of them is no-data)
+    float entering = 0.0f;
+    if (t < kBorderCells) {
+        const unsigned in_mask = __ldg(f.border_in + tile * kBorderCells + t);
+        if (in_mask) {
+            int rin, cin;
+            border_cell(t, rin, cin);
+            u128 src = 0;
+            unsigned m = in_mask;
+            while (m) {
+                const int q = __ffs(m) - 1;
+                m &= m - 1;
+                const int32_t id =
+                    __ldg(f.halo_exit + tile * kHaloSlots + halo_slot_of(rin + nb_dr(q), cin + nb_dc(q)));
+                if (id >= 0) src += to_u128(A[id]);
             }
+            entering = (src >> 96) ? __int_as_float(0x7fc00000) : fixed128_to_float(src & kValueMask, Fg);
         }
-    float tot, tmin;
-    int tflags;
-    tile_reduce(red, sum, mn, flags, tot, tmin, tflags);
-    const float bound = tot * 1.0009765625f;
-    const int F = tile_scale(bound);
-    if ((tflags & 1) || !(bound < 1.0e38f) || (tmin < INFINITY && tmin * pow2f(F) < kMinQuantum)) {
+    }
+    store_material(sm, xm);
+    sm.M[kEntryBase + t] = entering;
+    __syncthreads();
+    float x[kRun], sum;
+    unsigned mx, mn;
+    gather_run(sm, ca, x, mx, mn, sum);
+    tile_reduce(sm, mx, mn, sum);
+    unsigned poisoned = 0;  // bit j: the subtree of run entry j holds NaN / negative material or a no-data exit
+    uint32_t pv[kRunWords];
+    const bool clean = mx <= 0x7F800000u;  // uniform: no NaN, negative or -0 term in the tile
+    if (!clean) {
+        const unsigned bad = clean_run(ca, x, mx, mn, sum);
+        __syncthreads();  // red is reused
+        tile_reduce(sm, mx, mn, sum);
+        poison_counts(sm, bad);
+        load_run(pv_table, pv);
+#pragma unroll
+        for (int j = 0; j < kRun; ++j)
+            if (count_at(sm, kRun * t + j) != count_at(sm, (int)(run_at(pv, j) & kSlotMask))) poisoned |= 1u << j;
+        __syncthreads();  // S and warp_tot are free for the value scan
+    }
+    int F;
+    if (tile_fixed_scale(mx, mn, sum, F)) {
         if (t == 0) total[1] = 1ull;  // the walk engine redoes the call
         return;
     }
-    // NaN or negative material, or a no-data exit upstream: count them along the post-order first
-    unsigned poisoned = 0;  // bit 4 j + k: cell k of quad j has such a cell in its subtree
-    if (tflags & 2) {
+    unsigned long long a[kRun];
+    if (mn == 0xFFFFFFFFu || __uint_as_float(mn + 1u) * pow2f(F) >= 8388608.0f) {  // every term exact
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
+        for (int j = 0; j < kRun; ++j) a[j] = float_to_fixed64_exact(x[j], F);
+    } else {
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int p = half_at(pq[j], k);
-                S[scan_slot(p & (kTileCells - 1))] = (!(p & kInvalidPos) && !(quad_at(x[j], k) >= 0.0f)) ? 1ull : 0ull;
-            }
-        __syncthreads();
-        if (src_poison) atomicAdd(&S[scan_slot(src_pos)], 1ull);
-        __syncthreads();
-        tile_scan(S, warp_tot);
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int p = half_at(pq[j], k);
-                if (!(p & kInvalidPos) && subtree_sum(S, p, half_at(sq[j], k)) != 0) poisoned |= 1u << (4 * j + k);
-            }
-        __syncthreads();  // S is rewritten below
+        for (int j = 0; j < kRun; ++j) a[j] = float_to_fixed64(x[j], F);
     }
-    const float scale = pow2f(F);
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const int p = half_at(pq[j], k);
-            const float v = quad_at(x[j], k);
-            S[scan_slot(p & (kTileCells - 1))] =
-                (!(p & kInvalidPos) && v > 0.0f) ? __float2ull_rn(v * scale) : 0ull;
-        }
-    __syncthreads();
-    if (src_pos >= 0 && !src_poison) atomicAdd(&S[scan_slot(src_pos)], rescale_fixed(src & kValueMask, F - Fg));
-    __syncthreads();
-    tile_scan(S, warp_tot);
+    tile_prefix(sm, a);
+    load_run(pv_table, pv);
+    // results by position, put in cell order into M (its material was last read by the gather); a cell
+    // without in-tile upstream cells keeps its material there, which is its result
+    const float nan = __int_as_float(0x7fc00000);
     const float unscale = pow2f(-F);
+    const ulonglong2* own = reinterpret_cast<const ulonglong2*>(sm.S + kRun * t);
+#pragma unroll
+    for (int i = 0; i < kRunWords; ++i) {
+        const ulonglong2 s2 = own[i];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int j = 2 * i + h;
+            const unsigned w = run_at(ca, j), p = run_at(pv, j);
+            const bool keep = (p & kPrevRidge) && clean && !(w & kNoValue);  // result already in M
+            const bool write = !(w & kNoOutput) && !keep;
+            const unsigned long long before = write ? sm.S[p & kSlotMask] : 0ull;
+            const unsigned long long v = (h ? s2.y : s2.x) - before;  // < 2^62
+            // two 32-bit conversions, each rounded to nearest, and one fused rounding of their sum: within
+            // about one unit in the last place, and exact when v has at most 24 significant bits
+            const float r = __fmaf_rn(__uint2float_rn((unsigned)(v >> 32)), 4294967296.0f,
+                                      __uint2float_rn((unsigned)v)) * unscale;
+            if (write) sm.M[w & kIndexMask] = ((w & kNoValue) || ((poisoned >> j) & 1u)) ? nan : r;
+        }
+    }
+    __syncthreads();
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        float v[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const int p = half_at(pq[j], k);
-            v[k] = ((p & kInvalidPos) || ((poisoned >> (4 * j + k)) & 1u))
-                       ? __int_as_float(0x7fc00000)
-                       : __ull2float_rn(subtree_sum(S, p, half_at(sq[j], k))) * unscale;
-        }
         const int cell = quad_cell(j);
-        store_quad(out, g, tr * kTile + (cell >> 6), tc * kTile + (cell & 63), vec, make_float4(v[0], v[1], v[2], v[3]));
+        store_quad(out, g, tr * kTile + (cell >> 6), tc * kTile + (cell & 63), vec,
+                   *reinterpret_cast<const float4*>(sm.M + cell));
     }
 }
 
@@ -1206,15 +1360,15 @@ int tile_core_build(TopologyCore* core, cudaStream_t stream)
     k_halo_exits<<<blocks_for(nt * kHaloSlots, 256), 256, 0, stream>>>(core->fd, g, tc->exit_base, bitmap, rowpref,
                                                                       tc->halo_exit);
     // per-tile flow forests in post-order
-    TRY(cudaMalloc(&tc->tile_pos, nt * kTileCells * sizeof(uint16_t)), "tile forest");
-    TRY(cudaMalloc(&tc->tile_start, nt * kTileCells * sizeof(uint16_t)), "tile forest");
+    TRY(cudaMalloc(&tc->cell_at, nt * kRunPositions * sizeof(uint16_t)), "tile forest");
+    TRY(cudaMalloc(&tc->prev_at, nt * kRunPositions * sizeof(uint16_t)), "tile forest");
     TRY(cudaMalloc(&tc->exit_span, std::max<int64_t>(E, 1) * sizeof(uint32_t)), "exit span");
     TRY(cudaMalloc(&tc->border_in, nt * kBorderCells), "tile border masks");
     TRY(cudaFuncSetAttribute(k_tile_forest, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TileSmem)),
         "tile forest");
-    k_tile_forest<<<(unsigned)nt, kTileThreads, sizeof(TileSmem), stream>>>(
-        core->fd, g, tc->exit_base, tc->exit_local, tc->tile_pos, tc->tile_start, tc->exit_span, tc->border_in, flag);
-    tc->bytes += nt * kTileCells * 4 + E * 4 + nt * kBorderCells;
+    k_tile_forest<<<dim3((unsigned)g.tcols, (unsigned)g.trows), kTileThreads, sizeof(TileSmem), stream>>>(
+        core->fd, g, tc->exit_base, tc->exit_local, tc->cell_at, tc->prev_at, tc->exit_span, tc->border_in, flag);
+    tc->bytes += nt * kRunPositions * 4 + E * 4 + nt * kBorderCells;
     TRY(cudaGetLastError(), "tile build");
     TRY(cudaMemcpyAsync(&herr, flag, sizeof(int), cudaMemcpyDeviceToHost, stream), "tile flag");
     TRY(cudaStreamSynchronize(stream), "tile build");
@@ -1270,8 +1424,8 @@ void tile_core_free(TileCore* tc)
     cudaFree(tc->exit_pos);
     cudaFree(tc->exit_start);
     cudaFree(tc->halo_exit);
-    cudaFree(tc->tile_pos);
-    cudaFree(tc->tile_start);
+    cudaFree(tc->cell_at);
+    cudaFree(tc->prev_at);
     cudaFree(tc->exit_span);
     cudaFree(tc->border_in);
     delete tc;
@@ -1312,12 +1466,18 @@ int tile_accu_f32(const TopologyCore* core, TileScratch* s, const float* ext, fl
 {
     const TileCore* tc = core->tiles;
     TileGeom g{core->rows, core->cols, tc->trows, tc->tcols};
-    const TileForest f{tc->tile_pos, tc->tile_start, tc->border_in, tc->halo_exit};
+    const TileForest f{tc->cell_at, tc->prev_at, tc->border_in, tc->halo_exit};
     // rows move as float4 when the columns are a multiple of 4 and the arrays 16-byte aligned
     const bool cols4 = (core->cols & 3) == 0;
     const bool vec_in = cols4 && (!ext || (reinterpret_cast<uintptr_t>(ext) & 15) == 0);
     const bool vec_out = cols4 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
-    k_tile_exits<<<(unsigned)tc->ntiles, kTileThreads, 0, stream>>>(g, ext, ext_s, vec_in, f, tc->exit_base,
+    static const bool smem_ok = cudaFuncSetAttribute(k_tile_exits, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)sizeof(TileCallSmem)) == cudaSuccess &&
+                                cudaFuncSetAttribute(k_tile_accu, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)sizeof(TileCallSmem)) == cudaSuccess;
+    if (!smem_ok) return fail(LUE_GPU_ECUDA, "accu_f32 (tiles): shared memory attribute");
+    const dim3 tile_grid((unsigned)tc->tcols, (unsigned)tc->trows);
+    k_tile_exits<<<tile_grid, kTileThreads, sizeof(TileCallSmem), stream>>>(g, ext, ext_s, vec_in, f, tc->exit_base,
                                                                     tc->exit_span, tc->exit_pos, s->P,
                                                                     s->block_total);
     k_total<<<1, 1024, 0, stream>>>(s->block_total, tc->ntiles, s->total);
@@ -1331,7 +1491,7 @@ int tile_accu_f32(const TopologyCore* core, TileScratch* s, const float* ext, fl
         k_exit_sums<<<blocks_for(E, 256), 256, 0, stream>>>(E, tc->exit_pos, tc->exit_start, s->S, s->A, s->total);
         count_launches(4);
     }
-    k_tile_accu<<<(unsigned)tc->ntiles, kTileThreads, 0, stream>>>(g, ext, ext_s, vec_in && vec_out, out, f, s->A,
+    k_tile_accu<<<tile_grid, kTileThreads, sizeof(TileCallSmem), stream>>>(g, ext, ext_s, vec_in && vec_out, out, f, s->A,
                                                                    s->total);
     count_launches(1);
     return cuda_status(cudaGetLastError(), "accu_f32 (tiles)");
