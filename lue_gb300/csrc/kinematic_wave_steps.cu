@@ -150,6 +150,26 @@ extern "C" int lue_gpu_kinematic_wave_steps_f64_f32in(lue_gpu_topology* t, const
     cudaStream_t stream = (cudaStream_t)stream_;
     TopologyCore* core = t->core;
     const int64_t n = core->n;
+    if (!single_chunk) {
+        // the stage engine with the float-float solve, for a scalar beta that is a small rational p/m;
+        // LUE_GB300_KW_SOLVE=reference keeps the float64 solve of the level waves below
+        const char* e = getenv("LUE_GB300_KW_SOLVE");
+        BetaRational br{0, 0, (float)beta};
+        if (!(e && e[0] == 'r') && beta > 0.0) {
+            for (int m = 1; m <= 16; ++m) {
+                const double p = nearbyint(beta * m);
+                if (p >= 1.0 && p <= 64.0 && fabs(beta - p / m) <= 1e-15 * beta) {
+                    br = BetaRational{(int)p, m, (float)beta};
+                    break;
+                }
+            }
+        }
+        bool done = false;
+        if (int rc = stage_kinematic_wave_steps(t, current_outflow, inflow, inflow_scalar, alpha, alpha_scalar, beta,
+                                                time_step_duration, channel_length, steps, outflow, br, stream, &done))
+            return rc;
+        if (done) return LUE_GPU_OK;
+    }
     if (core->stats.cycle_cells > 0) {
         // the wave schedule needs levels for every cell: one single step per call, ping-pong buffers
         double* tmp = nullptr;

@@ -117,9 +117,22 @@ extern "C" int lue_gpu_accu_f32(lue_gpu_topology* t, const float* inflow, float 
     return cuda_status(cudaGetLastError(), "accu_f32");
 }
 
+// Float64 accu and the rules that are not plain sums run on the stage engine (stage_route.cuh) when the
+// topology has no flow cycles, else on the walk engine.  LUE_GB300_ENGINE=walk forces the walk engine.
+#define STAGE_OR_WALK(call)                          \
+    do {                                             \
+        bool done = false;                           \
+        if (int rc = (call)) return rc;              \
+        if (done) return LUE_GPU_OK;                 \
+    } while (0)
+
 extern "C" int lue_gpu_accu_f64(lue_gpu_topology* t, const double* inflow, double inflow_scalar, double* outflow,
                                 void* stream)
 {
+    if (int rc = check_topology(t, "accu_f64")) return rc;
+    if (!outflow) return fail(LUE_GPU_EINVAL, "accu_f64: NULL output");
+    STAGE_OR_WALK(stage_route_f64(t, (int)Rule::accu, inflow, inflow_scalar, nullptr, 0.0, outflow, nullptr,
+                                  (cudaStream_t)stream, &done));
     return route_f64<Rule::accu>(t, inflow, inflow_scalar, nullptr, 0.0, outflow, nullptr, stream, "accu_f64");
 }
 
@@ -127,6 +140,10 @@ extern "C" int lue_gpu_accu_threshold_f32(lue_gpu_topology* t, const float* infl
                                           const float* threshold, float threshold_scalar, float* flux, float* state,
                                           void* stream)
 {
+    if (int rc = check_topology(t, "accu_threshold_f32")) return rc;
+    if (!flux || !state) return fail(LUE_GPU_EINVAL, "accu_threshold_f32: NULL output");
+    STAGE_OR_WALK(stage_route_f32(t, (int)Rule::threshold, inflow, inflow_scalar, threshold, threshold_scalar, flux,
+                                  state, (cudaStream_t)stream, &done));
     return route_f32<Rule::threshold>(t, inflow, inflow_scalar, threshold, threshold_scalar, flux, state, stream,
                                       "accu_threshold_f32");
 }
@@ -135,6 +152,10 @@ extern "C" int lue_gpu_accu_threshold_f64(lue_gpu_topology* t, const double* inf
                                           const double* threshold, double threshold_scalar, double* flux,
                                           double* state, void* stream)
 {
+    if (int rc = check_topology(t, "accu_threshold_f64")) return rc;
+    if (!flux || !state) return fail(LUE_GPU_EINVAL, "accu_threshold_f64: NULL output");
+    STAGE_OR_WALK(stage_route_f64(t, (int)Rule::threshold, inflow, inflow_scalar, threshold, threshold_scalar, flux,
+                                  state, (cudaStream_t)stream, &done));
     return route_f64<Rule::threshold>(t, inflow, inflow_scalar, threshold, threshold_scalar, flux, state, stream,
                                       "accu_threshold_f64");
 }
@@ -143,6 +164,10 @@ extern "C" int lue_gpu_accu_fraction_f32(lue_gpu_topology* t, const float* inflo
                                          const float* fraction, float fraction_scalar, float* flux, float* state,
                                          void* stream)
 {
+    if (int rc = check_topology(t, "accu_fraction_f32")) return rc;
+    if (!flux || !state) return fail(LUE_GPU_EINVAL, "accu_fraction_f32: NULL output");
+    STAGE_OR_WALK(stage_route_f32(t, (int)Rule::fraction, inflow, inflow_scalar, fraction, fraction_scalar, flux,
+                                  state, (cudaStream_t)stream, &done));
     return route_f32<Rule::fraction>(t, inflow, inflow_scalar, fraction, fraction_scalar, flux, state, stream,
                                      "accu_fraction_f32");
 }
@@ -151,6 +176,10 @@ extern "C" int lue_gpu_accu_fraction_f64(lue_gpu_topology* t, const double* infl
                                          const double* fraction, double fraction_scalar, double* flux, double* state,
                                          void* stream)
 {
+    if (int rc = check_topology(t, "accu_fraction_f64")) return rc;
+    if (!flux || !state) return fail(LUE_GPU_EINVAL, "accu_fraction_f64: NULL output");
+    STAGE_OR_WALK(stage_route_f64(t, (int)Rule::fraction, inflow, inflow_scalar, fraction, fraction_scalar, flux,
+                                  state, (cudaStream_t)stream, &done));
     return route_f64<Rule::fraction>(t, inflow, inflow_scalar, fraction, fraction_scalar, flux, state, stream,
                                      "accu_fraction_f64");
 }
@@ -164,6 +193,10 @@ extern "C" int lue_gpu_kinematic_wave_f64(lue_gpu_topology* t, const double* cur
 {
     if (int rc = check_topology(t, "kinematic_wave_f64")) return rc;
     if (!outflow) return fail(LUE_GPU_EINVAL, "kinematic_wave_f64: NULL output");
+    STAGE_OR_WALK(stage_kinematic_wave_f64(t, current_outflow, current_outflow_scalar, inflow, inflow_scalar, alpha,
+                                           alpha_scalar, beta, beta_scalar, time_step_duration, channel_length,
+                                           channel_length_scalar, outflow, rational_beta(beta, beta_scalar),
+                                           (cudaStream_t)stream, &done));
     RouteKW<double> v{t->core->upmask, current_outflow, current_outflow_scalar, inflow, inflow_scalar, alpha,
                       alpha_scalar, beta, beta_scalar, time_step_duration, channel_length, channel_length_scalar,
                       outflow, t->core->cols, rational_beta(beta, beta_scalar)};
@@ -178,6 +211,9 @@ extern "C" int lue_gpu_kinematic_wave_f64_f32in(lue_gpu_topology* t, const doubl
 {
     if (int rc = check_topology(t, "kinematic_wave_f64_f32in")) return rc;
     if (!outflow) return fail(LUE_GPU_EINVAL, "kinematic_wave_f64_f32in: NULL output");
+    STAGE_OR_WALK(stage_kinematic_wave_f32in(t, current_outflow, current_outflow_scalar, inflow, inflow_scalar, alpha,
+                                             alpha_scalar, beta, time_step_duration, channel_length, outflow,
+                                             rational_beta(nullptr, beta), (cudaStream_t)stream, &done));
     RouteKW<float> v{t->core->upmask, current_outflow, current_outflow_scalar, inflow, inflow_scalar, alpha,
                      alpha_scalar, nullptr, beta, time_step_duration, nullptr, channel_length, outflow,
                      t->core->cols, rational_beta(nullptr, beta)};

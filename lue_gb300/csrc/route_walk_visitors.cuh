@@ -27,6 +27,57 @@ enum class Rule { accu, threshold, fraction };
 
 // --- float32: float-float running values ---------------------------------------------------------
 
+// The float32 cell rule on the float-float upstream sum t (already normalised or not) and the cell's
+// inputs: the outflow (out_hi + out_lo, passed on downstream) and the state.  False: the cell is no-data.
+template <Rule R>
+__device__ __forceinline__ bool rule_f32(FF t, bool nan, float x, float b, float& out_hi, float& out_lo, float& rem)
+{
+    if (R == Rule::accu) {
+        if (nan || isnan(x) || !(x >= 0.0f)) return false;
+        t.add(x);
+        t.normalise();
+        out_hi = t.hi;
+        out_lo = t.lo;
+    } else if (R == Rule::threshold) {
+        const float th = b;
+        if (nan || isnan(x) || isnan(th) || !(x >= 0.0f && th >= 0.0f)) return false;
+        t.add(x);
+        t.normalise();
+        // strict '>' on the compensated total (accu_threshold.hpp:157)
+        if (t.hi > th || (t.hi == th && t.lo > 0.0f)) {
+            FF d{0.0f, 0.0f};
+            two_sum(t.hi, -th, d.hi, d.lo);
+            d.lo = __fadd_rn(d.lo, t.lo);
+            d.normalise();
+            rem = th;
+            out_hi = d.hi;
+            out_lo = d.lo;
+        } else {
+            rem = __fadd_rn(t.hi, t.lo);
+            out_hi = 0.0f;
+            out_lo = 0.0f;
+        }
+    } else {
+        const float f = b;
+        if (nan || isnan(x) || isnan(f) || !(x >= 0.0f && f >= 0.0f && f <= 1.0f)) return false;
+        t.add(x);
+        t.normalise();
+        // flux = fraction * total, state = total - flux (accu_fraction.hpp:157-159)
+        float ph = __fmul_rn(f, t.hi);
+        float pl = __fmaf_rn(f, t.hi, -ph);
+        pl = __fmaf_rn(f, t.lo, pl);
+        FF d{ph, pl};
+        d.normalise();
+        FF r{0.0f, 0.0f};
+        two_sum(t.hi, -d.hi, r.hi, r.lo);
+        r.lo = __fadd_rn(r.lo, __fsub_rn(t.lo, d.lo));
+        rem = __fadd_rn(r.hi, r.lo);
+        out_hi = d.hi;
+        out_lo = d.lo;
+    }
+    return true;
+}
+
 template <Rule R>
 struct RouteF32 {
     const uint8_t* upmask;
@@ -59,63 +110,47 @@ struct RouteF32 {
             if (isnan(h)) nan = true;
             else t.add(h, load_cg(lo + u));
         }
-        float x = value_at(a, as, c);
-        if (R == Rule::accu) {
-            if (nan || isnan(x) || !(x >= 0.0f)) {
-                no_data(c);
-                return;
-            }
-            t.add(x);
-            t.normalise();
-            out[c] = t.hi;
-            lo[c] = t.lo;
-        } else if (R == Rule::threshold) {
-            float th = value_at(b, bs, c);
-            if (nan || isnan(x) || isnan(th) || !(x >= 0.0f && th >= 0.0f)) {
-                no_data(c);
-                return;
-            }
-            t.add(x);
-            t.normalise();
-            // strict '>' on the compensated total (accu_threshold.hpp:157)
-            if (t.hi > th || (t.hi == th && t.lo > 0.0f)) {
-                FF d{0.0f, 0.0f};
-                two_sum(t.hi, -th, d.hi, d.lo);
-                d.lo = __fadd_rn(d.lo, t.lo);
-                d.normalise();
-                rem[c] = th;
-                out[c] = d.hi;
-                lo[c] = d.lo;
-            } else {
-                rem[c] = __fadd_rn(t.hi, t.lo);
-                out[c] = 0.0f;
-                lo[c] = 0.0f;
-            }
-        } else {
-            float f = value_at(b, bs, c);
-            if (nan || isnan(x) || isnan(f) || !(x >= 0.0f && f >= 0.0f && f <= 1.0f)) {
-                no_data(c);
-                return;
-            }
-            t.add(x);
-            t.normalise();
-            // flux = fraction * total, state = total - flux (accu_fraction.hpp:157-159)
-            float ph = __fmul_rn(f, t.hi);
-            float pl = __fmaf_rn(f, t.hi, -ph);
-            pl = __fmaf_rn(f, t.lo, pl);
-            FF d{ph, pl};
-            d.normalise();
-            FF r{0.0f, 0.0f};
-            two_sum(t.hi, -d.hi, r.hi, r.lo);
-            r.lo = __fadd_rn(r.lo, __fsub_rn(t.lo, d.lo));
-            rem[c] = __fadd_rn(r.hi, r.lo);
-            out[c] = d.hi;
-            lo[c] = d.lo;
+        float oh = 0.0f, ol = 0.0f, r = 0.0f;
+        if (!rule_f32<R>(t, nan, value_at(a, as, c), R == Rule::accu ? 0.0f : value_at(b, bs, c), oh, ol, r)) {
+            no_data(c);
+            return;
         }
+        out[c] = oh;
+        lo[c] = ol;
+        if (R != Rule::accu) rem[c] = r;
     }
 };
 
 // --- float64: plain double arithmetic, like the reference's double instantiation ---------------------
+
+// The float64 cell rule on the upstream sum t: outflow and state.  False: the cell is no-data.
+template <Rule R>
+__device__ __forceinline__ bool rule_f64(double t, bool nan, double x, double b, double& out, double& rem)
+{
+    if (R == Rule::accu) {
+        if (nan || isnan(x) || !(x >= 0.0)) return false;
+        out = t + x;
+    } else if (R == Rule::threshold) {
+        const double th = b;
+        if (nan || isnan(x) || isnan(th) || !(x >= 0.0 && th >= 0.0)) return false;
+        t += x;
+        if (t > th) {
+            rem = th;
+            out = t - th;
+        } else {
+            rem = t;
+            out = 0.0;
+        }
+    } else {
+        const double f = b;
+        if (nan || isnan(x) || isnan(f) || !(x >= 0.0 && f >= 0.0 && f <= 1.0)) return false;
+        t += x;
+        const double d = f * t;
+        rem = t - d;
+        out = d;
+    }
+    return true;
+}
 
 template <Rule R>
 struct RouteF64 {
@@ -146,33 +181,27 @@ struct RouteF64 {
             if (isnan(h)) nan = true;
             else t += h;
         }
-        double x = value_at(a, as, c);
-        if (R == Rule::accu) {
-            if (nan || isnan(x) || !(x >= 0.0)) return no_data(c);
-            out[c] = t + x;
-        } else if (R == Rule::threshold) {
-            double th = value_at(b, bs, c);
-            if (nan || isnan(x) || isnan(th) || !(x >= 0.0 && th >= 0.0)) return no_data(c);
-            t += x;
-            if (t > th) {
-                rem[c] = th;
-                out[c] = t - th;
-            } else {
-                rem[c] = t;
-                out[c] = 0.0;
-            }
-        } else {
-            double f = value_at(b, bs, c);
-            if (nan || isnan(x) || isnan(f) || !(x >= 0.0 && f >= 0.0 && f <= 1.0)) return no_data(c);
-            t += x;
-            double d = f * t;
-            rem[c] = t - d;
-            out[c] = d;
-        }
+        double o = 0.0, r = 0.0;
+        if (!rule_f64<R>(t, nan, value_at(a, as, c), R == Rule::accu ? 0.0 : value_at(b, bs, c), o, r))
+            return no_data(c);
+        out[c] = o;
+        if (R != Rule::accu) rem[c] = r;
     }
 };
 
 // --- kinematic wave (float64 discharge; lateral inflow and alpha as TIn) ------------------------------
+
+// The kinematic-wave cell rule (kinematic_wave.hpp:416-456): NaN outside the domain, else the new
+// discharge from the upstream sum.
+__device__ __forceinline__ double rule_kw(double up, bool nan, double qc, double q, double al, double be, double dt,
+                                          double len, BetaRational br)
+{
+    if (nan || isnan(qc) || isnan(q) || isnan(al) || isnan(be) || isnan(dt) || isnan(len) ||
+        !(qc >= 0.0 && q >= 0.0 && len > 0.0))
+        return qnan<double>();
+    return br.m ? iterate_to_new_discharge_fast(up, qc, q, al, be, br, dt, len)
+                : iterate_to_new_discharge(up, qc, q, al, be, dt, len);
+}
 
 template <class TIn>
 struct RouteKW {
@@ -211,13 +240,7 @@ struct RouteKW {
         double al = alpha ? (double)__ldg(alpha + c) : alpha_s;
         double be = beta ? __ldg(beta + c) : beta_s;
         double len = dx ? __ldg(dx + c) : dx_s;
-        if (nan || isnan(qc) || isnan(q) || isnan(al) || isnan(be) || isnan(dt) || isnan(len) ||
-            !(qc >= 0.0 && q >= 0.0 && len > 0.0)) {
-            out[c] = qnan<double>();
-            return;
-        }
-        out[c] = br.m ? iterate_to_new_discharge_fast(up, qc, q, al, be, br, dt, len)
-                      : iterate_to_new_discharge(up, qc, q, al, be, dt, len);
+        out[c] = rule_kw(up, nan, qc, q, al, be, dt, len, br);
     }
 };
 

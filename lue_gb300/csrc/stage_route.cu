@@ -1,0 +1,1086 @@
+// stage_route.cu — the stage engine (see stage_route.cuh): build, the wave kernel and its cell rules,
+// and the routing entry points that use it.
+#include <algorithm>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "kinematic_wave_ff.cuh"
+#include "route_walk_visitors.cuh"
+#include "stage_route.cuh"
+#include "topology.cuh"
+
+namespace lue_gb300 {
+
+// ---------------------------------------------------------------------------------------------------
+// Build
+// ---------------------------------------------------------------------------------------------------
+
+// Crossing depth: the largest number of tile edges crossed by a flow path ending at the cell, by the
+// upstream-first walk of walk.cuh.
+struct CrossDepthVisitor {
+    const uint8_t* upmask;
+    int32_t* depth;
+    int64_t cols;
+    __device__ void enter(int64_t c)
+    {
+        const int64_t r = c / cols, col = c - r * cols;
+        const int64_t tr = r / kStageSide, tc = col / kStageSide;
+        unsigned m = __ldg(upmask + c);
+        int32_t d = 0;
+        while (m) {
+            const int k = __ffs(m) - 1;
+            m &= m - 1;
+            const int64_t ur = r + nb_dr(k), uc = col + nb_dc(k);
+            int32_t du = load_cg(depth + ur * cols + uc);
+            if (ur / kStageSide != tr || uc / kStageSide != tc) ++du;
+            d = du > d ? du : d;
+        }
+        depth[c] = d;
+    }
+    __device__ void no_data(int64_t c) { depth[c] = -1; }
+};
+
+struct StageGeom {
+    int64_t rows, cols, tcols;
+};
+
+// In-tile cell of position p of the tile (row-major) and its global index; false outside the array.
+__device__ __forceinline__ bool stage_cell(const StageGeom& g, int64_t tr, int64_t tc, int p, int64_t& gi)
+{
+    const int64_t r = tr * kStageSide + (p >> 5), c = tc * kStageSide + (p & 31);
+    gi = r * g.cols + c;
+    return r < g.rows && c < g.cols;
+}
+
+// Inclusive scan of one int per thread over the build CTA; total gets the block sum.
+__device__ __forceinline__ int build_scan(int v, int* warp_tot, int& total)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    int before = 0;
+    total = 0;
+    for (int w = 0; w < kStageBuildThreads / 32; ++w) {
+        const int s = warp_tot[w];
+        before += w < warp ? s : 0;
+        total += s;
+    }
+    __syncthreads();
+    return before + x;
+}
+
+struct StageSortSmem {
+    unsigned long long key[kStageCells];
+    int32_t d[kStageCells];
+    int16_t sd[kStageCells];  // downstream cell in the same stage, or -1
+    int16_t h[kStageCells];   // distance to the stage's most downstream cell
+    int16_t J[kStageCells];
+    int warp_tot[kStageBuildThreads / 32];
+};
+
+// Depth of in-tile cell p, or of the global cell gi when p < 0 (another tile).
+__device__ __forceinline__ int32_t depth_of(const StageSortSmem& sm, const int32_t* depth, int p, int64_t gi)
+{
+    return p >= 0 ? sm.d[p] : __ldg(depth + gi);
+}
+
+// Per tile: the order of its valid cells by (depth, round), the rounds, and per position a flag word
+// (bit 0: first cell of a stage, bit 1: the outflow leaves the stage, bits 2-5: inputs from other stages);
+// counts[4 tile ..] = stages, exits, inputs, valid cells.
+__global__ void __launch_bounds__(kStageBuildThreads)
+    k_stage_sort(const uint8_t* __restrict__ fd, const uint8_t* __restrict__ upmask, const int32_t* __restrict__ depth,
+                 StageGeom g, uint16_t* order, uint16_t* round_at, uint16_t* flags_at, int32_t* counts)
+{
+    __shared__ StageSortSmem sm;
+    const int64_t tr = blockIdx.y, tc = blockIdx.x, tile = tr * g.tcols + tc;
+    const int t = threadIdx.x;
+    for (int p = t; p < kStageCells; p += kStageBuildThreads) {
+        int64_t gi;
+        sm.d[p] = stage_cell(g, tr, tc, p, gi) ? __ldg(depth + gi) : -1;
+    }
+    __syncthreads();
+    for (int p = t; p < kStageCells; p += kStageBuildThreads) {
+        int s = -1;
+        int64_t gi;
+        if (sm.d[p] >= 0 && stage_cell(g, tr, tc, p, gi)) {
+            int dr, dc;
+            const int pr = (p >> 5) + 0, pc = p & 31;
+            if (d8_offset(__ldg(fd + gi), dr, dc)) {
+                const int qr = pr + dr, qc = pc + dc;
+                const int64_t gr = tr * kStageSide + qr, gc = tc * kStageSide + qc;
+                if (qr >= 0 && qr < kStageSide && qc >= 0 && qc < kStageSide && gr < g.rows && gc < g.cols &&
+                    sm.d[qr * kStageSide + qc] == sm.d[p])
+                    s = qr * kStageSide + qc;
+            }
+        }
+        sm.sd[p] = (int16_t)s;
+        sm.h[p] = (int16_t)(s >= 0 ? 1 : 0);
+        sm.J[p] = (int16_t)(s >= 0 ? s : p);
+    }
+    __syncthreads();
+    // distances to the stage's most downstream cell, by pointer jumping (chains of at most 1024 cells)
+    for (int it = 0; it < 10; ++it) {
+        int nh[2], nj[2];
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int p = t + k * kStageBuildThreads, j = sm.J[p];
+            nh[k] = sm.h[p] + (j != p ? sm.h[j] : 0);
+            nj[k] = sm.J[j];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int p = t + k * kStageBuildThreads;
+            sm.h[p] = (int16_t)nh[k];
+            sm.J[p] = (int16_t)nj[k];
+        }
+        __syncthreads();
+    }
+    for (int p = t; p < kStageCells; p += kStageBuildThreads)
+        sm.key[p] = sm.d[p] >= 0 ? ((unsigned long long)sm.d[p] << 20) | ((unsigned long long)(1023 - sm.h[p]) << 10) |
+                                       (unsigned long long)p
+                                 : ~0ull;
+    __syncthreads();
+    // bitonic sort, ascending
+    for (int k = 2; k <= kStageCells; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = t; i < kStageCells; i += kStageBuildThreads) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const unsigned long long a = sm.key[i], b = sm.key[l];
+                    const bool up = (i & k) == 0;
+                    if ((a > b) == up) {
+                        sm.key[i] = b;
+                        sm.key[l] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // per position (thread t: positions 2t, 2t + 1): stage starts, rounds, exits, inputs
+    int starts = 0, exits = 0, inputs = 0, valid = 0;
+    int first[2];
+    for (int k = 0; k < 2; ++k) {
+        const int i = 2 * t + k;
+        const unsigned long long key = sm.key[i];
+        first[k] = 0;
+        if (key == ~0ull) continue;
+        const int dd = (int)(key >> 20);
+        if (i == 0 || (int)(sm.key[i - 1] >> 20) != dd) {
+            first[k] = 1;
+            ++starts;
+        }
+        ++valid;
+    }
+    // the first position of each position's stage: inclusive max-scan of start positions
+    int mine = -1;
+    for (int k = 0; k < 2; ++k)
+        if (first[k]) mine = 2 * t + k;
+    {
+        const int lane = t & 31, warp = t >> 5;
+        int x = mine;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x = max(x, y);
+        }
+        if (lane == 31) sm.warp_tot[warp] = x;
+        __syncthreads();
+        int before = -1;
+        for (int w = 0; w < warp; ++w) before = max(before, sm.warp_tot[w]);
+        const int excl_lane = __shfl_up_sync(0xffffffffu, x, 1);
+        mine = max(before, lane ? excl_lane : -1);  // last start strictly before position 2t
+        __syncthreads();
+    }
+    for (int k = 0; k < 2; ++k) {
+        const int i = 2 * t + k;
+        const unsigned long long key = sm.key[i];
+        uint16_t flag = 0, rnd = 0;
+        if (key != ~0ull) {
+            if (first[k]) mine = i;
+            const int p = (int)(key & 1023), dd = (int)(key >> 20);
+            const int hh = 1023 - (int)((key >> 10) & 1023);
+            const int hs = 1023 - (int)((sm.key[mine] >> 10) & 1023);
+            rnd = (uint16_t)(hs - hh);
+            int64_t gi;
+            stage_cell(g, tr, tc, p, gi);
+            const int pr = p >> 5, pc = p & 31;
+            // exit: the downstream cell is valid and in another stage
+            int dr, dc;
+            bool ex = false;
+            if (d8_offset(__ldg(fd + gi), dr, dc)) {
+                const int64_t gr = tr * kStageSide + pr + dr, gc = tc * kStageSide + pc + dc;
+                if (gr >= 0 && gr < g.rows && gc >= 0 && gc < g.cols) {
+                    const int qr = pr + dr, qc = pc + dc;
+                    const bool in = qr >= 0 && qr < kStageSide && qc >= 0 && qc < kStageSide;
+                    const int32_t dv = depth_of(sm, depth, in ? qr * kStageSide + qc : -1, gr * g.cols + gc);
+                    ex = dv >= 0 && (!in || dv != dd);
+                }
+            }
+            // inputs: upstream cells in other stages
+            unsigned m = __ldg(upmask + gi), nin = 0;
+            while (m) {
+                const int q = __ffs(m) - 1;
+                m &= m - 1;
+                const int qr = pr + nb_dr(q), qc = pc + nb_dc(q);
+                const bool in = qr >= 0 && qr < kStageSide && qc >= 0 && qc < kStageSide;
+                if (!in || sm.d[qr * kStageSide + qc] != dd) ++nin;
+            }
+            flag = (uint16_t)(first[k] | (ex ? 2 : 0) | (nin << 2));
+            exits += ex;
+            inputs += (int)nin;
+            order[tile * kStageCells + i] = (uint16_t)p;
+        } else {
+            order[tile * kStageCells + i] = 0xFFFFu;
+        }
+        round_at[tile * kStageCells + i] = rnd;
+        flags_at[tile * kStageCells + i] = flag;
+    }
+    int tot;
+    build_scan(starts, sm.warp_tot, tot);
+    if (t == 0) counts[4 * tile + 0] = tot;
+    build_scan(exits, sm.warp_tot, tot);
+    if (t == 0) counts[4 * tile + 1] = tot;
+    build_scan(inputs, sm.warp_tot, tot);
+    if (t == 0) counts[4 * tile + 2] = tot;
+    build_scan(valid, sm.warp_tot, tot);
+    if (t == 0) counts[4 * tile + 3] = tot;
+}
+
+// Per tile, with the global bases of its stages, exits and inputs: stage records, exit rows (by
+// position, and by global cell for the input lists), meta, and the first input of each position.
+__global__ void __launch_bounds__(kStageBuildThreads)
+    k_stage_ids(const uint8_t* __restrict__ upmask, const int32_t* __restrict__ depth, StageGeom g,
+                const uint16_t* __restrict__ order, const uint16_t* __restrict__ round_at,
+                const uint16_t* __restrict__ flags_at, const int32_t* __restrict__ bases, int4* stage,
+                int32_t* stage_depth, int32_t* exit_id, int32_t* cell_exit, int32_t* input_at, uint2* meta)
+{
+    __shared__ int warp_tot[kStageBuildThreads / 32];
+    __shared__ int s_begin[kStageCells], s_count[kStageCells], s_rounds[kStageCells], s_in0[kStageCells];
+    __shared__ int s_nin[kStageCells];
+    __shared__ int32_t d[kStageCells];
+    const int64_t tr = blockIdx.y, tc = blockIdx.x, tile = tr * g.tcols + tc;
+    const int t = threadIdx.x;
+    for (int p = t; p < kStageCells; p += kStageBuildThreads) {
+        int64_t gi;
+        d[p] = stage_cell(g, tr, tc, p, gi) ? __ldg(depth + gi) : -1;
+        s_count[p] = 0;
+        s_rounds[p] = 0;
+        s_nin[p] = 0;
+    }
+    const int stage_base = bases[4 * tile + 0], exit_base = bases[4 * tile + 1], input_base = bases[4 * tile + 2];
+    uint16_t o[2], r[2], f[2];
+    int starts = 0, exits = 0, ins = 0;
+    for (int k = 0; k < 2; ++k) {
+        const int i = 2 * t + k;
+        o[k] = order[tile * kStageCells + i];
+        r[k] = round_at[tile * kStageCells + i];
+        f[k] = flags_at[tile * kStageCells + i];
+        if (o[k] != 0xFFFFu) {
+            starts += f[k] & 1;
+            exits += (f[k] >> 1) & 1;
+            ins += f[k] >> 2;
+        }
+    }
+    int tot;
+    const int s_excl = build_scan(starts, warp_tot, tot) - starts;
+    const int e_excl = build_scan(exits, warp_tot, tot) - exits;
+    const int i_excl = build_scan(ins, warp_tot, tot) - ins;
+    // stage of each position: the count of starts up to it, minus one
+    int local[2];
+    {
+        int s_run = s_excl, i_cur = i_excl;
+        for (int k = 0; k < 2; ++k) {
+            const int i = 2 * t + k;
+            local[k] = -1;
+            if (o[k] == 0xFFFFu) continue;
+            if (f[k] & 1) {
+                s_begin[s_run] = i;
+                s_in0[s_run] = i_cur;
+                ++s_run;
+            }
+            local[k] = s_run - 1;
+            i_cur += f[k] >> 2;
+        }
+    }
+    __syncthreads();
+    for (int k = 0; k < 2; ++k) {
+        if (local[k] < 0) continue;
+        atomicAdd(&s_count[local[k]], 1);
+        atomicMax(&s_rounds[local[k]], (int)r[k] + 1);
+        atomicAdd(&s_nin[local[k]], (int)(f[k] >> 2));
+    }
+    __syncthreads();
+    int e_run = e_excl, i_cur = i_excl;
+    for (int k = 0; k < 2; ++k) {
+        const int i = 2 * t + k;
+        const int64_t at = tile * kStageCells + i;
+        if (o[k] == 0xFFFFu) {
+            exit_id[at] = -1;
+            input_at[at] = -1;
+            meta[at] = make_uint2(0u, 0u);
+            continue;
+        }
+        const int p = o[k], pr = p >> 5, pc = p & 31, dd = d[p];
+        int64_t gi;
+        stage_cell(g, tr, tc, p, gi);
+        int32_t id = -1;
+        if ((f[k] >> 1) & 1) {
+            id = exit_base + e_run++;
+            cell_exit[gi] = id;
+        }
+        exit_id[at] = id;
+        const unsigned um = __ldg(upmask + gi);
+        unsigned em = 0, mm = um;
+        while (mm) {
+            const int q = __ffs(mm) - 1;
+            mm &= mm - 1;
+            const int qr = pr + nb_dr(q), qc = pc + nb_dc(q);
+            const bool in = qr >= 0 && qr < kStageSide && qc >= 0 && qc < kStageSide;
+            if (!in || d[qr * kStageSide + qc] != dd) em |= 1u << q;
+        }
+        const int ls = local[k];
+        input_at[at] = input_base + i_cur;
+        const unsigned first_input = (unsigned)(i_cur - s_in0[ls]);
+        i_cur += f[k] >> 2;
+        meta[at] = make_uint2((unsigned)p | ((unsigned)r[k] << 10), um | (em << 8) | (first_input << 16));
+        if (f[k] & 1) {
+            const int sid = stage_base + ls;
+            stage[sid] = make_int4((int)tile, s_begin[ls] | (s_count[ls] << 16), s_rounds[ls] | (s_nin[ls] << 16),
+                                   input_base + s_in0[ls]);
+            stage_depth[sid] = dd;
+        }
+    }
+}
+
+// Per tile, once every exit has its row: the input lists (the history row of each upstream cell in
+// another stage, in neighbour order).
+__global__ void __launch_bounds__(kStageBuildThreads)
+    k_stage_inputs(StageGeom g, const uint16_t* __restrict__ order, const uint2* __restrict__ meta,
+                   const int32_t* __restrict__ input_at, const int32_t* __restrict__ cell_exit, int32_t* inputs,
+                   int* error)
+{
+    const int64_t tr = blockIdx.y, tc = blockIdx.x, tile = tr * g.tcols + tc;
+    for (int i = threadIdx.x; i < kStageCells; i += kStageBuildThreads) {
+        const int64_t at = tile * kStageCells + i;
+        const uint16_t p = order[at];
+        if (p == 0xFFFFu) continue;
+        unsigned em = (meta[at].y >> 8) & 0xFFu;
+        if (!em) continue;
+        int64_t gi;
+        stage_cell(g, tr, tc, p, gi);
+        int32_t w = input_at[at];
+        while (em) {
+            const int q = __ffs(em) - 1;
+            em &= em - 1;
+            const int32_t id = cell_exit[gi + nb_dr(q) * g.cols + nb_dc(q)];
+            if (id < 0) *error = 1;
+            inputs[w++] = id;
+        }
+    }
+}
+
+static inline int64_t div_up(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stream, StageCore** out)
+{
+    *out = nullptr;
+    const int64_t n = core->n, rows = core->rows, cols = core->cols;
+    auto* sc = new (std::nothrow) StageCore();
+    if (!sc) return fail(LUE_GPU_ENOMEM, "stage topology: host allocation");
+    sc->trows = div_up(rows, kStageSide);
+    sc->tcols = div_up(cols, kStageSide);
+    sc->ntiles = sc->trows * sc->tcols;
+    const int64_t nt = sc->ntiles, np = nt * kStageCells;
+    if (sc->trows > 65535) {
+        delete sc;
+        return fail(LUE_GPU_ERANGE, "stage topology: more than 65535 rows of 32-cell tiles");
+    }
+    const StageGeom g{rows, cols, sc->tcols};
+    const dim3 grid((unsigned)sc->tcols, (unsigned)sc->trows);
+    int32_t *depth = nullptr, *counts = nullptr, *bases = nullptr, *cell_exit = nullptr, *input_at = nullptr;
+    int32_t *stage_depth = nullptr, *error = nullptr;
+    uint16_t *order = nullptr, *round_at = nullptr, *flags_at = nullptr;
+    std::vector<int32_t> hc(4 * nt), hb(4 * nt);
+    int herr = 0;
+    int rc = 0;
+#define TRY(call, what) \
+    if ((rc = cuda_status((call), what))) goto done
+    TRY(cudaMalloc(&depth, n * sizeof(int32_t)), "stage depth");
+    TRY(cudaMalloc(&order, np * sizeof(uint16_t)), "stage order");
+    TRY(cudaMalloc(&round_at, np * sizeof(uint16_t)), "stage rounds");
+    TRY(cudaMalloc(&flags_at, np * sizeof(uint16_t)), "stage flags");
+    TRY(cudaMalloc(&counts, 4 * nt * sizeof(int32_t)), "stage counts");
+    TRY(cudaMalloc(&bases, 4 * nt * sizeof(int32_t)), "stage bases");
+    TRY(cudaMalloc(&error, sizeof(int)), "stage flag");
+    TRY(cudaMemsetAsync(error, 0, sizeof(int), stream), "memset");
+    // crossing depths by the upstream-first walk
+    TRY(cudaMemcpyAsync(work, core->count, words_for(n) * 4, cudaMemcpyDeviceToDevice, stream), "stage depth");
+    {
+        WalkGrid wg{core->fd, core->count, work, rows, cols, n};
+        CrossDepthVisitor v{core->upmask, depth, cols};
+        k_walk<<<grid_all(n, 256), 256, 0, stream>>>(wg, v);
+    }
+    k_stage_sort<<<grid, kStageBuildThreads, 0, stream>>>(core->fd, core->upmask, depth, g, order, round_at, flags_at,
+                                                         counts);
+    count_launches(2);
+    TRY(cudaGetLastError(), "stage sort");
+    TRY(cudaMemcpyAsync(hc.data(), counts, 4 * nt * sizeof(int32_t), cudaMemcpyDeviceToHost, stream), "stage counts");
+    TRY(cudaStreamSynchronize(stream), "stage counts");
+    {
+        int64_t tot[3] = {0, 0, 0};
+        for (int64_t i = 0; i < nt; ++i) {
+            for (int k = 0; k < 3; ++k) {
+                hb[4 * i + k] = (int32_t)tot[k];
+                tot[k] += hc[4 * i + k];
+            }
+            hb[4 * i + 3] = 0;
+        }
+        if (tot[0] >= INT32_MAX || tot[1] >= INT32_MAX || tot[2] >= INT32_MAX) {
+            rc = fail(LUE_GPU_ERANGE, "stage topology: too many stages, exits or inputs");
+            goto done;
+        }
+        sc->nstages = tot[0];
+        sc->nexits = tot[1];
+        sc->ninputs = tot[2];
+    }
+    TRY(cudaMemcpyAsync(bases, hb.data(), 4 * nt * sizeof(int32_t), cudaMemcpyHostToDevice, stream), "stage bases");
+    TRY(cudaMalloc(&sc->stage, std::max<int64_t>(sc->nstages, 1) * sizeof(int4)), "stages");
+    TRY(cudaMalloc(&stage_depth, std::max<int64_t>(sc->nstages, 1) * sizeof(int32_t)), "stage depths");
+    TRY(cudaMalloc(&sc->exit_id, np * sizeof(int32_t)), "stage exits");
+    TRY(cudaMalloc(&sc->meta, np * sizeof(uint2)), "stage meta");
+    TRY(cudaMalloc(&sc->inputs, std::max<int64_t>(sc->ninputs, 1) * sizeof(int32_t)), "stage inputs");
+    TRY(cudaMalloc(&cell_exit, n * sizeof(int32_t)), "stage exit map");
+    TRY(cudaMalloc(&input_at, np * sizeof(int32_t)), "stage input map");
+    TRY(cudaMemsetAsync(cell_exit, 0xFF, n * sizeof(int32_t), stream), "memset");
+    k_stage_ids<<<grid, kStageBuildThreads, 0, stream>>>(core->upmask, depth, g, order, round_at, flags_at, bases,
+                                                        sc->stage, stage_depth, sc->exit_id, cell_exit, input_at,
+                                                        sc->meta);
+    k_stage_inputs<<<grid, kStageBuildThreads, 0, stream>>>(g, order, sc->meta, input_at, cell_exit, sc->inputs, error);
+    count_launches(2);
+    TRY(cudaGetLastError(), "stage ids");
+    {
+        // stages in wave order: counting sort by depth (host)
+        std::vector<int32_t> sd(sc->nstages);
+        std::vector<int4> srec(sc->nstages);
+        TRY(cudaMemcpyAsync(sd.data(), stage_depth, sc->nstages * sizeof(int32_t), cudaMemcpyDeviceToHost, stream),
+            "stage depths");
+        TRY(cudaMemcpyAsync(srec.data(), sc->stage, sc->nstages * sizeof(int4), cudaMemcpyDeviceToHost, stream),
+            "stage records");
+        TRY(cudaMemcpyAsync(&herr, error, sizeof(int), cudaMemcpyDeviceToHost, stream), "stage flag");
+        TRY(cudaStreamSynchronize(stream), "stage build");
+        if (herr) {
+            rc = fail(LUE_GPU_EINVAL, "stage topology: an input without a history row");
+            goto done;
+        }
+        int32_t maxd = 0;
+        for (int32_t v : sd) maxd = std::max(maxd, v);
+        sc->max_depth = sc->nstages ? maxd : -1;
+        std::vector<int64_t> off(maxd + 2, 0);
+        for (int32_t v : sd) ++off[v + 1];
+        int64_t mx = 0;
+        for (int32_t d = 0; d <= maxd; ++d) {
+            mx = std::max(mx, off[d + 1]);
+            off[d + 1] += off[d];
+        }
+        sc->max_stages_per_depth = mx;
+        std::vector<int32_t> ws(sc->nstages);
+        std::vector<int64_t> cur(off.begin(), off.end() - 1);
+        for (int64_t s = 0; s < sc->nstages; ++s) ws[cur[sd[s]]++] = (int32_t)s;
+        int64_t mi = 0;
+        for (const int4& r : srec) mi = std::max<int64_t>(mi, (unsigned)r.z >> 16);
+        sc->max_stage_inputs = mi;
+        sc->h_depth_offsets = off;
+        TRY(cudaMalloc(&sc->wave_stage, std::max<int64_t>(sc->nstages, 1) * sizeof(int32_t)), "wave order");
+        TRY(cudaMalloc(&sc->depth_offsets, off.size() * sizeof(int64_t)), "wave order");
+        TRY(cudaMemcpyAsync(sc->wave_stage, ws.data(), sc->nstages * sizeof(int32_t), cudaMemcpyHostToDevice, stream),
+            "wave order");
+        TRY(cudaMemcpyAsync(sc->depth_offsets, off.data(), off.size() * sizeof(int64_t), cudaMemcpyHostToDevice, stream),
+            "wave order");
+        TRY(cudaStreamSynchronize(stream), "stage build");  // the host vectors must outlive the copies
+    }
+    sc->bytes = sc->nstages * 20 + np * 12 + sc->ninputs * 4 + (int64_t)sc->h_depth_offsets.size() * 8;
+    if (getenv("LUE_GB300_VERBOSE"))
+        fprintf(stderr, "stage topology: %lld tiles, %lld stages, depth %lld, %lld exits, %lld inputs, "
+                        "at most %lld stages per depth and %lld inputs per stage\n",
+                (long long)nt, (long long)sc->nstages, (long long)sc->max_depth, (long long)sc->nexits,
+                (long long)sc->ninputs, (long long)sc->max_stages_per_depth, (long long)sc->max_stage_inputs);
+done:
+    cudaFree(depth);
+    cudaFree(counts);
+    cudaFree(bases);
+    cudaFree(cell_exit);
+    cudaFree(input_at);
+    cudaFree(stage_depth);
+    cudaFree(error);
+    cudaFree(order);
+    cudaFree(round_at);
+    cudaFree(flags_at);
+#undef TRY
+    if (rc) {
+        stage_core_free(sc);
+        return rc;
+    }
+    *out = sc;
+    return LUE_GPU_OK;
+}
+
+void stage_core_free(StageCore* sc)
+{
+    if (!sc) return;
+    cudaFree(sc->stage);
+    cudaFree(sc->wave_stage);
+    cudaFree(sc->depth_offsets);
+    cudaFree(sc->meta);
+    cudaFree(sc->exit_id);
+    cudaFree(sc->inputs);
+    delete sc;
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Waves
+// ---------------------------------------------------------------------------------------------------
+
+struct StageRunArgs {
+    const int4* stage;
+    const int32_t* wave_stage;
+    const int64_t* depth_offsets;
+    const uint2* meta;
+    const int32_t* exit_id;
+    const int32_t* inputs;
+    int64_t rows, cols, tcols, max_depth;
+    int steps, chunk, nchunks;
+    uint2* hist;  // [nexits * steps]: the outflow of every exit at every step, as 8 bytes
+};
+
+// One wave: stage (depth d, chunk c) for every c in [c_lo, c_lo + gridDim.y) with d = d_base + wave - c
+// (d_base 1 for the pipelined waves after the depth-0 launch).  A Rule supplies the per-cell state (Cell,
+// kept in shared memory by position), the accumulator of the upstream outflows (Acc) and the cell step.
+// In round r the active positions are those whose round lies in (r - ns, r]: one contiguous range of the
+// stage's order, shared out over the threads.
+template <class R>
+__global__ void __launch_bounds__(kStageThreads) k_stage_wave(StageRunArgs a, R rule, int wave, int c_lo, int d_base,
+                                                              int chunk)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint2* Qs = reinterpret_cast<uint2*>(smem_raw);                         // [2][1024] outflow by step parity
+    uint2* meta = Qs + 2 * kStageCells;                                      // [1024] by position
+    int32_t* ex = reinterpret_cast<int32_t*>(meta + kStageCells);            // [1024] history row or -1
+    uint16_t* rstart = reinterpret_cast<uint16_t*>(ex + kStageCells);        // [1028] first position of each round
+    typename R::Cell* cells = reinterpret_cast<typename R::Cell*>(rstart + kStageCells + 4);  // [1024]
+    uint2* hs = reinterpret_cast<uint2*>(cells + kStageCells);               // [inputs x steps of the chunk]
+    const int c = c_lo + (int)blockIdx.y, d = d_base + wave - c;
+    if (d < 0 || d > a.max_depth) return;
+    const int64_t si = a.depth_offsets[d] + blockIdx.x;
+    if (si >= a.depth_offsets[d + 1]) return;
+    const int4 st = a.stage[a.wave_stage[si]];
+    const int64_t tile = st.x;
+    const int begin = st.y & 0xFFFF, count = (int)((unsigned)st.y >> 16);
+    const int rounds = st.z & 0xFFFF, nin = (int)((unsigned)st.z >> 16);
+    const int64_t in_base = st.w;
+    const int t0 = c * chunk, ns = min(chunk, a.steps - t0);
+    const int64_t tr = tile / a.tcols, tc = tile - tr * a.tcols;
+    const int64_t row0 = tr * kStageSide, col0 = tc * kStageSide;
+    for (int i = threadIdx.x; i < nin * ns; i += kStageThreads) {
+        const int in = i / ns, t = i - in * ns;
+        hs[i] = a.hist[(int64_t)__ldg(a.inputs + in_base + in) * a.steps + t0 + t];
+    }
+    for (int i = threadIdx.x; i < count; i += kStageThreads) {
+        const int64_t at = tile * kStageCells + begin + i;
+        const uint2 m = __ldg(a.meta + at);
+        meta[i] = m;
+        ex[i] = __ldg(a.exit_id + at);
+        const int p = (int)(m.x & 1023u);
+        rule.load(cells[i], (row0 + (p >> 5)) * a.cols + col0 + (p & 31), c);
+        const int rd = (int)((m.x >> 10) & 1023u);
+        if (i == 0 || rd != (int)((__ldg(a.meta + at - 1).x >> 10) & 1023u)) rstart[rd] = (uint16_t)i;
+    }
+    if (threadIdx.x == 0) rstart[rounds] = (uint16_t)count;
+    __syncthreads();
+    const int nrounds = rounds + ns - 1;
+    for (int r = 0; r < nrounds; ++r) {
+        const int lo = rstart[max(0, r - ns + 1)], hi = rstart[min(rounds, r + 1)];
+        for (int i = lo + (int)threadIdx.x; i < hi; i += kStageThreads) {
+            const uint2 m = meta[i];
+            const int t = r - (int)((m.x >> 10) & 1023u);
+            const int p = (int)(m.x & 1023u);
+            const unsigned em = (m.y >> 8) & 0xFFu;
+            const int fi = (int)(m.y >> 16);
+            typename R::Acc acc = rule.begin();
+            unsigned um = m.y & 0xFFu;
+            while (um) {
+                const int q = __ffs(um) - 1;
+                um &= um - 1;
+                const uint2 v = ((em >> q) & 1u) ? hs[(fi + __popc(em & ((1u << q) - 1u))) * ns + t]
+                                                  : Qs[(t & 1) * kStageCells + p + nb_dr(q) * kStageSide + nb_dc(q)];
+                rule.add(acc, v);
+            }
+            const uint2 o = rule.step(cells[i], acc, (row0 + (p >> 5)) * a.cols + col0 + (p & 31), t0 + t);
+            Qs[(t & 1) * kStageCells + p] = o;
+            const int32_t e = ex[i];
+            if (e >= 0) a.hist[(int64_t)e * a.steps + t0 + t] = o;
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < count; i += kStageThreads) {
+        const int p = (int)(meta[i].x & 1023u);
+        rule.store(cells[i], (row0 + (p >> 5)) * a.cols + col0 + (p & 31), c, t0 + ns == a.steps);
+    }
+}
+
+template <class R>
+static size_t stage_smem(int64_t inputs_x_steps)
+{
+    return 2 * kStageCells * sizeof(uint2) + kStageCells * (sizeof(uint2) + sizeof(int32_t)) +
+           (kStageCells + 4) * sizeof(uint16_t) + kStageCells * sizeof(typename R::Cell) +
+           (size_t)inputs_x_steps * sizeof(uint2);
+}
+
+// --- rules -------------------------------------------------------------------------------------------
+
+// float32 accu / accu_threshold / accu_fraction, one step: the same cell rule and float-float upstream
+// sums as the walk engine (route_walk_visitors.cuh), so the results are the same bit for bit.
+template <Rule RR>
+struct StageF32 {
+    const float* a;
+    float as;
+    const float* b;
+    float bs;
+    float* out;
+    float* rem;
+    struct Cell {};
+    struct Acc {
+        FF t;
+        bool nan;
+    };
+    __device__ void load(Cell&, int64_t, int) const {}
+    __device__ Acc begin() const { return Acc{FF{0.0f, 0.0f}, false}; }
+    __device__ void add(Acc& acc, uint2 v) const
+    {
+        const float h = __uint_as_float(v.x);
+        if (isnan(h)) acc.nan = true;
+        else acc.t.add(h, __uint_as_float(v.y));
+    }
+    __device__ uint2 step(Cell&, const Acc& acc, int64_t g, int) const
+    {
+        float oh = 0.0f, ol = 0.0f, r = 0.0f;
+        if (!rule_f32<RR>(acc.t, acc.nan, value_at(a, as, g), RR == Rule::accu ? 0.0f : value_at(b, bs, g), oh, ol,
+                          r)) {
+            out[g] = qnan<float>();
+            if (RR != Rule::accu) rem[g] = qnan<float>();
+            return make_uint2(__float_as_uint(qnan<float>()), 0u);
+        }
+        out[g] = oh;
+        if (RR != Rule::accu) rem[g] = r;
+        return make_uint2(__float_as_uint(oh), __float_as_uint(ol));
+    }
+    __device__ void store(Cell&, int64_t, int, bool) const {}
+};
+
+template <Rule RR>
+struct StageF64 {
+    const double* a;
+    double as;
+    const double* b;
+    double bs;
+    double* out;
+    double* rem;
+    struct Cell {};
+    struct Acc {
+        double t;
+        bool nan;
+    };
+    __device__ void load(Cell&, int64_t, int) const {}
+    __device__ Acc begin() const { return Acc{0.0, false}; }
+    __device__ void add(Acc& acc, uint2 v) const
+    {
+        const double h = __hiloint2double((int)v.y, (int)v.x);
+        if (isnan(h)) acc.nan = true;
+        else acc.t += h;
+    }
+    __device__ uint2 step(Cell&, const Acc& acc, int64_t g, int) const
+    {
+        double o = 0.0, r = 0.0;
+        if (!rule_f64<RR>(acc.t, acc.nan, value_at(a, as, g), RR == Rule::accu ? 0.0 : value_at(b, bs, g), o, r)) {
+            o = qnan<double>();
+            r = qnan<double>();
+        }
+        out[g] = o;
+        if (RR != Rule::accu) rem[g] = r;
+        return make_uint2((unsigned)__double2loint(o), (unsigned)__double2hiint(o));
+    }
+    __device__ void store(Cell&, int64_t, int, bool) const {}
+};
+
+// kinematic wave, one step, float64: the walk engine's cell rule (route_walk_visitors.cuh).
+template <class TIn>
+struct StageKW64 {
+    RouteKW<TIn> v;  // inputs and constants (its out is the result raster)
+    struct Cell {};
+    struct Acc {
+        double up;
+        bool nan;
+    };
+    __device__ void load(Cell&, int64_t, int) const {}
+    __device__ Acc begin() const { return Acc{0.0, false}; }
+    __device__ void add(Acc& acc, uint2 x) const
+    {
+        const double h = __hiloint2double((int)x.y, (int)x.x);
+        if (isnan(h)) acc.nan = true;
+        else acc.up += h;
+    }
+    __device__ uint2 step(Cell&, const Acc& acc, int64_t c, int) const
+    {
+        const double qc = v.qcur ? __ldg(v.qcur + c) : v.qcur_s;
+        const double q = v.lateral ? (double)__ldg(v.lateral + c) : v.lateral_s;
+        const double al = v.alpha ? (double)__ldg(v.alpha + c) : v.alpha_s;
+        const double be = v.beta ? __ldg(v.beta + c) : v.beta_s;
+        const double len = v.dx ? __ldg(v.dx + c) : v.dx_s;
+        const double o = rule_kw(acc.up, acc.nan, qc, q, al, be, v.dt, len, v.br);
+        v.out[c] = o;
+        return make_uint2((unsigned)__double2loint(o), (unsigned)__double2hiint(o));
+    }
+    __device__ void store(Cell&, int64_t, int, bool) const {}
+};
+
+// kinematic wave, many steps, float-float (kinematic_wave_ff.cuh).  Between chunks the state of each cell
+// (discharge and its power, float-float) waits in state_q / state_p.
+struct StageKWFF {
+    const double* qcur;
+    const float* lateral;
+    float lateral_s;
+    const float* alpha;
+    float alpha_s;
+    float2* state_q;
+    float2* state_p;
+    double* out;
+    KWConstFF K;
+    struct Cell {
+        ffloat q, p;
+        float lat, al;
+    };
+    struct Acc {
+        ffloat up;
+        bool nan;
+    };
+    __device__ void load(Cell& cl, int64_t g, int chunk) const
+    {
+        cl.lat = lateral ? __ldg(lateral + g) : lateral_s;
+        cl.al = alpha ? __ldg(alpha + g) : alpha_s;
+        if (chunk == 0) {
+            cl.q = ff_from_double(__ldg(qcur + g));
+            cl.p = (cl.q.hi >= 0.0f) ? kw_power(cl.q, K.br, K.beta) : ffloat{__int_as_float(0x7fc00000), 0.0f};
+        } else {
+            const float2 q = state_q[g], p = state_p[g];
+            cl.q = ffloat{q.x, q.y};
+            cl.p = ffloat{p.x, p.y};
+        }
+    }
+    __device__ Acc begin() const { return Acc{ffloat{0.0f, 0.0f}, false}; }
+    __device__ void add(Acc& acc, uint2 x) const
+    {
+        const ffloat v{__uint_as_float(x.x), __uint_as_float(x.y)};
+        if (isnan(v.hi)) acc.nan = true;
+        else acc.up = ff_add(acc.up, v);
+    }
+    __device__ uint2 step(Cell& cl, const Acc& acc, int64_t, int) const
+    {
+        kw_step_ff(acc.up, acc.nan, cl.q, cl.p, cl.lat, cl.al, K);
+        return make_uint2(__float_as_uint(cl.q.hi), __float_as_uint(cl.q.lo));
+    }
+    __device__ void store(Cell& cl, int64_t g, int, bool last) const
+    {
+        if (last) {
+            out[g] = isnan(cl.q.hi) ? qnan<double>() : ff_to_double(cl.q);
+        } else {
+            state_q[g] = make_float2(cl.q.hi, cl.q.lo);
+            state_p[g] = make_float2(cl.p.hi, cl.p.lo);
+        }
+    }
+};
+
+// No-data flow direction: NaN in the outputs (cells outside every stage).
+template <class T>
+__global__ void k_stage_no_data(const uint8_t* fd, int64_t n, T* out, T* rem)
+{
+    for (int64_t c = grid_stride_begin(); c < n; c += grid_stride())
+        if (fd[c] == kNoData) {
+            out[c] = qnan<T>();
+            if (rem) rem[c] = qnan<T>();
+        }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Host
+// ---------------------------------------------------------------------------------------------------
+
+// The stage topology of t, built on first use; nullptr when the engine does not apply.
+static int stage_core_get(lue_gpu_topology* t, cudaStream_t stream, const StageCore** out)
+{
+    *out = nullptr;
+    TopologyCore* core = t->core;
+    if (core->stats.cycle_cells > 0) return LUE_GPU_OK;
+    std::lock_guard<std::mutex> lock(core->stage_mutex);
+    if (!core->stages && !core->stages_unavailable) {
+        StageCore* sc = nullptr;
+        const int rc = stage_core_build(core, t->work_count, stream, &sc);
+        if (rc == LUE_GPU_ERANGE) {
+            core->stages_unavailable = true;
+            return LUE_GPU_OK;
+        }
+        if (rc) return rc;
+        core->stages = sc;
+        core->bytes += sc->bytes;
+    }
+    *out = core->stages;
+    return LUE_GPU_OK;
+}
+
+template <class T>
+static int grow(lue_gpu_topology* t, T*& p, size_t& have, size_t need, cudaStream_t stream, const char* what)
+{
+    if (need <= have) return LUE_GPU_OK;
+    cudaStreamSynchronize(stream);  // the old buffer may still be in use
+    cudaFree(p);
+    p = nullptr;
+    have = 0;
+    if (int rc = cuda_status(cudaMalloc(&p, need), what)) return rc;
+    have = need;
+    (void)t;
+    return LUE_GPU_OK;
+}
+
+// Steps per chunk: at most LUE_GB300_STAGE_CHUNK (default 8), and the inputs' history of a chunk must fit
+// in shared memory.
+static int stage_chunk(const StageCore* sc, int steps)
+{
+    int chunk = 8;
+    if (const char* e = getenv("LUE_GB300_STAGE_CHUNK")) chunk = std::max(1, atoi(e));
+    chunk = std::min(chunk, steps);
+    const int64_t fit = kStageHistorySlots / std::max<int64_t>(1, sc->max_stage_inputs);
+    return (int)std::max<int64_t>(1, std::min<int64_t>(chunk, fit));
+}
+
+template <class R>
+static int launch_wave(const StageRunArgs& a, const R& rule, int64_t gx, int64_t gy, int wave, int c_lo, int d_base,
+                       int chunk, size_t smem, cudaStream_t stream)
+{
+    k_stage_wave<R><<<dim3((unsigned)gx, (unsigned)gy), kStageThreads, smem, stream>>>(a, rule, wave, c_lo, d_base,
+                                                                                       chunk);
+    return 1;
+}
+
+// `steps` steps of a rule over every stage.  Stages of depth 0 have no inputs: they run all steps in one
+// launch.  Deeper stages run in chunks of `chunk` steps, stage (depth d, chunk c) in wave (d - 1) + c.
+template <class R>
+static int stage_run(lue_gpu_topology* t, const StageCore* sc, const R& rule, int steps, int chunk,
+                     cudaStream_t stream, const char* what)
+{
+    const TopologyCore* core = t->core;
+    const int nchunks = (int)div_up(steps, chunk);
+    if ((int64_t)sc->max_stage_inputs * chunk > kStageHistorySlots)
+        return fail(LUE_GPU_ERANGE, std::string(what) + ": stage inputs beyond the shared-memory history");
+    const size_t hist = (size_t)std::max<int64_t>(sc->nexits, 1) * (size_t)steps * sizeof(uint2);
+    if (int rc = grow(t, t->stage_hist, t->stage_hist_bytes, hist, stream, what)) return rc;
+    StageRunArgs a{sc->stage,   sc->wave_stage, sc->depth_offsets, sc->meta,  sc->exit_id, sc->inputs,
+                   core->rows,  core->cols,     sc->tcols,         sc->max_depth, steps,   chunk,
+                   nchunks,     t->stage_hist};
+    const size_t smem = stage_smem<R>((int64_t)sc->max_stage_inputs * chunk);
+    static bool attr = false;
+    if (!attr) {
+        if (int rc = cuda_status(cudaFuncSetAttribute(k_stage_wave<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                      (int)stage_smem<R>(kStageHistorySlots)),
+                                 what))
+            return rc;
+        attr = true;
+    }
+    const std::vector<int64_t>& off = sc->h_depth_offsets;
+    const int64_t D = sc->max_depth;
+    if (D < 0) return LUE_GPU_OK;
+    int launches = 0;
+    // depth 0: every step at once
+    launches += launch_wave(a, rule, off[1] - off[0], 1, 0, 0, 0, steps, stage_smem<R>(0), stream);
+    // depths 1 ..: pipelined chunks
+    for (int64_t w = 0; w <= D - 1 + nchunks - 1; ++w) {
+        const int64_t c_lo = std::max<int64_t>(0, w - (D - 1)), c_hi = std::min<int64_t>(nchunks - 1, w);
+        int64_t gx = 0;
+        for (int64_t cc = c_lo; cc <= c_hi; ++cc) {
+            const int64_t dd = 1 + w - cc;
+            gx = std::max(gx, off[dd + 1] - off[dd]);
+        }
+        if (gx == 0) continue;
+        launches += launch_wave(a, rule, gx, c_hi - c_lo + 1, (int)w, (int)c_lo, 1, chunk, smem, stream);
+    }
+    count_launches(launches);
+    return cuda_status(cudaGetLastError(), what);
+}
+
+static bool stage_engine_off()
+{
+    const char* e = getenv("LUE_GB300_ENGINE");
+    return e && e[0] == 'w';
+}
+
+template <Rule RR>
+static int route_f32_rule(lue_gpu_topology* t, const StageCore* sc, const float* a, float as, const float* b, float bs,
+                          float* out, float* rem, cudaStream_t stream)
+{
+    const int64_t n = t->core->n;
+    k_stage_no_data<float><<<grid_for(n, 256), 256, 0, stream>>>(t->core->fd, n, out, rem);
+    count_launches(1);
+    StageF32<RR> rule{a, as, b, bs, out, rem};
+    return stage_run(t, sc, rule, 1, 1, stream, "stage route (float32)");
+}
+
+int stage_route_f32(lue_gpu_topology* t, int rule, const float* a, float as, const float* b, float bs, float* out,
+                    float* rem, cudaStream_t stream, bool* done)
+{
+    *done = false;
+    if (stage_engine_off()) return LUE_GPU_OK;
+    const StageCore* sc = nullptr;
+    if (int rc = stage_core_get(t, stream, &sc)) return rc;
+    if (!sc || sc->max_stage_inputs > kStageHistorySlots) return LUE_GPU_OK;
+    *done = true;
+    if (rule == (int)Rule::threshold)
+        return route_f32_rule<Rule::threshold>(t, sc, a, as, b, bs, out, rem, stream);
+    return route_f32_rule<Rule::fraction>(t, sc, a, as, b, bs, out, rem, stream);
+}
+
+template <Rule RR>
+static int route_f64_rule(lue_gpu_topology* t, const StageCore* sc, const double* a, double as, const double* b,
+                          double bs, double* out, double* rem, cudaStream_t stream)
+{
+    const int64_t n = t->core->n;
+    k_stage_no_data<double><<<grid_for(n, 256), 256, 0, stream>>>(t->core->fd, n, out, rem);
+    count_launches(1);
+    StageF64<RR> rule{a, as, b, bs, out, rem};
+    return stage_run(t, sc, rule, 1, 1, stream, "stage route (float64)");
+}
+
+int stage_route_f64(lue_gpu_topology* t, int rule, const double* a, double as, const double* b, double bs,
+                    double* out, double* rem, cudaStream_t stream, bool* done)
+{
+    *done = false;
+    if (stage_engine_off()) return LUE_GPU_OK;
+    const StageCore* sc = nullptr;
+    if (int rc = stage_core_get(t, stream, &sc)) return rc;
+    if (!sc || sc->max_stage_inputs > kStageHistorySlots) return LUE_GPU_OK;
+    *done = true;
+    if (rule == (int)Rule::accu) return route_f64_rule<Rule::accu>(t, sc, a, as, b, bs, out, rem, stream);
+    if (rule == (int)Rule::threshold)
+        return route_f64_rule<Rule::threshold>(t, sc, a, as, b, bs, out, rem, stream);
+    return route_f64_rule<Rule::fraction>(t, sc, a, as, b, bs, out, rem, stream);
+}
+
+int stage_kinematic_wave_f64(lue_gpu_topology* t, const double* qcur, double qcur_s, const double* lateral,
+                             double lateral_s, const double* alpha, double alpha_s, const double* beta, double beta_s,
+                             double dt, const double* dx, double dx_s, double* out, const BetaRational& br,
+                             cudaStream_t stream, bool* done)
+{
+    *done = false;
+    if (stage_engine_off()) return LUE_GPU_OK;
+    const StageCore* sc = nullptr;
+    if (int rc = stage_core_get(t, stream, &sc)) return rc;
+    if (!sc || sc->max_stage_inputs > kStageHistorySlots) return LUE_GPU_OK;
+    *done = true;
+    const int64_t n = t->core->n;
+    k_stage_no_data<double><<<grid_for(n, 256), 256, 0, stream>>>(t->core->fd, n, out, (double*)nullptr);
+    count_launches(1);
+    StageKW64<double> rule{RouteKW<double>{t->core->upmask, qcur, qcur_s, lateral, lateral_s, alpha, alpha_s, beta,
+                                           beta_s, dt, dx, dx_s, out, t->core->cols, br}};
+    return stage_run(t, sc, rule, 1, 1, stream, "kinematic_wave_f64 (stages)");
+}
+
+int stage_kinematic_wave_f32in(lue_gpu_topology* t, const double* qcur, double qcur_s, const float* lateral,
+                               double lateral_s, const float* alpha, double alpha_s, double beta, double dt, double dx,
+                               double* out, const BetaRational& br, cudaStream_t stream, bool* done)
+{
+    *done = false;
+    if (stage_engine_off()) return LUE_GPU_OK;
+    const StageCore* sc = nullptr;
+    if (int rc = stage_core_get(t, stream, &sc)) return rc;
+    if (!sc || sc->max_stage_inputs > kStageHistorySlots) return LUE_GPU_OK;
+    *done = true;
+    const int64_t n = t->core->n;
+    k_stage_no_data<double><<<grid_for(n, 256), 256, 0, stream>>>(t->core->fd, n, out, (double*)nullptr);
+    count_launches(1);
+    StageKW64<float> rule{RouteKW<float>{t->core->upmask, qcur, qcur_s, lateral, lateral_s, alpha, alpha_s, nullptr,
+                                         beta, dt, nullptr, dx, out, t->core->cols, br}};
+    return stage_run(t, sc, rule, 1, 1, stream, "kinematic_wave_f64_f32in (stages)");
+}
+
+static ffloat ff_split(double v)
+{
+    const float h = (float)v;
+    return ffloat{h, (float)(v - (double)h)};
+}
+
+int stage_kinematic_wave_steps(lue_gpu_topology* t, const double* qcur, const float* lateral, double lateral_s,
+                               const float* alpha, double alpha_s, double beta, double dt, double dx, int steps,
+                               double* out, const BetaRational& br, cudaStream_t stream, bool* done)
+{
+    *done = false;
+    if (stage_engine_off() || br.m == 0) return LUE_GPU_OK;
+    const StageCore* sc = nullptr;
+    if (int rc = stage_core_get(t, stream, &sc)) return rc;
+    if (!sc || sc->max_stage_inputs > kStageHistorySlots) return LUE_GPU_OK;
+    *done = true;
+    const int64_t n = t->core->n;
+    // the history of every exit for every step of a part of the call: parts of at most `fit` steps
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    const double budget = 0.4 * (double)free_b + (double)t->stage_hist_bytes;
+    const int64_t per_step = std::max<int64_t>(sc->nexits, 1) * (int64_t)sizeof(uint2);
+    const int fit = (int)std::max<int64_t>(1, std::min<int64_t>(steps, (int64_t)(budget / (double)per_step)));
+    KWConstFF K;
+    K.k = ff_split(dt / dx);
+    K.dt = ff_split(dt);
+    K.kf = (float)(dt / dx);
+    K.beta_f = (float)beta;
+    K.beta = beta;
+    K.dt_d = dt;
+    K.dx_d = dx;
+    K.br = br;
+    K.bad = std::isnan(beta) || std::isnan(dt) || std::isnan(dx) || !(dx > 0.0);
+    const int chunk = stage_chunk(sc, std::min(steps, fit));
+    if ((size_t)n * 2 * sizeof(float2) > t->stage_state_bytes && div_up(std::min(steps, fit), chunk) > 1) {
+        if (int rc = grow(t, t->stage_state, t->stage_state_bytes, (size_t)n * 2 * sizeof(float2), stream,
+                          "kinematic_wave_steps state"))
+            return rc;
+    }
+    double* tmp = nullptr;
+    if (steps > fit) {
+        if (int rc = cuda_status(cudaMalloc(&tmp, 2 * (size_t)n * sizeof(double)), "kinematic_wave_steps")) return rc;
+    }
+    const double* src = qcur;
+    int done_steps = 0, which = 0;
+    int rc = LUE_GPU_OK;
+    while (done_steps < steps) {
+        const int part = std::min(fit, steps - done_steps);
+        double* dst = done_steps + part == steps ? out : tmp + (size_t)which * n;
+        k_stage_no_data<double><<<grid_for(n, 256), 256, 0, stream>>>(t->core->fd, n, dst, (double*)nullptr);
+        count_launches(1);
+        StageKWFF rule{src, lateral, (float)lateral_s, alpha, (float)alpha_s, t->stage_state,
+                       t->stage_state ? t->stage_state + n : nullptr, dst, K};
+        rc = stage_run(t, sc, rule, part, stage_chunk(sc, part), stream, "kinematic_wave_steps (stages)");
+        if (rc) break;
+        src = dst;
+        which ^= 1;
+        done_steps += part;
+    }
+    if (tmp) {
+        cudaStreamSynchronize(stream);
+        cudaFree(tmp);
+    }
+    return rc;
+}
+
+}  // namespace lue_gb300

@@ -1,0 +1,90 @@
+// stage_route.cuh — the stage engine: routing rules that are not plain sums, swept tile by tile.
+//
+// accu_threshold, accu_fraction and kinematic_wave compute each cell from the sum of its upstream
+// outflows with a rule that does not distribute over sums, so they cannot use the prefix sums of the
+// tile engine.  The reference walks them cell by cell, partition by partition, with channel hand-off at
+// partition edges (ALG/definition/accumulating_router.hpp:525-599, 902-1209).  Here:
+//
+//   - The raster is cut into 32 x 32 tiles.  The crossing depth of a cell is the largest number of tile
+//     edges crossed by a flow path that ends at the cell.  A stage is the set of cells of one tile with
+//     the same crossing depth.  Every upstream cell of a stage lies in the stage itself, in a stage of
+//     lower depth, or nowhere: stages of depth d depend only on depths below d.
+//   - Inside a stage each cell gets a round: its distance, in cells, from the stage's most downstream
+//     cells, counted from the far end (rounds run upstream to downstream).  Every cell is exactly one
+//     round after each of its upstream cells in the stage, because each cell has one downstream cell.
+//   - A stage runs in one CTA: the cells of a round are computed together from shared memory, and the
+//     outflows that leave the stage go to a history in global memory, where later stages read them.
+//   - Time steps are pipelined: cell c does step t in round round(c) + t, so T steps of a stage take
+//     rounds + T - 1 rounds.  Steps are cut into chunks; stage (depth d, chunk c) runs in wave d + c, so
+//     chunks of different depths overlap in time.
+//
+// Built once per flow-direction raster (on the first call that needs it) and kept by the topology.
+#pragma once
+
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+
+namespace lue_gb300 {
+
+constexpr int kStageSide = 32;                        // tile side (cells)
+constexpr int kStageCells = kStageSide * kStageSide;  // 1024
+constexpr int kStageThreads = 256;                    // runtime CTA: four cells per thread
+constexpr int kStagePerThread = kStageCells / kStageThreads;
+constexpr int kStageBuildThreads = 512;               // build CTA: two cells per thread
+constexpr int kStageHistorySlots = 4096;              // shared-memory history entries (inputs x steps) per CTA
+
+// meta (per cell, by tile and position in the tile's stage order):
+//   x: in-tile cell (bits 0-9) | round (bits 10-19)
+//   y: upstream mask (bits 0-7) | mask of upstream cells in other stages (bits 8-15) | index of the cell's
+//      first input in its stage's input list (bits 16-31)
+struct StageCore {
+    int64_t trows = 0, tcols = 0, ntiles = 0;
+    int64_t nstages = 0, nexits = 0, ninputs = 0;
+    int64_t max_depth = 0;             // deepest stage
+    int64_t max_stage_inputs = 0;      // most inputs of one stage
+    int64_t max_stages_per_depth = 0;
+    int4* stage = nullptr;             // [nstages] tile, begin | count << 16, rounds | inputs << 16, input base
+    int32_t* wave_stage = nullptr;     // [nstages] stage ids sorted by depth
+    int64_t* depth_offsets = nullptr;  // [max_depth + 2] start of each depth in wave_stage (device)
+    std::vector<int64_t> h_depth_offsets;
+    uint2* meta = nullptr;             // [ntiles * 1024]
+    int32_t* exit_id = nullptr;        // [ntiles * 1024] history row of the cell, or -1 (outflow stays in the stage)
+    int32_t* inputs = nullptr;         // [ninputs] history row of the upstream cell of each edge into a stage
+    int64_t bytes = 0;
+};
+
+struct TopologyCore;
+struct BetaRational;
+
+// Builds the stage topology of an acyclic raster (work: a scratch array of words_for(n) counters).
+int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stream, StageCore** out);
+void stage_core_free(StageCore* sc);
+
+}  // namespace lue_gb300
+
+struct lue_gpu_topology;
+
+namespace lue_gb300 {
+
+// Routing on the stage engine.  *done is false when the engine does not apply to the topology (flow
+// cycles, or a raster beyond its limits): the caller then runs the walk engine.  rule: 1 threshold,
+// 2 fraction (the values of Rule in route_walk_visitors.cuh).
+int stage_route_f32(lue_gpu_topology* t, int rule, const float* a, float as, const float* b, float bs, float* out,
+                    float* rem, cudaStream_t stream, bool* done);
+int stage_route_f64(lue_gpu_topology* t, int rule, const double* a, double as, const double* b, double bs,
+                    double* out, double* rem, cudaStream_t stream, bool* done);
+int stage_kinematic_wave_f64(lue_gpu_topology* t, const double* qcur, double qcur_s, const double* lateral,
+                             double lateral_s, const double* alpha, double alpha_s, const double* beta, double beta_s,
+                             double dt, const double* dx, double dx_s, double* out, const BetaRational& br,
+                             cudaStream_t stream, bool* done);
+int stage_kinematic_wave_f32in(lue_gpu_topology* t, const double* qcur, double qcur_s, const float* lateral,
+                               double lateral_s, const float* alpha, double alpha_s, double beta, double dt, double dx,
+                               double* out, const BetaRational& br, cudaStream_t stream, bool* done);
+// `steps` kinematic-wave steps with the float-float solve (scalar rational beta).
+int stage_kinematic_wave_steps(lue_gpu_topology* t, const double* qcur, const float* lateral, double lateral_s,
+                               const float* alpha, double alpha_s, double beta, double dt, double dx, int steps,
+                               double* out, const BetaRational& br, cudaStream_t stream, bool* done);
+
+}  // namespace lue_gb300

@@ -156,6 +156,7 @@ static void free_core(TopologyCore* core)
     cudaFree(core->level);
     cudaFree(core->order);
     tile_core_free(core->tiles);
+    stage_core_free(core->stages);
     delete core;
 }
 
@@ -166,6 +167,8 @@ static void free_handle(lue_gpu_topology* t)
     cudaFree(t->lo);
     cudaFree(t->history);
     cudaFree(t->planes);
+    cudaFree(t->stage_hist);
+    cudaFree(t->stage_state);
     tile_scratch_free(&t->tile_scratch);
     if (t->core && --t->core->refs == 0) free_core(t->core);
     delete t;

@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "stage_route.cuh"
 #include "tile_accu.cuh"
 
 namespace lue_gb300 {
@@ -19,6 +20,9 @@ struct TopologyCore {
     TileCore* tiles = nullptr;  // tiled accu engine (acyclic rasters), else nullptr
     int32_t* order = nullptr;   // valid cells sorted by downstream level (built on first multi-step call)
     std::vector<int32_t> level_offsets;  // [levels + 1] start of each level in `order`
+    StageCore* stages = nullptr;         // stage engine (acyclic rasters; built on first use)
+    bool stages_unavailable = false;     // the raster is beyond the stage engine's limits
+    std::mutex stage_mutex;              // guards the first build (clones share the core)
     lue_gpu_topology_stats stats{};
     int64_t bytes = 0;
     std::atomic<int> refs{1};
@@ -35,6 +39,10 @@ struct lue_gpu_topology {
     size_t history_bytes = 0;
     double** planes = nullptr;       // device array of plane pointers
     size_t plane_capacity = 0;
+    uint2* stage_hist = nullptr;     // stage engine: outflow history of the stage exits (grown on demand)
+    size_t stage_hist_bytes = 0;
+    float2* stage_state = nullptr;   // stage engine: discharge and power of every cell between chunks
+    size_t stage_state_bytes = 0;
     int64_t scratch_bytes = 0;
 };
 

@@ -1,0 +1,144 @@
+"""The stage engine (accu_threshold, accu_fraction, float64 accu and kinematic_wave on acyclic rasters)
+against the walk engine and the oracle.
+
+The stage engine applies the same cell rules with the same float-float (float32) or float64 upstream
+sums, in the same neighbour order, as the walk engine, so one-step results agree bit for bit.  The
+multi-step kinematic wave uses a float-float solve; it is checked against the float64 oracle and for
+independence of its chunk size.  LUE_GB300_ENGINE=walk selects the walk engine for a call.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from lue_gb300 import synthetic
+from oracle import oracle
+from tests import parity
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lfr():
+    import torch
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    from lue_gb300 import framework
+    return framework
+
+
+class _env:
+    def __init__(self, **kv):
+        self.kv = kv
+
+    def __enter__(self):
+        self.old = {k: os.environ.get(k) for k in self.kv}
+        os.environ.update(self.kv)
+
+    def __exit__(self, *exc):
+        for k, v in self.old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
+def _raster(rows, cols, seed, amplitude=40.0, holes=0.0):
+    fd = synthetic.flow_direction(rows, cols, seed, amplitude, wavelength=max(rows, cols) / 2).copy()
+    rng = np.random.default_rng(seed)
+    if holes:
+        fd[rng.random(fd.shape) < holes] = 255
+    return fd, rng
+
+
+@pytest.mark.parametrize("shape", [(1024, 1024), (333, 777), (65, 31), (1, 300)])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+def test_threshold_and_fraction_equal_walk_engine(lfr, shape, dtype):
+    fd, rng = _raster(*shape, seed=31, holes=0.001)
+    m = rng.lognormal(0.0, 1.0, shape).astype(dtype)
+    m[rng.random(shape) < 0.001] = np.nan
+    m[rng.random(shape) < 0.001] = -1.0
+    thr = (rng.random(shape) * 0.5).astype(dtype)
+    frac = rng.random(shape).astype(dtype)
+    ps = (min(256, shape[0]), min(256, shape[1]))
+    a = lfr.from_numpy(fd, ps)
+    md, td, fdd = lfr.from_numpy(m, ps), lfr.from_numpy(thr, ps), lfr.from_numpy(frac, ps)
+    for op, b, name in ((lfr.accu_threshold, td, "threshold"), (lfr.accu_fraction, fdd, "fraction")):
+        stage = [lfr.to_numpy(x) for x in op(a, md, b)]
+        with _env(LUE_GB300_ENGINE="walk"):
+            walk = [lfr.to_numpy(x) for x in op(a, md, b)]
+        for s_, w_ in zip(stage, walk):
+            assert np.array_equal(s_, w_, equal_nan=True), name
+        ref = getattr(oracle, "accu_" + name)(fd, m.astype(np.float64), (thr if name == "threshold" else frac)
+                                              .astype(np.float64), ps, dtype=np.float64)
+        check = parity.assert_close32 if dtype == np.float32 else parity.assert_close64
+        check(stage[0], ref[0], f"{name} flux")
+        check(stage[1], ref[1], f"{name} state")
+
+
+def test_accu_f64_equals_walk_engine(lfr):
+    fd, rng = _raster(700, 900, seed=5, holes=0.0005)
+    m = rng.random(fd.shape)
+    a = lfr.from_numpy(fd)
+    md = lfr.from_numpy(m)
+    stage = lfr.to_numpy(lfr.accu(a, md))
+    with _env(LUE_GB300_ENGINE="walk"):
+        walk = lfr.to_numpy(lfr.accu(a, md))
+    assert np.array_equal(stage, walk, equal_nan=True)
+    parity.assert_close64(stage, oracle.accu(fd, m, (700, 900), dtype=np.float64), "accu f64")
+
+
+def _kw(rows, cols, seed):
+    d = synthetic.kinematic_wave_inputs(rows, cols, seed, amplitude=40.0)
+    return d
+
+
+def test_kinematic_wave_single_step_equals_walk_engine(lfr):
+    d = _kw(300, 500, 9)
+    fd = d["flow_direction"].copy()
+    fd[7, 11] = 255
+    a = lfr.from_numpy(fd)
+    args = (lfr.from_numpy(d["discharge"]), lfr.from_numpy(d["lateral_inflow"]), lfr.from_numpy(d["alpha"]),
+            0.6, 3600.0, 100.0)
+    stage = lfr.to_numpy(lfr.kinematic_wave(a, *args))
+    with _env(LUE_GB300_ENGINE="walk"):
+        walk = lfr.to_numpy(lfr.kinematic_wave(a, *args))
+    assert np.array_equal(stage, walk, equal_nan=True)
+
+
+@pytest.mark.parametrize("chunk", ["1", "3", "8", "64"])
+def test_kinematic_wave_steps_chunk_sizes(lfr, chunk):
+    """Chunks of the pipelined steps: every chunk size gives the oracle's discharge after 12 steps."""
+    d = _kw(257, 390, 4)
+    fd = d["flow_direction"]
+    a = lfr.from_numpy(fd)
+    lat, alpha, q0 = (lfr.from_numpy(d[k]) for k in ("lateral_inflow", "alpha", "discharge"))
+    with _env(LUE_GB300_STAGE_CHUNK=chunk):
+        got = lfr.to_numpy(lfr.kinematic_wave_steps(a, q0, lat, alpha, 0.6, 3600.0, 100.0, 12))
+    q = d["discharge"]
+    for _ in range(12):
+        q = oracle.kinematic_wave(fd, q, d["lateral_inflow"].astype(np.float64), d["alpha"].astype(np.float64),
+                                  0.6, 3600.0, 100.0, fd.shape, dtype=np.float64)
+    parity.assert_close64(got, q, f"kinematic_wave_steps chunk {chunk}")
+
+
+def test_kinematic_wave_steps_zero_and_no_data(lfr):
+    """Cells without water, cells whose discharge starts at 0 (the reference's DBL_MIN start), NaN
+    lateral inflow and no-data flow directions, over several chunks."""
+    d = _kw(200, 260, 12)
+    fd = d["flow_direction"].copy()
+    rng = np.random.default_rng(3)
+    fd[rng.random(fd.shape) < 0.002] = 255
+    q0 = d["discharge"].copy()
+    q0[rng.random(fd.shape) < 0.05] = 0.0
+    lat = d["lateral_inflow"].copy()
+    lat[rng.random(fd.shape) < 0.05] = 0.0
+    lat[rng.random(fd.shape) < 0.001] = np.nan
+    a = lfr.from_numpy(fd)
+    with _env(LUE_GB300_STAGE_CHUNK="4"):
+        got = lfr.to_numpy(lfr.kinematic_wave_steps(a, lfr.from_numpy(q0), lfr.from_numpy(lat),
+                                                    lfr.from_numpy(d["alpha"]), 0.6, 3600.0, 100.0, 9))
+    q = q0
+    for _ in range(9):
+        q = oracle.kinematic_wave(fd, q, lat.astype(np.float64), d["alpha"].astype(np.float64), 0.6, 3600.0, 100.0,
+                                  fd.shape, dtype=np.float64)
+    parity.assert_close64(got, q, "kinematic_wave_steps with zeros and no-data")
