@@ -6,13 +6,15 @@
 // every operation runs on the float32 pipes:
 //
 //   known = k*Qup + alpha*P_prev + dt*q                  (k = dt / dx; P_prev carried from the last step)
-//   Q0    = float32 Newton-Raphson from the reference's linearised guess (kinematic_wave.hpp:61-91)
-//   Q     = Q0 - f(Q0) / f'(Q0) with f(Q) = k*Q + alpha*Q^beta - known in float-float   (one Newton step
-//           from a float32 root: 1e-7 -> ~1e-14)
-//   P     = Q^beta from Q0^beta (see pow_rational_ff) moved to Q to first order
+//   Q0    = float32 Newton-Raphson with exp2/log2 powers, from the previous discharge (or the reference's
+//           linearised guess, kinematic_wave.hpp:61-91, when that is 0), to ~1e-6
+//   Q     = two Newton steps on f(Q) = k*Q + alpha*Q^beta - known in float-float (1e-6 -> 1e-12 -> ~1e-14),
+//           with one float-float power: the second step's power is the first one's moved along its
+//           Taylor series
+//   P     = Q^beta, the same way
 //
-// Q^beta for beta = p/m (beta = 0.6 is 3/5): y0 = powf(Q, beta), then one Newton step for y^m = Q^p in
-// float-float (integer powers only).  Cases outside this path run the float64 solve of
+// Q^beta for beta = p/m (beta = 0.6 is 3/5): y0 = __powf(Q, beta), then two Newton steps for y^m = Q^p
+// in float-float (integer powers only).  Cases outside this path run the float64 solve of
 // kinematic_wave.cuh (rare): no upstream discharge and no current discharge (the reference then starts
 // from DBL_MIN), a float32 Newton that does not settle, and Q outside [1e-12, 1e12].
 #pragma once
@@ -87,16 +89,57 @@ __device__ __forceinline__ ffloat ff_ipow(ffloat x, int e)  // e >= 1
     return r;
 }
 
-// x^(p/m) in float-float for 1e-12 <= x <= 1e12 (x^p and y^m stay in float range for p, m <= 3).
+// x^(p/m) in float-float for 1e-12 <= x <= 1e12 (x^p and y^m stay in float range for p <= 3, m <= 5):
+// y0 = __powf(x, beta) (exp2/log2 approximations, ~1e-6 relative), then two Newton steps for y^m = x^p
+// in float-float, each squaring the relative error (1e-6 -> 1e-12 -> float-float precision).
 __device__ __forceinline__ ffloat pow_rational_ff(ffloat x, BetaRational br)
 {
-    const float y0 = powf(x.hi, br.beta_f);
-    const ffloat ym = ff_ipow(ffloat{y0, 0.0f}, br.m);
+    const float y0 = __powf(x.hi, br.beta_f);
     const ffloat xp = ff_ipow(x, br.p);
-    const ffloat diff = ff_add(ym, ff_neg(xp));
-    float dm = (float)br.m;
-    for (int i = 1; i < br.m; ++i) dm *= y0;
-    return ff_two_sum(y0, -diff.hi / dm);
+    ffloat y{y0, 0.0f};
+#pragma unroll 1
+    for (int it = 0; it < 2; ++it) {
+        const ffloat diff = ff_add(ff_ipow(y, br.m), ff_neg(xp));
+        float dm = (float)br.m;
+        for (int i = 1; i < br.m; ++i) dm *= y.hi;
+        y = ff_add(y, ffloat{-__fdividef(diff.hi, dm), 0.0f});
+    }
+    return y;
+}
+
+// a + b with an error of about 2^-48 (|a| + |b|): enough wherever the result is not compared against
+// cancellation below that.
+__device__ __forceinline__ ffloat ff_add_sloppy(ffloat a, ffloat b)
+{
+    ffloat s = ff_two_sum(a.hi, b.hi);
+    s.lo = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+    return ff_fast_two_sum(s.hi, s.lo);
+}
+
+// y^e in float-float for a small compile-time or run-time exponent e >= 1.
+template <int E>
+__device__ __forceinline__ ffloat ff_pow_n(ffloat y, int e_runtime)
+{
+    const int e = E > 0 ? E : e_runtime;
+    ffloat r = y;
+#pragma unroll
+    for (int i = 1; i < (E > 0 ? E : 16); ++i) {
+        if (i >= e) break;
+        r = ff_mul(r, y);
+    }
+    return r;
+}
+template <int E>
+__device__ __forceinline__ float f_pow_n(float y, int e_runtime)
+{
+    const int e = E > 0 ? E : e_runtime;
+    float r = y;
+#pragma unroll
+    for (int i = 1; i < (E > 0 ? E : 16); ++i) {
+        if (i >= e) break;
+        r *= y;
+    }
+    return r;
 }
 
 // Whether float-float powers of x stay in range for beta = p/m.
@@ -142,35 +185,46 @@ __device__ __forceinline__ bool kw_step_ff(ffloat up, bool nan, ffloat& Q, ffloa
     if (fast) {
         // known right-hand side in float-float
         const ffloat known = ff_add(ff_add(ff_mul(K.k, up), ff_mul_f(P, al)), ff_mul_f(K.dt, lat));
-        // float32 Newton from the reference's linearised guess
+        // float32 Newton (exp2/log2 powers) from the previous discharge, or from the reference's linearised
+        // guess (kinematic_wave.hpp:61-91) when there is none; it settles to the ~1e-6 of those powers
         const float kf = K.kf, bf = K.beta_f, knf = known.hi;
-        const float mean = 0.5f * (Q.hi + up.hi);
-        const float abpq = al * bf * powf(mean, bf - 1.0f);
-        x = (kf * up.hi + abpq * Q.hi + K.dt.hi * lat) / (kf + abpq);
+        if (Q.hi > 0.0f) {
+            x = Q.hi;
+        } else {
+            const float mean = 0.5f * (Q.hi + up.hi);
+            const float abpq = al * bf * __powf(mean, bf - 1.0f);
+            x = (kf * up.hi + abpq * Q.hi + K.dt.hi * lat) / (kf + abpq);
+        }
         if (!(x > 1e-30f)) x = 1e-30f;
         bool converged = false;
-        for (int it = 0; it < 12; ++it) {
-            const float xb = powf(x, bf);
+        for (int it = 0; it < 16; ++it) {
+            const float xb = __powf(x, bf);
             const float f = kf * x + al * xb - knf;
-            const float df = kf + al * bf * xb / x;
-            float nx = x - f / df;
+            const float df = kf + __fdividef(al * bf * xb, x);
+            float nx = x - __fdividef(f, df);
             if (!(nx > 0.0f)) nx = 0.5f * x;
             const float dxr = fabsf(nx - x);
             x = nx;
-            if (dxr <= 4e-7f * x) {
+            if (dxr <= 1e-5f * x) {
                 converged = true;
                 break;
             }
         }
         fast = converged && isfinite(x) && ff_pow_ok(x, K.br);
         if (fast) {
-            // one float-float Newton step, and the power moved along with it
-            const ffloat y = pow_rational_ff(ffloat{x, 0.0f}, K.br);
-            const ffloat f = ff_add(ff_add(ff_mul_f(K.k, x), ff_mul_f(y, al)), ff_neg(known));
-            const float df = kf + al * bf * y.hi / x;
-            const float delta = f.hi / df;
-            Q = ff_two_sum(x, -delta);
-            P = ff_add(y, ffloat{-y.hi * bf * (delta / x), 0.0f});
+            // two float-float Newton steps (1e-6 -> 1e-12 -> ~1e-14); the power at the second point is the
+            // first one's moved by its Taylor series to second order, and the result's to first order
+            const ffloat y1 = pow_rational_ff(ffloat{x, 0.0f}, K.br);
+            const float df = kf + __fdividef(al * bf * y1.hi, x);
+            const ffloat f1 = ff_add(ff_add(ff_mul_f(K.k, x), ff_mul_f(y1, al)), ff_neg(known));
+            const float d1 = __fdividef(f1.hi, df);
+            const ffloat q1 = ff_two_sum(x, -d1);
+            const float r1 = -__fdividef(d1, x);
+            const ffloat y2 = ff_add(y1, ffloat{y1.hi * (bf * r1 + 0.5f * bf * (bf - 1.0f) * r1 * r1), 0.0f});
+            const ffloat f2 = ff_add(ff_add(ff_mul(K.k, q1), ff_mul_f(y2, al)), ff_neg(known));
+            const float d2 = __fdividef(f2.hi, df);
+            Q = ff_add(q1, ffloat{-d2, 0.0f});
+            P = ff_add(y2, ffloat{-y2.hi * bf * __fdividef(d2, x), 0.0f});
             return true;
         }
     }
@@ -180,6 +234,100 @@ __device__ __forceinline__ bool kw_step_ff(ffloat up, bool nan, ffloat& Q, ffloa
     Q = ff_from_double(q);
     P = q > 0.0 ? ff_from_double(pow(q, K.beta)) : ffloat{0.0f, 0.0f};
     return true;
+}
+
+// The kinematic-wave solve in the variable y = Q^(1/m), for beta = p/m: Q^beta = y^p and Q = y^m, so the
+// equation k*Q + alpha*Q^beta = known becomes the polynomial
+//
+//     g(y) = k*y^m + alpha*y^p - known = 0,     g'(y) = m*k*y^(m-1) + p*alpha*y^(p-1),
+//
+// which is increasing and convex for y > 0: Newton-Raphson needs no exp/log, converges monotonically
+// after its first step, and its float-float steps cost a few multiplications.  The cell state is y
+// (float-float); the outflow passed downstream is Q = y^m.  P and M are compile-time p and m, or 0 to
+// take them from K.br at run time.
+template <int P, int M>
+__device__ __forceinline__ ffloat kw_poly_g(ffloat y, float al, const ffloat& known, const KWConstFF& K)
+{
+    const ffloat ym = ff_pow_n<M>(y, K.br.m), yp = ff_pow_n<P>(y, K.br.p);
+    return ff_add_sloppy(ff_add_sloppy(ff_mul(K.k, ym), ff_mul_f(yp, al)), ff_neg(known));
+}
+
+// y = Q^(1/m) in float-float, for the state of a cell that starts from discharge Q (rare: once per call
+// and cell).
+template <int P, int M>
+__device__ __forceinline__ ffloat kw_poly_root(ffloat q, const KWConstFF& K)
+{
+    if (!(q.hi > 0.0f)) return ffloat{q.hi == 0.0f ? 0.0f : q.hi, 0.0f};
+    const int m = M > 0 ? M : K.br.m;
+    if (!(q.hi >= 1e-30f && q.hi <= 1e30f)) return ff_from_double(pow(ff_to_double(q), 1.0 / (double)m));
+    ffloat y{__powf(q.hi, 1.0f / (float)m), 0.0f};
+#pragma unroll 1
+    for (int it = 0; it < 3; ++it) {  // Newton on y^m - q: 1e-6 -> 1e-12 -> ~1e-14
+        const ffloat r = ff_add_sloppy(ff_pow_n<M>(y, m), ff_neg(q));
+        const float d = m > 1 ? (float)m * f_pow_n<(M > 1 ? M - 1 : 0)>(y.hi, m - 1) : 1.0f;
+        y = ff_add_sloppy(y, ffloat{-__fdividef(r.hi, d), 0.0f});
+    }
+    return y;
+}
+
+// One step of one cell in the variable y (see above).  y is the cell's state from the previous step and
+// becomes this step's; up is the upstream sum of this step; returns the outflow Q = y^m (NaN for
+// no-data).  The cases the polynomial path does not take run the float64 solve of the reference.
+template <int P, int M>
+__device__ __forceinline__ ffloat kw_step_poly(ffloat up, bool nan, ffloat& y, float lat, float al,
+                                               const KWConstFF& K)
+{
+    const float nanf = __int_as_float(0x7fc00000);
+    const int m = M > 0 ? M : K.br.m, p = P > 0 ? P : K.br.p;
+    if (nan || K.bad || isnan(y.hi) || isnan(lat) || isnan(al) || !(y.hi >= 0.0f) || !(lat >= 0.0f)) {
+        y = ffloat{nanf, 0.0f};
+        return y;
+    }
+    const float qprev_f = f_pow_n<M>(y.hi, m);
+    const bool flow = up.hi + qprev_f > 0.0f;
+    if (!flow && !(lat > 0.0f)) {  // no water (kinematic_wave.hpp:181-185)
+        y = ffloat{0.0f, 0.0f};
+        return y;
+    }
+    if (flow && y.hi > 1e-12f && y.hi < 1e12f && al > 0.0f) {
+        const ffloat known = ff_add_sloppy(ff_add_sloppy(ff_mul(K.k, up), ff_mul_f(ff_pow_n<P>(y, p), al)),
+                                           ff_mul_f(K.dt, lat));
+        const float kf = K.kf, knf = known.hi;
+        // float Newton from the previous state, to the float noise floor (~1e-7): it stops one step after
+        // a step below 3e-5 relative, which quadratic convergence takes far below that floor
+        float x = y.hi;
+        bool converged = false;
+#pragma unroll 1
+        for (int it = 0; it < 24; ++it) {
+            const float xm1 = m > 1 ? f_pow_n<(M > 1 ? M - 1 : 0)>(x, m - 1) : 1.0f;
+            const float xp1 = p > 1 ? f_pow_n<(P > 1 ? P - 1 : 0)>(x, p - 1) : 1.0f;
+            const float g = kf * xm1 * x + al * xp1 * x - knf;
+            const float dg = (float)m * kf * xm1 + (float)p * al * xp1;
+            float nx = x - __fdividef(g, dg);
+            if (!(nx > 0.0f)) nx = 0.5f * x;
+            const float dxr = fabsf(nx - x);
+            x = nx;
+            if (converged) break;
+            converged = dxr <= 3e-5f * x;
+        }
+        if (converged && x > 1e-12f && x < 1e12f) {
+            // one float-float Newton step from the float root x (1e-7 -> ~1e-14); the powers of x are
+            // float-float products of floats, and Q = y^m moves with y to first order
+            const ffloat ym = ff_pow_n<M>(ffloat{x, 0.0f}, m), yp = ff_pow_n<P>(ffloat{x, 0.0f}, p);
+            const ffloat g = ff_add_sloppy(ff_add_sloppy(ff_mul(K.k, ym), ff_mul_f(yp, al)), ff_neg(known));
+            const float xm1 = m > 1 ? f_pow_n<(M > 1 ? M - 1 : 0)>(x, m - 1) : 1.0f;
+            const float xp1 = p > 1 ? f_pow_n<(P > 1 ? P - 1 : 0)>(x, p - 1) : 1.0f;
+            const float dg = (float)m * kf * xm1 + (float)p * al * xp1;
+            const float delta = __fdividef(g.hi, dg);
+            y = ff_two_sum(x, -delta);
+            return ff_add_sloppy(ym, ffloat{-(float)m * xm1 * delta, 0.0f});
+        }
+    }
+    // the float64 solve of the reference (rare)
+    const double q = iterate_to_new_discharge(ff_to_double(up), ff_to_double(ff_pow_n<M>(y, m)), (double)lat, (double)al, K.beta,
+                                              K.dt_d, K.dx_d);
+    y = kw_poly_root<P, M>(ff_from_double(q), K);
+    return ff_pow_n<M>(y, m);
 }
 
 }  // namespace lue_gb300

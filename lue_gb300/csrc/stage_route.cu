@@ -496,7 +496,15 @@ int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stre
         std::vector<int64_t> cur(off.begin(), off.end() - 1);
         for (int64_t s = 0; s < sc->nstages; ++s) ws[cur[sd[s]]++] = (int32_t)s;
         int64_t mi = 0;
-        for (const int4& r : srec) mi = std::max<int64_t>(mi, (unsigned)r.z >> 16);
+        sc->h_depth_max_cells.assign(maxd + 1, 0);
+        sc->h_depth_max_inputs.assign(maxd + 1, 0);
+        for (int64_t s2 = 0; s2 < sc->nstages; ++s2) {
+            const int4& r = srec[s2];
+            const int cnt = (int)((unsigned)r.y >> 16), nin = (int)((unsigned)r.z >> 16);
+            mi = std::max<int64_t>(mi, nin);
+            sc->h_depth_max_cells[sd[s2]] = std::max(sc->h_depth_max_cells[sd[s2]], cnt);
+            sc->h_depth_max_inputs[sd[s2]] = std::max(sc->h_depth_max_inputs[sd[s2]], nin);
+        }
         sc->max_stage_inputs = mi;
         sc->h_depth_offsets = off;
         TRY(cudaMalloc(&sc->wave_stage, std::max<int64_t>(sc->nstages, 1) * sizeof(int32_t)), "wave order");
@@ -508,6 +516,27 @@ int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stre
         TRY(cudaStreamSynchronize(stream), "stage build");  // the host vectors must outlive the copies
     }
     sc->bytes = sc->nstages * 20 + np * 12 + sc->ninputs * 4 + (int64_t)sc->h_depth_offsets.size() * 8;
+    if (getenv("LUE_GB300_VERBOSE")) {
+        // rounds: the critical path of the waves is about the sum over depths of the longest stage
+        std::vector<int4> srec(sc->nstages);
+        cudaMemcpy(srec.data(), sc->stage, sc->nstages * sizeof(int4), cudaMemcpyDeviceToHost);
+        std::vector<int> deep_max(sc->max_depth + 1, 0);
+        std::vector<int32_t> sd(sc->nstages);
+        for (int64_t d = 0; d <= sc->max_depth; ++d)
+            for (int64_t k = sc->h_depth_offsets[d]; k < sc->h_depth_offsets[d + 1]; ++k) sd[k] = (int32_t)d;
+        std::vector<int32_t> ws(sc->nstages);
+        cudaMemcpy(ws.data(), sc->wave_stage, sc->nstages * sizeof(int32_t), cudaMemcpyDeviceToHost);
+        double sum_rounds = 0;
+        int64_t sum_max = 0;
+        for (int64_t k = 0; k < sc->nstages; ++k) {
+            const int rounds = srec[ws[k]].z & 0xFFFF;
+            sum_rounds += rounds;
+            deep_max[sd[k]] = std::max(deep_max[sd[k]], rounds);
+        }
+        for (int v : deep_max) sum_max += v;
+        fprintf(stderr, "stage rounds: mean %.1f per stage, sum over depths of the longest %lld\n",
+                sum_rounds / std::max<int64_t>(1, sc->nstages), (long long)sum_max);
+    }
     if (getenv("LUE_GB300_VERBOSE"))
         fprintf(stderr, "stage topology: %lld tiles, %lld stages, depth %lld, %lld exits, %lld inputs, "
                         "at most %lld stages per depth and %lld inputs per stage\n",
@@ -565,18 +594,41 @@ struct StageRunArgs {
 // (d_base 1 for the pipelined waves after the depth-0 launch).  A Rule supplies the per-cell state (Cell,
 // kept in shared memory by position), the accumulator of the upstream outflows (Acc) and the cell step.
 // In round r the active positions are those whose round lies in (r - ns, r]: one contiguous range of the
-// stage's order, shared out over the threads.
+// stage's order, shared out over the NT threads.  Shared memory: the outflows by in-tile cell and step
+// parity, then per position meta, the inputs' history, and per position history row, cell state and
+// round starts; the launch provides enough for its largest stage.
 template <class R>
-__global__ void __launch_bounds__(kStageThreads) k_stage_wave(StageRunArgs a, R rule, int wave, int c_lo, int d_base,
-                                                              int chunk)
+struct StageLayout {
+    uint2* Qs;
+    uint2* meta;
+    uint2* hs;
+    int32_t* ex;
+    typename R::Cell* cells;
+    uint16_t* rstart;
+    __device__ StageLayout(unsigned char* base, int count, int hist)
+    {
+        Qs = reinterpret_cast<uint2*>(base);
+        meta = Qs + 2 * kStageCells;
+        hs = meta + count;
+        ex = reinterpret_cast<int32_t*>(hs + hist);
+        // 16-byte aligned: a Cell may hold doubles
+        cells = reinterpret_cast<typename R::Cell*>((reinterpret_cast<uintptr_t>(ex + count) + 15) & ~uintptr_t(15));
+        // round up to 4 bytes: a Cell may be a 1-byte empty struct
+        rstart = reinterpret_cast<uint16_t*>((reinterpret_cast<uintptr_t>(cells + count) + 3) & ~uintptr_t(3));
+    }
+};
+
+template <class R>
+static size_t stage_smem(int64_t cells, int64_t inputs_x_steps)
+{
+    return (2 * kStageCells + cells + inputs_x_steps) * sizeof(uint2) +
+           cells * (sizeof(int32_t) + sizeof(typename R::Cell)) + (cells + 2) * sizeof(uint16_t) + 32;  // + alignment
+}
+
+template <class R, int NT>
+__global__ void __launch_bounds__(NT) k_stage_wave(StageRunArgs a, R rule, int wave, int c_lo, int d_base, int chunk)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    uint2* Qs = reinterpret_cast<uint2*>(smem_raw);                         // [2][1024] outflow by step parity
-    uint2* meta = Qs + 2 * kStageCells;                                      // [1024] by position
-    int32_t* ex = reinterpret_cast<int32_t*>(meta + kStageCells);            // [1024] history row or -1
-    uint16_t* rstart = reinterpret_cast<uint16_t*>(ex + kStageCells);        // [1028] first position of each round
-    typename R::Cell* cells = reinterpret_cast<typename R::Cell*>(rstart + kStageCells + 4);  // [1024]
-    uint2* hs = reinterpret_cast<uint2*>(cells + kStageCells);               // [inputs x steps of the chunk]
     const int c = c_lo + (int)blockIdx.y, d = d_base + wave - c;
     if (d < 0 || d > a.max_depth) return;
     const int64_t si = a.depth_offsets[d] + blockIdx.x;
@@ -587,29 +639,33 @@ __global__ void __launch_bounds__(kStageThreads) k_stage_wave(StageRunArgs a, R 
     const int rounds = st.z & 0xFFFF, nin = (int)((unsigned)st.z >> 16);
     const int64_t in_base = st.w;
     const int t0 = c * chunk, ns = min(chunk, a.steps - t0);
+    StageLayout<R> L(smem_raw, count, nin * ns);
     const int64_t tr = tile / a.tcols, tc = tile - tr * a.tcols;
     const int64_t row0 = tr * kStageSide, col0 = tc * kStageSide;
-    for (int i = threadIdx.x; i < nin * ns; i += kStageThreads) {
+    for (int i = threadIdx.x; i < nin * ns; i += NT) {
         const int in = i / ns, t = i - in * ns;
-        hs[i] = a.hist[(int64_t)__ldg(a.inputs + in_base + in) * a.steps + t0 + t];
+        L.hs[i] = a.hist[(int64_t)__ldg(a.inputs + in_base + in) * a.steps + t0 + t];
     }
-    for (int i = threadIdx.x; i < count; i += kStageThreads) {
+    for (int i = threadIdx.x; i < count; i += NT) {
         const int64_t at = tile * kStageCells + begin + i;
         const uint2 m = __ldg(a.meta + at);
-        meta[i] = m;
-        ex[i] = __ldg(a.exit_id + at);
+        L.meta[i] = m;
+        L.ex[i] = __ldg(a.exit_id + at);
         const int p = (int)(m.x & 1023u);
-        rule.load(cells[i], (row0 + (p >> 5)) * a.cols + col0 + (p & 31), c);
-        const int rd = (int)((m.x >> 10) & 1023u);
-        if (i == 0 || rd != (int)((__ldg(a.meta + at - 1).x >> 10) & 1023u)) rstart[rd] = (uint16_t)i;
+        rule.load(L.cells[i], (row0 + (p >> 5)) * a.cols + col0 + (p & 31), c);
     }
-    if (threadIdx.x == 0) rstart[rounds] = (uint16_t)count;
+    __syncthreads();
+    for (int i = threadIdx.x; i < count; i += NT) {
+        const int rd = (int)((L.meta[i].x >> 10) & 1023u);
+        if (i == 0 || rd != (int)((L.meta[i - 1].x >> 10) & 1023u)) L.rstart[rd] = (uint16_t)i;
+    }
+    if (threadIdx.x == 0) L.rstart[rounds] = (uint16_t)count;
     __syncthreads();
     const int nrounds = rounds + ns - 1;
     for (int r = 0; r < nrounds; ++r) {
-        const int lo = rstart[max(0, r - ns + 1)], hi = rstart[min(rounds, r + 1)];
-        for (int i = lo + (int)threadIdx.x; i < hi; i += kStageThreads) {
-            const uint2 m = meta[i];
+        const int lo = L.rstart[max(0, r - ns + 1)], hi = L.rstart[min(rounds, r + 1)];
+        for (int i = lo + (int)threadIdx.x; i < hi; i += NT) {
+            const uint2 m = L.meta[i];
             const int t = r - (int)((m.x >> 10) & 1023u);
             const int p = (int)(m.x & 1023u);
             const unsigned em = (m.y >> 8) & 0xFFu;
@@ -619,29 +675,21 @@ __global__ void __launch_bounds__(kStageThreads) k_stage_wave(StageRunArgs a, R 
             while (um) {
                 const int q = __ffs(um) - 1;
                 um &= um - 1;
-                const uint2 v = ((em >> q) & 1u) ? hs[(fi + __popc(em & ((1u << q) - 1u))) * ns + t]
-                                                  : Qs[(t & 1) * kStageCells + p + nb_dr(q) * kStageSide + nb_dc(q)];
+                const uint2 v = ((em >> q) & 1u) ? L.hs[(fi + __popc(em & ((1u << q) - 1u))) * ns + t]
+                                                  : L.Qs[(t & 1) * kStageCells + p + nb_dr(q) * kStageSide + nb_dc(q)];
                 rule.add(acc, v);
             }
-            const uint2 o = rule.step(cells[i], acc, (row0 + (p >> 5)) * a.cols + col0 + (p & 31), t0 + t);
-            Qs[(t & 1) * kStageCells + p] = o;
-            const int32_t e = ex[i];
+            const uint2 o = rule.step(L.cells[i], acc, (row0 + (p >> 5)) * a.cols + col0 + (p & 31), t0 + t);
+            L.Qs[(t & 1) * kStageCells + p] = o;
+            const int32_t e = L.ex[i];
             if (e >= 0) a.hist[(int64_t)e * a.steps + t0 + t] = o;
         }
         __syncthreads();
     }
-    for (int i = threadIdx.x; i < count; i += kStageThreads) {
-        const int p = (int)(meta[i].x & 1023u);
-        rule.store(cells[i], (row0 + (p >> 5)) * a.cols + col0 + (p & 31), c, t0 + ns == a.steps);
+    for (int i = threadIdx.x; i < count; i += NT) {
+        const int p = (int)(L.meta[i].x & 1023u);
+        rule.store(L.cells[i], (row0 + (p >> 5)) * a.cols + col0 + (p & 31), c, t0 + ns == a.steps);
     }
-}
-
-template <class R>
-static size_t stage_smem(int64_t inputs_x_steps)
-{
-    return 2 * kStageCells * sizeof(uint2) + kStageCells * (sizeof(uint2) + sizeof(int32_t)) +
-           (kStageCells + 4) * sizeof(uint16_t) + kStageCells * sizeof(typename R::Cell) +
-           (size_t)inputs_x_steps * sizeof(uint2);
 }
 
 // --- rules -------------------------------------------------------------------------------------------
@@ -656,12 +704,18 @@ struct StageF32 {
     float bs;
     float* out;
     float* rem;
-    struct Cell {};
+    struct Cell {
+        float x, b;  // inflow and threshold / fraction, loaded with the stage
+    };
     struct Acc {
         FF t;
         bool nan;
     };
-    __device__ void load(Cell&, int64_t, int) const {}
+    __device__ void load(Cell& cl, int64_t g, int) const
+    {
+        cl.x = value_at(a, as, g);
+        cl.b = RR == Rule::accu ? 0.0f : value_at(b, bs, g);
+    }
     __device__ Acc begin() const { return Acc{FF{0.0f, 0.0f}, false}; }
     __device__ void add(Acc& acc, uint2 v) const
     {
@@ -669,11 +723,10 @@ struct StageF32 {
         if (isnan(h)) acc.nan = true;
         else acc.t.add(h, __uint_as_float(v.y));
     }
-    __device__ uint2 step(Cell&, const Acc& acc, int64_t g, int) const
+    __device__ uint2 step(Cell& cl, const Acc& acc, int64_t g, int) const
     {
         float oh = 0.0f, ol = 0.0f, r = 0.0f;
-        if (!rule_f32<RR>(acc.t, acc.nan, value_at(a, as, g), RR == Rule::accu ? 0.0f : value_at(b, bs, g), oh, ol,
-                          r)) {
+        if (!rule_f32<RR>(acc.t, acc.nan, cl.x, cl.b, oh, ol, r)) {
             out[g] = qnan<float>();
             if (RR != Rule::accu) rem[g] = qnan<float>();
             return make_uint2(__float_as_uint(qnan<float>()), 0u);
@@ -693,12 +746,18 @@ struct StageF64 {
     double bs;
     double* out;
     double* rem;
-    struct Cell {};
+    struct Cell {
+        double x, b;  // inflow and threshold / fraction, loaded with the stage
+    };
     struct Acc {
         double t;
         bool nan;
     };
-    __device__ void load(Cell&, int64_t, int) const {}
+    __device__ void load(Cell& cl, int64_t g, int) const
+    {
+        cl.x = value_at(a, as, g);
+        cl.b = RR == Rule::accu ? 0.0 : value_at(b, bs, g);
+    }
     __device__ Acc begin() const { return Acc{0.0, false}; }
     __device__ void add(Acc& acc, uint2 v) const
     {
@@ -706,10 +765,10 @@ struct StageF64 {
         if (isnan(h)) acc.nan = true;
         else acc.t += h;
     }
-    __device__ uint2 step(Cell&, const Acc& acc, int64_t g, int) const
+    __device__ uint2 step(Cell& cl, const Acc& acc, int64_t g, int) const
     {
         double o = 0.0, r = 0.0;
-        if (!rule_f64<RR>(acc.t, acc.nan, value_at(a, as, g), RR == Rule::accu ? 0.0 : value_at(b, bs, g), o, r)) {
+        if (!rule_f64<RR>(acc.t, acc.nan, cl.x, cl.b, o, r)) {
             o = qnan<double>();
             r = qnan<double>();
         }
@@ -724,12 +783,21 @@ struct StageF64 {
 template <class TIn>
 struct StageKW64 {
     RouteKW<TIn> v;  // inputs and constants (its out is the result raster)
-    struct Cell {};
+    struct Cell {
+        double qc, q, al, be, len;  // the cell's inputs, loaded with the stage
+    };
     struct Acc {
         double up;
         bool nan;
     };
-    __device__ void load(Cell&, int64_t, int) const {}
+    __device__ void load(Cell& cl, int64_t c, int) const
+    {
+        cl.qc = v.qcur ? __ldg(v.qcur + c) : v.qcur_s;
+        cl.q = v.lateral ? (double)__ldg(v.lateral + c) : v.lateral_s;
+        cl.al = v.alpha ? (double)__ldg(v.alpha + c) : v.alpha_s;
+        cl.be = v.beta ? __ldg(v.beta + c) : v.beta_s;
+        cl.len = v.dx ? __ldg(v.dx + c) : v.dx_s;
+    }
     __device__ Acc begin() const { return Acc{0.0, false}; }
     __device__ void add(Acc& acc, uint2 x) const
     {
@@ -737,34 +805,29 @@ struct StageKW64 {
         if (isnan(h)) acc.nan = true;
         else acc.up += h;
     }
-    __device__ uint2 step(Cell&, const Acc& acc, int64_t c, int) const
+    __device__ uint2 step(Cell& cl, const Acc& acc, int64_t c, int) const
     {
-        const double qc = v.qcur ? __ldg(v.qcur + c) : v.qcur_s;
-        const double q = v.lateral ? (double)__ldg(v.lateral + c) : v.lateral_s;
-        const double al = v.alpha ? (double)__ldg(v.alpha + c) : v.alpha_s;
-        const double be = v.beta ? __ldg(v.beta + c) : v.beta_s;
-        const double len = v.dx ? __ldg(v.dx + c) : v.dx_s;
-        const double o = rule_kw(acc.up, acc.nan, qc, q, al, be, v.dt, len, v.br);
+        const double o = rule_kw(acc.up, acc.nan, cl.qc, cl.q, cl.al, cl.be, v.dt, cl.len, v.br);
         v.out[c] = o;
         return make_uint2((unsigned)__double2loint(o), (unsigned)__double2hiint(o));
     }
     __device__ void store(Cell&, int64_t, int, bool) const {}
 };
 
-// kinematic wave, many steps, float-float (kinematic_wave_ff.cuh).  Between chunks the state of each cell
-// (discharge and its power, float-float) waits in state_q / state_p.
-struct StageKWFF {
+// kinematic wave, many steps, in float-float and the variable y = Q^(1/m) (kinematic_wave_ff.cuh).
+// Between chunks the state y of each cell waits in state_y.
+template <int P, int M>
+struct StageKWPoly {
     const double* qcur;
     const float* lateral;
     float lateral_s;
     const float* alpha;
     float alpha_s;
-    float2* state_q;
-    float2* state_p;
+    float2* state_y;
     double* out;
     KWConstFF K;
     struct Cell {
-        ffloat q, p;
+        ffloat y;
         float lat, al;
     };
     struct Acc {
@@ -776,12 +839,10 @@ struct StageKWFF {
         cl.lat = lateral ? __ldg(lateral + g) : lateral_s;
         cl.al = alpha ? __ldg(alpha + g) : alpha_s;
         if (chunk == 0) {
-            cl.q = ff_from_double(__ldg(qcur + g));
-            cl.p = (cl.q.hi >= 0.0f) ? kw_power(cl.q, K.br, K.beta) : ffloat{__int_as_float(0x7fc00000), 0.0f};
+            cl.y = kw_poly_root<P, M>(ff_from_double(__ldg(qcur + g)), K);
         } else {
-            const float2 q = state_q[g], p = state_p[g];
-            cl.q = ffloat{q.x, q.y};
-            cl.p = ffloat{p.x, p.y};
+            const float2 y = state_y[g];
+            cl.y = ffloat{y.x, y.y};
         }
     }
     __device__ Acc begin() const { return Acc{ffloat{0.0f, 0.0f}, false}; }
@@ -789,21 +850,17 @@ struct StageKWFF {
     {
         const ffloat v{__uint_as_float(x.x), __uint_as_float(x.y)};
         if (isnan(v.hi)) acc.nan = true;
-        else acc.up = ff_add(acc.up, v);
+        else acc.up = ff_add_sloppy(acc.up, v);
     }
     __device__ uint2 step(Cell& cl, const Acc& acc, int64_t, int) const
     {
-        kw_step_ff(acc.up, acc.nan, cl.q, cl.p, cl.lat, cl.al, K);
-        return make_uint2(__float_as_uint(cl.q.hi), __float_as_uint(cl.q.lo));
+        const ffloat q = kw_step_poly<P, M>(acc.up, acc.nan, cl.y, cl.lat, cl.al, K);
+        return make_uint2(__float_as_uint(q.hi), __float_as_uint(q.lo));
     }
     __device__ void store(Cell& cl, int64_t g, int, bool last) const
     {
-        if (last) {
-            out[g] = isnan(cl.q.hi) ? qnan<double>() : ff_to_double(cl.q);
-        } else {
-            state_q[g] = make_float2(cl.q.hi, cl.q.lo);
-            state_p[g] = make_float2(cl.p.hi, cl.p.lo);
-        }
+        if (last) out[g] = isnan(cl.y.hi) ? qnan<double>() : ff_to_double(ff_pow_n<M>(cl.y, K.br.m));
+        else state_y[g] = make_float2(cl.y.hi, cl.y.lo);
     }
 };
 
@@ -869,13 +926,35 @@ static int stage_chunk(const StageCore* sc, int steps)
     return (int)std::max<int64_t>(1, std::min<int64_t>(chunk, fit));
 }
 
+template <class R, int NT>
+static int set_smem_limit(const char* what)
+{
+    static bool done = false;
+    if (done) return LUE_GPU_OK;
+    if (int rc = cuda_status(cudaFuncSetAttribute(k_stage_wave<R, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  (int)stage_smem<R>(kStageCells, kStageHistorySlots)),
+                             what))
+        return rc;
+    done = true;
+    return LUE_GPU_OK;
+}
+
+// One launch over gy chunks of the stages of depths d_base + wave - c: 64 threads per CTA when their
+// largest stage has at most 256 cells, else kStageThreads; shared memory for the largest stage.
 template <class R>
 static int launch_wave(const StageRunArgs& a, const R& rule, int64_t gx, int64_t gy, int wave, int c_lo, int d_base,
-                       int chunk, size_t smem, cudaStream_t stream)
+                       int chunk, int64_t max_cells, int64_t max_hist, cudaStream_t stream, const char* what)
 {
-    k_stage_wave<R><<<dim3((unsigned)gx, (unsigned)gy), kStageThreads, smem, stream>>>(a, rule, wave, c_lo, d_base,
-                                                                                       chunk);
-    return 1;
+    const size_t smem = stage_smem<R>(max_cells, max_hist);
+    const dim3 grid((unsigned)gx, (unsigned)gy);
+    if (max_cells <= 256) {
+        if (int rc = set_smem_limit<R, 64>(what)) return rc;
+        k_stage_wave<R, 64><<<grid, 64, smem, stream>>>(a, rule, wave, c_lo, d_base, chunk);
+    } else {
+        if (int rc = set_smem_limit<R, kStageThreads>(what)) return rc;
+        k_stage_wave<R, kStageThreads><<<grid, kStageThreads, smem, stream>>>(a, rule, wave, c_lo, d_base, chunk);
+    }
+    return LUE_GPU_OK;
 }
 
 // `steps` steps of a rule over every stage.  Stages of depth 0 have no inputs: they run all steps in one
@@ -893,31 +972,28 @@ static int stage_run(lue_gpu_topology* t, const StageCore* sc, const R& rule, in
     StageRunArgs a{sc->stage,   sc->wave_stage, sc->depth_offsets, sc->meta,  sc->exit_id, sc->inputs,
                    core->rows,  core->cols,     sc->tcols,         sc->max_depth, steps,   chunk,
                    nchunks,     t->stage_hist};
-    const size_t smem = stage_smem<R>((int64_t)sc->max_stage_inputs * chunk);
-    static bool attr = false;
-    if (!attr) {
-        if (int rc = cuda_status(cudaFuncSetAttribute(k_stage_wave<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                      (int)stage_smem<R>(kStageHistorySlots)),
-                                 what))
-            return rc;
-        attr = true;
-    }
     const std::vector<int64_t>& off = sc->h_depth_offsets;
     const int64_t D = sc->max_depth;
     if (D < 0) return LUE_GPU_OK;
     int launches = 0;
     // depth 0: every step at once
-    launches += launch_wave(a, rule, off[1] - off[0], 1, 0, 0, 0, steps, stage_smem<R>(0), stream);
+    if (int rc = launch_wave(a, rule, off[1] - off[0], 1, 0, 0, 0, steps, sc->h_depth_max_cells[0], 0, stream, what))
+        return rc;
+    ++launches;
     // depths 1 ..: pipelined chunks
     for (int64_t w = 0; w <= D - 1 + nchunks - 1; ++w) {
         const int64_t c_lo = std::max<int64_t>(0, w - (D - 1)), c_hi = std::min<int64_t>(nchunks - 1, w);
-        int64_t gx = 0;
+        int64_t gx = 0, mc = 0, mh = 0;
         for (int64_t cc = c_lo; cc <= c_hi; ++cc) {
             const int64_t dd = 1 + w - cc;
             gx = std::max(gx, off[dd + 1] - off[dd]);
+            mc = std::max<int64_t>(mc, sc->h_depth_max_cells[dd]);
+            mh = std::max<int64_t>(mh, (int64_t)sc->h_depth_max_inputs[dd] * std::min(chunk, steps - (int)cc * chunk));
         }
         if (gx == 0) continue;
-        launches += launch_wave(a, rule, gx, c_hi - c_lo + 1, (int)w, (int)c_lo, 1, chunk, smem, stream);
+        if (int rc = launch_wave(a, rule, gx, c_hi - c_lo + 1, (int)w, (int)c_lo, 1, chunk, mc, mh, stream, what))
+            return rc;
+        ++launches;
     }
     count_launches(launches);
     return cuda_status(cudaGetLastError(), what);
@@ -999,6 +1075,11 @@ int stage_kinematic_wave_f64(lue_gpu_topology* t, const double* qcur, double qcu
     return stage_run(t, sc, rule, 1, 1, stream, "kinematic_wave_f64 (stages)");
 }
 
+static ffloat ff_split(double v);
+static KWConstFF kw_constants(double beta, double dt, double dx, const BetaRational& br);
+
+// One step with float32 lateral inflow and alpha: the float-float solve in y = Q^(1/m) when beta is a
+// small rational p/m (the result agrees with the float64 solve to ~1e-13), else the float64 solve.
 int stage_kinematic_wave_f32in(lue_gpu_topology* t, const double* qcur, double qcur_s, const float* lateral,
                                double lateral_s, const float* alpha, double alpha_s, double beta, double dt, double dx,
                                double* out, const BetaRational& br, cudaStream_t stream, bool* done)
@@ -1012,6 +1093,15 @@ int stage_kinematic_wave_f32in(lue_gpu_topology* t, const double* qcur, double q
     const int64_t n = t->core->n;
     k_stage_no_data<double><<<grid_for(n, 256), 256, 0, stream>>>(t->core->fd, n, out, (double*)nullptr);
     count_launches(1);
+    if (qcur && br.m >= 1 && br.m <= 16 && br.p >= 1 && br.p <= 16) {
+        const KWConstFF K = kw_constants(beta, dt, dx, br);
+        if (br.p == 3 && br.m == 5) {
+            StageKWPoly<3, 5> rule{qcur, lateral, (float)lateral_s, alpha, (float)alpha_s, nullptr, out, K};
+            return stage_run(t, sc, rule, 1, 1, stream, "kinematic_wave_f64_f32in (stages)");
+        }
+        StageKWPoly<0, 0> rule{qcur, lateral, (float)lateral_s, alpha, (float)alpha_s, nullptr, out, K};
+        return stage_run(t, sc, rule, 1, 1, stream, "kinematic_wave_f64_f32in (stages)");
+    }
     StageKW64<float> rule{RouteKW<float>{t->core->upmask, qcur, qcur_s, lateral, lateral_s, alpha, alpha_s, nullptr,
                                          beta, dt, nullptr, dx, out, t->core->cols, br}};
     return stage_run(t, sc, rule, 1, 1, stream, "kinematic_wave_f64_f32in (stages)");
@@ -1023,12 +1113,27 @@ static ffloat ff_split(double v)
     return ffloat{h, (float)(v - (double)h)};
 }
 
+static KWConstFF kw_constants(double beta, double dt, double dx, const BetaRational& br)
+{
+    KWConstFF K;
+    K.k = ff_split(dt / dx);
+    K.dt = ff_split(dt);
+    K.kf = (float)(dt / dx);
+    K.beta_f = (float)beta;
+    K.beta = beta;
+    K.dt_d = dt;
+    K.dx_d = dx;
+    K.br = br;
+    K.bad = std::isnan(beta) || std::isnan(dt) || std::isnan(dx) || !(dx > 0.0);
+    return K;
+}
+
 int stage_kinematic_wave_steps(lue_gpu_topology* t, const double* qcur, const float* lateral, double lateral_s,
                                const float* alpha, double alpha_s, double beta, double dt, double dx, int steps,
                                double* out, const BetaRational& br, cudaStream_t stream, bool* done)
 {
     *done = false;
-    if (stage_engine_off() || br.m == 0) return LUE_GPU_OK;
+    if (stage_engine_off() || br.m == 0 || br.m > 16 || br.p > 16) return LUE_GPU_OK;
     const StageCore* sc = nullptr;
     if (int rc = stage_core_get(t, stream, &sc)) return rc;
     if (!sc || sc->max_stage_inputs > kStageHistorySlots) return LUE_GPU_OK;
@@ -1040,19 +1145,10 @@ int stage_kinematic_wave_steps(lue_gpu_topology* t, const double* qcur, const fl
     const double budget = 0.4 * (double)free_b + (double)t->stage_hist_bytes;
     const int64_t per_step = std::max<int64_t>(sc->nexits, 1) * (int64_t)sizeof(uint2);
     const int fit = (int)std::max<int64_t>(1, std::min<int64_t>(steps, (int64_t)(budget / (double)per_step)));
-    KWConstFF K;
-    K.k = ff_split(dt / dx);
-    K.dt = ff_split(dt);
-    K.kf = (float)(dt / dx);
-    K.beta_f = (float)beta;
-    K.beta = beta;
-    K.dt_d = dt;
-    K.dx_d = dx;
-    K.br = br;
-    K.bad = std::isnan(beta) || std::isnan(dt) || std::isnan(dx) || !(dx > 0.0);
+    const KWConstFF K = kw_constants(beta, dt, dx, br);
     const int chunk = stage_chunk(sc, std::min(steps, fit));
-    if ((size_t)n * 2 * sizeof(float2) > t->stage_state_bytes && div_up(std::min(steps, fit), chunk) > 1) {
-        if (int rc = grow(t, t->stage_state, t->stage_state_bytes, (size_t)n * 2 * sizeof(float2), stream,
+    if ((size_t)n * sizeof(float2) > t->stage_state_bytes && div_up(std::min(steps, fit), chunk) > 1) {
+        if (int rc = grow(t, t->stage_state, t->stage_state_bytes, (size_t)n * sizeof(float2), stream,
                           "kinematic_wave_steps state"))
             return rc;
     }
@@ -1068,9 +1164,13 @@ int stage_kinematic_wave_steps(lue_gpu_topology* t, const double* qcur, const fl
         double* dst = done_steps + part == steps ? out : tmp + (size_t)which * n;
         k_stage_no_data<double><<<grid_for(n, 256), 256, 0, stream>>>(t->core->fd, n, dst, (double*)nullptr);
         count_launches(1);
-        StageKWFF rule{src, lateral, (float)lateral_s, alpha, (float)alpha_s, t->stage_state,
-                       t->stage_state ? t->stage_state + n : nullptr, dst, K};
-        rc = stage_run(t, sc, rule, part, stage_chunk(sc, part), stream, "kinematic_wave_steps (stages)");
+        if (br.p == 3 && br.m == 5) {
+            StageKWPoly<3, 5> rule{src, lateral, (float)lateral_s, alpha, (float)alpha_s, t->stage_state, dst, K};
+            rc = stage_run(t, sc, rule, part, stage_chunk(sc, part), stream, "kinematic_wave_steps (stages)");
+        } else {
+            StageKWPoly<0, 0> rule{src, lateral, (float)lateral_s, alpha, (float)alpha_s, t->stage_state, dst, K};
+            rc = stage_run(t, sc, rule, part, stage_chunk(sc, part), stream, "kinematic_wave_steps (stages)");
+        }
         if (rc) break;
         src = dst;
         which ^= 1;

@@ -49,6 +49,8 @@ struct StageCore {
     int32_t* wave_stage = nullptr;     // [nstages] stage ids sorted by depth
     int64_t* depth_offsets = nullptr;  // [max_depth + 2] start of each depth in wave_stage (device)
     std::vector<int64_t> h_depth_offsets;
+    std::vector<int32_t> h_depth_max_cells;   // [max_depth + 1] largest stage of each depth (cells)
+    std::vector<int32_t> h_depth_max_inputs;  // [max_depth + 1] most inputs of a stage of each depth
     uint2* meta = nullptr;             // [ntiles * 1024]
     int32_t* exit_id = nullptr;        // [ntiles * 1024] history row of the cell, or -1 (outflow stays in the stage)
     int32_t* inputs = nullptr;         // [ninputs] history row of the upstream cell of each edge into a stage

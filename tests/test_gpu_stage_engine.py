@@ -92,17 +92,28 @@ def _kw(rows, cols, seed):
     return d
 
 
-def test_kinematic_wave_single_step_equals_walk_engine(lfr):
+def test_kinematic_wave_single_step_against_walk_engine(lfr):
+    """float32 lateral inflow and alpha with beta = 3/5: the stage engine's float-float solve in
+    y = Q^(1/5) against the walk engine's float64 solve (~1e-13); float64 rasters: the same float64 solve
+    on both engines, bit for bit."""
     d = _kw(300, 500, 9)
     fd = d["flow_direction"].copy()
     fd[7, 11] = 255
     a = lfr.from_numpy(fd)
-    args = (lfr.from_numpy(d["discharge"]), lfr.from_numpy(d["lateral_inflow"]), lfr.from_numpy(d["alpha"]),
-            0.6, 3600.0, 100.0)
-    stage = lfr.to_numpy(lfr.kinematic_wave(a, *args))
-    with _env(LUE_GB300_ENGINE="walk"):
-        walk = lfr.to_numpy(lfr.kinematic_wave(a, *args))
-    assert np.array_equal(stage, walk, equal_nan=True)
+    for lat, alpha, exact in ((d["lateral_inflow"], d["alpha"], False),
+                              (d["lateral_inflow"].astype(np.float64), d["alpha"].astype(np.float64), True)):
+        args = (lfr.from_numpy(d["discharge"]), lfr.from_numpy(lat), lfr.from_numpy(alpha), 0.6, 3600.0, 100.0)
+        stage = lfr.to_numpy(lfr.kinematic_wave(a, *args))
+        with _env(LUE_GB300_ENGINE="walk"):
+            walk = lfr.to_numpy(lfr.kinematic_wave(a, *args))
+        if exact:
+            assert np.array_equal(stage, walk, equal_nan=True)
+        else:
+            assert np.array_equal(np.isnan(stage), np.isnan(walk))
+            assert parity.rel_error(stage, walk, parity.FLOOR64)[0] <= 1e-12
+        want = oracle.kinematic_wave(fd, d["discharge"], lat.astype(np.float64), alpha.astype(np.float64), 0.6,
+                                     3600.0, 100.0, fd.shape, dtype=np.float64)
+        parity.assert_close64(stage, want, "kinematic_wave one step")
 
 
 @pytest.mark.parametrize("chunk", ["1", "3", "8", "64"])
