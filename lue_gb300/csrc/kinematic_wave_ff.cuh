@@ -293,9 +293,22 @@ __device__ __forceinline__ ffloat kw_step_poly(ffloat up, bool nan, ffloat& y, f
         const ffloat known = ff_add_sloppy(ff_add_sloppy(ff_mul(K.k, up), ff_mul_f(ff_pow_n<P>(y, p), al)),
                                            ff_mul_f(K.dt, lat));
         const float kf = K.kf, knf = known.hi;
-        // float Newton from the previous state, to the float noise floor (~1e-7): it stops one step after
-        // a step below 3e-5 relative, which quadratic convergence takes far below that floor
+        // float Newton to the float noise floor (~1e-7): it stops one step after a step below 3e-5
+        // relative, which quadratic convergence takes far below that floor.  It starts from the better
+        // (smaller |g|) of the previous state and the reference's linearised guess (kinematic_wave.hpp:
+        // 61-91) taken to the power 1/m: after a jump in upstream discharge the previous state can be
+        // orders of magnitude off, and Newton on y^m closes such a gap only by a factor of about
+        // (m - 1) / m per step.
         float x = y.hi;
+        {
+            const float q0 = qprev_f, mean = 0.5f * (q0 + up.hi);
+            const float abpq = al * K.beta_f * __powf(mean, K.beta_f - 1.0f);
+            const float guess = __fdividef(kf * up.hi + abpq * q0 + K.dt.hi * lat, kf + abpq);
+            const float xg = guess > 0.0f ? __powf(guess, 1.0f / (float)m) : 0.0f;
+            const float ga = kf * f_pow_n<M>(x, m) + al * f_pow_n<P>(x, p) - knf;
+            const float gb = kf * f_pow_n<M>(xg, m) + al * f_pow_n<P>(xg, p) - knf;
+            if (xg > 0.0f && isfinite(gb) && fabsf(gb) < fabsf(ga)) x = xg;
+        }
         bool converged = false;
 #pragma unroll 1
         for (int it = 0; it < 24; ++it) {

@@ -939,15 +939,19 @@ static int set_smem_limit(const char* what)
     return LUE_GPU_OK;
 }
 
-// One launch over gy chunks of the stages of depths d_base + wave - c: 64 threads per CTA when their
-// largest stage has at most 256 cells, else kStageThreads; shared memory for the largest stage.
+// One launch over gy chunks of the stages of depths d_base + wave - c: one warp per CTA when their largest
+// stage has at most 64 cells, 64 threads up to 256 cells, else kStageThreads; shared memory for the
+// largest stage.
 template <class R>
 static int launch_wave(const StageRunArgs& a, const R& rule, int64_t gx, int64_t gy, int wave, int c_lo, int d_base,
                        int chunk, int64_t max_cells, int64_t max_hist, cudaStream_t stream, const char* what)
 {
     const size_t smem = stage_smem<R>(max_cells, max_hist);
     const dim3 grid((unsigned)gx, (unsigned)gy);
-    if (max_cells <= 256) {
+    if (max_cells <= 64) {
+        if (int rc = set_smem_limit<R, 32>(what)) return rc;
+        k_stage_wave<R, 32><<<grid, 32, smem, stream>>>(a, rule, wave, c_lo, d_base, chunk);
+    } else if (max_cells <= 256) {
         if (int rc = set_smem_limit<R, 64>(what)) return rc;
         k_stage_wave<R, 64><<<grid, 64, smem, stream>>>(a, rule, wave, c_lo, d_base, chunk);
     } else {
