@@ -915,11 +915,11 @@ static int grow(lue_gpu_topology* t, T*& p, size_t& have, size_t need, cudaStrea
     return LUE_GPU_OK;
 }
 
-// Steps per chunk: at most LUE_GB300_STAGE_CHUNK (default 8), and the inputs' history of a chunk must fit
-// in shared memory.
+// Steps per chunk: at most LUE_GB300_STAGE_CHUNK (default 32), and the inputs' history of a chunk must
+// fit in shared memory.
 static int stage_chunk(const StageCore* sc, int steps)
 {
-    int chunk = 8;
+    int chunk = 32;
     if (const char* e = getenv("LUE_GB300_STAGE_CHUNK")) chunk = std::max(1, atoi(e));
     chunk = std::min(chunk, steps);
     const int64_t fit = kStageHistorySlots / std::max<int64_t>(1, sc->max_stage_inputs);
