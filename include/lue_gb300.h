@@ -14,6 +14,14 @@
  *   value_policies::accu_fraction(fd, inflow, fraction)
  *                                      value_policies/accu_fraction.hpp:33-90
  *                                                                  lue_gpu_accu_fraction_f32 / _f64
+ *   value_policies::accu_capacity / accu_trigger (fd, inflow, capacity | trigger)
+ *                                      value_policies/accu_{capacity,trigger}.hpp
+ *                                                                  lue_gpu_accu_{capacity,trigger}_f32 / _f64
+ *   value_policies::upstream / downstream (fd, material)
+ *                                      value_policies/{upstream,downstream}.hpp
+ *                                                                  lue_gpu_{upstream,downstream}_f32 / _f64
+ *   downstream_distance(fd, cell_size) downstream_distance.hpp:31-44
+ *                                                                  lue_gpu_downstream_distance_f32 / _f64
  *   value_policies::kinematic_wave(fd, current_outflow, inflow, alpha, beta,
  *                                  time_step_duration, channel_length)
  *                                      value_policies/kinematic_wave.hpp:43-91
@@ -140,6 +148,51 @@ int lue_gpu_accu_fraction_f32(lue_gpu_topology* topology, const float* inflow, f
 int lue_gpu_accu_fraction_f64(lue_gpu_topology* topology, const double* inflow, double inflow_scalar,
                               const double* fraction, double fraction_scalar, double* flux, double* state,
                               void* stream);
+
+/* accu_capacity (value_policies/accu_capacity.hpp, definition/accu_capacity.hpp enter_cell): total =
+ * upstream + inflow; what flows on is min(total, capacity), the rest stays: (outflow, remainder).
+ * Domain inflow >= 0 && capacity >= 0. */
+int lue_gpu_accu_capacity_f32(lue_gpu_topology* topology, const float* inflow, float inflow_scalar,
+                              const float* capacity, float capacity_scalar, float* outflow, float* remainder,
+                              void* stream);
+int lue_gpu_accu_capacity_f64(lue_gpu_topology* topology, const double* inflow, double inflow_scalar,
+                              const double* capacity, double capacity_scalar, double* outflow, double* remainder,
+                              void* stream);
+
+/* accu_trigger (value_policies/accu_trigger.hpp, definition/accu_trigger.hpp enter_cell): total =
+ * upstream + inflow; if total < trigger everything stays (0, total), else it all flows on (total, 0).
+ * Domain inflow >= 0 && trigger >= 0. */
+int lue_gpu_accu_trigger_f32(lue_gpu_topology* topology, const float* inflow, float inflow_scalar,
+                             const float* trigger, float trigger_scalar, float* outflow, float* remainder,
+                             void* stream);
+int lue_gpu_accu_trigger_f64(lue_gpu_topology* topology, const double* inflow, double inflow_scalar,
+                             const double* trigger, double trigger_scalar, double* outflow, double* remainder,
+                             void* stream);
+
+/* upstream (value_policies/upstream.hpp, definition/upstream.hpp:9-160): per cell the sum of the material
+ * of the neighbours that drain into it; no-data where the flow direction or the cell's own material is
+ * no-data, or a draining neighbour's material is.  A focal operation: it takes the flow direction
+ * raster itself (row-major, rows x cols), no topology. */
+int lue_gpu_upstream_f32(const uint8_t* flow_direction, int64_t rows, int64_t cols, const float* material,
+                         float* out, void* stream);
+int lue_gpu_upstream_f64(const uint8_t* flow_direction, int64_t rows, int64_t cols, const double* material,
+                         double* out, void* stream);
+
+/* downstream (value_policies/downstream.hpp, definition/downstream.hpp:9-158): per cell the material of
+ * its downstream cell; its own material for a sink; 0 where the flow leaves the array; no-data where the
+ * flow direction or the cell's own or the downstream material is no-data. */
+int lue_gpu_downstream_f32(const uint8_t* flow_direction, int64_t rows, int64_t cols, const float* material,
+                           float* out, void* stream);
+int lue_gpu_downstream_f64(const uint8_t* flow_direction, int64_t rows, int64_t cols, const double* material,
+                           double* out, void* stream);
+
+/* downstream_distance (downstream_distance.hpp:9-44, definition/downstream_distance.hpp:9-75): the
+ * length of the step to the downstream cell: cell_size for N, W, E, S; sqrt(2) * cell_size for the
+ * diagonals; 0 for a sink; NaN for a no-data flow direction. */
+int lue_gpu_downstream_distance_f32(const uint8_t* flow_direction, int64_t rows, int64_t cols, float cell_size,
+                                    float* out, void* stream);
+int lue_gpu_downstream_distance_f64(const uint8_t* flow_direction, int64_t rows, int64_t cols, double cell_size,
+                                    double* out, void* stream);
 
 /* kinematic_wave: one time step of non-linear kinematic-wave routing; per cell the Newton-Raphson
  * solve of definition/kinematic_wave.hpp:145-254 with the upstream new discharge.

@@ -198,7 +198,58 @@ inline int fraction_call<double>(lue_gpu_topology* t, const double* a, double as
     return lue_gpu_accu_fraction_f64(t, a, as, b, bs, o1, o2, s);
 }
 
+#define LUE_GB300_TWO_OUTPUT_CALL(NAME)                                                                       \
+    template <typename F>                                                                                     \
+    inline int NAME##_call(lue_gpu_topology* t, const F* a, F as, const F* b, F bs, F* o1, F* o2, cudaStream_t s); \
+    template <>                                                                                               \
+    inline int NAME##_call<float>(lue_gpu_topology * t, const float* a, float as, const float* b, float bs,    \
+                                  float* o1, float* o2, cudaStream_t s)                                       \
+    {                                                                                                         \
+        return lue_gpu_accu_##NAME##_f32(t, a, as, b, bs, o1, o2, s);                                          \
+    }                                                                                                         \
+    template <>                                                                                               \
+    inline int NAME##_call<double>(lue_gpu_topology * t, const double* a, double as, const double* b,          \
+                                   double bs, double* o1, double* o2, cudaStream_t s)                          \
+    {                                                                                                         \
+        return lue_gpu_accu_##NAME##_f64(t, a, as, b, bs, o1, o2, s);                                          \
+    }
+LUE_GB300_TWO_OUTPUT_CALL(capacity)
+LUE_GB300_TWO_OUTPUT_CALL(trigger)
+#undef LUE_GB300_TWO_OUTPUT_CALL
+
+inline int one_hop_call(bool up, const std::uint8_t* fd, std::int64_t r, std::int64_t c, const float* m, float* o,
+                        cudaStream_t s)
+{
+    return up ? lue_gpu_upstream_f32(fd, r, c, m, o, s) : lue_gpu_downstream_f32(fd, r, c, m, o, s);
+}
+inline int one_hop_call(bool up, const std::uint8_t* fd, std::int64_t r, std::int64_t c, const double* m, double* o,
+                        cudaStream_t s)
+{
+    return up ? lue_gpu_upstream_f64(fd, r, c, m, o, s) : lue_gpu_downstream_f64(fd, r, c, m, o, s);
+}
+inline int distance_call(const std::uint8_t* fd, std::int64_t r, std::int64_t c, float cell, float* o, cudaStream_t s)
+{
+    return lue_gpu_downstream_distance_f32(fd, r, c, cell, o, s);
+}
+inline int distance_call(const std::uint8_t* fd, std::int64_t r, std::int64_t c, double cell, double* o,
+                         cudaStream_t s)
+{
+    return lue_gpu_downstream_distance_f64(fd, r, c, cell, o, s);
+}
+
 }  // namespace detail
+
+// downstream_distance(flow_direction, cell_size) (downstream_distance.hpp:31-44): the length of each
+// cell's step to its downstream cell; no-data (NaN) for a no-data flow direction.
+template <typename F>
+PartitionedArray<F> downstream_distance(const PartitionedArray<std::uint8_t>& fd, F cell_size,
+                                        cudaStream_t stream = nullptr)
+{
+    PartitionedArray<F> out(fd.shape(), fd.partition_shape());
+    check(detail::distance_call(fd.data(), fd.shape()[0], fd.shape()[1], cell_size, out.data(), stream),
+          "downstream_distance");
+    return out;
+}
 
 template <typename Count = std::uint8_t>
 PartitionedArray<Count> inflow_count(const PartitionedArray<std::uint8_t>& flow_direction, cudaStream_t stream = nullptr)
@@ -262,6 +313,59 @@ std::tuple<PartitionedArray<F>, PartitionedArray<F>> accu_fraction(const Partiti
                                    state.data(), stream),
           "accu_fraction");
     return {std::move(flux), std::move(state)};
+}
+
+// accu_capacity(flow_direction, inflow, capacity) -> (outflow, remainder).
+template <typename F, typename Inflow, typename Capacity>
+std::tuple<PartitionedArray<F>, PartitionedArray<F>> accu_capacity(const PartitionedArray<std::uint8_t>& fd,
+                                                                   const Inflow& inflow, const Capacity& capacity,
+                                                                   cudaStream_t stream = nullptr)
+{
+    auto a = detail::arg<F>(fd, inflow);
+    auto b = detail::arg<F>(fd, capacity);
+    PartitionedArray<F> outflow(fd.shape(), fd.partition_shape()), remainder(fd.shape(), fd.partition_shape());
+    check(detail::capacity_call<F>(fd.topology(stream).handle(), a.ptr, a.value, b.ptr, b.value, outflow.data(),
+                                   remainder.data(), stream),
+          "accu_capacity");
+    return {std::move(outflow), std::move(remainder)};
+}
+
+// accu_trigger(flow_direction, inflow, trigger) -> (outflow, remainder).
+template <typename F, typename Inflow, typename Trigger>
+std::tuple<PartitionedArray<F>, PartitionedArray<F>> accu_trigger(const PartitionedArray<std::uint8_t>& fd,
+                                                                  const Inflow& inflow, const Trigger& trigger,
+                                                                  cudaStream_t stream = nullptr)
+{
+    auto a = detail::arg<F>(fd, inflow);
+    auto b = detail::arg<F>(fd, trigger);
+    PartitionedArray<F> outflow(fd.shape(), fd.partition_shape()), remainder(fd.shape(), fd.partition_shape());
+    check(detail::trigger_call<F>(fd.topology(stream).handle(), a.ptr, a.value, b.ptr, b.value, outflow.data(),
+                                  remainder.data(), stream),
+          "accu_trigger");
+    return {std::move(outflow), std::move(remainder)};
+}
+
+// upstream(flow_direction, material) / downstream(flow_direction, material): one-hop operations.
+template <typename F>
+PartitionedArray<F> upstream(const PartitionedArray<std::uint8_t>& fd, const PartitionedArray<F>& material,
+                             cudaStream_t stream = nullptr)
+{
+    detail::verify_compatible(fd, material);
+    PartitionedArray<F> out(fd.shape(), fd.partition_shape());
+    check(detail::one_hop_call(true, fd.data(), fd.shape()[0], fd.shape()[1], material.data(), out.data(), stream),
+          "upstream");
+    return out;
+}
+
+template <typename F>
+PartitionedArray<F> downstream(const PartitionedArray<std::uint8_t>& fd, const PartitionedArray<F>& material,
+                               cudaStream_t stream = nullptr)
+{
+    detail::verify_compatible(fd, material);
+    PartitionedArray<F> out(fd.shape(), fd.partition_shape());
+    check(detail::one_hop_call(false, fd.data(), fd.shape()[0], fd.shape()[1], material.data(), out.data(), stream),
+          "downstream");
+    return out;
 }
 
 // kinematic_wave(flow_direction, current_outflow, inflow, alpha, beta, time_step_duration, channel_length):

@@ -184,6 +184,24 @@ extern "C" int lue_gpu_accu_fraction_f64(lue_gpu_topology* t, const double* infl
                                      "accu_fraction_f64");
 }
 
+// accu_capacity / accu_trigger: the same routers with the cell rules of ALG/definition/accu_capacity.hpp
+// and ALG/definition/accu_trigger.hpp (enter_cell).
+#define TWO_OUTPUT_OP(NAME, RULE, T, ROUTE, STAGE)                                                           \
+    extern "C" int lue_gpu_##NAME(lue_gpu_topology* t, const T* inflow, T inflow_scalar, const T* other,     \
+                                  T other_scalar, T* outflow, T* remainder, void* stream)                     \
+    {                                                                                                         \
+        if (int rc = check_topology(t, #NAME)) return rc;                                                     \
+        if (!outflow || !remainder) return fail(LUE_GPU_EINVAL, #NAME ": NULL output");                       \
+        STAGE_OR_WALK(STAGE(t, (int)RULE, inflow, inflow_scalar, other, other_scalar, outflow, remainder,      \
+                            (cudaStream_t)stream, &done));                                                    \
+        return ROUTE<RULE>(t, inflow, inflow_scalar, other, other_scalar, outflow, remainder, stream, #NAME); \
+    }
+
+TWO_OUTPUT_OP(accu_capacity_f32, Rule::capacity, float, route_f32, stage_route_f32)
+TWO_OUTPUT_OP(accu_capacity_f64, Rule::capacity, double, route_f64, stage_route_f64)
+TWO_OUTPUT_OP(accu_trigger_f32, Rule::trigger, float, route_f32, stage_route_f32)
+TWO_OUTPUT_OP(accu_trigger_f64, Rule::trigger, double, route_f64, stage_route_f64)
+
 extern "C" int lue_gpu_kinematic_wave_f64(lue_gpu_topology* t, const double* current_outflow,
                                           double current_outflow_scalar, const double* inflow, double inflow_scalar,
                                           const double* alpha, double alpha_scalar, const double* beta,

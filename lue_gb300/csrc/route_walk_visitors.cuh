@@ -23,7 +23,7 @@ __device__ __forceinline__ float qnan<float>() { return __int_as_float(0x7fc0000
 template <>
 __device__ __forceinline__ double qnan<double>() { return __longlong_as_double(0x7ff8000000000000ll); }
 
-enum class Rule { accu, threshold, fraction };
+enum class Rule { accu, threshold, fraction, capacity, trigger };
 
 // --- float32: float-float running values ---------------------------------------------------------
 
@@ -56,6 +56,40 @@ __device__ __forceinline__ bool rule_f32(FF t, bool nan, float x, float b, float
             rem = __fadd_rn(t.hi, t.lo);
             out_hi = 0.0f;
             out_lo = 0.0f;
+        }
+    } else if (R == Rule::capacity) {
+        // what flows on is capped at the capacity, the rest stays (accu_capacity.hpp enter_cell)
+        const float cap = b;
+        if (nan || isnan(x) || isnan(cap) || !(x >= 0.0f && cap >= 0.0f)) return false;
+        t.add(x);
+        t.normalise();
+        if (t.hi > cap || (t.hi == cap && t.lo > 0.0f)) {
+            FF d{0.0f, 0.0f};
+            two_sum(t.hi, -cap, d.hi, d.lo);
+            d.lo = __fadd_rn(d.lo, t.lo);
+            rem = __fadd_rn(d.hi, d.lo);
+            out_hi = cap;
+            out_lo = 0.0f;
+        } else {
+            rem = 0.0f;
+            out_hi = t.hi;
+            out_lo = t.lo;
+        }
+    } else if (R == Rule::trigger) {
+        // the total flows on once it reaches the trigger, else it all stays (accu_trigger.hpp enter_cell,
+        // strict '<')
+        const float trig = b;
+        if (nan || isnan(x) || isnan(trig) || !(x >= 0.0f && trig >= 0.0f)) return false;
+        t.add(x);
+        t.normalise();
+        if (t.hi < trig || (t.hi == trig && t.lo < 0.0f)) {
+            rem = __fadd_rn(t.hi, t.lo);
+            out_hi = 0.0f;
+            out_lo = 0.0f;
+        } else {
+            rem = 0.0f;
+            out_hi = t.hi;
+            out_lo = t.lo;
         }
     } else {
         const float f = b;
@@ -141,6 +175,26 @@ __device__ __forceinline__ bool rule_f64(double t, bool nan, double x, double b,
             rem = t;
             out = 0.0;
         }
+    } else if (R == Rule::capacity) {
+        const double cap = b;
+        if (nan || isnan(x) || isnan(cap) || !(x >= 0.0 && cap >= 0.0)) return false;
+        t += x;
+        rem = 0.0;
+        if (t > cap) {
+            rem = t - cap;
+            t = cap;
+        }
+        out = t;
+    } else if (R == Rule::trigger) {
+        const double trig = b;
+        if (nan || isnan(x) || isnan(trig) || !(x >= 0.0 && trig >= 0.0)) return false;
+        t += x;
+        rem = 0.0;
+        if (t < trig) {
+            rem = t;
+            t = 0.0;
+        }
+        out = t;
     } else {
         const double f = b;
         if (nan || isnan(x) || isnan(f) || !(x >= 0.0 && f >= 0.0 && f <= 1.0)) return false;

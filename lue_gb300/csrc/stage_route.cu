@@ -1029,9 +1029,12 @@ int stage_route_f32(lue_gpu_topology* t, int rule, const float* a, float as, con
     if (int rc = stage_core_get(t, stream, &sc)) return rc;
     if (!sc || sc->max_stage_inputs > kStageHistorySlots) return LUE_GPU_OK;
     *done = true;
-    if (rule == (int)Rule::threshold)
-        return route_f32_rule<Rule::threshold>(t, sc, a, as, b, bs, out, rem, stream);
-    return route_f32_rule<Rule::fraction>(t, sc, a, as, b, bs, out, rem, stream);
+    switch (rule) {
+        case (int)Rule::threshold: return route_f32_rule<Rule::threshold>(t, sc, a, as, b, bs, out, rem, stream);
+        case (int)Rule::fraction: return route_f32_rule<Rule::fraction>(t, sc, a, as, b, bs, out, rem, stream);
+        case (int)Rule::capacity: return route_f32_rule<Rule::capacity>(t, sc, a, as, b, bs, out, rem, stream);
+        default: return route_f32_rule<Rule::trigger>(t, sc, a, as, b, bs, out, rem, stream);
+    }
 }
 
 template <Rule RR>
@@ -1054,10 +1057,13 @@ int stage_route_f64(lue_gpu_topology* t, int rule, const double* a, double as, c
     if (int rc = stage_core_get(t, stream, &sc)) return rc;
     if (!sc || sc->max_stage_inputs > kStageHistorySlots) return LUE_GPU_OK;
     *done = true;
-    if (rule == (int)Rule::accu) return route_f64_rule<Rule::accu>(t, sc, a, as, b, bs, out, rem, stream);
-    if (rule == (int)Rule::threshold)
-        return route_f64_rule<Rule::threshold>(t, sc, a, as, b, bs, out, rem, stream);
-    return route_f64_rule<Rule::fraction>(t, sc, a, as, b, bs, out, rem, stream);
+    switch (rule) {
+        case (int)Rule::accu: return route_f64_rule<Rule::accu>(t, sc, a, as, b, bs, out, rem, stream);
+        case (int)Rule::threshold: return route_f64_rule<Rule::threshold>(t, sc, a, as, b, bs, out, rem, stream);
+        case (int)Rule::fraction: return route_f64_rule<Rule::fraction>(t, sc, a, as, b, bs, out, rem, stream);
+        case (int)Rule::capacity: return route_f64_rule<Rule::capacity>(t, sc, a, as, b, bs, out, rem, stream);
+        default: return route_f64_rule<Rule::trigger>(t, sc, a, as, b, bs, out, rem, stream);
+    }
 }
 
 int stage_kinematic_wave_f64(lue_gpu_topology* t, const double* qcur, double qcur_s, const double* lateral,

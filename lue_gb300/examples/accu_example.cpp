@@ -1,6 +1,7 @@
 // accu_example.cpp — the reference's back_and_forth accu case (accu_test.cpp:1248-1308) and the
-// pcraster manual example of accu_threshold (accu_threshold_test.cpp:65-132) through the C++ mirror of
-// lue::value_policies.  Prints the results row-major, one raster per line; exit status 0 on success.
+// pcraster manual example of accu_threshold (accu_threshold_test.cpp:65-132), with accu_capacity,
+// accu_trigger, upstream, downstream and downstream_distance on the same rasters, through the C++ mirror
+// of lue::value_policies.  Prints the results row-major, one raster per line; exit status 0 on success.
 #include <cstdio>
 #include <vector>
 
@@ -38,6 +39,20 @@ int main()
         std::printf("\n");
         for (float v : st) std::printf("%g ", v);
         std::printf("\n");
+
+        // accu_capacity and accu_trigger on the same rasters (accu_capacity_test.cpp:65-134,
+        // accu_trigger_test.cpp:65-134), upstream / downstream of the inflow, downstream_distance
+        auto [cap_out, cap_rem] = value_policies::accu_capacity<float>(fd, in, Scalar<float>{1.5f});
+        auto [trig_out, trig_rem] = value_policies::accu_trigger<float>(fd, in, Scalar<float>{1.5f});
+        auto up = value_policies::upstream(fd, in);
+        auto down = value_policies::downstream(fd, in);
+        auto dist = downstream_distance(fd, 2.0f);
+        for (auto* a : {&cap_out, &cap_rem, &trig_out, &trig_rem, &up, &down, &dist}) {
+            std::vector<float> v(25);
+            a->to_host(v.data());
+            for (float x : v) std::printf("%g ", x);
+            std::printf("\n");
+        }
 
         // a shape mismatch throws, like the reference's verify_compatible
         auto other = PartitionedArray<float>(Shape{5, 6}, Shape{5, 6});

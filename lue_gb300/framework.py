@@ -224,6 +224,60 @@ def accu_fraction(flow_direction, inflow, fraction):
                        fraction, "fraction")
 
 
+def accu_capacity(flow_direction, inflow, capacity):
+    """value_policies::accu_capacity: (outflow, remainder); what flows on is capped at the capacity."""
+    L = _lib.lib()
+    return _two_output(L.lue_gpu_accu_capacity_f32, L.lue_gpu_accu_capacity_f64, flow_direction, inflow, capacity,
+                       "capacity")
+
+
+def accu_trigger(flow_direction, inflow, trigger):
+    """value_policies::accu_trigger: (outflow, remainder); the total flows on once it reaches the trigger."""
+    L = _lib.lib()
+    return _two_output(L.lue_gpu_accu_trigger_f32, L.lue_gpu_accu_trigger_f64, flow_direction, inflow, trigger,
+                       "trigger")
+
+
+def _one_hop(fn32, fn64, flow_direction, material, name):
+    if not isinstance(material, PartitionedArray):
+        raise TypeError(f"{name}: material must be a PartitionedArray")
+    if material.shape != flow_direction.shape:
+        raise _lib.LueGpuError(2, f"{name}: shape {material.shape} differs from flow direction shape "
+                                  f"{flow_direction.shape}")
+    _check_partitioning(flow_direction, material)
+    if material.dtype not in (torch.float32, torch.float64):
+        raise TypeError(f"{name}: material must be float32 or float64")
+    out = _empty(flow_direction, material.dtype)
+    fn = fn32 if material.dtype == torch.float32 else fn64
+    fd = flow_direction.data
+    _lib.check(fn(fd.data_ptr(), fd.shape[0], fd.shape[1], material.data.data_ptr(), out.data_ptr(), _stream(fd)))
+    return PartitionedArray(out, flow_direction.partition_shape)
+
+
+def upstream(flow_direction, material):
+    """value_policies::upstream: per cell the sum of the material of the neighbours draining into it."""
+    L = _lib.lib()
+    return _one_hop(L.lue_gpu_upstream_f32, L.lue_gpu_upstream_f64, flow_direction, material, "upstream")
+
+
+def downstream(flow_direction, material):
+    """value_policies::downstream: per cell the material of its downstream cell."""
+    L = _lib.lib()
+    return _one_hop(L.lue_gpu_downstream_f32, L.lue_gpu_downstream_f64, flow_direction, material, "downstream")
+
+
+def downstream_distance(flow_direction, cell_size, dtype=torch.float32):
+    """downstream_distance: the length of each cell's step to its downstream cell."""
+    if dtype not in (torch.float32, torch.float64):
+        raise TypeError("downstream_distance: dtype must be float32 or float64")
+    out = _empty(flow_direction, dtype)
+    L = _lib.lib()
+    fn = L.lue_gpu_downstream_distance_f32 if dtype == torch.float32 else L.lue_gpu_downstream_distance_f64
+    fd = flow_direction.data
+    _lib.check(fn(fd.data_ptr(), fd.shape[0], fd.shape[1], float(cell_size), out.data_ptr(), _stream(fd)))
+    return PartitionedArray(out, flow_direction.partition_shape)
+
+
 def kinematic_wave(flow_direction, current_outflow, inflow, alpha, beta, time_step_duration, channel_length):
     """One time step; float64 discharge.  Float32 inflow/alpha rasters with scalar beta and channel
     length take the mixed-precision entry point (exact float32 -> float64 promotion per cell)."""

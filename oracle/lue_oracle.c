@@ -25,6 +25,11 @@
  *                    accu_threshold ....................... ALG/definition/accu_threshold.hpp:29-260
  *                    accu_fraction ........................ ALG/definition/accu_fraction.hpp:29-253
  *                    kinematic_wave ....................... ALG/definition/kinematic_wave.hpp:13-456
+ *                    accu_capacity, accu_trigger .......... ALG/definition/accu_{capacity,trigger}.hpp
+ *                                                            (enter_cell)
+ *   - one-hop and local operations: upstream .............. ALG/definition/upstream.hpp:9-160
+ *                                   downstream ............ ALG/definition/downstream.hpp:9-158
+ *                                   downstream_distance ... ALG/definition/downstream_distance.hpp:9-75
  *   - value-policy domains ................................ ALG/value_policies/{accu,accu_threshold,
  *                                                            accu_fraction,kinematic_wave}.hpp:15-21
  *
@@ -313,7 +318,7 @@ float lue_oracle_iterate_to_new_discharge_f32(float upstream, float current, flo
 /* The accumulating router, instantiated for float and double                                       */
 /* ------------------------------------------------------------------------------------------------ */
 
-enum { OP_ACCU = 0, OP_THRESHOLD = 1, OP_FRACTION = 2, OP_KINEMATIC_WAVE = 3 };
+enum { OP_ACCU = 0, OP_THRESHOLD = 1, OP_FRACTION = 2, OP_KINEMATIC_WAVE = 3, OP_CAPACITY = 4, OP_TRIGGER = 5 };
 
 #define REAL float
 #define SFX f32
@@ -412,3 +417,86 @@ int lue_oracle_d8_flow_direction(const double* z, int64_t rows, int64_t cols, ui
         }
     return 0;
 }
+
+/*
+ * upstream (ALG/definition/upstream.hpp:9-160): the sum of the material of the neighbours draining into
+ * each cell, in the order NW, N, NE, W, E, SW, S, SE; no-data where the cell's flow direction or its own
+ * material is no-data, or where a contributing neighbour's material is no-data.  Outside the array the
+ * flow-direction halo points away from the array (ALG/policy/flow_direction_halo.hpp), so nothing
+ * enters from there.
+ *
+ * downstream (ALG/definition/downstream.hpp:9-158): the material of each cell's downstream cell; the
+ * cell's own material for a sink (code 5, and any code that is not a direction); 0 where the flow
+ * leaves the array (the material halo is filled with 0); no-data where the cell's flow direction or
+ * material, or the downstream material, is no-data.
+ */
+#define NB_ORDER_DR(k) ((k) < 3 ? -1 : ((k) < 5 ? 0 : 1))
+static const int NB_DC[8] = {-1, 0, 1, -1, 1, -1, 0, 1};
+static const uint8_t NB_INFLOW[8] = {3, 2, 1, 6, 4, 9, 8, 7};  /* code of a neighbour draining here */
+
+#define ONE_HOP(T, SFX_)                                                                                  \
+    int lue_oracle_upstream_##SFX_(const uint8_t* fd, int64_t rows, int64_t cols, const T* m, T* out)       \
+    {                                                                                                     \
+        for (int64_t r = 0; r < rows; ++r)                                                                \
+            for (int64_t c = 0; c < cols; ++c) {                                                          \
+                const int64_t i = r * cols + c;                                                           \
+                if (fd[i] == U8_NO_DATA || isnan(m[i])) {                                                 \
+                    out[i] = (T)NAN;                                                                      \
+                    continue;                                                                             \
+                }                                                                                         \
+                T s = 0;                                                                                  \
+                int nd = 0;                                                                               \
+                for (int k = 0; k < 8 && !nd; ++k) {                                                      \
+                    const int64_t rr = r + NB_ORDER_DR(k), cc = c + NB_DC[k];                             \
+                    if (rr < 0 || rr >= rows || cc < 0 || cc >= cols) continue;                           \
+                    const int64_t j = rr * cols + cc;                                                     \
+                    if (fd[j] != NB_INFLOW[k]) continue;                                                  \
+                    if (isnan(m[j])) nd = 1;                                                              \
+                    else s += m[j];                                                                       \
+                }                                                                                         \
+                out[i] = nd ? (T)NAN : s;                                                                 \
+            }                                                                                             \
+        return 0;                                                                                         \
+    }                                                                                                     \
+    int lue_oracle_downstream_##SFX_(const uint8_t* fd, int64_t rows, int64_t cols, const T* m, T* out)     \
+    {                                                                                                     \
+        for (int64_t r = 0; r < rows; ++r)                                                                \
+            for (int64_t c = 0; c < cols; ++c) {                                                          \
+                const int64_t i = r * cols + c;                                                           \
+                if (fd[i] == U8_NO_DATA || isnan(m[i])) {                                                 \
+                    out[i] = (T)NAN;                                                                      \
+                    continue;                                                                             \
+                }                                                                                         \
+                int dr, dc;                                                                               \
+                d8_offset(fd[i], &dr, &dc);                                                               \
+                if (dr == 0 && dc == 0) {                                                                 \
+                    out[i] = m[i];                                                                        \
+                    continue;                                                                             \
+                }                                                                                         \
+                const int64_t rr = r + dr, cc = c + dc;                                                   \
+                if (rr < 0 || rr >= rows || cc < 0 || cc >= cols) {                                       \
+                    out[i] = 0;                                                                           \
+                    continue;                                                                             \
+                }                                                                                         \
+                out[i] = m[rr * cols + cc];                                                               \
+            }                                                                                             \
+        return 0;                                                                                         \
+    }                                                                                                     \
+    /* downstream_distance (ALG/definition/downstream_distance.hpp:9-75): the cell size for N, W, E, S,    \
+       sqrt(2) * cell size for the diagonals, 0 otherwise; no-data (NaN) for a no-data flow direction. */  \
+    int lue_oracle_downstream_distance_##SFX_(const uint8_t* fd, int64_t rows, int64_t cols, T cell_size,   \
+                                              T* out)                                                     \
+    {                                                                                                     \
+        const T diag = (T)sqrt((double)2) * cell_size;                                                    \
+        for (int64_t i = 0; i < rows * cols; ++i) {                                                       \
+            const uint8_t code = fd[i];                                                                   \
+            if (code == U8_NO_DATA) out[i] = (T)NAN;                                                      \
+            else if (code == 7 || code == 9 || code == 1 || code == 3) out[i] = diag;                     \
+            else if (code == 8 || code == 4 || code == 6 || code == 2) out[i] = cell_size;                \
+            else out[i] = 0;                                                                              \
+        }                                                                                                 \
+        return 0;                                                                                         \
+    }
+
+ONE_HOP(float, f32)
+ONE_HOP(double, f64)

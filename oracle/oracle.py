@@ -47,6 +47,11 @@ def lib():
             f.argtypes = [p, i64, i64, i64, i64, p, real, p, real, p, p, i32]
             f = getattr(L, f"lue_oracle_kinematic_wave_{sfx}")
             f.argtypes = [p, i64, i64, i64, i64, p, real, p, real, p, real, p, real, real, p, real, p, i32]
+            for op in ("accu_capacity", "accu_trigger"):
+                getattr(L, f"lue_oracle_{op}_{sfx}").argtypes = [p, i64, i64, i64, i64, p, real, p, real, p, p, i32]
+            getattr(L, f"lue_oracle_upstream_{sfx}").argtypes = [p, i64, i64, p, p]
+            getattr(L, f"lue_oracle_downstream_{sfx}").argtypes = [p, i64, i64, p, p]
+            getattr(L, f"lue_oracle_downstream_distance_{sfx}").argtypes = [p, i64, i64, real, p]
         L.lue_oracle_inflow_count.argtypes = [p, i64, i64, i64, i64, i32, p]
         L.lue_oracle_downstream_level.argtypes = [p, i64, i64, p]
         L.lue_oracle_d8_flow_direction.argtypes = [p, i64, i64, p]
@@ -155,6 +160,56 @@ def accu_fraction(fd, inflow, fraction, partition_shape=None, dtype=np.float32, 
         flux.ctypes.data, state.ctypes.data, nthreads))
     del k0, k1
     return flux, state
+
+
+def _two_output(op, fd, inflow, other, partition_shape, dtype, nthreads):
+    fd = _fd(fd)
+    pr, pc = _pshape(fd, partition_shape)
+    t = np.dtype(dtype).type
+    p0, s0, k0 = _raster(inflow, fd.shape, t)
+    p1, s1, k1 = _raster(other, fd.shape, t)
+    outflow = np.empty(fd.shape, dtype)
+    remainder = np.empty(fd.shape, dtype)
+    _check(getattr(lib(), f"lue_oracle_{op}_{_sfx(dtype)}")(
+        fd.ctypes.data, fd.shape[0], fd.shape[1], pr, pc, p0, s0, p1, s1,
+        outflow.ctypes.data, remainder.ctypes.data, nthreads))
+    del k0, k1
+    return outflow, remainder
+
+
+def accu_capacity(fd, inflow, capacity, partition_shape=None, dtype=np.float32, nthreads=1):
+    """(outflow, remainder): what flows on is capped at the capacity, the rest stays."""
+    return _two_output("accu_capacity", fd, inflow, capacity, partition_shape, dtype, nthreads)
+
+
+def accu_trigger(fd, inflow, trigger, partition_shape=None, dtype=np.float32, nthreads=1):
+    """(outflow, remainder): the total flows on once it reaches the trigger, else it all stays."""
+    return _two_output("accu_trigger", fd, inflow, trigger, partition_shape, dtype, nthreads)
+
+
+def _one_hop(op, fd, material, dtype):
+    fd = _fd(fd)
+    m = np.ascontiguousarray(material, dtype)
+    out = np.empty(fd.shape, dtype)
+    _check(getattr(lib(), f"lue_oracle_{op}_{_sfx(dtype)}")(fd.ctypes.data, fd.shape[0], fd.shape[1],
+                                                           m.ctypes.data, out.ctypes.data))
+    return out
+
+
+def upstream(fd, material, dtype=np.float64):
+    return _one_hop("upstream", fd, material, dtype)
+
+
+def downstream(fd, material, dtype=np.float64):
+    return _one_hop("downstream", fd, material, dtype)
+
+
+def downstream_distance(fd, cell_size, dtype=np.float64):
+    fd = _fd(fd)
+    out = np.empty(fd.shape, dtype)
+    _check(getattr(lib(), f"lue_oracle_downstream_distance_{_sfx(dtype)}")(
+        fd.ctypes.data, fd.shape[0], fd.shape[1], np.dtype(dtype).type(cell_size), out.ctypes.data))
+    return out
 
 
 def kinematic_wave(fd, current_outflow, inflow, alpha, beta, time_step_duration, channel_length,

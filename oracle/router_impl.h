@@ -116,6 +116,28 @@ static inline void FN(enter_cell)(FN(Router) * R, int64_t i)
             }
             break;
         }
+        case OP_CAPACITY: {  /* ALG/definition/accu_capacity.hpp enter_cell */
+            REAL e = VAL(R->a0, R->a0s, i), c = VAL(R->a1, R->a1s, i);
+            if (isnan(e) || isnan(c) || !(e >= 0 && c >= 0)) {
+                FN(mark_no_data)(R, i);
+            } else {
+                *o += e;
+                R->rem[i] = 0;
+                if (*o > c) { R->rem[i] = *o - c; *o = c; }
+            }
+            break;
+        }
+        case OP_TRIGGER: {  /* ALG/definition/accu_trigger.hpp enter_cell */
+            REAL e = VAL(R->a0, R->a0s, i), t = VAL(R->a1, R->a1s, i);
+            if (isnan(e) || isnan(t) || !(e >= 0 && t >= 0)) {
+                FN(mark_no_data)(R, i);
+            } else {
+                *o += e;
+                R->rem[i] = 0;
+                if (*o < t) { R->rem[i] = *o; *o = 0; }
+            }
+            break;
+        }
         case OP_KINEMATIC_WAVE: {
             REAL qc = VAL(R->a0, R->a0s, i), q = VAL(R->a1, R->a1s, i);
             REAL al = VAL(R->alpha, R->alphas, i), be = VAL(R->beta, R->betas, i);
@@ -368,6 +390,30 @@ int FN(lue_oracle_accu_fraction)(const uint8_t* fd, int64_t rows, int64_t cols, 
     FN(Router) R;
     if (FN(setup)(&R, OP_FRACTION, fd, rows, cols, prow, pcol)) return -1;
     R.a0 = ext; R.a0s = ext_scalar; R.a1 = frac; R.a1s = frac_scalar; R.out = flux; R.rem = state;
+    return FN(route)(&R, nthreads);
+}
+
+/* value_policies::accu_capacity: (outflow, remainder); domain inflow >= 0 && capacity >= 0
+   (ALG/value_policies/accu_capacity.hpp:15-18). */
+int FN(lue_oracle_accu_capacity)(const uint8_t* fd, int64_t rows, int64_t cols, int64_t prow, int64_t pcol,
+                                 const REAL* ext, REAL ext_scalar, const REAL* cap, REAL cap_scalar,
+                                 REAL* outflow, REAL* remainder, int nthreads)
+{
+    FN(Router) R;
+    if (FN(setup)(&R, OP_CAPACITY, fd, rows, cols, prow, pcol)) return -1;
+    R.a0 = ext; R.a0s = ext_scalar; R.a1 = cap; R.a1s = cap_scalar; R.out = outflow; R.rem = remainder;
+    return FN(route)(&R, nthreads);
+}
+
+/* value_policies::accu_trigger: (outflow, remainder); domain inflow >= 0 && trigger >= 0
+   (ALG/value_policies/accu_trigger.hpp:15-18). */
+int FN(lue_oracle_accu_trigger)(const uint8_t* fd, int64_t rows, int64_t cols, int64_t prow, int64_t pcol,
+                                const REAL* ext, REAL ext_scalar, const REAL* trig, REAL trig_scalar,
+                                REAL* outflow, REAL* remainder, int nthreads)
+{
+    FN(Router) R;
+    if (FN(setup)(&R, OP_TRIGGER, fd, rows, cols, prow, pcol)) return -1;
+    R.a0 = ext; R.a0s = ext_scalar; R.a1 = trig; R.a1s = trig_scalar; R.out = outflow; R.rem = remainder;
     return FN(route)(&R, nthreads);
 }
 

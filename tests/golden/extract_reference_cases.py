@@ -17,6 +17,8 @@ Sources read (paths within the reference project):
 - source/framework/algorithm/test/kinematic_wave_test.cpp
 - source/framework/algorithm/test/inflow_count_test.cpp
 - source/framework/algorithm/test/d8_flow_direction_test.cpp
+- source/framework/algorithm/test/accu_capacity_test.cpp, accu_trigger_test.cpp
+- source/framework/algorithm/test/upstream_test.cpp, downstream_test.cpp, downstream_distance_test.cpp
 
 Each ``create_partitioned_array(shape, partition_shape, {{partition}, ...})`` literal lists its
 partitions in row-major partition order, each partition's cells row-major.  Partition extents follow
@@ -179,7 +181,7 @@ def eval_scalar(expr, env, kind="f"):
 def eval_shape(expr, env):
     e = expr.strip()
     e = re.sub(r"^lue::test::", "", e)
-    m = re.fullmatch(r"\{?\{\s*(\d+)\s*,\s*(\d+)\s*\}\}?", e)
+    m = re.fullmatch(r"\{?\{?\s*(\d+)\s*,\s*(\d+)\s*\}?\}?", e)
     if m:
         return (int(m.group(1)), int(m.group(2)))
     m = re.fullmatch(r"(\w+)\.shape\(\)", e)
@@ -312,7 +314,8 @@ def parse_fixtures(text):
     return fixtures
 
 
-OPS = ("accu_threshold", "accu_fraction", "kinematic_wave", "accu")
+OPS = ("accu_threshold", "accu_fraction", "kinematic_wave", "accu", "accu_capacity", "accu_trigger", "upstream",
+       "downstream")
 
 
 def extract_file(path, rel, fixtures, cases):
@@ -456,6 +459,36 @@ def extract_d8(path, rel, fixtures, cases):
                           "compare": "equal"})
 
 
+def extract_downstream_distance(path, rel, fixtures, cases):
+    """downstream_distance_test.cpp: a flow-direction literal, the cell size and the distances wanted
+    (q stands for sqrt(2) * cell size)."""
+    text = strip_comments(open(path).read())
+    for name, line, body in test_cases(text):
+        env = Env(base_env())
+        m = re.search(r"cell_size\s*\{\s*([0-9.]+)\s*\}", body)
+        if not m:
+            continue
+        cell = float(m.group(1))
+        env.values["q"] = math.sqrt(2.0) * cell
+        for st in split_statements(body):
+            s1 = " ".join(st.split())
+            mm = re.match(r".*?\b(array_shape|partition_shape)\s*\{(.*)\}$", s1)
+            if mm and "Shape" in s1:
+                env.shapes[mm.group(1)] = eval_shape(mm.group(2), env)
+        arrays = {}
+        for mm in re.finditer(r"(flow_direction|result_we_want)\s*=\s*lue::test::create_partitioned_array", body):
+            start = mm.start(0) + body[mm.start(0):].index("lue::test::")
+            close = matching(body, body.index("(", body.index(">", start)), "(", ")")
+            kind_env = Env(env)
+            arrays[mm.group(1)] = eval_array(body[start:close + 1], kind_env, fixtures)
+        if set(arrays) != {"flow_direction", "result_we_want"}:
+            continue
+        cases.append({"file": rel, "line": line, "name": name, "op": "downstream_distance",
+                      "partition_shape": arrays["flow_direction"]["partition_shape"],
+                      "flow_direction": arr(arrays["flow_direction"]), "cell_size": cell,
+                      "expected": {"distance": arr(arrays["result_we_want"])}, "compare": "close"})
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("LUE_REFERENCE", "/root/reference"))
@@ -465,8 +498,11 @@ def main():
     fixtures = parse_fixtures(strip_comments(open(os.path.join(tdir, "flow_accumulation.cpp.in")).read()))
     cases = []
     for f in ("accu_test.cpp", "accu_threshold_test.cpp", "accu_fraction_test.cpp",
-              "kinematic_wave_test.cpp", "inflow_count_test.cpp"):
+              "kinematic_wave_test.cpp", "inflow_count_test.cpp", "accu_capacity_test.cpp",
+              "accu_trigger_test.cpp", "upstream_test.cpp", "downstream_test.cpp"):
         extract_file(os.path.join(tdir, f), f"{TEST_DIR}/{f}", fixtures, cases)
+    extract_downstream_distance(os.path.join(tdir, "downstream_distance_test.cpp"),
+                                f"{TEST_DIR}/downstream_distance_test.cpp", fixtures, cases)
     extract_d8(os.path.join(tdir, "d8_flow_direction_test.cpp"), f"{TEST_DIR}/d8_flow_direction_test.cpp",
                fixtures, cases)
     with open(a.out, "w") as fh:

@@ -24,4 +24,18 @@ def test_cpp_mirror_known_answers():
     state = np.array([float(v) for v in lines[2].split()], np.float32).reshape(5, 5)
     assert np.array_equal(flux, golden.f32(case["expected"]["outflow_we_got"]))
     assert np.array_equal(state, golden.f32(case["expected"]["residue_we_got"]))
-    assert lines[3] == "shape mismatch rejected"
+    # accu_capacity / accu_trigger against the reference's pcraster manual example 1 of each
+    rows = [np.array([float(v) for v in lines[k].split()], np.float32).reshape(5, 5) for k in range(3, 10)]
+    for op, (o, r) in (("accu_capacity", rows[0:2]), ("accu_trigger", rows[2:4])):
+        case = [c for c in golden.load(op) if c["name"] == "pcraster_manual_example1"][0]
+        assert np.array_equal(o, golden.f32(case["expected"]["outflow_we_got"])), op
+        assert np.array_equal(r, golden.f32(case["expected"]["residue_we_got"])), op
+    # upstream / downstream / downstream_distance against the oracle on the same rasters
+    from oracle import oracle
+    fd = golden.u8(case["flow_direction"])
+    inflow = golden.f32(case["inputs"]["inflow"]["raster"]).astype(np.float32)
+    assert np.array_equal(rows[4], oracle.upstream(fd, inflow, np.float32))
+    assert np.array_equal(rows[5], oracle.downstream(fd, inflow, np.float32))
+    # printed with %g: six significant digits
+    np.testing.assert_allclose(rows[6], oracle.downstream_distance(fd, 2.0, np.float32), rtol=1e-5)
+    assert lines[10] == "shape mismatch rejected"

@@ -38,6 +38,13 @@ def run_case(lfr, c, dtype):
         other = "threshold" if op == "accu_threshold" else "fraction"
         flux, state = fn(fd, arg("inflow"), arg(other))
         return {"outflow_we_got": lfr.to_numpy(flux), "residue_we_got": lfr.to_numpy(state)}
+    if op in ("accu_capacity", "accu_trigger"):
+        fn = getattr(lfr, op)
+        out, rem = fn(fd, arg("inflow"), arg("capacity" if op == "accu_capacity" else "trigger"))
+        return {"outflow_we_got": lfr.to_numpy(out), "residue_we_got": lfr.to_numpy(rem)}
+    if op in ("upstream", "downstream"):
+        m = lfr.from_numpy(np.asarray(golden.arg(ins["material"], dtype)), ps)
+        return {"material_we_got": lfr.to_numpy(getattr(lfr, op)(fd, m))}
     if op == "kinematic_wave":
         out = lfr.kinematic_wave(fd, *[arg(k) for k in ("current_outflow", "inflow", "alpha", "beta",
                                                           "time_step_duration", "channel_length")])
@@ -45,7 +52,8 @@ def run_case(lfr, c, dtype):
     raise AssertionError(op)
 
 
-ROUTING = [c for c in golden.load() if c["op"] in ("accu", "accu_threshold", "accu_fraction")]
+ROUTING = [c for c in golden.load() if c["op"] in ("accu", "accu_threshold", "accu_fraction", "accu_capacity",
+                                                   "accu_trigger", "upstream", "downstream")]
 KW = golden.load("kinematic_wave")
 
 
@@ -101,3 +109,17 @@ def test_d8_flow_direction_case(lfr, case, dtype):
     z = golden.arg({"raster": case["elevation"]}, dtype)
     got = lfr.to_numpy(lfr.d8_flow_direction(lfr.from_numpy(z)))
     assert (got == np.array(case["expected"]["flow_direction"], np.uint8)).all(), got
+
+
+DISTANCE = golden.load("downstream_distance")
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+@pytest.mark.parametrize("case", DISTANCE, ids=[golden.case_id(c) for c in DISTANCE])
+def test_downstream_distance_case(lfr, case, dtype):
+    import torch
+    fd = lfr.from_numpy(golden.u8(case["flow_direction"]), case["partition_shape"])
+    got = lfr.to_numpy(lfr.downstream_distance(fd, case["cell_size"],
+                                               torch.float32 if dtype == np.float32 else torch.float64))
+    assert got.dtype == dtype
+    assert_matches(got, golden.f32(case["expected"]["distance"]), "close")

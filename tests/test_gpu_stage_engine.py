@@ -153,3 +153,45 @@ def test_kinematic_wave_steps_zero_and_no_data(lfr):
         q = oracle.kinematic_wave(fd, q, lat.astype(np.float64), d["alpha"].astype(np.float64), 0.6, 3600.0, 100.0,
                                   fd.shape, dtype=np.float64)
     parity.assert_close64(got, q, "kinematic_wave_steps with zeros and no-data")
+
+
+@pytest.mark.parametrize("shape", [(1024, 1024), (333, 777), (1, 300)])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+def test_capacity_and_trigger_equal_walk_engine(lfr, shape, dtype):
+    fd, rng = _raster(*shape, seed=41, holes=0.001)
+    m = rng.lognormal(0.0, 1.0, shape).astype(dtype)
+    m[rng.random(shape) < 0.001] = np.nan
+    m[rng.random(shape) < 0.001] = -1.0
+    limit = (rng.random(shape) * 20.0).astype(dtype)
+    ps = (min(256, shape[0]), min(256, shape[1]))
+    a = lfr.from_numpy(fd, ps)
+    md, ld = lfr.from_numpy(m, ps), lfr.from_numpy(limit, ps)
+    for name in ("accu_capacity", "accu_trigger"):
+        op = getattr(lfr, name)
+        stage = [lfr.to_numpy(x) for x in op(a, md, ld)]
+        with _env(LUE_GB300_ENGINE="walk"):
+            walk = [lfr.to_numpy(x) for x in op(a, md, ld)]
+        for s_, w_ in zip(stage, walk):
+            assert np.array_equal(s_, w_, equal_nan=True), name
+        ref = getattr(oracle, name)(fd, m.astype(np.float64), limit.astype(np.float64), ps, dtype=np.float64)
+        check = parity.assert_close32 if dtype == np.float32 else parity.assert_close64
+        check(stage[0], ref[0], f"{name} outflow")
+        check(stage[1], ref[1], f"{name} remainder")
+
+
+@pytest.mark.parametrize("shape", [(517, 1031), (64, 32), (1, 77), (77, 1)])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+def test_upstream_downstream_distance_against_oracle(lfr, shape, dtype):
+    import torch
+    fd, rng = _raster(*shape, seed=19, holes=0.01)
+    fd = fd.copy()
+    fd[rng.random(shape) < 0.005] = 5       # sinks
+    m = rng.random(shape).astype(dtype)
+    m[rng.random(shape) < 0.01] = np.nan
+    a = lfr.from_numpy(fd)
+    md = lfr.from_numpy(m)
+    assert np.array_equal(lfr.to_numpy(lfr.upstream(a, md)), oracle.upstream(fd, m, dtype), equal_nan=True)
+    assert np.array_equal(lfr.to_numpy(lfr.downstream(a, md)), oracle.downstream(fd, m, dtype), equal_nan=True)
+    tdt = torch.float32 if dtype == np.float32 else torch.float64
+    got = lfr.to_numpy(lfr.downstream_distance(a, 2.5, tdt))
+    assert np.array_equal(got, oracle.downstream_distance(fd, 2.5, dtype), equal_nan=True)

@@ -1,8 +1,8 @@
 """Pin the CPU oracle to the reference's own known-answer tests.
 
 Every case in tests/golden/reference_cases.json was extracted from the reference's Boost.Test sources
-(source/framework/algorithm/test/{accu,accu_threshold,accu_fraction,kinematic_wave,inflow_count}
-_test.cpp) by tests/golden/extract_reference_cases.py.  The comparison rules restate the reference's
+(source/framework/algorithm/test/{accu,accu_threshold,accu_fraction,accu_capacity,accu_trigger,
+kinematic_wave,inflow_count,upstream,downstream,downstream_distance,d8_flow_direction}_test.cpp) by tests/golden/extract_reference_cases.py.  The comparison rules restate the reference's
 test helpers (source/framework/test/include/lue/framework/test/compare.hpp):
 
 - ``check_arrays_are_equal``: element-wise equality, NaN == NaN (compare.hpp:52-100);
@@ -56,6 +56,13 @@ def run_case(c, dtype):
         flux, state = oracle.accu_fraction(fd, golden.arg(ins["inflow"], dtype),
                                            golden.arg(ins["fraction"], dtype), ps, dtype)
         return {"outflow_we_got": flux, "residue_we_got": state}
+    if op in ("accu_capacity", "accu_trigger"):
+        other = "capacity" if op == "accu_capacity" else "trigger"
+        out, rem = getattr(oracle, op)(fd, golden.arg(ins["inflow"], dtype), golden.arg(ins[other], dtype), ps,
+                                       dtype)
+        return {"outflow_we_got": out, "residue_we_got": rem}
+    if op in ("upstream", "downstream"):
+        return {"material_we_got": getattr(oracle, op)(fd, golden.arg(ins["material"], dtype), dtype)}
     if op == "kinematic_wave":
         a = [golden.arg(ins[k], dtype) for k in ("current_outflow", "inflow", "alpha", "beta",
                                                   "time_step_duration", "channel_length")]
@@ -63,7 +70,8 @@ def run_case(c, dtype):
     raise AssertionError(op)
 
 
-ROUTING = [c for c in golden.load() if c["op"] in ("accu", "accu_threshold", "accu_fraction", "kinematic_wave")]
+ROUTING = [c for c in golden.load() if c["op"] in ("accu", "accu_threshold", "accu_fraction", "kinematic_wave",
+                                                   "accu_capacity", "accu_trigger", "upstream", "downstream")]
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
@@ -129,3 +137,13 @@ def test_d8_flow_direction_case(case):
     z = golden.arg({"raster": case["elevation"]}, np.float32)
     got = oracle.d8_flow_direction(z)
     assert (got == np.array(case["expected"]["flow_direction"], np.uint8)).all(), got
+
+
+DISTANCE = golden.load("downstream_distance")
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+@pytest.mark.parametrize("case", DISTANCE, ids=[golden.case_id(c) for c in DISTANCE])
+def test_downstream_distance_case(case, dtype):
+    got = oracle.downstream_distance(golden.u8(case["flow_direction"]), case["cell_size"], dtype)
+    assert_matches(got, golden.f32(case["expected"]["distance"]), "close")
