@@ -79,9 +79,10 @@ __device__ __forceinline__ int build_scan(int v, int* warp_tot, int& total)
 struct StageSortSmem {
     unsigned long long key[kStageCells];
     int32_t d[kStageCells];
-    int16_t sd[kStageCells];  // downstream cell in the same stage, or -1
-    int16_t h[kStageCells];   // distance to the stage's most downstream cell
+    int16_t sd[kStageCells];  // downstream cell in the same depth group, or -1
+    int16_t h[kStageCells];   // distance to the depth group's most downstream cell
     int16_t J[kStageCells];
+    int16_t ss[kStageCells];  // by in-tile cell: the sorted position of the first cell of its stage, or -1
     int warp_tot[kStageBuildThreads / 32];
 };
 
@@ -91,12 +92,15 @@ __device__ __forceinline__ int32_t depth_of(const StageSortSmem& sm, const int32
     return p >= 0 ? sm.d[p] : __ldg(depth + gi);
 }
 
-// Per tile: the order of its valid cells by (depth, round), the rounds, and per position a flag word
-// (bit 0: first cell of a stage, bit 1: the outflow leaves the stage, bits 2-5: inputs from other stages);
-// counts[4 tile ..] = stages, exits, inputs, valid cells.
+// Per tile: the order of its valid cells by (depth, distance to the depth group's most downstream cell),
+// cut into stages of at most `cap` consecutive cells of one depth; the rounds; and per position a flag
+// word (bit 0: first cell of a stage, bit 1: the outflow leaves the stage, bits 2-9: mask of the upstream
+// neighbours in other stages); counts[4 tile ..] = stages, exits, inputs, valid cells.  The cells of a
+// depth group sorted by decreasing distance have every upstream cell of the group before them, so any cut
+// of that order into consecutive pieces gives stages whose in-tile inputs come from earlier stages.
 __global__ void __launch_bounds__(kStageBuildThreads)
     k_stage_sort(const uint8_t* __restrict__ fd, const uint8_t* __restrict__ upmask, const int32_t* __restrict__ depth,
-                 StageGeom g, uint16_t* order, uint16_t* round_at, uint16_t* flags_at, int32_t* counts)
+                 StageGeom g, int cap, uint16_t* order, uint16_t* round_at, uint16_t* flags_at, int32_t* counts)
 {
     __shared__ StageSortSmem sm;
     const int64_t tr = blockIdx.y, tc = blockIdx.x, tile = tr * g.tcols + tc;
@@ -165,22 +169,14 @@ __global__ void __launch_bounds__(kStageBuildThreads)
             __syncthreads();
         }
     }
-    // per position (thread t: positions 2t, 2t + 1): stage starts, rounds, exits, inputs
-    int starts = 0, exits = 0, inputs = 0, valid = 0;
+    // per position (thread t: positions 2t, 2t + 1): depth-group starts
     int first[2];
     for (int k = 0; k < 2; ++k) {
         const int i = 2 * t + k;
         const unsigned long long key = sm.key[i];
-        first[k] = 0;
-        if (key == ~0ull) continue;
-        const int dd = (int)(key >> 20);
-        if (i == 0 || (int)(sm.key[i - 1] >> 20) != dd) {
-            first[k] = 1;
-            ++starts;
-        }
-        ++valid;
+        first[k] = key != ~0ull && (i == 0 || (int)(sm.key[i - 1] >> 20) != (int)(key >> 20));
     }
-    // the first position of each position's stage: inclusive max-scan of start positions
+    // the first position of each position's depth group: inclusive max-scan of start positions
     int mine = -1;
     for (int k = 0; k < 2; ++k)
         if (first[k]) mine = 2 * t + k;
@@ -200,15 +196,30 @@ __global__ void __launch_bounds__(kStageBuildThreads)
         mine = max(before, lane ? excl_lane : -1);  // last start strictly before position 2t
         __syncthreads();
     }
+    // stages: pieces of `cap` consecutive positions of a depth group
+    int stage_first[2];
+    for (int p = t; p < kStageCells; p += kStageBuildThreads) sm.ss[p] = -1;
+    __syncthreads();
+    for (int k = 0; k < 2; ++k) {
+        const int i = 2 * t + k;
+        const unsigned long long key = sm.key[i];
+        stage_first[k] = -1;
+        if (key == ~0ull) continue;
+        if (first[k]) mine = i;
+        stage_first[k] = mine + (i - mine) / cap * cap;
+        sm.ss[key & 1023] = (int16_t)stage_first[k];
+    }
+    __syncthreads();
+    int starts = 0, exits = 0, inputs = 0, valid = 0;
     for (int k = 0; k < 2; ++k) {
         const int i = 2 * t + k;
         const unsigned long long key = sm.key[i];
         uint16_t flag = 0, rnd = 0;
         if (key != ~0ull) {
-            if (first[k]) mine = i;
-            const int p = (int)(key & 1023), dd = (int)(key >> 20);
+            const int sf = stage_first[k];
+            const int p = (int)(key & 1023);
             const int hh = 1023 - (int)((key >> 10) & 1023);
-            const int hs = 1023 - (int)((sm.key[mine] >> 10) & 1023);
+            const int hs = 1023 - (int)((sm.key[sf] >> 10) & 1023);
             rnd = (uint16_t)(hs - hh);
             int64_t gi;
             stage_cell(g, tr, tc, p, gi);
@@ -221,22 +232,24 @@ __global__ void __launch_bounds__(kStageBuildThreads)
                 if (gr >= 0 && gr < g.rows && gc >= 0 && gc < g.cols) {
                     const int qr = pr + dr, qc = pc + dc;
                     const bool in = qr >= 0 && qr < kStageSide && qc >= 0 && qc < kStageSide;
-                    const int32_t dv = depth_of(sm, depth, in ? qr * kStageSide + qc : -1, gr * g.cols + gc);
-                    ex = dv >= 0 && (!in || dv != dd);
+                    ex = in ? sm.d[qr * kStageSide + qc] >= 0 && sm.ss[qr * kStageSide + qc] != sf
+                            : __ldg(depth + gr * g.cols + gc) >= 0;
                 }
             }
             // inputs: upstream cells in other stages
-            unsigned m = __ldg(upmask + gi), nin = 0;
+            unsigned m = __ldg(upmask + gi), em = 0;
             while (m) {
                 const int q = __ffs(m) - 1;
                 m &= m - 1;
                 const int qr = pr + nb_dr(q), qc = pc + nb_dc(q);
                 const bool in = qr >= 0 && qr < kStageSide && qc >= 0 && qc < kStageSide;
-                if (!in || sm.d[qr * kStageSide + qc] != dd) ++nin;
+                if (!in || sm.ss[qr * kStageSide + qc] != sf) em |= 1u << q;
             }
-            flag = (uint16_t)(first[k] | (ex ? 2 : 0) | (nin << 2));
+            flag = (uint16_t)((i == sf ? 1 : 0) | (ex ? 2 : 0) | (em << 2));
+            starts += i == sf;
             exits += ex;
-            inputs += (int)nin;
+            inputs += __popc(em);
+            ++valid;
             order[tile * kStageCells + i] = (uint16_t)p;
         } else {
             order[tile * kStageCells + i] = 0xFFFFu;
@@ -261,7 +274,8 @@ __global__ void __launch_bounds__(kStageBuildThreads)
     k_stage_ids(const uint8_t* __restrict__ upmask, const int32_t* __restrict__ depth, StageGeom g,
                 const uint16_t* __restrict__ order, const uint16_t* __restrict__ round_at,
                 const uint16_t* __restrict__ flags_at, const int32_t* __restrict__ bases, int4* stage,
-                int32_t* stage_depth, int32_t* exit_id, int32_t* cell_exit, int32_t* input_at, uint2* meta)
+                int32_t* stage_depth, int32_t* exit_id, int32_t* cell_exit, int32_t* input_at, uint2* meta,
+                int32_t* exit_stage)
 {
     __shared__ int warp_tot[kStageBuildThreads / 32];
     __shared__ int s_begin[kStageCells], s_count[kStageCells], s_rounds[kStageCells], s_in0[kStageCells];
@@ -287,7 +301,7 @@ __global__ void __launch_bounds__(kStageBuildThreads)
         if (o[k] != 0xFFFFu) {
             starts += f[k] & 1;
             exits += (f[k] >> 1) & 1;
-            ins += f[k] >> 2;
+            ins += __popc(f[k] >> 2);
         }
     }
     int tot;
@@ -308,7 +322,7 @@ __global__ void __launch_bounds__(kStageBuildThreads)
                 ++s_run;
             }
             local[k] = s_run - 1;
-            i_cur += f[k] >> 2;
+            i_cur += __popc(f[k] >> 2);
         }
     }
     __syncthreads();
@@ -316,7 +330,7 @@ __global__ void __launch_bounds__(kStageBuildThreads)
         if (local[k] < 0) continue;
         atomicAdd(&s_count[local[k]], 1);
         atomicMax(&s_rounds[local[k]], (int)r[k] + 1);
-        atomicAdd(&s_nin[local[k]], (int)(f[k] >> 2));
+        atomicAdd(&s_nin[local[k]], __popc(f[k] >> 2));
     }
     __syncthreads();
     int e_run = e_excl, i_cur = i_excl;
@@ -329,28 +343,21 @@ __global__ void __launch_bounds__(kStageBuildThreads)
             meta[at] = make_uint2(0u, 0u);
             continue;
         }
-        const int p = o[k], pr = p >> 5, pc = p & 31, dd = d[p];
+        const int p = o[k], dd = d[p];
         int64_t gi;
         stage_cell(g, tr, tc, p, gi);
         int32_t id = -1;
         if ((f[k] >> 1) & 1) {
             id = exit_base + e_run++;
             cell_exit[gi] = id;
+            exit_stage[id] = stage_base + local[k];
         }
         exit_id[at] = id;
-        const unsigned um = __ldg(upmask + gi);
-        unsigned em = 0, mm = um;
-        while (mm) {
-            const int q = __ffs(mm) - 1;
-            mm &= mm - 1;
-            const int qr = pr + nb_dr(q), qc = pc + nb_dc(q);
-            const bool in = qr >= 0 && qr < kStageSide && qc >= 0 && qc < kStageSide;
-            if (!in || d[qr * kStageSide + qc] != dd) em |= 1u << q;
-        }
+        const unsigned um = __ldg(upmask + gi), em = f[k] >> 2;
         const int ls = local[k];
         input_at[at] = input_base + i_cur;
         const unsigned first_input = (unsigned)(i_cur - s_in0[ls]);
-        i_cur += f[k] >> 2;
+        i_cur += __popc(em);
         meta[at] = make_uint2((unsigned)p | ((unsigned)r[k] << 10), um | (em << 8) | (first_input << 16));
         if (f[k] & 1) {
             const int sid = stage_base + ls;
@@ -388,6 +395,60 @@ __global__ void __launch_bounds__(kStageBuildThreads)
     }
 }
 
+// Stage ids of the exits -> positions in the wave order.
+__global__ void k_remap_i32(int32_t* v, int64_t n, const int32_t* __restrict__ map)
+{
+    for (int64_t i = grid_stride_begin(); i < n; i += grid_stride()) v[i] = map[v[i]];
+}
+
+// Per stage (block per position k of the wave order): the stages whose exits feed it, each with the
+// earliest round at which one of its cells consumes them, and the latest round of the stage's own exits.
+// Pass 1 (list == nullptr) counts the producers; pass 2 writes them at offsets[k].
+__global__ void __launch_bounds__(256)
+    k_stage_producers(const int4* __restrict__ stage, const int32_t* __restrict__ wave_stage, int64_t nstages,
+                      const uint2* __restrict__ meta, const int32_t* __restrict__ exit_id,
+                      const int32_t* __restrict__ inputs, const int32_t* __restrict__ exit_stage, int32_t* counts,
+                      int32_t* max_exit_round, const int64_t* __restrict__ offsets, int2* list)
+{
+    extern __shared__ int2 pairs[];  // [inputs of the stage]: (producer position, consumer round)
+    __shared__ int s_max_exit;
+    const int64_t k = blockIdx.x;
+    if (k >= nstages) return;
+    const int4 st = stage[wave_stage[k]];
+    const int64_t tile = st.x;
+    const int begin = st.y & 0xFFFF, count = (int)((unsigned)st.y >> 16), nin = (int)((unsigned)st.z >> 16);
+    const int64_t in_base = st.w;
+    if (threadIdx.x == 0) s_max_exit = -1;
+    __syncthreads();
+    for (int i = threadIdx.x; i < count; i += blockDim.x) {
+        const int64_t at = tile * kStageCells + begin + i;
+        const uint2 m = meta[at];
+        const int rd = (int)((m.x >> 10) & 1023u);
+        if (exit_id[at] >= 0) atomicMax(&s_max_exit, rd);
+        const unsigned em = (m.y >> 8) & 0xFFu;
+        const int fi = (int)(m.y >> 16), ne = __popc(em);
+        for (int j = 0; j < ne; ++j) pairs[fi + j] = make_int2(exit_stage[inputs[in_base + fi + j]], rd);
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    // distinct producers with their smallest consumer round (nin is small: at most a few hundred)
+    int distinct = 0;
+    for (int i = 0; i < nin; ++i) {
+        int2 pi = pairs[i];
+        int j = 0;
+        for (; j < distinct; ++j)
+            if (pairs[j].x == pi.x) break;
+        if (j == distinct) pairs[distinct++] = pi;
+        else pairs[j].y = min(pairs[j].y, pi.y);
+    }
+    if (!list) {
+        counts[k] = distinct;
+        max_exit_round[k] = s_max_exit;
+    } else {
+        for (int j = 0; j < distinct; ++j) list[offsets[k] + j] = pairs[j];
+    }
+}
+
 static inline int64_t div_up(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
 int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stream, StageCore** out)
@@ -396,6 +457,7 @@ int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stre
     const int64_t n = core->n, rows = core->rows, cols = core->cols;
     auto* sc = new (std::nothrow) StageCore();
     if (!sc) return fail(LUE_GPU_ENOMEM, "stage topology: host allocation");
+    if (const char* e = getenv("LUE_GB300_STAGE_CAP")) sc->cap = std::max(1, std::min(kStageCells, atoi(e)));
     sc->trows = div_up(rows, kStageSide);
     sc->tcols = div_up(cols, kStageSide);
     sc->ntiles = sc->trows * sc->tcols;
@@ -407,7 +469,7 @@ int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stre
     const StageGeom g{rows, cols, sc->tcols};
     const dim3 grid((unsigned)sc->tcols, (unsigned)sc->trows);
     int32_t *depth = nullptr, *counts = nullptr, *bases = nullptr, *cell_exit = nullptr, *input_at = nullptr;
-    int32_t *stage_depth = nullptr, *error = nullptr;
+    int32_t *stage_depth = nullptr, *error = nullptr, *exit_stage = nullptr, *pos_of = nullptr, *pcount = nullptr;
     uint16_t *order = nullptr, *round_at = nullptr, *flags_at = nullptr;
     std::vector<int32_t> hc(4 * nt), hb(4 * nt);
     int herr = 0;
@@ -429,8 +491,8 @@ int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stre
         CrossDepthVisitor v{core->upmask, depth, cols};
         k_walk<<<grid_all(n, 256), 256, 0, stream>>>(wg, v);
     }
-    k_stage_sort<<<grid, kStageBuildThreads, 0, stream>>>(core->fd, core->upmask, depth, g, order, round_at, flags_at,
-                                                         counts);
+    k_stage_sort<<<grid, kStageBuildThreads, 0, stream>>>(core->fd, core->upmask, depth, g, sc->cap, order, round_at,
+                                                         flags_at, counts);
     count_launches(2);
     TRY(cudaGetLastError(), "stage sort");
     TRY(cudaMemcpyAsync(hc.data(), counts, 4 * nt * sizeof(int32_t), cudaMemcpyDeviceToHost, stream), "stage counts");
@@ -461,9 +523,10 @@ int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stre
     TRY(cudaMalloc(&cell_exit, n * sizeof(int32_t)), "stage exit map");
     TRY(cudaMalloc(&input_at, np * sizeof(int32_t)), "stage input map");
     TRY(cudaMemsetAsync(cell_exit, 0xFF, n * sizeof(int32_t), stream), "memset");
+    TRY(cudaMalloc(&exit_stage, std::max<int64_t>(sc->nexits, 1) * sizeof(int32_t)), "stage exit owners");
     k_stage_ids<<<grid, kStageBuildThreads, 0, stream>>>(core->upmask, depth, g, order, round_at, flags_at, bases,
                                                         sc->stage, stage_depth, sc->exit_id, cell_exit, input_at,
-                                                        sc->meta);
+                                                        sc->meta, exit_stage);
     k_stage_inputs<<<grid, kStageBuildThreads, 0, stream>>>(g, order, sc->meta, input_at, cell_exit, sc->inputs, error);
     count_launches(2);
     TRY(cudaGetLastError(), "stage ids");
@@ -495,27 +558,60 @@ int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stre
         std::vector<int32_t> ws(sc->nstages);
         std::vector<int64_t> cur(off.begin(), off.end() - 1);
         for (int64_t s = 0; s < sc->nstages; ++s) ws[cur[sd[s]]++] = (int32_t)s;
-        int64_t mi = 0;
-        sc->h_depth_max_cells.assign(maxd + 1, 0);
-        sc->h_depth_max_inputs.assign(maxd + 1, 0);
         for (int64_t s2 = 0; s2 < sc->nstages; ++s2) {
             const int4& r = srec[s2];
-            const int cnt = (int)((unsigned)r.y >> 16), nin = (int)((unsigned)r.z >> 16);
-            mi = std::max<int64_t>(mi, nin);
-            sc->h_depth_max_cells[sd[s2]] = std::max(sc->h_depth_max_cells[sd[s2]], cnt);
-            sc->h_depth_max_inputs[sd[s2]] = std::max(sc->h_depth_max_inputs[sd[s2]], nin);
+            sc->max_stage_cells = std::max<int64_t>(sc->max_stage_cells, (int)((unsigned)r.y >> 16));
+            sc->max_stage_inputs = std::max<int64_t>(sc->max_stage_inputs, (int)((unsigned)r.z >> 16));
         }
-        sc->max_stage_inputs = mi;
         sc->h_depth_offsets = off;
         TRY(cudaMalloc(&sc->wave_stage, std::max<int64_t>(sc->nstages, 1) * sizeof(int32_t)), "wave order");
-        TRY(cudaMalloc(&sc->depth_offsets, off.size() * sizeof(int64_t)), "wave order");
         TRY(cudaMemcpyAsync(sc->wave_stage, ws.data(), sc->nstages * sizeof(int32_t), cudaMemcpyHostToDevice, stream),
             "wave order");
-        TRY(cudaMemcpyAsync(sc->depth_offsets, off.data(), off.size() * sizeof(int64_t), cudaMemcpyHostToDevice, stream),
-            "wave order");
         TRY(cudaStreamSynchronize(stream), "stage build");  // the host vectors must outlive the copies
+        // dataflow order: exit owners as wave positions, then each stage's producers
+        std::vector<int32_t> pos(sc->nstages);
+        for (int64_t k = 0; k < sc->nstages; ++k) pos[ws[k]] = (int32_t)k;
+        TRY(cudaMalloc(&pos_of, std::max<int64_t>(sc->nstages, 1) * sizeof(int32_t)), "wave positions");
+        TRY(cudaMemcpyAsync(pos_of, pos.data(), sc->nstages * sizeof(int32_t), cudaMemcpyHostToDevice, stream),
+            "wave positions");
+        if (sc->nexits > 0)
+            k_remap_i32<<<grid_for(sc->nexits, 256), 256, 0, stream>>>(exit_stage, sc->nexits, pos_of);
+        TRY(cudaMalloc(&pcount, std::max<int64_t>(sc->nstages, 1) * sizeof(int32_t)), "producers");
+        TRY(cudaMalloc(&sc->max_exit_round, std::max<int64_t>(sc->nstages, 1) * sizeof(int32_t)), "producers");
+        TRY(cudaMalloc(&sc->prod_offsets, (sc->nstages + 1) * sizeof(int64_t)), "producers");
+        const size_t psm = (size_t)std::max<int64_t>(sc->max_stage_inputs, 1) * sizeof(int2);
+        if (psm > 48 * 1024)
+            TRY(cudaFuncSetAttribute(k_stage_producers, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm),
+                "producers");
+        if (sc->nstages > 0)
+            k_stage_producers<<<(unsigned)sc->nstages, 256, psm, stream>>>(sc->stage, sc->wave_stage, sc->nstages,
+                                                                          sc->meta, sc->exit_id, sc->inputs,
+                                                                          exit_stage, pcount, sc->max_exit_round,
+                                                                          nullptr, nullptr);
+        std::vector<int32_t> pc(sc->nstages);
+        std::vector<int64_t> po(sc->nstages + 1, 0);
+        TRY(cudaMemcpyAsync(pc.data(), pcount, sc->nstages * sizeof(int32_t), cudaMemcpyDeviceToHost, stream),
+            "producers");
+        TRY(cudaStreamSynchronize(stream), "producers");
+        for (int64_t k = 0; k < sc->nstages; ++k) {
+            po[k + 1] = po[k] + pc[k];
+            sc->max_producers = std::max<int64_t>(sc->max_producers, pc[k]);
+        }
+        TRY(cudaMemcpyAsync(sc->prod_offsets, po.data(), (sc->nstages + 1) * sizeof(int64_t), cudaMemcpyHostToDevice,
+                            stream),
+            "producers");
+        TRY(cudaMalloc(&sc->prod, std::max<int64_t>(po[sc->nstages], 1) * sizeof(int2)), "producers");
+        if (sc->nstages > 0)
+            k_stage_producers<<<(unsigned)sc->nstages, 256, psm, stream>>>(sc->stage, sc->wave_stage, sc->nstages,
+                                                                          sc->meta, sc->exit_id, sc->inputs,
+                                                                          exit_stage, pcount, sc->max_exit_round,
+                                                                          sc->prod_offsets, sc->prod);
+        count_launches(3);
+        TRY(cudaGetLastError(), "producers");
+        TRY(cudaStreamSynchronize(stream), "producers");  // po must outlive the copy
+        sc->bytes += (sc->nstages + 1) * 8 + po[sc->nstages] * 8 + sc->nstages * 4;
     }
-    sc->bytes = sc->nstages * 20 + np * 12 + sc->ninputs * 4 + (int64_t)sc->h_depth_offsets.size() * 8;
+    sc->bytes += sc->nstages * 20 + np * 12 + sc->ninputs * 4 + (int64_t)sc->h_depth_offsets.size() * 8;
     if (getenv("LUE_GB300_VERBOSE")) {
         // rounds: the critical path of the waves is about the sum over depths of the longest stage
         std::vector<int4> srec(sc->nstages);
@@ -536,6 +632,44 @@ int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stre
         for (int v : deep_max) sum_max += v;
         fprintf(stderr, "stage rounds: mean %.1f per stage, sum over depths of the longest %lld\n",
                 sum_rounds / std::max<int64_t>(1, sc->nstages), (long long)sum_max);
+        // dataflow critical path of one step, in rounds, with a hand-off of h rounds per producer edge
+        std::vector<int64_t> po(sc->nstages + 1);
+        cudaMemcpy(po.data(), sc->prod_offsets, po.size() * sizeof(int64_t), cudaMemcpyDeviceToHost);
+        std::vector<int2> pr(std::max<int64_t>(1, po[sc->nstages]));
+        cudaMemcpy(pr.data(), sc->prod, po[sc->nstages] * sizeof(int2), cudaMemcpyDeviceToHost);
+        std::vector<int32_t> mx(sc->nstages);
+        cudaMemcpy(mx.data(), sc->max_exit_round, sc->nstages * sizeof(int32_t), cudaMemcpyDeviceToHost);
+        for (int h : {0, 2, 5}) {
+            std::vector<int64_t> start(sc->nstages, 0);
+            int64_t crit = 0;
+            for (int64_t k = 0; k < sc->nstages; ++k) {
+                int64_t s0 = 0;
+                for (int64_t j = po[k]; j < po[k + 1]; ++j)
+                    s0 = std::max<int64_t>(s0, start[pr[j].x] + mx[pr[j].x] + 1 + h - pr[j].y);
+                start[k] = s0;
+                crit = std::max<int64_t>(crit, s0 + (srec[ws[k]].z & 0xFFFF));
+            }
+            fprintf(stderr, "stage dataflow critical path (hand-off %d rounds): %lld rounds\n", h, (long long)crit);
+            // a stage that starts once all its producers are done
+            crit = 0;
+            for (int64_t k = 0; k < sc->nstages; ++k) {
+                int64_t s0 = 0;
+                for (int64_t j = po[k]; j < po[k + 1]; ++j)
+                    s0 = std::max<int64_t>(s0, start[pr[j].x] + mx[pr[j].x] + 1 + h);
+                start[k] = s0;
+                crit = std::max<int64_t>(crit, s0 + (srec[ws[k]].z & 0xFFFF));
+            }
+            fprintf(stderr, "stage dataflow critical path, all inputs first (hand-off %d rounds): %lld rounds\n", h,
+                    (long long)crit);
+        }
+        std::vector<int> sizes;
+        for (int64_t k = sc->h_depth_offsets[std::min<int64_t>(1, sc->max_depth)]; k < sc->nstages; ++k)
+            sizes.push_back((int)((unsigned)srec[ws[k]].y >> 16));
+        std::sort(sizes.begin(), sizes.end());
+        if (!sizes.empty())
+            fprintf(stderr, "stage cells at depth >= 1: p50 %d p90 %d p99 %d max %d; producers at most %lld\n",
+                    sizes[sizes.size() / 2], sizes[sizes.size() * 9 / 10], sizes[sizes.size() * 99 / 100],
+                    sizes.back(), (long long)sc->max_producers);
     }
     if (getenv("LUE_GB300_VERBOSE"))
         fprintf(stderr, "stage topology: %lld tiles, %lld stages, depth %lld, %lld exits, %lld inputs, "
@@ -548,6 +682,9 @@ done:
     cudaFree(bases);
     cudaFree(cell_exit);
     cudaFree(input_at);
+    cudaFree(exit_stage);
+    cudaFree(pos_of);
+    cudaFree(pcount);
     cudaFree(stage_depth);
     cudaFree(error);
     cudaFree(order);
@@ -567,84 +704,150 @@ void stage_core_free(StageCore* sc)
     if (!sc) return;
     cudaFree(sc->stage);
     cudaFree(sc->wave_stage);
-    cudaFree(sc->depth_offsets);
     cudaFree(sc->meta);
     cudaFree(sc->exit_id);
     cudaFree(sc->inputs);
+    cudaFree(sc->prod_offsets);
+    cudaFree(sc->prod);
+    cudaFree(sc->max_exit_round);
     delete sc;
 }
 
 // ---------------------------------------------------------------------------------------------------
-// Waves
+// Runtime: one dataflow launch
 // ---------------------------------------------------------------------------------------------------
+//
+// One launch runs every stage with all the steps of the call.  Each CTA takes the next stage of the
+// wave order (stages sorted by depth; the stages of one depth group of a tile in their order) from a
+// ticket counter, so every stage it waits for (a producer: a stage whose exits feed it, always earlier
+// in that order) has been taken by a CTA that started earlier and waits only on stages taken before it.
+// Inside a stage, cell c does step t in round round(c) + t, so T steps take rounds + T - 1 rounds; the
+// active positions of round r (round in (r - T, r]) are one contiguous range of the stage's order.
+// After each round a stage publishes how many steps of all its exits are in the history (progress[k]);
+// before each round a stage waits until each producer has published the steps that round consumes.
+// A wait gives up after `polls` polls (kFlowPolls, about a second): it sets error[0], every other wait
+// then gives up at once, the outputs of the call are set to NaN and the next call on the topology
+// returns LUE_GPU_ETIMEDOUT.
+
+constexpr int kFlowPolls = 1 << 22;
 
 struct StageRunArgs {
     const int4* stage;
     const int32_t* wave_stage;
-    const int64_t* depth_offsets;
     const uint2* meta;
     const int32_t* exit_id;
     const int32_t* inputs;
-    int64_t rows, cols, tcols, max_depth;
-    int steps, chunk, nchunks;
+    int64_t rows, cols, tcols;
+    int steps;
     uint2* hist;  // [nexits * steps]: the outflow of every exit at every step, as 8 bytes
 };
 
-// One wave: stage (depth d, chunk c) for every c in [c_lo, c_lo + gridDim.y) with d = d_base + wave - c
-// (d_base 1 for the pipelined waves after the depth-0 launch).  A Rule supplies the per-cell state (Cell,
-// kept in shared memory by position), the accumulator of the upstream outflows (Acc) and the cell step.
-// In round r the active positions are those whose round lies in (r - ns, r]: one contiguous range of the
-// stage's order, shared out over the NT threads.  Shared memory: the outflows by in-tile cell and step
-// parity, then per position meta, the inputs' history, and per position history row, cell state and
-// round starts; the launch provides enough for its largest stage.
+struct StageFlowArgs {
+    const int64_t* prod_offsets;
+    const int2* prod;
+    const int32_t* max_exit_round;
+    int* progress;  // [nstages], zeroed before the launch
+    int* ticket;    // zeroed before the launch
+    int* error;     // [1]
+    int64_t nstages;
+    int polls;      // poll limit of one wait
+    int64_t stuck;  // test hook: the position of a stage whose first wait never ends (-1: none)
+};
+
+__device__ __forceinline__ int ld_acquire(const int* p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v)
+{
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Waits until *p >= need and returns *p; gives up (returns `need`: the caller's results are then not
+// valid) after `polls` polls, setting *error, or once another wait has given up.
+__device__ __forceinline__ int flow_wait(const int* p, int need, int* error, int polls)
+{
+    for (int it = 0; it < polls; ++it) {
+        const int v = ld_acquire(p);
+        if (v >= need) return v;
+        if (*((volatile int*)error)) return need;
+        __nanosleep(64);
+    }
+    atomicExch(error, 1);
+    return need;
+}
+
+// Shared memory of a stage of at most `cap` cells: the stage position of each in-tile cell, the outflows
+// by step parity and position, per position meta / history row / cell state / round starts, the history
+// rows of the stage's inputs, and per producer its position, the earliest round that consumes it and
+// the steps of it known to be in the history.
 template <class R>
-struct StageLayout {
+struct FlowLayout {
+    int16_t* local;
     uint2* Qs;
     uint2* meta;
-    uint2* hs;
     int32_t* ex;
     typename R::Cell* cells;
     uint16_t* rstart;
-    __device__ StageLayout(unsigned char* base, int count, int hist)
+    int32_t* in_rows;
+    int2* prod;
+    int* have;
+    uint2* in_vals;
+    __device__ FlowLayout(unsigned char* base, int count, int nin, int np)
     {
-        Qs = reinterpret_cast<uint2*>(base);
-        meta = Qs + 2 * kStageCells;
-        hs = meta + count;
-        ex = reinterpret_cast<int32_t*>(hs + hist);
+        local = reinterpret_cast<int16_t*>(base);
+        Qs = reinterpret_cast<uint2*>(local + kStageCells);
+        meta = Qs + 2 * count;
+        ex = reinterpret_cast<int32_t*>(meta + count);
         // 16-byte aligned: a Cell may hold doubles
         cells = reinterpret_cast<typename R::Cell*>((reinterpret_cast<uintptr_t>(ex + count) + 15) & ~uintptr_t(15));
         // round up to 4 bytes: a Cell may be a 1-byte empty struct
         rstart = reinterpret_cast<uint16_t*>((reinterpret_cast<uintptr_t>(cells + count) + 3) & ~uintptr_t(3));
+        in_rows = reinterpret_cast<int32_t*>((reinterpret_cast<uintptr_t>(rstart + count + 2) + 3) & ~uintptr_t(3));
+        prod = reinterpret_cast<int2*>((reinterpret_cast<uintptr_t>(in_rows + nin) + 7) & ~uintptr_t(7));
+        have = reinterpret_cast<int*>(prod + np);
+        in_vals = reinterpret_cast<uint2*>((reinterpret_cast<uintptr_t>(have + np) + 7) & ~uintptr_t(7));
     }
 };
 
 template <class R>
-static size_t stage_smem(int64_t cells, int64_t inputs_x_steps)
+static size_t flow_smem(int64_t cells, int64_t inputs, int64_t producers)
 {
-    return (2 * kStageCells + cells + inputs_x_steps) * sizeof(uint2) +
-           cells * (sizeof(int32_t) + sizeof(typename R::Cell)) + (cells + 2) * sizeof(uint16_t) + 32;  // + alignment
+    return kStageCells * sizeof(int16_t) + cells * (3 * sizeof(uint2) + sizeof(int32_t) + sizeof(typename R::Cell)) +
+           (cells + 2) * sizeof(uint16_t) + inputs * (sizeof(int32_t) + sizeof(uint2)) +
+           producers * (sizeof(int2) + sizeof(int)) + 64;  // + alignment
 }
 
-template <class R, int NT>
-__global__ void __launch_bounds__(NT) k_stage_wave(StageRunArgs a, R rule, int wave, int c_lo, int d_base, int chunk)
+// A Rule supplies the per-cell state (Cell, kept in shared memory by position), the accumulator of the
+// upstream outflows (Acc), the cell step and the final store.  ONE (a call of one step): the stage first
+// waits for all its producers and loads all its inputs into shared memory at once, so that its rounds
+// read shared memory only; with many steps it waits and reads round by round.
+template <class R, int NT, bool ONE>
+__global__ void __launch_bounds__(NT) k_stage_flow(StageRunArgs a, StageFlowArgs f, R rule)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int c = c_lo + (int)blockIdx.y, d = d_base + wave - c;
-    if (d < 0 || d > a.max_depth) return;
-    const int64_t si = a.depth_offsets[d] + blockIdx.x;
-    if (si >= a.depth_offsets[d + 1]) return;
-    const int4 st = a.stage[a.wave_stage[si]];
+    __shared__ int s_ticket;
+    if (threadIdx.x == 0) s_ticket = atomicAdd(f.ticket, 1);
+    __syncthreads();
+    const int64_t k = s_ticket;
+    if (k >= f.nstages) return;
+    const int4 st = a.stage[a.wave_stage[k]];
     const int64_t tile = st.x;
     const int begin = st.y & 0xFFFF, count = (int)((unsigned)st.y >> 16);
     const int rounds = st.z & 0xFFFF, nin = (int)((unsigned)st.z >> 16);
     const int64_t in_base = st.w;
-    const int t0 = c * chunk, ns = min(chunk, a.steps - t0);
-    StageLayout<R> L(smem_raw, count, nin * ns);
+    const int ns = a.steps;
+    const int64_t p0 = f.prod_offsets[k];
+    const int np = (int)(f.prod_offsets[k + 1] - p0);
+    FlowLayout<R> L(smem_raw, count, nin, np);
     const int64_t tr = tile / a.tcols, tc = tile - tr * a.tcols;
     const int64_t row0 = tr * kStageSide, col0 = tc * kStageSide;
-    for (int i = threadIdx.x; i < nin * ns; i += NT) {
-        const int in = i / ns, t = i - in * ns;
-        L.hs[i] = a.hist[(int64_t)__ldg(a.inputs + in_base + in) * a.steps + t0 + t];
+    for (int i = threadIdx.x; i < nin; i += NT) L.in_rows[i] = __ldg(a.inputs + in_base + i);
+    for (int i = threadIdx.x; i < np; i += NT) {
+        L.prod[i] = __ldg(f.prod + p0 + i);
+        L.have[i] = 0;
     }
     for (int i = threadIdx.x; i < count; i += NT) {
         const int64_t at = tile * kStageCells + begin + i;
@@ -652,7 +855,8 @@ __global__ void __launch_bounds__(NT) k_stage_wave(StageRunArgs a, R rule, int w
         L.meta[i] = m;
         L.ex[i] = __ldg(a.exit_id + at);
         const int p = (int)(m.x & 1023u);
-        rule.load(L.cells[i], (row0 + (p >> 5)) * a.cols + col0 + (p & 31), c);
+        L.local[p] = (int16_t)i;
+        rule.load(L.cells[i], (row0 + (p >> 5)) * a.cols + col0 + (p & 31));
     }
     __syncthreads();
     for (int i = threadIdx.x; i < count; i += NT) {
@@ -660,9 +864,27 @@ __global__ void __launch_bounds__(NT) k_stage_wave(StageRunArgs a, R rule, int w
         if (i == 0 || rd != (int)((L.meta[i - 1].x >> 10) & 1023u)) L.rstart[rd] = (uint16_t)i;
     }
     if (threadIdx.x == 0) L.rstart[rounds] = (uint16_t)count;
+    const int max_exit = __ldg(f.max_exit_round + k);
     __syncthreads();
+    if (ONE) {
+        for (int i = threadIdx.x; i < np; i += NT) flow_wait(f.progress + L.prod[i].x, 1, f.error, f.polls);
+        if (k == f.stuck && threadIdx.x == 0) flow_wait(f.progress + k, ns + 1, f.error, f.polls);
+        __syncthreads();
+        for (int i = threadIdx.x; i < nin; i += NT) L.in_vals[i] = __ldcg(a.hist + L.in_rows[i]);
+    }
     const int nrounds = rounds + ns - 1;
+    int published = 0;
     for (int r = 0; r < nrounds; ++r) {
+        if (!ONE) {
+            // the producers' steps this round consumes: round r consumes step r - round(c) at cell c
+            for (int i = threadIdx.x; i < np; i += NT) {
+                const int2 pq = L.prod[i];
+                const int need = min(ns, r - pq.y + 1);
+                if (need > L.have[i]) L.have[i] = flow_wait(f.progress + pq.x, need, f.error, f.polls);
+            }
+            if (r == 0 && k == f.stuck && threadIdx.x == 0) flow_wait(f.progress + k, ns + 1, f.error, f.polls);
+        }
+        __syncthreads();
         const int lo = L.rstart[max(0, r - ns + 1)], hi = L.rstart[min(rounds, r + 1)];
         for (int i = lo + (int)threadIdx.x; i < hi; i += NT) {
             const uint2 m = L.meta[i];
@@ -670,25 +892,37 @@ __global__ void __launch_bounds__(NT) k_stage_wave(StageRunArgs a, R rule, int w
             const int p = (int)(m.x & 1023u);
             const unsigned em = (m.y >> 8) & 0xFFu;
             const int fi = (int)(m.y >> 16);
+            uint2* Qt = L.Qs + (t & 1) * count;
             typename R::Acc acc = rule.begin();
             unsigned um = m.y & 0xFFu;
             while (um) {
                 const int q = __ffs(um) - 1;
                 um &= um - 1;
-                const uint2 v = ((em >> q) & 1u) ? L.hs[(fi + __popc(em & ((1u << q) - 1u))) * ns + t]
-                                                  : L.Qs[(t & 1) * kStageCells + p + nb_dr(q) * kStageSide + nb_dc(q)];
+                const int e_in = fi + __popc(em & ((1u << q) - 1u));
+                const uint2 v = ((em >> q) & 1u)
+                                    ? (ONE ? L.in_vals[e_in] : __ldcg(a.hist + (int64_t)L.in_rows[e_in] * ns + t))
+                                    : Qt[L.local[p + nb_dr(q) * kStageSide + nb_dc(q)]];
                 rule.add(acc, v);
             }
-            const uint2 o = rule.step(L.cells[i], acc, (row0 + (p >> 5)) * a.cols + col0 + (p & 31), t0 + t);
-            L.Qs[(t & 1) * kStageCells + p] = o;
+            const uint2 o = rule.step(L.cells[i], acc, (row0 + (p >> 5)) * a.cols + col0 + (p & 31), t);
+            Qt[i] = o;
             const int32_t e = L.ex[i];
-            if (e >= 0) a.hist[(int64_t)e * a.steps + t0 + t] = o;
+            if (e >= 0) __stcg(a.hist + (int64_t)e * ns + t, o);
         }
+        // The barrier orders every thread's history writes before thread 0's release, which makes them
+        // visible at GPU scope before the progress that announces them (the pattern of a grid barrier).
         __syncthreads();
+        if (threadIdx.x == 0 && max_exit >= 0) {
+            const int prog = min(ns, max(0, r + 1 - max_exit));
+            if (prog > published) {
+                st_release(f.progress + k, prog);
+                published = prog;
+            }
+        }
     }
     for (int i = threadIdx.x; i < count; i += NT) {
         const int p = (int)(L.meta[i].x & 1023u);
-        rule.store(L.cells[i], (row0 + (p >> 5)) * a.cols + col0 + (p & 31), c, t0 + ns == a.steps);
+        rule.store(L.cells[i], (row0 + (p >> 5)) * a.cols + col0 + (p & 31));
     }
 }
 
@@ -704,6 +938,9 @@ struct StageF32 {
     float bs;
     float* out;
     float* rem;
+    using Out = float;
+    __host__ __device__ float* out_raster() const { return out; }
+    __host__ __device__ float* rem_raster() const { return RR == Rule::accu ? nullptr : rem; }
     struct Cell {
         float x, b;  // inflow and threshold / fraction, loaded with the stage
     };
@@ -711,7 +948,7 @@ struct StageF32 {
         FF t;
         bool nan;
     };
-    __device__ void load(Cell& cl, int64_t g, int) const
+    __device__ void load(Cell& cl, int64_t g) const
     {
         cl.x = value_at(a, as, g);
         cl.b = RR == Rule::accu ? 0.0f : value_at(b, bs, g);
@@ -735,7 +972,7 @@ struct StageF32 {
         if (RR != Rule::accu) rem[g] = r;
         return make_uint2(__float_as_uint(oh), __float_as_uint(ol));
     }
-    __device__ void store(Cell&, int64_t, int, bool) const {}
+    __device__ void store(Cell&, int64_t) const {}
 };
 
 template <Rule RR>
@@ -746,6 +983,9 @@ struct StageF64 {
     double bs;
     double* out;
     double* rem;
+    using Out = double;
+    __host__ __device__ double* out_raster() const { return out; }
+    __host__ __device__ double* rem_raster() const { return RR == Rule::accu ? nullptr : rem; }
     struct Cell {
         double x, b;  // inflow and threshold / fraction, loaded with the stage
     };
@@ -753,7 +993,7 @@ struct StageF64 {
         double t;
         bool nan;
     };
-    __device__ void load(Cell& cl, int64_t g, int) const
+    __device__ void load(Cell& cl, int64_t g) const
     {
         cl.x = value_at(a, as, g);
         cl.b = RR == Rule::accu ? 0.0 : value_at(b, bs, g);
@@ -776,13 +1016,16 @@ struct StageF64 {
         if (RR != Rule::accu) rem[g] = r;
         return make_uint2((unsigned)__double2loint(o), (unsigned)__double2hiint(o));
     }
-    __device__ void store(Cell&, int64_t, int, bool) const {}
+    __device__ void store(Cell&, int64_t) const {}
 };
 
 // kinematic wave, one step, float64: the walk engine's cell rule (route_walk_visitors.cuh).
 template <class TIn>
 struct StageKW64 {
     RouteKW<TIn> v;  // inputs and constants (its out is the result raster)
+    using Out = double;
+    __host__ __device__ double* out_raster() const { return v.out; }
+    __host__ __device__ double* rem_raster() const { return nullptr; }
     struct Cell {
         double qc, q, al, be, len;  // the cell's inputs, loaded with the stage
     };
@@ -790,7 +1033,7 @@ struct StageKW64 {
         double up;
         bool nan;
     };
-    __device__ void load(Cell& cl, int64_t c, int) const
+    __device__ void load(Cell& cl, int64_t c) const
     {
         cl.qc = v.qcur ? __ldg(v.qcur + c) : v.qcur_s;
         cl.q = v.lateral ? (double)__ldg(v.lateral + c) : v.lateral_s;
@@ -811,11 +1054,10 @@ struct StageKW64 {
         v.out[c] = o;
         return make_uint2((unsigned)__double2loint(o), (unsigned)__double2hiint(o));
     }
-    __device__ void store(Cell&, int64_t, int, bool) const {}
+    __device__ void store(Cell&, int64_t) const {}
 };
 
 // kinematic wave, many steps, in float-float and the variable y = Q^(1/m) (kinematic_wave_ff.cuh).
-// Between chunks the state y of each cell waits in state_y.
 template <int P, int M>
 struct StageKWPoly {
     const double* qcur;
@@ -823,9 +1065,11 @@ struct StageKWPoly {
     float lateral_s;
     const float* alpha;
     float alpha_s;
-    float2* state_y;
     double* out;
     KWConstFF K;
+    using Out = double;
+    __host__ __device__ double* out_raster() const { return out; }
+    __host__ __device__ double* rem_raster() const { return nullptr; }
     struct Cell {
         ffloat y;
         float lat, al;
@@ -834,16 +1078,11 @@ struct StageKWPoly {
         ffloat up;
         bool nan;
     };
-    __device__ void load(Cell& cl, int64_t g, int chunk) const
+    __device__ void load(Cell& cl, int64_t g) const
     {
         cl.lat = lateral ? __ldg(lateral + g) : lateral_s;
         cl.al = alpha ? __ldg(alpha + g) : alpha_s;
-        if (chunk == 0) {
-            cl.y = kw_poly_root<P, M>(ff_from_double(__ldg(qcur + g)), K);
-        } else {
-            const float2 y = state_y[g];
-            cl.y = ffloat{y.x, y.y};
-        }
+        cl.y = kw_poly_root<P, M>(ff_from_double(__ldg(qcur + g)), K);
     }
     __device__ Acc begin() const { return Acc{ffloat{0.0f, 0.0f}, false}; }
     __device__ void add(Acc& acc, uint2 x) const
@@ -857,10 +1096,9 @@ struct StageKWPoly {
         const ffloat q = kw_step_poly<P, M>(acc.up, acc.nan, cl.y, cl.lat, cl.al, K);
         return make_uint2(__float_as_uint(q.hi), __float_as_uint(q.lo));
     }
-    __device__ void store(Cell& cl, int64_t g, int, bool last) const
+    __device__ void store(Cell& cl, int64_t g) const
     {
-        if (last) out[g] = isnan(cl.y.hi) ? qnan<double>() : ff_to_double(ff_pow_n<M>(cl.y, K.br.m));
-        else state_y[g] = make_float2(cl.y.hi, cl.y.lo);
+        out[g] = isnan(cl.y.hi) ? qnan<double>() : ff_to_double(ff_pow_n<M>(cl.y, K.br.m));
     }
 };
 
@@ -915,91 +1153,92 @@ static int grow(lue_gpu_topology* t, T*& p, size_t& have, size_t need, cudaStrea
     return LUE_GPU_OK;
 }
 
-// Steps per chunk: at most LUE_GB300_STAGE_CHUNK (default 32), and the inputs' history of a chunk must
-// fit in shared memory.
-static int stage_chunk(const StageCore* sc, int steps)
+// Marks every output NaN after a dataflow wait gave up (the results are not valid).
+template <class T>
+__global__ void k_invalidate_if(const int* error, T* out, T* rem, int64_t n)
 {
-    int chunk = 32;
-    if (const char* e = getenv("LUE_GB300_STAGE_CHUNK")) chunk = std::max(1, atoi(e));
-    chunk = std::min(chunk, steps);
-    const int64_t fit = kStageHistorySlots / std::max<int64_t>(1, sc->max_stage_inputs);
-    return (int)std::max<int64_t>(1, std::min<int64_t>(chunk, fit));
-}
-
-template <class R, int NT>
-static int set_smem_limit(const char* what)
-{
-    static bool done = false;
-    if (done) return LUE_GPU_OK;
-    if (int rc = cuda_status(cudaFuncSetAttribute(k_stage_wave<R, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  (int)stage_smem<R>(kStageCells, kStageHistorySlots)),
-                             what))
-        return rc;
-    done = true;
-    return LUE_GPU_OK;
-}
-
-// One launch over gy chunks of the stages of depths d_base + wave - c: one warp per CTA when their largest
-// stage has at most 64 cells, 64 threads up to 256 cells, else kStageThreads; shared memory for the
-// largest stage.
-template <class R>
-static int launch_wave(const StageRunArgs& a, const R& rule, int64_t gx, int64_t gy, int wave, int c_lo, int d_base,
-                       int chunk, int64_t max_cells, int64_t max_hist, cudaStream_t stream, const char* what)
-{
-    const size_t smem = stage_smem<R>(max_cells, max_hist);
-    const dim3 grid((unsigned)gx, (unsigned)gy);
-    if (max_cells <= 64) {
-        if (int rc = set_smem_limit<R, 32>(what)) return rc;
-        k_stage_wave<R, 32><<<grid, 32, smem, stream>>>(a, rule, wave, c_lo, d_base, chunk);
-    } else if (max_cells <= 256) {
-        if (int rc = set_smem_limit<R, 64>(what)) return rc;
-        k_stage_wave<R, 64><<<grid, 64, smem, stream>>>(a, rule, wave, c_lo, d_base, chunk);
-    } else {
-        if (int rc = set_smem_limit<R, kStageThreads>(what)) return rc;
-        k_stage_wave<R, kStageThreads><<<grid, kStageThreads, smem, stream>>>(a, rule, wave, c_lo, d_base, chunk);
+    if (!*error) return;
+    for (int64_t i = grid_stride_begin(); i < n; i += grid_stride()) {
+        out[i] = qnan<T>();
+        if (rem) rem[i] = qnan<T>();
     }
+}
+
+template <class R, int NT, bool ONE>
+static int launch_flow(const StageRunArgs& a, const StageFlowArgs& fa, const R& rule, unsigned blocks, size_t smem,
+                       cudaStream_t stream, const char* what)
+{
+    static size_t have = 48 * 1024;
+    if (smem > have) {
+        if (int rc = cuda_status(cudaFuncSetAttribute(k_stage_flow<R, NT, ONE>,
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                                 what))
+            return rc;
+        have = smem;
+    }
+    k_stage_flow<R, NT, ONE><<<blocks, NT, smem, stream>>>(a, fa, rule);
     return LUE_GPU_OK;
 }
 
-// `steps` steps of a rule over every stage.  Stages of depth 0 have no inputs: they run all steps in one
-// launch.  Deeper stages run in chunks of `chunk` steps, stage (depth d, chunk c) in wave (d - 1) + c.
+template <class R, bool ONE>
+static int launch_flow(const StageRunArgs& a, const StageFlowArgs& fa, const R& rule, unsigned blocks,
+                       int64_t max_cells, size_t smem, cudaStream_t stream, const char* what)
+{
+    if (max_cells <= 128) return launch_flow<R, 32, ONE>(a, fa, rule, blocks, smem, stream, what);
+    if (max_cells <= 256) return launch_flow<R, 64, ONE>(a, fa, rule, blocks, smem, stream, what);
+    return launch_flow<R, kStageThreads, ONE>(a, fa, rule, blocks, smem, stream, what);
+}
+
+// `steps` steps of a rule over every stage, in one dataflow launch (k_stage_flow); one warp per CTA for
+// stages of up to 128 cells.
 template <class R>
-static int stage_run(lue_gpu_topology* t, const StageCore* sc, const R& rule, int steps, int chunk,
-                     cudaStream_t stream, const char* what)
+static int stage_run(lue_gpu_topology* t, const StageCore* sc, const R& rule, int steps, cudaStream_t stream,
+                     const char* what)
 {
     const TopologyCore* core = t->core;
-    const int nchunks = (int)div_up(steps, chunk);
-    if ((int64_t)sc->max_stage_inputs * chunk > kStageHistorySlots)
-        return fail(LUE_GPU_ERANGE, std::string(what) + ": stage inputs beyond the shared-memory history");
+    if (sc->nstages == 0) return LUE_GPU_OK;
+    if (t->stage_flow_error && *t->stage_flow_error) {
+        *t->stage_flow_error = 0;
+        return fail(LUE_GPU_ETIMEDOUT, std::string(what) +
+                                           ": a wait between stages of an earlier call gave up; its outputs are NaN");
+    }
     const size_t hist = (size_t)std::max<int64_t>(sc->nexits, 1) * (size_t)steps * sizeof(uint2);
     if (int rc = grow(t, t->stage_hist, t->stage_hist_bytes, hist, stream, what)) return rc;
-    StageRunArgs a{sc->stage,   sc->wave_stage, sc->depth_offsets, sc->meta,  sc->exit_id, sc->inputs,
-                   core->rows,  core->cols,     sc->tcols,         sc->max_depth, steps,   chunk,
-                   nchunks,     t->stage_hist};
-    const std::vector<int64_t>& off = sc->h_depth_offsets;
-    const int64_t D = sc->max_depth;
-    if (D < 0) return LUE_GPU_OK;
-    int launches = 0;
-    // depth 0: every step at once
-    if (int rc = launch_wave(a, rule, off[1] - off[0], 1, 0, 0, 0, steps, sc->h_depth_max_cells[0], 0, stream, what))
-        return rc;
-    ++launches;
-    // depths 1 ..: pipelined chunks
-    for (int64_t w = 0; w <= D - 1 + nchunks - 1; ++w) {
-        const int64_t c_lo = std::max<int64_t>(0, w - (D - 1)), c_hi = std::min<int64_t>(nchunks - 1, w);
-        int64_t gx = 0, mc = 0, mh = 0;
-        for (int64_t cc = c_lo; cc <= c_hi; ++cc) {
-            const int64_t dd = 1 + w - cc;
-            gx = std::max(gx, off[dd + 1] - off[dd]);
-            mc = std::max<int64_t>(mc, sc->h_depth_max_cells[dd]);
-            mh = std::max<int64_t>(mh, (int64_t)sc->h_depth_max_inputs[dd] * std::min(chunk, steps - (int)cc * chunk));
-        }
-        if (gx == 0) continue;
-        if (int rc = launch_wave(a, rule, gx, c_hi - c_lo + 1, (int)w, (int)c_lo, 1, chunk, mc, mh, stream, what))
+    const size_t flow = (size_t)(sc->nstages + 2) * sizeof(int);
+    if (int rc = grow(t, t->stage_flow, t->stage_flow_bytes, flow, stream, what)) return rc;
+    if (!t->stage_flow_error) {
+        if (int rc = cuda_status(cudaHostAlloc(&t->stage_flow_error, sizeof(int), cudaHostAllocDefault), what))
             return rc;
-        ++launches;
+        *t->stage_flow_error = 0;
     }
-    count_launches(launches);
+    int* progress = t->stage_flow;
+    int* ticket = progress + sc->nstages;
+    int* error = ticket + 1;
+    if (int rc = cuda_status(cudaMemsetAsync(progress, 0, flow, stream), what)) return rc;
+    StageRunArgs a{sc->stage, sc->wave_stage, sc->meta, sc->exit_id, sc->inputs, core->rows, core->cols, sc->tcols,
+                   steps, t->stage_hist};
+    StageFlowArgs fa{sc->prod_offsets, sc->prod, sc->max_exit_round, progress, ticket, error, sc->nstages,
+                     kFlowPolls, -1};
+    if (const char* e = getenv("LUE_GB300_FLOW_STUCK_STAGE")) {  // test hook: see StageFlowArgs::stuck
+        fa.stuck = std::max<int64_t>(0, std::min<int64_t>(atoll(e), sc->nstages - 1));
+        fa.polls = 1 << 16;
+    }
+    const int64_t mc = sc->max_stage_cells;
+    const size_t smem = flow_smem<R>(mc, sc->max_stage_inputs, sc->max_producers);
+    const unsigned blocks = (unsigned)sc->nstages;
+    if (getenv("LUE_GB300_VERBOSE"))
+        fprintf(stderr, "%s: dataflow launch of %u stages, largest %lld cells, %zu B shared memory\n", what, blocks,
+                (long long)mc, smem);
+    if (int rc = steps == 1 ? launch_flow<R, true>(a, fa, rule, blocks, mc, smem, stream, what)
+                            : launch_flow<R, false>(a, fa, rule, blocks, mc, smem, stream, what))
+        return rc;
+    const int64_t n = core->n;
+    k_invalidate_if<typename R::Out><<<grid_for(n, 256), 256, 0, stream>>>(error, rule.out_raster(), rule.rem_raster(),
+                                                                         n);
+    if (int rc = cuda_status(
+            cudaMemcpyAsync(t->stage_flow_error, error, sizeof(int), cudaMemcpyDeviceToHost, stream), what))
+        return rc;
+    count_launches(2);
     return cuda_status(cudaGetLastError(), what);
 }
 
@@ -1017,7 +1256,7 @@ static int route_f32_rule(lue_gpu_topology* t, const StageCore* sc, const float*
     k_stage_no_data<float><<<grid_for(n, 256), 256, 0, stream>>>(t->core->fd, n, out, rem);
     count_launches(1);
     StageF32<RR> rule{a, as, b, bs, out, rem};
-    return stage_run(t, sc, rule, 1, 1, stream, "stage route (float32)");
+    return stage_run(t, sc, rule, 1, stream, "stage route (float32)");
 }
 
 int stage_route_f32(lue_gpu_topology* t, int rule, const float* a, float as, const float* b, float bs, float* out,
@@ -1027,7 +1266,7 @@ int stage_route_f32(lue_gpu_topology* t, int rule, const float* a, float as, con
     if (stage_engine_off()) return LUE_GPU_OK;
     const StageCore* sc = nullptr;
     if (int rc = stage_core_get(t, stream, &sc)) return rc;
-    if (!sc || sc->max_stage_inputs > kStageHistorySlots) return LUE_GPU_OK;
+    if (!sc) return LUE_GPU_OK;
     *done = true;
     switch (rule) {
         case (int)Rule::threshold: return route_f32_rule<Rule::threshold>(t, sc, a, as, b, bs, out, rem, stream);
@@ -1045,7 +1284,7 @@ static int route_f64_rule(lue_gpu_topology* t, const StageCore* sc, const double
     k_stage_no_data<double><<<grid_for(n, 256), 256, 0, stream>>>(t->core->fd, n, out, rem);
     count_launches(1);
     StageF64<RR> rule{a, as, b, bs, out, rem};
-    return stage_run(t, sc, rule, 1, 1, stream, "stage route (float64)");
+    return stage_run(t, sc, rule, 1, stream, "stage route (float64)");
 }
 
 int stage_route_f64(lue_gpu_topology* t, int rule, const double* a, double as, const double* b, double bs,
@@ -1055,7 +1294,7 @@ int stage_route_f64(lue_gpu_topology* t, int rule, const double* a, double as, c
     if (stage_engine_off()) return LUE_GPU_OK;
     const StageCore* sc = nullptr;
     if (int rc = stage_core_get(t, stream, &sc)) return rc;
-    if (!sc || sc->max_stage_inputs > kStageHistorySlots) return LUE_GPU_OK;
+    if (!sc) return LUE_GPU_OK;
     *done = true;
     switch (rule) {
         case (int)Rule::accu: return route_f64_rule<Rule::accu>(t, sc, a, as, b, bs, out, rem, stream);
@@ -1075,14 +1314,14 @@ int stage_kinematic_wave_f64(lue_gpu_topology* t, const double* qcur, double qcu
     if (stage_engine_off()) return LUE_GPU_OK;
     const StageCore* sc = nullptr;
     if (int rc = stage_core_get(t, stream, &sc)) return rc;
-    if (!sc || sc->max_stage_inputs > kStageHistorySlots) return LUE_GPU_OK;
+    if (!sc) return LUE_GPU_OK;
     *done = true;
     const int64_t n = t->core->n;
     k_stage_no_data<double><<<grid_for(n, 256), 256, 0, stream>>>(t->core->fd, n, out, (double*)nullptr);
     count_launches(1);
     StageKW64<double> rule{RouteKW<double>{t->core->upmask, qcur, qcur_s, lateral, lateral_s, alpha, alpha_s, beta,
                                            beta_s, dt, dx, dx_s, out, t->core->cols, br}};
-    return stage_run(t, sc, rule, 1, 1, stream, "kinematic_wave_f64 (stages)");
+    return stage_run(t, sc, rule, 1, stream, "kinematic_wave_f64 (stages)");
 }
 
 static ffloat ff_split(double v);
@@ -1098,7 +1337,7 @@ int stage_kinematic_wave_f32in(lue_gpu_topology* t, const double* qcur, double q
     if (stage_engine_off()) return LUE_GPU_OK;
     const StageCore* sc = nullptr;
     if (int rc = stage_core_get(t, stream, &sc)) return rc;
-    if (!sc || sc->max_stage_inputs > kStageHistorySlots) return LUE_GPU_OK;
+    if (!sc) return LUE_GPU_OK;
     *done = true;
     const int64_t n = t->core->n;
     k_stage_no_data<double><<<grid_for(n, 256), 256, 0, stream>>>(t->core->fd, n, out, (double*)nullptr);
@@ -1106,15 +1345,15 @@ int stage_kinematic_wave_f32in(lue_gpu_topology* t, const double* qcur, double q
     if (qcur && br.m >= 1 && br.m <= 16 && br.p >= 1 && br.p <= 16) {
         const KWConstFF K = kw_constants(beta, dt, dx, br);
         if (br.p == 3 && br.m == 5) {
-            StageKWPoly<3, 5> rule{qcur, lateral, (float)lateral_s, alpha, (float)alpha_s, nullptr, out, K};
-            return stage_run(t, sc, rule, 1, 1, stream, "kinematic_wave_f64_f32in (stages)");
+            StageKWPoly<3, 5> rule{qcur, lateral, (float)lateral_s, alpha, (float)alpha_s, out, K};
+            return stage_run(t, sc, rule, 1, stream, "kinematic_wave_f64_f32in (stages)");
         }
-        StageKWPoly<0, 0> rule{qcur, lateral, (float)lateral_s, alpha, (float)alpha_s, nullptr, out, K};
-        return stage_run(t, sc, rule, 1, 1, stream, "kinematic_wave_f64_f32in (stages)");
+        StageKWPoly<0, 0> rule{qcur, lateral, (float)lateral_s, alpha, (float)alpha_s, out, K};
+        return stage_run(t, sc, rule, 1, stream, "kinematic_wave_f64_f32in (stages)");
     }
     StageKW64<float> rule{RouteKW<float>{t->core->upmask, qcur, qcur_s, lateral, lateral_s, alpha, alpha_s, nullptr,
                                          beta, dt, nullptr, dx, out, t->core->cols, br}};
-    return stage_run(t, sc, rule, 1, 1, stream, "kinematic_wave_f64_f32in (stages)");
+    return stage_run(t, sc, rule, 1, stream, "kinematic_wave_f64_f32in (stages)");
 }
 
 static ffloat ff_split(double v)
@@ -1146,7 +1385,7 @@ int stage_kinematic_wave_steps(lue_gpu_topology* t, const double* qcur, const fl
     if (stage_engine_off() || br.m == 0 || br.m > 16 || br.p > 16) return LUE_GPU_OK;
     const StageCore* sc = nullptr;
     if (int rc = stage_core_get(t, stream, &sc)) return rc;
-    if (!sc || sc->max_stage_inputs > kStageHistorySlots) return LUE_GPU_OK;
+    if (!sc) return LUE_GPU_OK;
     *done = true;
     const int64_t n = t->core->n;
     // the history of every exit for every step of a part of the call: parts of at most `fit` steps
@@ -1156,12 +1395,6 @@ int stage_kinematic_wave_steps(lue_gpu_topology* t, const double* qcur, const fl
     const int64_t per_step = std::max<int64_t>(sc->nexits, 1) * (int64_t)sizeof(uint2);
     const int fit = (int)std::max<int64_t>(1, std::min<int64_t>(steps, (int64_t)(budget / (double)per_step)));
     const KWConstFF K = kw_constants(beta, dt, dx, br);
-    const int chunk = stage_chunk(sc, std::min(steps, fit));
-    if ((size_t)n * sizeof(float2) > t->stage_state_bytes && div_up(std::min(steps, fit), chunk) > 1) {
-        if (int rc = grow(t, t->stage_state, t->stage_state_bytes, (size_t)n * sizeof(float2), stream,
-                          "kinematic_wave_steps state"))
-            return rc;
-    }
     double* tmp = nullptr;
     if (steps > fit) {
         if (int rc = cuda_status(cudaMalloc(&tmp, 2 * (size_t)n * sizeof(double)), "kinematic_wave_steps")) return rc;
@@ -1175,11 +1408,11 @@ int stage_kinematic_wave_steps(lue_gpu_topology* t, const double* qcur, const fl
         k_stage_no_data<double><<<grid_for(n, 256), 256, 0, stream>>>(t->core->fd, n, dst, (double*)nullptr);
         count_launches(1);
         if (br.p == 3 && br.m == 5) {
-            StageKWPoly<3, 5> rule{src, lateral, (float)lateral_s, alpha, (float)alpha_s, t->stage_state, dst, K};
-            rc = stage_run(t, sc, rule, part, stage_chunk(sc, part), stream, "kinematic_wave_steps (stages)");
+            StageKWPoly<3, 5> rule{src, lateral, (float)lateral_s, alpha, (float)alpha_s, dst, K};
+            rc = stage_run(t, sc, rule, part, stream, "kinematic_wave_steps (stages)");
         } else {
-            StageKWPoly<0, 0> rule{src, lateral, (float)lateral_s, alpha, (float)alpha_s, t->stage_state, dst, K};
-            rc = stage_run(t, sc, rule, part, stage_chunk(sc, part), stream, "kinematic_wave_steps (stages)");
+            StageKWPoly<0, 0> rule{src, lateral, (float)lateral_s, alpha, (float)alpha_s, dst, K};
+            rc = stage_run(t, sc, rule, part, stream, "kinematic_wave_steps (stages)");
         }
         if (rc) break;
         src = dst;

@@ -6,17 +6,19 @@
 // partition edges (ALG/definition/accumulating_router.hpp:525-599, 902-1209).  Here:
 //
 //   - The raster is cut into 32 x 32 tiles.  The crossing depth of a cell is the largest number of tile
-//     edges crossed by a flow path that ends at the cell.  A stage is the set of cells of one tile with
-//     the same crossing depth.  Every upstream cell of a stage lies in the stage itself, in a stage of
-//     lower depth, or nowhere: stages of depth d depend only on depths below d.
-//   - Inside a stage each cell gets a round: its distance, in cells, from the stage's most downstream
-//     cells, counted from the far end (rounds run upstream to downstream).  Every cell is exactly one
-//     round after each of its upstream cells in the stage, because each cell has one downstream cell.
+//     edges crossed by a flow path that ends at the cell.  The cells of one tile with the same crossing
+//     depth form a depth group; every upstream cell of a group lies in the group itself, in a group of
+//     lower depth, or nowhere.
+//   - The cells of a group are sorted by decreasing distance, in cells, to the group's most downstream
+//     cells, so every in-group upstream cell of a cell comes before it.  A stage is a run of at most
+//     `cap` (128) consecutive cells of that order; the rounds of a stage count that distance from its
+//     first cell, and every cell is exactly one round after each of its upstream cells in the stage
+//     (each cell has one downstream cell).  Outflows that go to another stage are exits.
 //   - A stage runs in one CTA: the cells of a round are computed together from shared memory, and the
-//     outflows that leave the stage go to a history in global memory, where later stages read them.
+//     exits' outflows go to a history in global memory, where later stages read them.
 //   - Time steps are pipelined: cell c does step t in round round(c) + t, so T steps of a stage take
-//     rounds + T - 1 rounds.  Steps are cut into chunks; stage (depth d, chunk c) runs in wave d + c, so
-//     chunks of different depths overlap in time.
+//     rounds + T - 1 rounds.  All stages and steps run in one launch in which each stage waits, step by
+//     step, for the exits it reads (stage_route.cu, k_stage_flow).
 //
 // Built once per flow-direction raster (on the first call that needs it) and kept by the topology.
 #pragma once
@@ -30,10 +32,9 @@ namespace lue_gb300 {
 
 constexpr int kStageSide = 32;                        // tile side (cells)
 constexpr int kStageCells = kStageSide * kStageSide;  // 1024
-constexpr int kStageThreads = 256;                    // runtime CTA: four cells per thread
-constexpr int kStagePerThread = kStageCells / kStageThreads;
+constexpr int kStageThreads = 256;                    // runtime CTA for stages of more than 256 cells
 constexpr int kStageBuildThreads = 512;               // build CTA: two cells per thread
-constexpr int kStageHistorySlots = 4096;              // shared-memory history entries (inputs x steps) per CTA
+constexpr int kStageCap = 128;                        // default largest stage (cells; LUE_GB300_STAGE_CAP)
 
 // meta (per cell, by tile and position in the tile's stage order):
 //   x: in-tile cell (bits 0-9) | round (bits 10-19)
@@ -42,18 +43,23 @@ constexpr int kStageHistorySlots = 4096;              // shared-memory history e
 struct StageCore {
     int64_t trows = 0, tcols = 0, ntiles = 0;
     int64_t nstages = 0, nexits = 0, ninputs = 0;
+    int cap = kStageCap;               // most cells of one stage
     int64_t max_depth = 0;             // deepest stage
+    int64_t max_stage_cells = 0;       // most cells of one stage (at most cap)
     int64_t max_stage_inputs = 0;      // most inputs of one stage
     int64_t max_stages_per_depth = 0;
     int4* stage = nullptr;             // [nstages] tile, begin | count << 16, rounds | inputs << 16, input base
-    int32_t* wave_stage = nullptr;     // [nstages] stage ids sorted by depth
-    int64_t* depth_offsets = nullptr;  // [max_depth + 2] start of each depth in wave_stage (device)
-    std::vector<int64_t> h_depth_offsets;
-    std::vector<int32_t> h_depth_max_cells;   // [max_depth + 1] largest stage of each depth (cells)
-    std::vector<int32_t> h_depth_max_inputs;  // [max_depth + 1] most inputs of a stage of each depth
+    int32_t* wave_stage = nullptr;     // [nstages] stage ids sorted by depth (the wave order)
+    std::vector<int64_t> h_depth_offsets;  // [max_depth + 2] start of each depth in wave_stage
     uint2* meta = nullptr;             // [ntiles * 1024]
     int32_t* exit_id = nullptr;        // [ntiles * 1024] history row of the cell, or -1 (outflow stays in the stage)
     int32_t* inputs = nullptr;         // [ninputs] history row of the upstream cell of each edge into a stage
+    // Dataflow order (by position k in wave_stage): the stages whose exits feed stage k, each with the
+    // earliest round at which stage k consumes them, and the latest round of stage k's own exits.
+    int64_t* prod_offsets = nullptr;   // [nstages + 1]
+    int2* prod = nullptr;              // [prod_offsets[nstages]] (producer position, earliest consumer round)
+    int32_t* max_exit_round = nullptr; // [nstages] -1 without exits
+    int64_t max_producers = 0;
     int64_t bytes = 0;
 };
 

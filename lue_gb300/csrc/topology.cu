@@ -168,7 +168,8 @@ static void free_handle(lue_gpu_topology* t)
     cudaFree(t->history);
     cudaFree(t->planes);
     cudaFree(t->stage_hist);
-    cudaFree(t->stage_state);
+    cudaFree(t->stage_flow);
+    cudaFreeHost(t->stage_flow_error);
     tile_scratch_free(&t->tile_scratch);
     if (t->core && --t->core->refs == 0) free_core(t->core);
     delete t;

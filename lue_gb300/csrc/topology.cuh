@@ -41,8 +41,9 @@ struct lue_gpu_topology {
     size_t plane_capacity = 0;
     uint2* stage_hist = nullptr;     // stage engine: outflow history of the stage exits (grown on demand)
     size_t stage_hist_bytes = 0;
-    float2* stage_state = nullptr;   // stage engine: discharge and power of every cell between chunks
-    size_t stage_state_bytes = 0;
+    int* stage_flow = nullptr;       // stage engine, dataflow mode: per-stage progress, ticket and error flag
+    size_t stage_flow_bytes = 0;
+    int* stage_flow_error = nullptr; // pinned: the error flag of the last dataflow launch, read by the next call
     int64_t scratch_bytes = 0;
 };
 

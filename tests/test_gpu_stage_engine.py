@@ -3,8 +3,9 @@ against the walk engine and the oracle.
 
 The stage engine applies the same cell rules with the same float-float (float32) or float64 upstream
 sums, in the same neighbour order, as the walk engine, so one-step results agree bit for bit.  The
-multi-step kinematic wave uses a float-float solve; it is checked against the float64 oracle and for
-independence of its chunk size.  LUE_GB300_ENGINE=walk selects the walk engine for a call.
+multi-step kinematic wave uses a float-float solve; it is checked against the float64 oracle.  Results
+do not depend on the largest stage (LUE_GB300_STAGE_CAP, read when a topology builds its stages): only
+where an upstream outflow is read from changes.  LUE_GB300_ENGINE=walk selects the walk engine for a call.
 """
 import os
 
@@ -116,25 +117,25 @@ def test_kinematic_wave_single_step_against_walk_engine(lfr):
         parity.assert_close64(stage, want, "kinematic_wave one step")
 
 
-@pytest.mark.parametrize("chunk", ["1", "3", "8", "64"])
-def test_kinematic_wave_steps_chunk_sizes(lfr, chunk):
-    """Chunks of the pipelined steps: every chunk size gives the oracle's discharge after 12 steps."""
+@pytest.mark.parametrize("cap", ["1", "7", "64", "1024"])
+def test_kinematic_wave_steps_stage_caps(lfr, cap):
+    """Stages of at most 1, 7, 64 or 1024 cells give the oracle's discharge after 12 steps."""
     d = _kw(257, 390, 4)
     fd = d["flow_direction"]
     a = lfr.from_numpy(fd)
     lat, alpha, q0 = (lfr.from_numpy(d[k]) for k in ("lateral_inflow", "alpha", "discharge"))
-    with _env(LUE_GB300_STAGE_CHUNK=chunk):
+    with _env(LUE_GB300_STAGE_CAP=cap):
         got = lfr.to_numpy(lfr.kinematic_wave_steps(a, q0, lat, alpha, 0.6, 3600.0, 100.0, 12))
     q = d["discharge"]
     for _ in range(12):
         q = oracle.kinematic_wave(fd, q, d["lateral_inflow"].astype(np.float64), d["alpha"].astype(np.float64),
                                   0.6, 3600.0, 100.0, fd.shape, dtype=np.float64)
-    parity.assert_close64(got, q, f"kinematic_wave_steps chunk {chunk}")
+    parity.assert_close64(got, q, f"kinematic_wave_steps, stages of at most {cap} cells")
 
 
 def test_kinematic_wave_steps_zero_and_no_data(lfr):
     """Cells without water, cells whose discharge starts at 0 (the reference's DBL_MIN start), NaN
-    lateral inflow and no-data flow directions, over several chunks."""
+    lateral inflow and no-data flow directions."""
     d = _kw(200, 260, 12)
     fd = d["flow_direction"].copy()
     rng = np.random.default_rng(3)
@@ -145,9 +146,8 @@ def test_kinematic_wave_steps_zero_and_no_data(lfr):
     lat[rng.random(fd.shape) < 0.05] = 0.0
     lat[rng.random(fd.shape) < 0.001] = np.nan
     a = lfr.from_numpy(fd)
-    with _env(LUE_GB300_STAGE_CHUNK="4"):
-        got = lfr.to_numpy(lfr.kinematic_wave_steps(a, lfr.from_numpy(q0), lfr.from_numpy(lat),
-                                                    lfr.from_numpy(d["alpha"]), 0.6, 3600.0, 100.0, 9))
+    got = lfr.to_numpy(lfr.kinematic_wave_steps(a, lfr.from_numpy(q0), lfr.from_numpy(lat),
+                                                lfr.from_numpy(d["alpha"]), 0.6, 3600.0, 100.0, 9))
     q = q0
     for _ in range(9):
         q = oracle.kinematic_wave(fd, q, lat.astype(np.float64), d["alpha"].astype(np.float64), 0.6, 3600.0, 100.0,
@@ -195,3 +195,58 @@ def test_upstream_downstream_distance_against_oracle(lfr, shape, dtype):
     tdt = torch.float32 if dtype == np.float32 else torch.float64
     got = lfr.to_numpy(lfr.downstream_distance(a, 2.5, tdt))
     assert np.array_equal(got, oracle.downstream_distance(fd, 2.5, dtype), equal_nan=True)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+def test_results_do_not_depend_on_the_stage_cap(lfr, dtype):
+    """Stages of at most 1, 32, 128 (default) or 1024 cells: the same cells, rules and sums in the same
+    neighbour order, so the same bits."""
+    fd, rng = _raster(1536, 700, seed=77, holes=0.0005)
+    m = rng.lognormal(0.0, 1.0, fd.shape).astype(dtype)
+    thr = (rng.random(fd.shape) * 0.5).astype(dtype)
+    ps = (512, 350)
+    md, td = lfr.from_numpy(m, ps), lfr.from_numpy(thr, ps)
+    results = {}
+    for cap in ("1", "32", "128", "1024"):
+        with _env(LUE_GB300_STAGE_CAP=cap):
+            a = lfr.from_numpy(fd, ps)
+            results[cap] = [lfr.to_numpy(x) for op in (lfr.accu_threshold, lfr.accu_capacity) for x in op(a, md, td)]
+    for cap, got in results.items():
+        for g, w in zip(got, results["128"]):
+            assert np.array_equal(g, w, equal_nan=True), cap
+
+
+def test_kinematic_wave_steps_do_not_depend_on_the_stage_cap(lfr):
+    d = _kw(700, 900, 21)
+    args = tuple(lfr.from_numpy(d[k]) for k in ("discharge", "lateral_inflow", "alpha")) + (0.6, 3600.0, 100.0, 17)
+    results = {}
+    for cap in ("16", "128", "1024"):
+        with _env(LUE_GB300_STAGE_CAP=cap):
+            a = lfr.from_numpy(d["flow_direction"])
+            results[cap] = lfr.to_numpy(lfr.kinematic_wave_steps(a, *args))
+    for cap, got in results.items():
+        assert np.array_equal(got, results["128"], equal_nan=True), cap
+
+
+def test_dataflow_wait_that_gives_up_is_reported(lfr):
+    """A stage whose first wait can never end (LUE_GB300_FLOW_STUCK_STAGE: it waits for a step of its own
+    that it has not published) gives up after a bounded number of polls: every output of the call is NaN,
+    the next call on the topology returns LUE_GPU_ETIMEDOUT, and the call after that is valid again."""
+    import torch
+    from lue_gb300 import _lib
+    fd, rng = _raster(512, 512, seed=3)
+    m = rng.random(fd.shape).astype(np.float32)
+    thr = np.full(fd.shape, 0.1, np.float32)
+    a = lfr.from_numpy(fd)
+    md, td = lfr.from_numpy(m), lfr.from_numpy(thr)
+    want = [lfr.to_numpy(x) for x in lfr.accu_threshold(a, md, td)]
+    with _env(LUE_GB300_FLOW_STUCK_STAGE="0"):
+        bad = [lfr.to_numpy(x) for x in lfr.accu_threshold(a, md, td)]
+    torch.cuda.synchronize()
+    assert all(np.isnan(x).all() for x in bad)
+    with pytest.raises(_lib.LueGpuError) as e:
+        lfr.accu_threshold(a, md, td)
+    assert e.value.status == 5
+    again = [lfr.to_numpy(x) for x in lfr.accu_threshold(a, md, td)]
+    for g, w in zip(again, want):
+        assert np.array_equal(g, w, equal_nan=True)
