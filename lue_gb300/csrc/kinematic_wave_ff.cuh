@@ -74,39 +74,6 @@ __device__ __forceinline__ ffloat ff_from_double(double d)
 }
 __device__ __forceinline__ double ff_to_double(ffloat a) { return (double)a.hi + (double)a.lo; }
 
-__device__ __forceinline__ ffloat ff_ipow(ffloat x, int e)  // e >= 1
-{
-    ffloat r = x, b = x;
-    bool first = true;
-    while (e) {
-        if (e & 1) {
-            r = first ? b : ff_mul(r, b);
-            first = false;
-        }
-        e >>= 1;
-        if (e) b = ff_mul(b, b);
-    }
-    return r;
-}
-
-// x^(p/m) in float-float for 1e-12 <= x <= 1e12 (x^p and y^m stay in float range for p <= 3, m <= 5):
-// y0 = __powf(x, beta) (exp2/log2 approximations, ~1e-6 relative), then two Newton steps for y^m = x^p
-// in float-float, each squaring the relative error (1e-6 -> 1e-12 -> float-float precision).
-__device__ __forceinline__ ffloat pow_rational_ff(ffloat x, BetaRational br)
-{
-    const float y0 = __powf(x.hi, br.beta_f);
-    const ffloat xp = ff_ipow(x, br.p);
-    ffloat y{y0, 0.0f};
-#pragma unroll 1
-    for (int it = 0; it < 2; ++it) {
-        const ffloat diff = ff_add(ff_ipow(y, br.m), ff_neg(xp));
-        float dm = (float)br.m;
-        for (int i = 1; i < br.m; ++i) dm *= y.hi;
-        y = ff_add(y, ffloat{-__fdividef(diff.hi, dm), 0.0f});
-    }
-    return y;
-}
-
 // a + b with an error of about 2^-48 (|a| + |b|): enough wherever the result is not compared against
 // cancellation below that.
 __device__ __forceinline__ ffloat ff_add_sloppy(ffloat a, ffloat b)
@@ -142,20 +109,6 @@ __device__ __forceinline__ float f_pow_n(float y, int e_runtime)
     return r;
 }
 
-// Whether float-float powers of x stay in range for beta = p/m.
-__device__ __forceinline__ bool ff_pow_ok(float x, BetaRational br)
-{
-    return br.p <= 3 && br.m <= 5 && x >= 1e-12f && x <= 1e12f;
-}
-
-// Q^beta in float-float, through float64 when the float-float path is out of range.
-__device__ __forceinline__ ffloat kw_power(ffloat q, BetaRational br, double beta)
-{
-    if (q.hi == 0.0f) return ffloat{0.0f, 0.0f};
-    if (ff_pow_ok(q.hi, br)) return pow_rational_ff(q, br);
-    return ff_from_double(pow(ff_to_double(q), beta));
-}
-
 struct KWConstFF {
     ffloat k;       // dt / dx
     ffloat dt;
@@ -164,77 +117,6 @@ struct KWConstFF {
     BetaRational br;
     bool bad;       // NaN beta / dt / dx, or dx <= 0: every cell is no-data
 };
-
-// One step of one cell.  Q and P (= Q^beta) are the cell's discharge and power from the previous step
-// and become this step's; up is the upstream sum of this step.  Returns false (Q, P = NaN) for no-data.
-__device__ __forceinline__ bool kw_step_ff(ffloat up, bool nan, ffloat& Q, ffloat& P, float lat, float al,
-                                           const KWConstFF& K)
-{
-    const float nanf = __int_as_float(0x7fc00000);
-    if (nan || K.bad || isnan(Q.hi) || isnan(lat) || isnan(al) || !(Q.hi >= 0.0f) || !(lat >= 0.0f)) {
-        Q = P = ffloat{nanf, 0.0f};
-        return false;
-    }
-    const bool flow = up.hi + Q.hi > 0.0f;
-    if (!flow && !(lat > 0.0f)) {  // no water (kinematic_wave.hpp:181-185)
-        Q = P = ffloat{0.0f, 0.0f};
-        return true;
-    }
-    float x = 0.0f;
-    bool fast = flow;
-    if (fast) {
-        // known right-hand side in float-float
-        const ffloat known = ff_add(ff_add(ff_mul(K.k, up), ff_mul_f(P, al)), ff_mul_f(K.dt, lat));
-        // float32 Newton (exp2/log2 powers) from the previous discharge, or from the reference's linearised
-        // guess (kinematic_wave.hpp:61-91) when there is none; it settles to the ~1e-6 of those powers
-        const float kf = K.kf, bf = K.beta_f, knf = known.hi;
-        if (Q.hi > 0.0f) {
-            x = Q.hi;
-        } else {
-            const float mean = 0.5f * (Q.hi + up.hi);
-            const float abpq = al * bf * __powf(mean, bf - 1.0f);
-            x = (kf * up.hi + abpq * Q.hi + K.dt.hi * lat) / (kf + abpq);
-        }
-        if (!(x > 1e-30f)) x = 1e-30f;
-        bool converged = false;
-        for (int it = 0; it < 16; ++it) {
-            const float xb = __powf(x, bf);
-            const float f = kf * x + al * xb - knf;
-            const float df = kf + __fdividef(al * bf * xb, x);
-            float nx = x - __fdividef(f, df);
-            if (!(nx > 0.0f)) nx = 0.5f * x;
-            const float dxr = fabsf(nx - x);
-            x = nx;
-            if (dxr <= 1e-5f * x) {
-                converged = true;
-                break;
-            }
-        }
-        fast = converged && isfinite(x) && ff_pow_ok(x, K.br);
-        if (fast) {
-            // two float-float Newton steps (1e-6 -> 1e-12 -> ~1e-14); the power at the second point is the
-            // first one's moved by its Taylor series to second order, and the result's to first order
-            const ffloat y1 = pow_rational_ff(ffloat{x, 0.0f}, K.br);
-            const float df = kf + __fdividef(al * bf * y1.hi, x);
-            const ffloat f1 = ff_add(ff_add(ff_mul_f(K.k, x), ff_mul_f(y1, al)), ff_neg(known));
-            const float d1 = __fdividef(f1.hi, df);
-            const ffloat q1 = ff_two_sum(x, -d1);
-            const float r1 = -__fdividef(d1, x);
-            const ffloat y2 = ff_add(y1, ffloat{y1.hi * (bf * r1 + 0.5f * bf * (bf - 1.0f) * r1 * r1), 0.0f});
-            const ffloat f2 = ff_add(ff_add(ff_mul(K.k, q1), ff_mul_f(y2, al)), ff_neg(known));
-            const float d2 = __fdividef(f2.hi, df);
-            Q = ff_add(q1, ffloat{-d2, 0.0f});
-            P = ff_add(y2, ffloat{-y2.hi * bf * __fdividef(d2, x), 0.0f});
-            return true;
-        }
-    }
-    // the float64 solve of the reference (rare)
-    const double q = iterate_to_new_discharge(ff_to_double(up), ff_to_double(Q), (double)lat, (double)al, K.beta,
-                                              K.dt_d, K.dx_d);
-    Q = ff_from_double(q);
-    P = q > 0.0 ? ff_from_double(pow(q, K.beta)) : ffloat{0.0f, 0.0f};
-    return true;
-}
 
 // The kinematic-wave solve in the variable y = Q^(1/m), for beta = p/m: Q^beta = y^p and Q = y^m, so the
 // equation k*Q + alpha*Q^beta = known becomes the polynomial

@@ -457,7 +457,7 @@ int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stre
     const int64_t n = core->n, rows = core->rows, cols = core->cols;
     auto* sc = new (std::nothrow) StageCore();
     if (!sc) return fail(LUE_GPU_ENOMEM, "stage topology: host allocation");
-    if (const char* e = getenv("LUE_GB300_STAGE_CAP")) sc->cap = std::max(1, std::min(kStageCells, atoi(e)));
+    if (const char* e = getenv("LUE_GB300_STAGE_CAP")) sc->cap = std::max(1, std::min(kStageMaxCap, atoi(e)));
     sc->trows = div_up(rows, kStageSide);
     sc->tcols = div_up(cols, kStageSide);
     sc->ntiles = sc->trows * sc->tcols;
@@ -752,7 +752,15 @@ struct StageFlowArgs {
     int64_t nstages;
     int polls;      // poll limit of one wait
     int64_t stuck;  // test hook: the position of a stage whose first wait never ends (-1: none)
+    unsigned long long* trace;  // [4 nstages] or null: start, rounds begin, time in waits, end (ns)
 };
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long v;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(v));
+    return v;
+}
 
 __device__ __forceinline__ int ld_acquire(const int* p)
 {
@@ -779,60 +787,84 @@ __device__ __forceinline__ int flow_wait(const int* p, int need, int* error, int
     return need;
 }
 
-// Shared memory of a stage of at most `cap` cells: the stage position of each in-tile cell, the outflows
-// by step parity and position, per position meta / history row / cell state / round starts, the history
-// rows of the stage's inputs, and per producer its position, the earliest round that consumes it and
-// the steps of it known to be in the history.
+// Shared memory of a stage of at most kStageMaxCap cells: the stage position of each in-tile cell, the
+// outflows by step parity and position, per position meta / history row / cell state / round starts, per
+// input (an upstream cell in another stage) its history row, value and cell, and per producer its
+// position, the earliest round that consumes it and the steps of it known to be in the history.
 template <class R>
 struct FlowLayout {
-    int16_t* local;
+    uint8_t* local;
     uint2* Qs;
     uint2* meta;
     int32_t* ex;
     typename R::Cell* cells;
     uint16_t* rstart;
+    uint2* in_vals;
     int32_t* in_rows;
+    uint8_t* in_cell;
     int2* prod;
     int* have;
-    uint2* in_vals;
     __device__ FlowLayout(unsigned char* base, int count, int nin, int np)
     {
-        local = reinterpret_cast<int16_t*>(base);
+        local = base;
         Qs = reinterpret_cast<uint2*>(local + kStageCells);
         meta = Qs + 2 * count;
-        ex = reinterpret_cast<int32_t*>(meta + count);
-        // 16-byte aligned: a Cell may hold doubles
-        cells = reinterpret_cast<typename R::Cell*>((reinterpret_cast<uintptr_t>(ex + count) + 15) & ~uintptr_t(15));
-        // round up to 4 bytes: a Cell may be a 1-byte empty struct
-        rstart = reinterpret_cast<uint16_t*>((reinterpret_cast<uintptr_t>(cells + count) + 3) & ~uintptr_t(3));
-        in_rows = reinterpret_cast<int32_t*>((reinterpret_cast<uintptr_t>(rstart + count + 2) + 3) & ~uintptr_t(3));
+        in_vals = meta + count;
+        ex = reinterpret_cast<int32_t*>(in_vals + nin);
+        in_rows = ex + count;
         prod = reinterpret_cast<int2*>((reinterpret_cast<uintptr_t>(in_rows + nin) + 7) & ~uintptr_t(7));
         have = reinterpret_cast<int*>(prod + np);
-        in_vals = reinterpret_cast<uint2*>((reinterpret_cast<uintptr_t>(have + np) + 7) & ~uintptr_t(7));
+        // 16-byte aligned: a Cell may hold doubles
+        cells = reinterpret_cast<typename R::Cell*>((reinterpret_cast<uintptr_t>(have + np) + 15) & ~uintptr_t(15));
+        // round up to 4 bytes: a Cell may be a 1-byte empty struct
+        rstart = reinterpret_cast<uint16_t*>((reinterpret_cast<uintptr_t>(cells + count) + 3) & ~uintptr_t(3));
+        in_cell = reinterpret_cast<uint8_t*>(rstart + count + 2);
     }
 };
 
 template <class R>
 static size_t flow_smem(int64_t cells, int64_t inputs, int64_t producers)
 {
-    return kStageCells * sizeof(int16_t) + cells * (3 * sizeof(uint2) + sizeof(int32_t) + sizeof(typename R::Cell)) +
-           (cells + 2) * sizeof(uint16_t) + inputs * (sizeof(int32_t) + sizeof(uint2)) +
-           producers * (sizeof(int2) + sizeof(int)) + 64;  // + alignment
+    return kStageCells + cells * (3 * sizeof(uint2) + sizeof(int32_t) + sizeof(typename R::Cell)) +
+           (cells + 2) * sizeof(uint16_t) + inputs * (sizeof(uint2) + sizeof(int32_t) + 1) +
+           producers * (sizeof(int2) + sizeof(int)) + 32;  // + alignment
 }
+
+// Waits until every producer has published the steps that round r consumes (round r consumes step
+// r - round(c) at cell c): each thread waits for its share of the producers.
+template <int NT>
+__device__ __forceinline__ void flow_wait_round(const StageFlowArgs& f, const int2* prod, int* have, int np, int ns,
+                                                int r)
+{
+    for (int i = threadIdx.x; i < np; i += NT) {
+        const int2 pq = prod[i];
+        const int need = min(ns, r - pq.y + 1);
+        if (need > have[i]) have[i] = flow_wait(f.progress + pq.x, need, f.error, f.polls);
+    }
+}
+
+constexpr int kFlowPrefetch = 2;  // inputs per thread loaded one round ahead into registers
 
 // A Rule supplies the per-cell state (Cell, kept in shared memory by position), the accumulator of the
 // upstream outflows (Acc), the cell step and the final store.  ONE (a call of one step): the stage first
 // waits for all its producers and loads all its inputs into shared memory at once, so that its rounds
-// read shared memory only; with many steps it waits and reads round by round.
+// read shared memory only.  With many steps, round r waits for the inputs of round r + 1 and loads them
+// into registers before its own cells, and puts them into shared memory after them, so that their load
+// overlaps the round's arithmetic.
 template <class R, int NT, bool ONE>
 __global__ void __launch_bounds__(NT) k_stage_flow(StageRunArgs a, StageFlowArgs f, R rule)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_ticket;
+    __shared__ unsigned long long s_wait;  // tracing: time in waits
     if (threadIdx.x == 0) s_ticket = atomicAdd(f.ticket, 1);
     __syncthreads();
     const int64_t k = s_ticket;
     if (k >= f.nstages) return;
+    if (f.trace && threadIdx.x == 0) {
+        f.trace[4 * k] = global_ns();
+        s_wait = 0;
+    }
     const int4 st = a.stage[a.wave_stage[k]];
     const int64_t tile = st.x;
     const int begin = st.y & 0xFFFF, count = (int)((unsigned)st.y >> 16);
@@ -855,7 +887,9 @@ __global__ void __launch_bounds__(NT) k_stage_flow(StageRunArgs a, StageFlowArgs
         L.meta[i] = m;
         L.ex[i] = __ldg(a.exit_id + at);
         const int p = (int)(m.x & 1023u);
-        L.local[p] = (int16_t)i;
+        L.local[p] = (uint8_t)i;
+        const int fi = (int)(m.y >> 16), ne = __popc((m.y >> 8) & 0xFFu);
+        for (int j = 0; j < ne; ++j) L.in_cell[fi + j] = (uint8_t)i;
         rule.load(L.cells[i], (row0 + (p >> 5)) * a.cols + col0 + (p & 31));
     }
     __syncthreads();
@@ -865,26 +899,41 @@ __global__ void __launch_bounds__(NT) k_stage_flow(StageRunArgs a, StageFlowArgs
     }
     if (threadIdx.x == 0) L.rstart[rounds] = (uint16_t)count;
     const int max_exit = __ldg(f.max_exit_round + k);
+    if (f.trace && threadIdx.x == 0) f.trace[4 * k + 1] = global_ns();
+    // the inputs of round 0 (ONE: of every round)
+    flow_wait_round<NT>(f, L.prod, L.have, np, ns, ONE ? ns + rounds : 0);
+    if (k == f.stuck && threadIdx.x == 0) flow_wait(f.progress + k, ns + 1, f.error, f.polls);
     __syncthreads();
-    if (ONE) {
-        for (int i = threadIdx.x; i < np; i += NT) flow_wait(f.progress + L.prod[i].x, 1, f.error, f.polls);
-        if (k == f.stuck && threadIdx.x == 0) flow_wait(f.progress + k, ns + 1, f.error, f.polls);
-        __syncthreads();
-        for (int i = threadIdx.x; i < nin; i += NT) L.in_vals[i] = __ldcg(a.hist + L.in_rows[i]);
+    if (f.trace && threadIdx.x == 0) s_wait += global_ns() - f.trace[4 * k + 1];
+    {
+        const int s_hi = ONE ? nin : (rounds > 1 ? (int)(L.meta[L.rstart[1]].y >> 16) : nin);
+        for (int s = threadIdx.x; s < s_hi; s += NT) L.in_vals[s] = __ldcg(a.hist + (int64_t)L.in_rows[s] * ns);
     }
     const int nrounds = rounds + ns - 1;
     int published = 0;
     for (int r = 0; r < nrounds; ++r) {
-        if (!ONE) {
-            // the producers' steps this round consumes: round r consumes step r - round(c) at cell c
-            for (int i = threadIdx.x; i < np; i += NT) {
-                const int2 pq = L.prod[i];
-                const int need = min(ns, r - pq.y + 1);
-                if (need > L.have[i]) L.have[i] = flow_wait(f.progress + pq.x, need, f.error, f.polls);
+        // the inputs of round r + 1: wait, then load into registers
+        uint2 pv[kFlowPrefetch];
+        int s_lo = 0, s_hi = 0;
+        if (!ONE && r + 1 < nrounds) {
+            if (f.trace && threadIdx.x == 0) s_wait -= global_ns();
+            flow_wait_round<NT>(f, L.prod, L.have, np, ns, r + 1);
+            __syncthreads();
+            if (f.trace && threadIdx.x == 0) s_wait += global_ns();
+            const int lo = L.rstart[max(0, r + 2 - ns)], hi = L.rstart[min(rounds, r + 2)];
+            s_lo = (int)(L.meta[lo].y >> 16);
+            s_hi = hi < count ? (int)(L.meta[hi].y >> 16) : nin;
+#pragma unroll
+            for (int j = 0; j < kFlowPrefetch; ++j) {
+                const int s = s_lo + (int)threadIdx.x + j * NT;
+                if (s < s_hi) {
+                    const int t = r + 1 - (int)((L.meta[L.in_cell[s]].x >> 10) & 1023u);
+                    pv[j] = __ldcg(a.hist + (int64_t)L.in_rows[s] * ns + t);
+                }
             }
-            if (r == 0 && k == f.stuck && threadIdx.x == 0) flow_wait(f.progress + k, ns + 1, f.error, f.polls);
+        } else {
+            __syncthreads();
         }
-        __syncthreads();
         const int lo = L.rstart[max(0, r - ns + 1)], hi = L.rstart[min(rounds, r + 1)];
         for (int i = lo + (int)threadIdx.x; i < hi; i += NT) {
             const uint2 m = L.meta[i];
@@ -898,10 +947,8 @@ __global__ void __launch_bounds__(NT) k_stage_flow(StageRunArgs a, StageFlowArgs
             while (um) {
                 const int q = __ffs(um) - 1;
                 um &= um - 1;
-                const int e_in = fi + __popc(em & ((1u << q) - 1u));
-                const uint2 v = ((em >> q) & 1u)
-                                    ? (ONE ? L.in_vals[e_in] : __ldcg(a.hist + (int64_t)L.in_rows[e_in] * ns + t))
-                                    : Qt[L.local[p + nb_dr(q) * kStageSide + nb_dc(q)]];
+                const uint2 v = ((em >> q) & 1u) ? L.in_vals[fi + __popc(em & ((1u << q) - 1u))]
+                                                  : Qt[L.local[p + nb_dr(q) * kStageSide + nb_dc(q)]];
                 rule.add(acc, v);
             }
             const uint2 o = rule.step(L.cells[i], acc, (row0 + (p >> 5)) * a.cols + col0 + (p & 31), t);
@@ -919,10 +966,25 @@ __global__ void __launch_bounds__(NT) k_stage_flow(StageRunArgs a, StageFlowArgs
                 published = prog;
             }
         }
+        if (!ONE && r + 1 < nrounds) {
+#pragma unroll
+            for (int j = 0; j < kFlowPrefetch; ++j) {
+                const int s = s_lo + (int)threadIdx.x + j * NT;
+                if (s < s_hi) L.in_vals[s] = pv[j];
+            }
+            for (int s = s_lo + (int)threadIdx.x + kFlowPrefetch * NT; s < s_hi; s += NT) {
+                const int t = r + 1 - (int)((L.meta[L.in_cell[s]].x >> 10) & 1023u);
+                L.in_vals[s] = __ldcg(a.hist + (int64_t)L.in_rows[s] * ns + t);
+            }
+        }
     }
     for (int i = threadIdx.x; i < count; i += NT) {
         const int p = (int)(L.meta[i].x & 1023u);
         rule.store(L.cells[i], (row0 + (p >> 5)) * a.cols + col0 + (p & 31));
+    }
+    if (f.trace && threadIdx.x == 0) {
+        f.trace[4 * k + 2] = s_wait;
+        f.trace[4 * k + 3] = global_ns();
     }
 }
 
@@ -1164,6 +1226,27 @@ __global__ void k_invalidate_if(const int* error, T* out, T* rem, int64_t n)
     }
 }
 
+static void stage_trace_write(const StageCore* sc, unsigned long long* trace, const char* path, cudaStream_t stream)
+{
+    std::vector<unsigned long long> tr((size_t)sc->nstages * 4);
+    std::vector<int32_t> ws(sc->nstages);
+    std::vector<int4> srec(sc->nstages);
+    cudaMemcpyAsync(tr.data(), trace, tr.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(ws.data(), sc->wave_stage, ws.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(srec.data(), sc->stage, srec.size() * sizeof(int4), cudaMemcpyDeviceToHost, stream);
+    cudaStreamSynchronize(stream);
+    cudaFree(trace);
+    FILE* fp = fopen(path, "wb");
+    if (!fp) return;
+    for (int64_t k = 0; k < sc->nstages; ++k) {
+        const int4 r = srec[ws[k]];
+        const int64_t rec[8] = {(int64_t)tr[4 * k], (int64_t)tr[4 * k + 1], (int64_t)tr[4 * k + 2], (int64_t)tr[4 * k + 3],
+                                r.x, (int64_t)((unsigned)r.y >> 16), r.z & 0xFFFF, (int64_t)((unsigned)r.z >> 16)};
+        fwrite(rec, sizeof(rec), 1, fp);
+    }
+    fclose(fp);
+}
+
 template <class R, int NT, bool ONE>
 static int launch_flow(const StageRunArgs& a, const StageFlowArgs& fa, const R& rule, unsigned blocks, size_t smem,
                        cudaStream_t stream, const char* what)
@@ -1180,13 +1263,19 @@ static int launch_flow(const StageRunArgs& a, const StageFlowArgs& fa, const R& 
     return LUE_GPU_OK;
 }
 
+// Threads per stage: LUE_GB300_STAGE_THREADS (32, 64, 128 or 256), else by the largest stage.
 template <class R, bool ONE>
 static int launch_flow(const StageRunArgs& a, const StageFlowArgs& fa, const R& rule, unsigned blocks,
                        int64_t max_cells, size_t smem, cudaStream_t stream, const char* what)
 {
-    if (max_cells <= 128) return launch_flow<R, 32, ONE>(a, fa, rule, blocks, smem, stream, what);
-    if (max_cells <= 256) return launch_flow<R, 64, ONE>(a, fa, rule, blocks, smem, stream, what);
-    return launch_flow<R, kStageThreads, ONE>(a, fa, rule, blocks, smem, stream, what);
+    int nt = max_cells <= 128 ? 32 : max_cells <= 256 ? 64 : kStageThreads;
+    if (const char* e = getenv("LUE_GB300_STAGE_THREADS")) nt = atoi(e);
+    switch (nt) {
+        case 32: return launch_flow<R, 32, ONE>(a, fa, rule, blocks, smem, stream, what);
+        case 64: return launch_flow<R, 64, ONE>(a, fa, rule, blocks, smem, stream, what);
+        case 128: return launch_flow<R, 128, ONE>(a, fa, rule, blocks, smem, stream, what);
+        default: return launch_flow<R, kStageThreads, ONE>(a, fa, rule, blocks, smem, stream, what);
+    }
 }
 
 // `steps` steps of a rule over every stage, in one dataflow launch (k_stage_flow); one warp per CTA for
@@ -1218,7 +1307,15 @@ static int stage_run(lue_gpu_topology* t, const StageCore* sc, const R& rule, in
     StageRunArgs a{sc->stage, sc->wave_stage, sc->meta, sc->exit_id, sc->inputs, core->rows, core->cols, sc->tcols,
                    steps, t->stage_hist};
     StageFlowArgs fa{sc->prod_offsets, sc->prod, sc->max_exit_round, progress, ticket, error, sc->nstages,
-                     kFlowPolls, -1};
+                     kFlowPolls, -1, nullptr};
+    // tracing (LUE_GB300_STAGE_TRACE=file): per stage in wave order its start, the start of its rounds,
+    // its time in waits and its end (globaltimer ns), then tile, cells, rounds and inputs, written after
+    // the launch as int64 records of 8
+    const char* trace_path = getenv("LUE_GB300_STAGE_TRACE");
+    if (trace_path) {
+        if (int rc = cuda_status(cudaMalloc(&fa.trace, (size_t)sc->nstages * 4 * sizeof(unsigned long long)), what))
+            return rc;
+    }
     if (const char* e = getenv("LUE_GB300_FLOW_STUCK_STAGE")) {  // test hook: see StageFlowArgs::stuck
         fa.stuck = std::max<int64_t>(0, std::min<int64_t>(atoll(e), sc->nstages - 1));
         fa.polls = 1 << 16;
@@ -1239,6 +1336,7 @@ static int stage_run(lue_gpu_topology* t, const StageCore* sc, const R& rule, in
             cudaMemcpyAsync(t->stage_flow_error, error, sizeof(int), cudaMemcpyDeviceToHost, stream), what))
         return rc;
     count_launches(2);
+    if (trace_path) stage_trace_write(sc, fa.trace, trace_path, stream);
     return cuda_status(cudaGetLastError(), what);
 }
 

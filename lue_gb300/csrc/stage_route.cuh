@@ -35,6 +35,7 @@ constexpr int kStageCells = kStageSide * kStageSide;  // 1024
 constexpr int kStageThreads = 256;                    // runtime CTA for stages of more than 256 cells
 constexpr int kStageBuildThreads = 512;               // build CTA: two cells per thread
 constexpr int kStageCap = 128;                        // default largest stage (cells; LUE_GB300_STAGE_CAP)
+constexpr int kStageMaxCap = 256;                     // stage positions fit in a byte
 
 // meta (per cell, by tile and position in the tile's stage order):
 //   x: in-tile cell (bits 0-9) | round (bits 10-19)

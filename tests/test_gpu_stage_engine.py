@@ -117,9 +117,9 @@ def test_kinematic_wave_single_step_against_walk_engine(lfr):
         parity.assert_close64(stage, want, "kinematic_wave one step")
 
 
-@pytest.mark.parametrize("cap", ["1", "7", "64", "1024"])
+@pytest.mark.parametrize("cap", ["1", "7", "64", "256"])
 def test_kinematic_wave_steps_stage_caps(lfr, cap):
-    """Stages of at most 1, 7, 64 or 1024 cells give the oracle's discharge after 12 steps."""
+    """Stages of at most 1, 7, 64 or 256 cells give the oracle's discharge after 12 steps."""
     d = _kw(257, 390, 4)
     fd = d["flow_direction"]
     a = lfr.from_numpy(fd)
@@ -199,7 +199,7 @@ def test_upstream_downstream_distance_against_oracle(lfr, shape, dtype):
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
 def test_results_do_not_depend_on_the_stage_cap(lfr, dtype):
-    """Stages of at most 1, 32, 128 (default) or 1024 cells: the same cells, rules and sums in the same
+    """Stages of at most 1, 32, 128 (default) or 256 cells: the same cells, rules and sums in the same
     neighbour order, so the same bits."""
     fd, rng = _raster(1536, 700, seed=77, holes=0.0005)
     m = rng.lognormal(0.0, 1.0, fd.shape).astype(dtype)
@@ -207,7 +207,7 @@ def test_results_do_not_depend_on_the_stage_cap(lfr, dtype):
     ps = (512, 350)
     md, td = lfr.from_numpy(m, ps), lfr.from_numpy(thr, ps)
     results = {}
-    for cap in ("1", "32", "128", "1024"):
+    for cap in ("1", "32", "128", "256"):
         with _env(LUE_GB300_STAGE_CAP=cap):
             a = lfr.from_numpy(fd, ps)
             results[cap] = [lfr.to_numpy(x) for op in (lfr.accu_threshold, lfr.accu_capacity) for x in op(a, md, td)]
@@ -220,7 +220,7 @@ def test_kinematic_wave_steps_do_not_depend_on_the_stage_cap(lfr):
     d = _kw(700, 900, 21)
     args = tuple(lfr.from_numpy(d[k]) for k in ("discharge", "lateral_inflow", "alpha")) + (0.6, 3600.0, 100.0, 17)
     results = {}
-    for cap in ("16", "128", "1024"):
+    for cap in ("16", "128", "256"):
         with _env(LUE_GB300_STAGE_CAP=cap):
             a = lfr.from_numpy(d["flow_direction"])
             results[cap] = lfr.to_numpy(lfr.kinematic_wave_steps(a, *args))
