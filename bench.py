@@ -19,6 +19,7 @@ Reported (one JSON line, rank 0):
              measured HBM copy bandwidth; traffic from the committed ncu summary when present.
   cpu_baseline  the CPU oracle (a restatement of the reference's partitioned ridge walk, threaded
              one task per partition) on a bounded sample, rank 0 only.
+  extra.accu_threshold  accu_threshold over the same raster and material (threshold uniform [0, 0.5)).
   extra.kinematic_wave  kinematic_wave steps over the 8192 x 8192 workload (float64 discharge).
 
 --impl reference times the reference algorithm on the CPU (the oracle port, every host core), since
@@ -42,6 +43,7 @@ sys.path.insert(0, ROOT)
 
 ACCU_BYTES_PER_CELL = 9      # fd 1 + material 4 + outflow 4
 KW_BYTES_PER_CELL = 25       # fd 1 + Q_cur 8 + lateral 4 + alpha 4 + Q_new 8
+THRESHOLD_BYTES_PER_CELL = 17  # fd 1 + material 4 + threshold 4 + flux 4 + state 4
 REF_SAMPLE_ROWS = 4096       # reference-arm / cpu_baseline sample: the top 4096 rows, all columns
 METRIC = "accu Mcells/s (16384^2 D8 raster, float32 material)"  # the headline metric, on accu_16k
 
@@ -289,32 +291,39 @@ def bench_ours(args, world, rank, local):
     ev_in = [torch.cuda.Event() for _ in range(e2e_steps)]
     ev_c = [torch.cuda.Event() for _ in range(e2e_steps)]
     ev_out = [torch.cuda.Event() for _ in range(e2e_steps)]
-    torch.cuda.synchronize()
-    barrier(world)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(s_in)
-    s_c.wait_event(e0)
-    s_out.wait_event(e0)
-    for k in range(e2e_steps):
-        b = k % 2
-        if k >= 2:
-            s_in.wait_event(ev_c[k - 2])  # in_d[b] is free once step k-2 has routed
-        with torch.cuda.stream(s_in):
-            in_d[b].copy_(m_host.view(rows, cols), non_blocking=True)
-        ev_in[k].record(s_in)
-        s_c.wait_event(ev_in[k])
-        if k >= 2:
-            s_c.wait_event(ev_out[k - 2])  # out_d[b] is free once step k-2 is downloaded
-        _lib.check(L.lue_gpu_accu_f32(topo.handle, in_d[b].data_ptr(), 0.0, out_d[b].data_ptr(), s_c.cuda_stream))
-        ev_c[k].record(s_c)
-        s_out.wait_event(ev_c[k])
-        with torch.cuda.stream(s_out):
-            out_host[b].copy_(out_d[b], non_blocking=True)
-        ev_out[k].record(s_out)
-    e1.record(s_out)
-    torch.cuda.synchronize()
-    e2e_s = max_over_ranks(e0.elapsed_time(e1) / 1000.0, world)
+
+    def e2e_trial():
+        torch.cuda.synchronize()
+        barrier(world)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(s_in)
+        s_c.wait_event(e0)
+        s_out.wait_event(e0)
+        for k in range(e2e_steps):
+            b = k % 2
+            if k >= 2:
+                s_in.wait_event(ev_c[k - 2])  # in_d[b] is free once step k-2 has routed
+            with torch.cuda.stream(s_in):
+                in_d[b].copy_(m_host.view(rows, cols), non_blocking=True)
+            ev_in[k].record(s_in)
+            s_c.wait_event(ev_in[k])
+            if k >= 2:
+                s_c.wait_event(ev_out[k - 2])  # out_d[b] is free once step k-2 is downloaded
+            _lib.check(L.lue_gpu_accu_f32(topo.handle, in_d[b].data_ptr(), 0.0, out_d[b].data_ptr(),
+                                          s_c.cuda_stream))
+            ev_c[k].record(s_c)
+            s_out.wait_event(ev_c[k])
+            with torch.cuda.stream(s_out):
+                out_host[b].copy_(out_d[b], non_blocking=True)
+            ev_out[k].record(s_out)
+        e1.record(s_out)
+        torch.cuda.synchronize()
+        return max_over_ranks(e0.elapsed_time(e1) / 1000.0, world)
+
+    # The host memory and its link are shared with the other jobs of the machine: best of three trials
+    e2e_trials = [e2e_trial() for _ in range(3)]
+    e2e_s = min(e2e_trials)
     e2e_value = world * n * e2e_steps / e2e_s / 1e6
     assert torch.equal(out_host[(e2e_steps - 1) % 2], out.data.cpu()), "end-to-end result differs"
 
@@ -335,6 +344,8 @@ def bench_ours(args, world, rank, local):
         torch.cuda.synchronize()
         torch.cuda.empty_cache()
 
+    if args.threshold_calls > 0 and rank == 0:
+        leg("accu_threshold", lambda a, d: bench_threshold(a, d, fd_d, m_d, inputs))
     if args.kinematic_wave_steps > 0 and rank == 0:
         leg("kinematic_wave", bench_kinematic_wave)
     if not args.no_ensemble and rank == 0:
@@ -364,6 +375,7 @@ def bench_ours(args, world, rank, local):
                    "tile_exits": stats.get("tile_exits", 0), "exit_forest_depth": stats.get("exit_forest_depth", 0)},
         "e2e": {"value": round(e2e_value, 3), "unit": "Mcells/s", "h2d_bytes_per_step": 4 * n,
                 "d2h_bytes_per_step": 4 * n, "steps": e2e_steps,
+                "trials_ms_per_step": [round(1000 * x / e2e_steps, 2) for x in e2e_trials], "timed": "best of 3 trials",
                 "overlap": "upload of step k+1 and download of step k-1 beside the routing of step k "
                            "(three streams, double buffers, pinned host memory)"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
@@ -380,6 +392,47 @@ def bench_ours(args, world, rank, local):
         "extra": extra,
     }
     print(json.dumps(line), flush=True)
+
+
+def bench_threshold(args, dev, fd_d, m_d, inputs):
+    """C2's second operation: accu_threshold over the same raster and material, threshold float32
+    uniform [0, 0.5) (seeded); the stage engine (one dataflow launch).  Mass balance: what the cells keep
+    plus what leaves at outlets and sinks equals the material put in."""
+    import torch
+
+    from lue_gb300 import framework as lfr
+
+    rows, cols = inputs["material"].shape
+    n = rows * cols
+    rng = np.random.default_rng(17)
+    thr = lfr.PartitionedArray(torch.from_numpy(rng.random((rows, cols), dtype=np.float32) * 0.5).to(dev),
+                               fd_d.partition_shape)
+    stream = torch.cuda.current_stream(dev)
+    t0 = time.perf_counter()
+    flux, state = lfr.accu_threshold(fd_d, m_d, thr)  # builds the stages
+    torch.cuda.synchronize()
+    first_s = time.perf_counter() - t0
+    calls = args.threshold_calls
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(calls):
+        flux, state = lfr.accu_threshold(fd_d, m_d, thr)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    s = e0.elapsed_time(e1) / 1000.0 / calls
+    mask = outlet_mask(fd_d.data)
+    total_in = float(m_d.data.double().sum())
+    kept = float(state.data.double().sum())
+    left = float(flux.data.double()[mask].sum())
+    return {"workload": f"accu_16k raster and material, threshold uniform [0, 0.5) float32 ({rows}x{cols})",
+            "calls": calls, "ms_per_call": round(1000 * s, 3), "value": round(n / s / 1e6, 3), "unit": "Mcells/s",
+            "roofline_frac_hbm": round(THRESHOLD_BYTES_PER_CELL * n / s / 1e9 / peaks()[0], 4),
+            "bytes_per_cell": THRESHOLD_BYTES_PER_CELL,
+            "first_call_ms": round(1000 * first_s, 2),
+            "engine": "stage engine: 32 x 32 tiles cut into stages of at most 128 cells by crossing depth, one "
+                      "dataflow launch (lue_gpu_accu_threshold_f32)",
+            "mass_balance": {"material_in": total_in, "kept_plus_outlet_flux": kept + left,
+                             "rel_err": abs(kept + left - total_in) / total_in}}
 
 
 def bench_kinematic_wave(args, dev):
@@ -493,6 +546,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="accu_16k")
     ap.add_argument("--kinematic-wave-steps", type=int, default=100)
+    ap.add_argument("--threshold-calls", type=int, default=3)
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--serve-sequential", type=int, default=32)
