@@ -395,13 +395,13 @@ __global__ void __launch_bounds__(kStageBuildThreads)
     }
 }
 
-// Stage ids of the exits -> positions in the wave order.
+// Stage ids of the exits -> positions in the depth order.
 __global__ void k_remap_i32(int32_t* v, int64_t n, const int32_t* __restrict__ map)
 {
     for (int64_t i = grid_stride_begin(); i < n; i += grid_stride()) v[i] = map[v[i]];
 }
 
-// Per stage (block per position k of the wave order): the stages whose exits feed it, each with the
+// Per stage (block per position k of the depth order): the stages whose exits feed it, each with the
 // earliest round at which one of its cells consumes them, and the latest round of the stage's own exits.
 // Pass 1 (list == nullptr) counts the producers; pass 2 writes them at offsets[k].
 __global__ void __launch_bounds__(256)
@@ -531,7 +531,8 @@ int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stre
     count_launches(2);
     TRY(cudaGetLastError(), "stage ids");
     {
-        // stages in wave order: counting sort by depth (host)
+        // stages in depth order: counting sort by depth (host); any order with every producer before its
+        // consumers would do, and the ticket order below is one
         std::vector<int32_t> sd(sc->nstages);
         std::vector<int4> srec(sc->nstages);
         TRY(cudaMemcpyAsync(sd.data(), stage_depth, sc->nstages * sizeof(int32_t), cudaMemcpyDeviceToHost, stream),
@@ -563,7 +564,6 @@ int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stre
             sc->max_stage_cells = std::max<int64_t>(sc->max_stage_cells, (int)((unsigned)r.y >> 16));
             sc->max_stage_inputs = std::max<int64_t>(sc->max_stage_inputs, (int)((unsigned)r.z >> 16));
         }
-        sc->h_depth_offsets = off;
         TRY(cudaMalloc(&sc->wave_stage, std::max<int64_t>(sc->nstages, 1) * sizeof(int32_t)), "wave order");
         TRY(cudaMemcpyAsync(sc->wave_stage, ws.data(), sc->nstages * sizeof(int32_t), cudaMemcpyHostToDevice, stream),
             "wave order");
@@ -610,48 +610,73 @@ int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stre
         TRY(cudaGetLastError(), "producers");
         TRY(cudaStreamSynchronize(stream), "producers");  // po must outlive the copy
         sc->bytes += (sc->nstages + 1) * 8 + po[sc->nstages] * 8 + sc->nstages * 4;
+        // Ticket order: the stages sorted by their earliest start in a model of a one-step call (a stage
+        // starts kHandOffRounds after the last exit round of its last producer), so that CTAs take stages
+        // about in the order in which their inputs become ready.  A producer's start is always earlier
+        // than its consumers', so the order keeps every producer before the stages it feeds.
+        {
+            constexpr int64_t kHandOffRounds = 2;
+            const int64_t ns = sc->nstages, npairs = po[ns];
+            std::vector<int2> pr(std::max<int64_t>(1, npairs));
+            std::vector<int32_t> mxr(ns);
+            TRY(cudaMemcpy(pr.data(), sc->prod, npairs * sizeof(int2), cudaMemcpyDeviceToHost), "stage order");
+            TRY(cudaMemcpy(mxr.data(), sc->max_exit_round, ns * sizeof(int32_t), cudaMemcpyDeviceToHost),
+                "stage order");
+            std::vector<int64_t> start(ns, 0);
+            int64_t last = 0;
+            for (int64_t k = 0; k < ns; ++k) {
+                int64_t s0 = 0;
+                for (int64_t j = po[k]; j < po[k + 1]; ++j)
+                    s0 = std::max<int64_t>(s0, start[pr[j].x] + mxr[pr[j].x] + 1 + kHandOffRounds);
+                start[k] = s0;
+                last = std::max(last, s0);
+            }
+            // counting sort by start, stable (ties keep the depth order)
+            std::vector<int64_t> bucket(last + 2, 0);
+            for (int64_t k = 0; k < ns; ++k) ++bucket[start[k] + 1];
+            for (int64_t v = 0; v <= last; ++v) bucket[v + 1] += bucket[v];
+            std::vector<int32_t> newpos(ns);
+            for (int64_t k = 0; k < ns; ++k) newpos[k] = (int32_t)bucket[start[k]]++;
+            std::vector<int32_t> ws2(ns), mx2(ns), cnt2(ns);
+            for (int64_t k = 0; k < ns; ++k) {
+                ws2[newpos[k]] = ws[k];
+                mx2[newpos[k]] = mxr[k];
+                cnt2[newpos[k]] = (int32_t)(po[k + 1] - po[k]);
+            }
+            std::vector<int64_t> po2(ns + 1, 0);
+            for (int64_t j = 0; j < ns; ++j) po2[j + 1] = po2[j] + cnt2[j];
+            std::vector<int2> pr2(std::max<int64_t>(1, npairs));
+            for (int64_t k = 0; k < ns; ++k) {
+                int64_t w = po2[newpos[k]];
+                for (int64_t j = po[k]; j < po[k + 1]; ++j) pr2[w++] = make_int2(newpos[pr[j].x], pr[j].y);
+            }
+            TRY(cudaMemcpy(sc->wave_stage, ws2.data(), ns * sizeof(int32_t), cudaMemcpyHostToDevice), "stage order");
+            TRY(cudaMemcpy(sc->max_exit_round, mx2.data(), ns * sizeof(int32_t), cudaMemcpyHostToDevice),
+                "stage order");
+            TRY(cudaMemcpy(sc->prod_offsets, po2.data(), (ns + 1) * sizeof(int64_t), cudaMemcpyHostToDevice),
+                "stage order");
+            TRY(cudaMemcpy(sc->prod, pr2.data(), npairs * sizeof(int2), cudaMemcpyHostToDevice), "stage order");
+        }
     }
-    sc->bytes += sc->nstages * 20 + np * 12 + sc->ninputs * 4 + (int64_t)sc->h_depth_offsets.size() * 8;
+    sc->bytes += sc->nstages * 20 + np * 12 + sc->ninputs * 4;
     if (getenv("LUE_GB300_VERBOSE")) {
-        // rounds: the critical path of the waves is about the sum over depths of the longest stage
+        // the critical path of a one-step call, in rounds, with a hand-off of h rounds per producer edge
         std::vector<int4> srec(sc->nstages);
         cudaMemcpy(srec.data(), sc->stage, sc->nstages * sizeof(int4), cudaMemcpyDeviceToHost);
-        std::vector<int> deep_max(sc->max_depth + 1, 0);
-        std::vector<int32_t> sd(sc->nstages);
-        for (int64_t d = 0; d <= sc->max_depth; ++d)
-            for (int64_t k = sc->h_depth_offsets[d]; k < sc->h_depth_offsets[d + 1]; ++k) sd[k] = (int32_t)d;
         std::vector<int32_t> ws(sc->nstages);
         cudaMemcpy(ws.data(), sc->wave_stage, sc->nstages * sizeof(int32_t), cudaMemcpyDeviceToHost);
-        double sum_rounds = 0;
-        int64_t sum_max = 0;
-        for (int64_t k = 0; k < sc->nstages; ++k) {
-            const int rounds = srec[ws[k]].z & 0xFFFF;
-            sum_rounds += rounds;
-            deep_max[sd[k]] = std::max(deep_max[sd[k]], rounds);
-        }
-        for (int v : deep_max) sum_max += v;
-        fprintf(stderr, "stage rounds: mean %.1f per stage, sum over depths of the longest %lld\n",
-                sum_rounds / std::max<int64_t>(1, sc->nstages), (long long)sum_max);
-        // dataflow critical path of one step, in rounds, with a hand-off of h rounds per producer edge
         std::vector<int64_t> po(sc->nstages + 1);
         cudaMemcpy(po.data(), sc->prod_offsets, po.size() * sizeof(int64_t), cudaMemcpyDeviceToHost);
         std::vector<int2> pr(std::max<int64_t>(1, po[sc->nstages]));
         cudaMemcpy(pr.data(), sc->prod, po[sc->nstages] * sizeof(int2), cudaMemcpyDeviceToHost);
         std::vector<int32_t> mx(sc->nstages);
         cudaMemcpy(mx.data(), sc->max_exit_round, sc->nstages * sizeof(int32_t), cudaMemcpyDeviceToHost);
+        double sum_rounds = 0;
+        for (int64_t k = 0; k < sc->nstages; ++k) sum_rounds += srec[ws[k]].z & 0xFFFF;
+        fprintf(stderr, "stage rounds: mean %.1f per stage\n", sum_rounds / std::max<int64_t>(1, sc->nstages));
         for (int h : {0, 2, 5}) {
             std::vector<int64_t> start(sc->nstages, 0);
             int64_t crit = 0;
-            for (int64_t k = 0; k < sc->nstages; ++k) {
-                int64_t s0 = 0;
-                for (int64_t j = po[k]; j < po[k + 1]; ++j)
-                    s0 = std::max<int64_t>(s0, start[pr[j].x] + mx[pr[j].x] + 1 + h - pr[j].y);
-                start[k] = s0;
-                crit = std::max<int64_t>(crit, s0 + (srec[ws[k]].z & 0xFFFF));
-            }
-            fprintf(stderr, "stage dataflow critical path (hand-off %d rounds): %lld rounds\n", h, (long long)crit);
-            // a stage that starts once all its producers are done
-            crit = 0;
             for (int64_t k = 0; k < sc->nstages; ++k) {
                 int64_t s0 = 0;
                 for (int64_t j = po[k]; j < po[k + 1]; ++j)
@@ -659,15 +684,13 @@ int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stre
                 start[k] = s0;
                 crit = std::max<int64_t>(crit, s0 + (srec[ws[k]].z & 0xFFFF));
             }
-            fprintf(stderr, "stage dataflow critical path, all inputs first (hand-off %d rounds): %lld rounds\n", h,
-                    (long long)crit);
+            fprintf(stderr, "stage dataflow critical path (hand-off %d rounds): %lld rounds\n", h, (long long)crit);
         }
         std::vector<int> sizes;
-        for (int64_t k = sc->h_depth_offsets[std::min<int64_t>(1, sc->max_depth)]; k < sc->nstages; ++k)
-            sizes.push_back((int)((unsigned)srec[ws[k]].y >> 16));
+        for (int64_t k = 0; k < sc->nstages; ++k) sizes.push_back((int)((unsigned)srec[ws[k]].y >> 16));
         std::sort(sizes.begin(), sizes.end());
         if (!sizes.empty())
-            fprintf(stderr, "stage cells at depth >= 1: p50 %d p90 %d p99 %d max %d; producers at most %lld\n",
+            fprintf(stderr, "stage cells: p50 %d p90 %d p99 %d max %d; producers at most %lld\n",
                     sizes[sizes.size() / 2], sizes[sizes.size() * 9 / 10], sizes[sizes.size() * 99 / 100],
                     sizes.back(), (long long)sc->max_producers);
     }
@@ -718,9 +741,9 @@ void stage_core_free(StageCore* sc)
 // ---------------------------------------------------------------------------------------------------
 //
 // One launch runs every stage with all the steps of the call.  Each CTA takes the next stage of the
-// wave order (stages sorted by depth; the stages of one depth group of a tile in their order) from a
-// ticket counter, so every stage it waits for (a producer: a stage whose exits feed it, always earlier
-// in that order) has been taken by a CTA that started earlier and waits only on stages taken before it.
+// ticket order (stage_core_build) from a ticket counter, so every stage it waits for (a producer: a
+// stage whose exits feed it, always earlier in that order) has been taken by a CTA that started earlier
+// and waits only on stages taken before it.
 // Inside a stage, cell c does step t in round round(c) + t, so T steps take rounds + T - 1 rounds; the
 // active positions of round r (round in (r - T, r]) are one contiguous range of the stage's order.
 // After each round a stage publishes how many steps of all its exits are in the history (progress[k]);
@@ -1245,6 +1268,16 @@ static void stage_trace_write(const StageCore* sc, unsigned long long* trace, co
         fwrite(rec, sizeof(rec), 1, fp);
     }
     fclose(fp);
+    // the producers: per stage its offset into the (producer position, earliest round) pairs
+    std::vector<int64_t> po(sc->nstages + 1);
+    cudaMemcpy(po.data(), sc->prod_offsets, po.size() * sizeof(int64_t), cudaMemcpyDeviceToHost);
+    std::vector<int2> pr(std::max<int64_t>(1, po[sc->nstages]));
+    cudaMemcpy(pr.data(), sc->prod, po[sc->nstages] * sizeof(int2), cudaMemcpyDeviceToHost);
+    fp = fopen((std::string(path) + ".prod").c_str(), "wb");
+    if (!fp) return;
+    fwrite(po.data(), sizeof(int64_t), po.size(), fp);
+    fwrite(pr.data(), sizeof(int2), po[sc->nstages], fp);
+    fclose(fp);
 }
 
 template <class R, int NT, bool ONE>
@@ -1308,7 +1341,7 @@ static int stage_run(lue_gpu_topology* t, const StageCore* sc, const R& rule, in
                    steps, t->stage_hist};
     StageFlowArgs fa{sc->prod_offsets, sc->prod, sc->max_exit_round, progress, ticket, error, sc->nstages,
                      kFlowPolls, -1, nullptr};
-    // tracing (LUE_GB300_STAGE_TRACE=file): per stage in wave order its start, the start of its rounds,
+    // tracing (LUE_GB300_STAGE_TRACE=file): per stage in ticket order its start, the start of its rounds,
     // its time in waits and its end (globaltimer ns), then tile, cells, rounds and inputs, written after
     // the launch as int64 records of 8
     const char* trace_path = getenv("LUE_GB300_STAGE_TRACE");

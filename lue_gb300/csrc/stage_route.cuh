@@ -50,8 +50,7 @@ struct StageCore {
     int64_t max_stage_inputs = 0;      // most inputs of one stage
     int64_t max_stages_per_depth = 0;
     int4* stage = nullptr;             // [nstages] tile, begin | count << 16, rounds | inputs << 16, input base
-    int32_t* wave_stage = nullptr;     // [nstages] stage ids sorted by depth (the wave order)
-    std::vector<int64_t> h_depth_offsets;  // [max_depth + 2] start of each depth in wave_stage
+    int32_t* wave_stage = nullptr;     // [nstages] stage ids in ticket order (see stage_core_build)
     uint2* meta = nullptr;             // [ntiles * 1024]
     int32_t* exit_id = nullptr;        // [ntiles * 1024] history row of the cell, or -1 (outflow stays in the stage)
     int32_t* inputs = nullptr;         // [ninputs] history row of the upstream cell of each edge into a stage
