@@ -127,6 +127,42 @@ struct KWConstFF {
 // after its first step, and its float-float steps cost a few multiplications.  The cell state is y
 // (float-float); the outflow passed downstream is Q = y^m.  P and M are compile-time p and m, or 0 to
 // take them from K.br at run time.
+// x^(p-1) and x^(m-1) from one chain of products (P, M compile-time, or 0 for run-time p, m <= 16).
+template <int P, int M>
+__device__ __forceinline__ void f_powers(float x, int p, int m, float& xp1, float& xm1)
+{
+    constexpr int kTop = P > 0 && M > 0 ? (P > M ? P : M) - 1 : 15;
+    const int top = max(p, m) - 1;
+    float r = 1.0f;
+    xp1 = 1.0f;
+    xm1 = 1.0f;
+#pragma unroll
+    for (int e = 1; e <= kTop; ++e) {
+        if (e > top) break;
+        r = e == 1 ? x : r * x;
+        if (e == p - 1) xp1 = r;
+        if (e == m - 1) xm1 = r;
+    }
+}
+
+// x^p and x^m in float-float for a float x, from one chain of float-float products by x.
+template <int P, int M>
+__device__ __forceinline__ void ff_powers_f(float x, int p, int m, ffloat& yp, ffloat& ym)
+{
+    constexpr int kTop = P > 0 && M > 0 ? (P > M ? P : M) : 16;
+    const int top = max(p, m);
+    ffloat r{x, 0.0f};
+    yp = r;
+    ym = r;
+#pragma unroll
+    for (int e = 2; e <= kTop; ++e) {
+        if (e > top) break;
+        r = e == 2 ? ff_prod(x, x) : ff_mul_f(r, x);
+        if (e == p) yp = r;
+        if (e == m) ym = r;
+    }
+}
+
 template <int P, int M>
 __device__ __forceinline__ ffloat kw_poly_g(ffloat y, float al, const ffloat& known, const KWConstFF& K)
 {
@@ -175,43 +211,52 @@ __device__ __forceinline__ ffloat kw_step_poly(ffloat up, bool nan, ffloat& y, f
         const ffloat known = ff_add_sloppy(ff_add_sloppy(ff_mul(K.k, up), ff_mul_f(ff_pow_n<P>(y, p), al)),
                                            ff_mul_f(K.dt, lat));
         const float kf = K.kf, knf = known.hi;
-        // float Newton to the float noise floor (~1e-7): it stops one step after a step below 3e-5
-        // relative, which quadratic convergence takes far below that floor.  It starts from the better
+        // Float Newton to the float noise floor: it stops after a step below 3e-5 relative, which leaves
+        // an error of about (3e-5)^2, far below that floor (quadratic convergence, g'' / g' ~ 1 / y).
+        // It starts from the previous state, or, when that is more than 1 % off in g, from the better
         // (smaller |g|) of the previous state and the reference's linearised guess (kinematic_wave.hpp:
         // 61-91) taken to the power 1/m: after a jump in upstream discharge the previous state can be
         // orders of magnitude off, and Newton on y^m closes such a gap only by a factor of about
         // (m - 1) / m per step.
         float x = y.hi;
         {
-            const float q0 = qprev_f, mean = 0.5f * (q0 + up.hi);
-            const float abpq = al * K.beta_f * __powf(mean, K.beta_f - 1.0f);
-            const float guess = __fdividef(kf * up.hi + abpq * q0 + K.dt.hi * lat, kf + abpq);
-            const float xg = guess > 0.0f ? __powf(guess, 1.0f / (float)m) : 0.0f;
-            const float ga = kf * f_pow_n<M>(x, m) + al * f_pow_n<P>(x, p) - knf;
-            const float gb = kf * f_pow_n<M>(xg, m) + al * f_pow_n<P>(xg, p) - knf;
-            if (xg > 0.0f && isfinite(gb) && fabsf(gb) < fabsf(ga)) x = xg;
+            float xm1, xp1;
+            f_powers<P, M>(x, p, m, xp1, xm1);
+            const float ga = kf * xm1 * x + al * xp1 * x - knf;
+            if (!(fabsf(ga) <= 0.01f * fabsf(knf))) {
+                const float q0 = qprev_f, mean = 0.5f * (q0 + up.hi);
+                const float abpq = al * K.beta_f * __powf(mean, K.beta_f - 1.0f);
+                const float guess = __fdividef(kf * up.hi + abpq * q0 + K.dt.hi * lat, kf + abpq);
+                const float xg = guess > 0.0f ? __powf(guess, 1.0f / (float)m) : 0.0f;
+                f_powers<P, M>(xg, p, m, xp1, xm1);
+                const float gb = kf * xm1 * xg + al * xp1 * xg - knf;
+                if (xg > 0.0f && isfinite(gb) && fabsf(gb) < fabsf(ga)) x = xg;
+            }
         }
         bool converged = false;
 #pragma unroll 1
         for (int it = 0; it < 24; ++it) {
-            const float xm1 = m > 1 ? f_pow_n<(M > 1 ? M - 1 : 0)>(x, m - 1) : 1.0f;
-            const float xp1 = p > 1 ? f_pow_n<(P > 1 ? P - 1 : 0)>(x, p - 1) : 1.0f;
+            float xm1, xp1;
+            f_powers<P, M>(x, p, m, xp1, xm1);
             const float g = kf * xm1 * x + al * xp1 * x - knf;
             const float dg = (float)m * kf * xm1 + (float)p * al * xp1;
             float nx = x - __fdividef(g, dg);
             if (!(nx > 0.0f)) nx = 0.5f * x;
             const float dxr = fabsf(nx - x);
             x = nx;
-            if (converged) break;
-            converged = dxr <= 3e-5f * x;
+            if (dxr <= 3e-5f * x) {
+                converged = true;
+                break;
+            }
         }
         if (converged && x > 1e-12f && x < 1e12f) {
             // one float-float Newton step from the float root x (1e-7 -> ~1e-14); the powers of x are
             // float-float products of floats, and Q = y^m moves with y to first order
-            const ffloat ym = ff_pow_n<M>(ffloat{x, 0.0f}, m), yp = ff_pow_n<P>(ffloat{x, 0.0f}, p);
+            ffloat yp, ym;
+            ff_powers_f<P, M>(x, p, m, yp, ym);
             const ffloat g = ff_add_sloppy(ff_add_sloppy(ff_mul(K.k, ym), ff_mul_f(yp, al)), ff_neg(known));
-            const float xm1 = m > 1 ? f_pow_n<(M > 1 ? M - 1 : 0)>(x, m - 1) : 1.0f;
-            const float xp1 = p > 1 ? f_pow_n<(P > 1 ? P - 1 : 0)>(x, p - 1) : 1.0f;
+            float xm1, xp1;
+            f_powers<P, M>(x, p, m, xp1, xm1);
             const float dg = (float)m * kf * xm1 + (float)p * al * xp1;
             const float delta = __fdividef(g.hi, dg);
             y = ff_two_sum(x, -delta);

@@ -753,6 +753,7 @@ void stage_core_free(StageCore* sc)
 // returns LUE_GPU_ETIMEDOUT.
 
 constexpr int kFlowPolls = 1 << 22;
+constexpr int kPublishEvery = 4;  // steps per publication of a stage's progress (a release fence each)
 
 struct StageRunArgs {
     const int4* stage;
@@ -773,8 +774,9 @@ struct StageFlowArgs {
     int* ticket;    // zeroed before the launch
     int* error;     // [1]
     int64_t nstages;
-    int polls;      // poll limit of one wait
-    int64_t stuck;  // test hook: the position of a stage whose first wait never ends (-1: none)
+    int polls;          // poll limit of one wait
+    int publish_every;  // steps between two publications of a stage's progress
+    int64_t stuck;      // test hook: the position of a stage whose first wait never ends (-1: none)
     unsigned long long* trace;  // [4 nstages] or null: start, rounds begin, time in waits, end (ns)
 };
 
@@ -983,8 +985,9 @@ __global__ void __launch_bounds__(NT) k_stage_flow(StageRunArgs a, StageFlowArgs
         // visible at GPU scope before the progress that announces them (the pattern of a grid barrier).
         __syncthreads();
         if (threadIdx.x == 0 && max_exit >= 0) {
+            // every publish_every steps (a release fence each time), and the last step
             const int prog = min(ns, max(0, r + 1 - max_exit));
-            if (prog > published) {
+            if (prog > published && (prog - published >= f.publish_every || prog == ns)) {
                 st_release(f.progress + k, prog);
                 published = prog;
             }
@@ -1340,7 +1343,8 @@ static int stage_run(lue_gpu_topology* t, const StageCore* sc, const R& rule, in
     StageRunArgs a{sc->stage, sc->wave_stage, sc->meta, sc->exit_id, sc->inputs, core->rows, core->cols, sc->tcols,
                    steps, t->stage_hist};
     StageFlowArgs fa{sc->prod_offsets, sc->prod, sc->max_exit_round, progress, ticket, error, sc->nstages,
-                     kFlowPolls, -1, nullptr};
+                     kFlowPolls, kPublishEvery, -1, nullptr};
+    if (const char* e = getenv("LUE_GB300_PUBLISH_EVERY")) fa.publish_every = std::max(1, atoi(e));
     // tracing (LUE_GB300_STAGE_TRACE=file): per stage in ticket order its start, the start of its rounds,
     // its time in waits and its end (globaltimer ns), then tile, cells, rounds and inputs, written after
     // the launch as int64 records of 8
