@@ -51,6 +51,8 @@ class Topology {
     Topology& operator=(const Topology&) = delete;
     ~Topology() { lue_gpu_topology_destroy(_h); }
     lue_gpu_topology* handle() const { return _h; }
+    // Builds now what the first stage-engine call would build (lue_gpu_topology_prepare).
+    void prepare(cudaStream_t stream) { check(lue_gpu_topology_prepare(_h, stream), "topology prepare"); }
 
    private:
     lue_gpu_topology* _h = nullptr;

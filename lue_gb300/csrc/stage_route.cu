@@ -1205,6 +1205,15 @@ __global__ void k_stage_no_data(const uint8_t* fd, int64_t n, T* out, T* rem)
 // Host
 // ---------------------------------------------------------------------------------------------------
 
+static int stage_core_get(lue_gpu_topology* t, cudaStream_t stream, const StageCore** out);
+
+int stage_prepare(lue_gpu_topology* t, cudaStream_t stream)
+{
+    const StageCore* sc = nullptr;
+    if (int rc = stage_core_get(t, stream, &sc)) return rc;
+    return cuda_status(cudaStreamSynchronize(stream), "topology_prepare");
+}
+
 // The stage topology of t, built on first use; nullptr when the engine does not apply.
 static int stage_core_get(lue_gpu_topology* t, cudaStream_t stream, const StageCore** out)
 {
@@ -1227,17 +1236,58 @@ static int stage_core_get(lue_gpu_topology* t, cudaStream_t stream, const StageC
     return LUE_GPU_OK;
 }
 
+// Per-handle buffers that grow with the calls come from a stream-ordered pool of the device that keeps
+// the memory it is given back (no release threshold): growing one waits for nothing but the handle's
+// own stream, and a freed block serves the next growth without a device-wide synchronisation.
+static cudaMemPool_t stage_pool()
+{
+    static std::mutex mu;
+    static cudaMemPool_t pools[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev < 0 || dev >= 64) return nullptr;
+    if (!pools[dev]) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        if (cudaMemPoolCreate(&pools[dev], &props) != cudaSuccess) {
+            pools[dev] = nullptr;
+            return nullptr;
+        }
+        unsigned long long keep = ~0ull;
+        cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    return pools[dev];
+}
+
+void stage_buffers_free(lue_gpu_topology* t)
+{
+    if (!t->stage_hist && !t->stage_flow) return;
+    cudaDeviceSynchronize();  // the handle's streams are unknown here: wait for all work
+    if (t->stage_hist) cudaFreeAsync(t->stage_hist, nullptr);
+    if (t->stage_flow) cudaFreeAsync(t->stage_flow, nullptr);
+    cudaStreamSynchronize(nullptr);
+    t->stage_hist = nullptr;
+    t->stage_flow = nullptr;
+    t->stage_hist_bytes = t->stage_flow_bytes = 0;
+    if (cudaMemPool_t pool = stage_pool()) cudaMemPoolTrimTo(pool, 0);
+}
+
 template <class T>
 static int grow(lue_gpu_topology* t, T*& p, size_t& have, size_t need, cudaStream_t stream, const char* what)
 {
     if (need <= have) return LUE_GPU_OK;
-    cudaStreamSynchronize(stream);  // the old buffer may still be in use
-    cudaFree(p);
+    (void)t;
+    cudaMemPool_t pool = stage_pool();
+    if (!pool) return fail(LUE_GPU_ECUDA, std::string(what) + ": no memory pool");
+    if (p) cudaFreeAsync(p, stream);  // after the stream's earlier uses of the buffer
     p = nullptr;
     have = 0;
-    if (int rc = cuda_status(cudaMalloc(&p, need), what)) return rc;
+    if (int rc = cuda_status(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&p), need, pool, stream), what))
+        return rc;
     have = need;
-    (void)t;
     return LUE_GPU_OK;
 }
 
@@ -1331,11 +1381,7 @@ static int stage_run(lue_gpu_topology* t, const StageCore* sc, const R& rule, in
     if (int rc = grow(t, t->stage_hist, t->stage_hist_bytes, hist, stream, what)) return rc;
     const size_t flow = (size_t)(sc->nstages + 2) * sizeof(int);
     if (int rc = grow(t, t->stage_flow, t->stage_flow_bytes, flow, stream, what)) return rc;
-    if (!t->stage_flow_error) {
-        if (int rc = cuda_status(cudaHostAlloc(&t->stage_flow_error, sizeof(int), cudaHostAllocDefault), what))
-            return rc;
-        *t->stage_flow_error = 0;
-    }
+    if (!t->stage_flow_error) return fail(LUE_GPU_ECUDA, std::string(what) + ": no error word");
     int* progress = t->stage_flow;
     int* ticket = progress + sc->nstages;
     int* error = ticket + 1;

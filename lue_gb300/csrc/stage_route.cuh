@@ -79,6 +79,11 @@ namespace lue_gb300 {
 // Routing on the stage engine.  *done is false when the engine does not apply to the topology (flow
 // cycles, or a raster beyond its limits): the caller then runs the walk engine.  rule: a value of Rule
 // (route_walk_visitors.cuh): 0 accu (float64 only), 1 threshold, 2 fraction, 3 capacity, 4 trigger.
+// Frees the handle's stage buffers (history, flow counters) back to their pool, after the work queued so
+// far on the default stream.
+void stage_buffers_free(lue_gpu_topology* t);
+// Builds the stage topology of t now (lue_gpu_topology_prepare).
+int stage_prepare(lue_gpu_topology* t, cudaStream_t stream);
 int stage_route_f32(lue_gpu_topology* t, int rule, const float* a, float as, const float* b, float bs, float* out,
                     float* rem, cudaStream_t stream, bool* done);
 int stage_route_f64(lue_gpu_topology* t, int rule, const double* a, double as, const double* b, double bs,

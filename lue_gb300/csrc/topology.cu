@@ -139,6 +139,10 @@ int allocate_scratch(lue_gpu_topology* t)
         return rc;
     }
     t->scratch_bytes = words_for(n) * 4 + n * (int64_t)sizeof(float);
+    // the stage engine's timeout flag, read by the host on the next call (pinned, written by a copy)
+    rc = cuda_status(cudaHostAlloc(&t->stage_flow_error, sizeof(int), cudaHostAllocDefault), "scratch flag");
+    if (rc) return rc;
+    *t->stage_flow_error = 0;
     if (t->core->tiles) {
         rc = tile_scratch_alloc(t->core->tiles, &t->tile_scratch);
         if (rc) return rc;
@@ -167,8 +171,7 @@ static void free_handle(lue_gpu_topology* t)
     cudaFree(t->lo);
     cudaFree(t->history);
     cudaFree(t->planes);
-    cudaFree(t->stage_hist);
-    cudaFree(t->stage_flow);
+    stage_buffers_free(t);
     cudaFreeHost(t->stage_flow_error);
     tile_scratch_free(&t->tile_scratch);
     if (t->core && --t->core->refs == 0) free_core(t->core);
@@ -295,6 +298,12 @@ extern "C" int lue_gpu_topology_clone(const lue_gpu_topology* topology, lue_gpu_
     }
     *clone = t;
     return LUE_GPU_OK;
+}
+
+extern "C" int lue_gpu_topology_prepare(lue_gpu_topology* topology, void* stream)
+{
+    if (!topology) return fail(LUE_GPU_EINVAL, "topology_prepare: NULL topology");
+    return stage_prepare(topology, (cudaStream_t)stream);
 }
 
 extern "C" int lue_gpu_topology_destroy(lue_gpu_topology* topology)

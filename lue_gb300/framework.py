@@ -83,6 +83,13 @@ class Topology:
         _lib.check(_lib.lib().lue_gpu_topology_clone(self.handle, ctypes.byref(h)))
         return Topology._from_handle(h, self.shape, self.device)
 
+    def prepare(self):
+        """Builds the structures that the first call of a stage-engine operation (accu_threshold,
+        accu_fraction, accu_capacity, accu_trigger, float64 accu, kinematic_wave) would build."""
+        import torch
+        _lib.check(_lib.lib().lue_gpu_topology_prepare(self.handle,
+                                                       torch.cuda.current_stream(self.device).cuda_stream))
+
     def stats(self):
         s = _lib.TopologyStats()
         _lib.check(_lib.lib().lue_gpu_topology_get_stats(self.handle, ctypes.byref(s)))

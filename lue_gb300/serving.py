@@ -83,12 +83,31 @@ class Server:
         self.torch, self.lfr, self.device = torch, lfr, torch.device(device)
         self.grids = [lfr.from_numpy(fd, device=self.device) for fd in pool_fds]
         self.topologies = [g.topology() for g in self.grids]
+        # everything a request would otherwise build or allocate on its first call: the stage
+        # structures of each grid, one handle (scratch) per grid, and pinned result buffers
         self.free_clones = collections.defaultdict(list)
+        for g, t in enumerate(self.topologies):
+            t.prepare()
+            self.free_clones[g].append(t.clone())
+        self._warm_pinned(slots)
         self.streams = [torch.cuda.Stream(self.device) for _ in range(slots)]
         free, _ = torch.cuda.mem_get_info(self.device)
         self.budget = int(free * hbm_fraction)
         self.in_use = 0
         torch.cuda.synchronize(self.device)
+
+    def _warm_pinned(self, slots):
+        """Fills the pinned host allocator's cache (sizes rounded up to powers of two) with enough result
+        buffers of each size class for the concurrent requests."""
+        torch = self.torch
+        sizes = set()
+        for g in self.grids:
+            n = int(np.prod(g.shape))
+            for b in (4 * n, 8 * n):
+                sizes.add(1 << (b - 1).bit_length())
+        per_class = max(1, slots // 4)
+        held = [torch.empty(s, dtype=torch.uint8, pin_memory=True) for s in sorted(sizes) for _ in range(per_class)]
+        del held
 
     def cells(self, r):
         return int(np.prod(self.grids[r.grid].shape))
