@@ -1236,9 +1236,8 @@ static int stage_core_get(lue_gpu_topology* t, cudaStream_t stream, const StageC
     return LUE_GPU_OK;
 }
 
-// Per-handle buffers that grow with the calls come from a stream-ordered pool of the device that keeps
-// the memory it is given back (no release threshold): growing one waits for nothing but the handle's
-// own stream, and a freed block serves the next growth without a device-wide synchronisation.
+// Per-handle buffers that grow with the calls come from a stream-ordered pool of the device: growing one
+// waits for nothing but the handle's own stream (no device-wide synchronisation, unlike cudaFree).
 static cudaMemPool_t stage_pool()
 {
     static std::mutex mu;
@@ -1282,11 +1281,23 @@ static int grow(lue_gpu_topology* t, T*& p, size_t& have, size_t need, cudaStrea
     (void)t;
     cudaMemPool_t pool = stage_pool();
     if (!pool) return fail(LUE_GPU_ECUDA, std::string(what) + ": no memory pool");
-    if (p) cudaFreeAsync(p, stream);  // after the stream's earlier uses of the buffer
+    if (p) {
+        // after the stream's earlier uses of the buffer; the pool then gives its memory back, so that a
+        // larger buffer can use it (a pool does not join a freed block to a new, larger one)
+        cudaFreeAsync(p, stream);
+        cudaStreamSynchronize(stream);
+        cudaMemPoolTrimTo(pool, 0);
+    }
     p = nullptr;
     have = 0;
-    if (int rc = cuda_status(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&p), need, pool, stream), what))
-        return rc;
+    const cudaError_t e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&p), need, pool, stream);
+    if (e != cudaSuccess) {
+        size_t free_b = 0, total_b = 0;
+        cudaMemGetInfo(&free_b, &total_b);
+        return fail(e == cudaErrorMemoryAllocation ? LUE_GPU_ENOMEM : LUE_GPU_ECUDA,
+                    std::string(what) + ": " + cudaGetErrorString(e) + " (" + std::to_string(need >> 20) +
+                        " MiB asked, " + std::to_string(free_b >> 20) + " MiB free)");
+    }
     have = need;
     return LUE_GPU_OK;
 }
