@@ -414,12 +414,27 @@ def bench_threshold(args, dev, fd_d, m_d, inputs):
     first_s = time.perf_counter() - t0
     calls = args.threshold_calls
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(calls):
-        flux, state = lfr.accu_threshold(fd_d, m_d, thr)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    s = e0.elapsed_time(e1) / 1000.0 / calls
+
+    def timed():
+        nonlocal flux, state
+        e0.record(stream)
+        for _ in range(calls):
+            flux, state = lfr.accu_threshold(fd_d, m_d, thr)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1000.0 / calls
+
+    default_schedule = fd_d.topology().stage_schedule()
+    s = s_default = timed()
+    tuned = None
+    if not args.no_autotune:
+        t0 = time.perf_counter()
+        best = lfr.autotune_stage_schedule(fd_d, lambda: lfr.accu_threshold(fd_d, m_d, thr))
+        tune_s = time.perf_counter() - t0
+        s = timed()
+        tuned = {"schedule": {k: best[k] for k in ("cap", "threads", "publish_every")},
+                 "tuner_ms_of_best": round(best["ms"], 3), "tuning_s": round(tune_s, 2),
+                 "ms_per_call": round(1000 * s, 3)}
     mask = outlet_mask(fd_d.data)
     total_in = float(m_d.data.double().sum())
     kept = float(state.data.double().sum())
@@ -429,7 +444,10 @@ def bench_threshold(args, dev, fd_d, m_d, inputs):
             "roofline_frac_hbm": round(THRESHOLD_BYTES_PER_CELL * n / s / 1e9 / peaks()[0], 4),
             "bytes_per_cell": THRESHOLD_BYTES_PER_CELL,
             "first_call_ms": round(1000 * first_s, 2),
-            "engine": "stage engine: 32 x 32 tiles cut into stages of at most 128 cells by crossing depth, one "
+            "default_schedule": {"schedule": default_schedule, "ms_per_call": round(1000 * s_default, 3)},
+            "autotuned": tuned,
+            "timed_schedule": "autotuned (lue_gpu_autotune_stage_schedule)" if tuned else "default",
+            "engine": "stage engine: 32 x 32 tiles cut into stages of at most `cap` cells by crossing depth, one "
                       "dataflow launch (lue_gpu_accu_threshold_f32)",
             "mass_balance": {"material_in": total_in, "kept_plus_outlet_flux": kept + left,
                              "rel_err": abs(kept + left - total_in) / total_in}}
@@ -457,11 +475,17 @@ def bench_kinematic_wave(args, dev):
     lfr.kinematic_wave_steps(fd, q, lat, alpha, 0.6, 3600.0, 100.0, T)  # builds the stages + history
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    out = lfr.kinematic_wave_steps(fd, q, lat, alpha, 0.6, 3600.0, 100.0, T)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    s_multi = e0.elapsed_time(e1) / 1000.0
+
+    def timed_multi():
+        e0.record(stream)
+        o = lfr.kinematic_wave_steps(fd, q, lat, alpha, 0.6, 3600.0, 100.0, T)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return o, e0.elapsed_time(e1) / 1000.0
+
+    default_schedule = fd.topology().stage_schedule()
+    out, s_multi = timed_multi()
+    s_default = s_multi
     single_steps = 3
     qq = q
     e0.record(stream)
@@ -470,11 +494,23 @@ def bench_kinematic_wave(args, dev):
     e1.record(stream)
     torch.cuda.synchronize()
     s_single = e0.elapsed_time(e1) / 1000.0 / single_steps
+    tuned = None
+    if not args.no_autotune:
+        t0 = time.perf_counter()
+        best = lfr.autotune_stage_schedule(fd, lambda: lfr.kinematic_wave_steps(fd, q, lat, alpha, 0.6, 3600.0, 100.0, T))
+        tune_s = time.perf_counter() - t0
+        out, s_multi = timed_multi()
+        tuned = {"schedule": {k: best[k] for k in ("cap", "threads", "publish_every")},
+                 "tuner_ms_of_best": round(best["ms"], 3), "tuning_s": round(tune_s, 2),
+                 "ms_per_step": round(1000 * s_multi / T, 3)}
     finite = torch.isfinite(out.data)
     return {"workload": "kw_8k (8192x8192, float64 discharge, float32 rain and alpha, beta 0.6, dt 3600 s, dx 100 m)",
             "steps": T, "ms_per_step": round(1000 * s_multi / T, 3),
             "value": round(n * T / s_multi / 1e6, 3), "unit": "Mcells/s",
             "roofline_frac_hbm": round(KW_BYTES_PER_CELL * n * T / s_multi / 1e9 / peaks()[0], 4),
+            "default_schedule": {"schedule": default_schedule, "ms_per_step": round(1000 * s_default / T, 3)},
+            "autotuned": tuned,
+            "timed_schedule": "autotuned (lue_gpu_autotune_stage_schedule)" if tuned else "default",
             "single_step_call_ms": round(1000 * s_single, 3),
             "single_step_call_mcells_per_s": round(n / s_single / 1e6, 3),
             "engine": "stage engine, pipelined steps, float-float solve in y = Q^(1/5) "
@@ -551,6 +587,7 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--serve-sequential", type=int, default=32)
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="time the stage legs with the default schedule only")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -111,6 +111,41 @@ int lue_gpu_topology_get_stats(const lue_gpu_topology* topology, lue_gpu_topolog
  * reference keeps no state between calls.) */
 int lue_gpu_topology_prepare(lue_gpu_topology* topology, void* stream);
 
+/* Schedule of the stage engine (accu_threshold, accu_fraction, accu_capacity, accu_trigger, float64 accu,
+ * kinematic_wave).  No reference counterpart: the reference's schedule is HPX's task order over its
+ * partitions.  Results do not depend on the schedule, only the time a call takes does.
+ *   cap            most cells of one stage (1..256, default 128).  It belongs to the stage structures,
+ *                  which the clones of a handle share: setting another cap frees them (they are rebuilt by
+ *                  the next call that needs them, after all work on the device) and is refused with
+ *                  LUE_GPU_EINVAL while clones exist.  0 keeps the current cap.
+ *   threads        threads per stage CTA: 32, 64, 128 or 256; 0 picks them by the largest stage.
+ *   publish_every  time steps between two publications of a stage's progress in multi-step calls
+ *                  (a release fence each); 0 is the default (4).
+ *   ms             lue_gpu_autotune_stage_schedule: measured time of one call with this schedule. */
+typedef struct lue_gpu_stage_schedule {
+    int32_t cap;
+    int32_t threads;
+    int32_t publish_every;
+    float ms;
+} lue_gpu_stage_schedule;
+int lue_gpu_topology_get_stage_schedule(const lue_gpu_topology* topology, lue_gpu_stage_schedule* schedule);
+int lue_gpu_topology_set_stage_schedule(lue_gpu_topology* topology, const lue_gpu_stage_schedule* schedule);
+
+/* A call to time: issues one routing call on `topology` on `stream` and returns its status. */
+typedef int (*lue_gpu_stage_call)(lue_gpu_topology* topology, void* user, void* stream);
+
+/* Autotuner of the stage schedule (no reference counterpart).  Times `call` (CUDA events on `stream`,
+ * after one untimed run per candidate, which builds the stage structures of a new cap) for candidate
+ * schedules: stage
+ * caps 64, 128 and 256, then publication intervals 1, 2, 4 and 8 with the best cap, then 32, 64 and 128
+ * threads per stage with the best of those.  Each timing is the mean of `repeats` calls (>= 1).  The
+ * fastest schedule stays set on the handle and is returned in *best.  When clones share the stage
+ * structures, the cap is not changed.  Synchronous: returns when the timings are done.  The outputs of
+ * `call` hold its last run, which is the same for every schedule.  A failing call ends the tuning with its
+ * status and the schedule the handle had before. */
+int lue_gpu_autotune_stage_schedule(lue_gpu_topology* topology, lue_gpu_stage_call call, void* user, int repeats,
+                                    void* stream, lue_gpu_stage_schedule* best);
+
 /* inflow_count<uint8>(DefaultValuePolicies, fd): number of neighbours draining into each cell,
  * 255 where the flow direction is no-data.  value_policies = 0 gives DefaultPolicies (255 is an
  * unknown code, i.e. a sink; definition/inflow_count.hpp:9-15). */

@@ -28,6 +28,17 @@ class TopologyStats(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class StageSchedule(ctypes.Structure):
+    _fields_ = [("cap", ctypes.c_int32), ("threads", ctypes.c_int32), ("publish_every", ctypes.c_int32),
+                ("ms", ctypes.c_float)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+# int (*)(lue_gpu_topology*, void* user, void* stream): one routing call for the autotuner to time
+STAGE_CALL = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p)
+
 _lib = None
 
 
@@ -73,6 +84,9 @@ def _declare(L):
         "lue_gpu_downstream_distance_f64": ([p, i64, i64, d, p, p], i32),
         "lue_gpu_d8_flow_direction_f32": ([p, i64, i64, p, p], i32),
         "lue_gpu_d8_flow_direction_f64": ([p, i64, i64, p, p], i32),
+        "lue_gpu_topology_get_stage_schedule": ([p, ctypes.POINTER(StageSchedule)], i32),
+        "lue_gpu_topology_set_stage_schedule": ([p, ctypes.POINTER(StageSchedule)], i32),
+        "lue_gpu_autotune_stage_schedule": ([p, STAGE_CALL, p, i32, p, ctypes.POINTER(StageSchedule)], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)

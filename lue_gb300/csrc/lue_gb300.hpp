@@ -15,6 +15,7 @@
 
 #include <array>
 #include <cstdint>
+#include <exception>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -53,6 +54,45 @@ class Topology {
     lue_gpu_topology* handle() const { return _h; }
     // Builds now what the first stage-engine call would build (lue_gpu_topology_prepare).
     void prepare(cudaStream_t stream) { check(lue_gpu_topology_prepare(_h, stream), "topology prepare"); }
+
+    // The stage engine's schedule (lue_gpu_topology_{get,set}_stage_schedule); results do not depend on it.
+    lue_gpu_stage_schedule stage_schedule() const
+    {
+        lue_gpu_stage_schedule s{};
+        check(lue_gpu_topology_get_stage_schedule(_h, &s), "stage_schedule");
+        return s;
+    }
+    void set_stage_schedule(const lue_gpu_stage_schedule& s)
+    {
+        check(lue_gpu_topology_set_stage_schedule(_h, &s), "set_stage_schedule");
+    }
+
+    // Autotunes the stage schedule for `call`, a callable that issues one routing call over this topology on
+    // `stream`; keeps the fastest schedule and returns it (lue_gpu_autotune_stage_schedule).  An exception
+    // thrown by `call` ends the tuning and is rethrown.
+    template <typename Call>
+    lue_gpu_stage_schedule autotune_stage_schedule(Call&& call, cudaStream_t stream, int repeats = 1)
+    {
+        struct Context {
+            std::remove_reference_t<Call>* call;
+            std::exception_ptr error;
+        } ctx{&call, nullptr};
+        lue_gpu_stage_call trampoline = [](lue_gpu_topology*, void* user, void*) -> int {
+            auto* c = static_cast<Context*>(user);
+            try {
+                (*c->call)();
+                return LUE_GPU_OK;
+            } catch (...) {
+                c->error = std::current_exception();
+                return LUE_GPU_EINVAL;
+            }
+        };
+        lue_gpu_stage_schedule best{};
+        const int rc = lue_gpu_autotune_stage_schedule(_h, trampoline, &ctx, repeats, stream, &best);
+        if (ctx.error) std::rethrow_exception(ctx.error);
+        check(rc, "autotune_stage_schedule");
+        return best;
+    }
 
    private:
     lue_gpu_topology* _h = nullptr;

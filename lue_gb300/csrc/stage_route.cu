@@ -457,7 +457,8 @@ int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stre
     const int64_t n = core->n, rows = core->rows, cols = core->cols;
     auto* sc = new (std::nothrow) StageCore();
     if (!sc) return fail(LUE_GPU_ENOMEM, "stage topology: host allocation");
-    if (const char* e = getenv("LUE_GB300_STAGE_CAP")) sc->cap = std::max(1, std::min(kStageMaxCap, atoi(e)));
+    if (core->stage_cap > 0) sc->cap = std::min(kStageMaxCap, core->stage_cap);
+    else if (const char* e = getenv("LUE_GB300_STAGE_CAP")) sc->cap = std::max(1, std::min(kStageMaxCap, atoi(e)));
     sc->trows = div_up(rows, kStageSide);
     sc->tcols = div_up(cols, kStageSide);
     sc->ntiles = sc->trows * sc->tcols;
@@ -1236,6 +1237,58 @@ static int stage_core_get(lue_gpu_topology* t, cudaStream_t stream, const StageC
     return LUE_GPU_OK;
 }
 
+// The stage cap the stage structures of t have (when built) or will be built with.
+static int effective_cap(const TopologyCore* core)
+{
+    if (core->stages) return core->stages->cap;
+    if (core->stage_cap > 0) return core->stage_cap;
+    if (const char* e = getenv("LUE_GB300_STAGE_CAP")) return std::max(1, std::min(kStageMaxCap, atoi(e)));
+    return kStageCap;
+}
+
+void stage_schedule_get(const lue_gpu_topology* t, int* cap, int* threads, int* publish_every)
+{
+    *cap = effective_cap(t->core);
+    *threads = t->stage_threads;
+    if (!*threads)
+        if (const char* e = getenv("LUE_GB300_STAGE_THREADS")) *threads = atoi(e);
+    *publish_every = t->publish_every;
+    if (!*publish_every) {
+        *publish_every = kPublishEvery;
+        if (const char* e = getenv("LUE_GB300_PUBLISH_EVERY")) *publish_every = std::max(1, atoi(e));
+    }
+}
+
+int stage_schedule_set(lue_gpu_topology* t, int cap, int threads, int publish_every)
+{
+    if (cap < 0 || cap > kStageMaxCap)
+        return fail(LUE_GPU_EINVAL, "stage schedule: cap must be 0 (keep) or 1.." + std::to_string(kStageMaxCap));
+    if (threads != 0 && threads != 32 && threads != 64 && threads != 128 && threads != 256)
+        return fail(LUE_GPU_EINVAL, "stage schedule: threads must be 0 (by stage size), 32, 64, 128 or 256");
+    if (publish_every < 0) return fail(LUE_GPU_EINVAL, "stage schedule: publish_every must be >= 0");
+    TopologyCore* core = t->core;
+    if (cap > 0) {
+        std::lock_guard<std::mutex> lock(core->stage_mutex);
+        if (cap != effective_cap(core)) {
+            if (core->refs.load() > 1)
+                return fail(LUE_GPU_EINVAL, "stage schedule: the stage structures are shared with " +
+                                                std::to_string(core->refs.load() - 1) +
+                                                " clone(s); change the cap before cloning");
+            if (core->stages) {
+                // the handle's streams are unknown here: wait for all work before the structures go
+                if (int rc = cuda_status(cudaDeviceSynchronize(), "stage schedule")) return rc;
+                core->bytes -= core->stages->bytes;
+                stage_core_free(core->stages);
+                core->stages = nullptr;
+            }
+            core->stage_cap = cap;  // rebuilt with it by the next call that needs them
+        }
+    }
+    t->stage_threads = threads;
+    t->publish_every = publish_every;
+    return LUE_GPU_OK;
+}
+
 // Per-handle buffers that grow with the calls come from a stream-ordered pool of the device: growing one
 // waits for nothing but the handle's own stream (no device-wide synchronisation, unlike cudaFree).
 static cudaMemPool_t stage_pool()
@@ -1360,13 +1413,16 @@ static int launch_flow(const StageRunArgs& a, const StageFlowArgs& fa, const R& 
     return LUE_GPU_OK;
 }
 
-// Threads per stage: LUE_GB300_STAGE_THREADS (32, 64, 128 or 256), else by the largest stage.
+// Threads per stage: the handle's schedule (`threads`, 32, 64, 128 or 256), else LUE_GB300_STAGE_THREADS,
+// else by the largest stage.  Every loop of k_stage_flow strides by the CTA size, so any of them is valid
+// for any stage size.
 template <class R, bool ONE>
 static int launch_flow(const StageRunArgs& a, const StageFlowArgs& fa, const R& rule, unsigned blocks,
-                       int64_t max_cells, size_t smem, cudaStream_t stream, const char* what)
+                       int64_t max_cells, size_t smem, int threads, cudaStream_t stream, const char* what)
 {
     int nt = max_cells <= 128 ? 32 : max_cells <= 256 ? 64 : kStageThreads;
-    if (const char* e = getenv("LUE_GB300_STAGE_THREADS")) nt = atoi(e);
+    if (threads > 0) nt = threads;
+    else if (const char* e = getenv("LUE_GB300_STAGE_THREADS")) nt = atoi(e);
     switch (nt) {
         case 32: return launch_flow<R, 32, ONE>(a, fa, rule, blocks, smem, stream, what);
         case 64: return launch_flow<R, 64, ONE>(a, fa, rule, blocks, smem, stream, what);
@@ -1401,7 +1457,8 @@ static int stage_run(lue_gpu_topology* t, const StageCore* sc, const R& rule, in
                    steps, t->stage_hist};
     StageFlowArgs fa{sc->prod_offsets, sc->prod, sc->max_exit_round, progress, ticket, error, sc->nstages,
                      kFlowPolls, kPublishEvery, -1, nullptr};
-    if (const char* e = getenv("LUE_GB300_PUBLISH_EVERY")) fa.publish_every = std::max(1, atoi(e));
+    if (t->publish_every > 0) fa.publish_every = t->publish_every;
+    else if (const char* e = getenv("LUE_GB300_PUBLISH_EVERY")) fa.publish_every = std::max(1, atoi(e));
     // tracing (LUE_GB300_STAGE_TRACE=file): per stage in ticket order its start, the start of its rounds,
     // its time in waits and its end (globaltimer ns), then tile, cells, rounds and inputs, written after
     // the launch as int64 records of 8
@@ -1420,8 +1477,8 @@ static int stage_run(lue_gpu_topology* t, const StageCore* sc, const R& rule, in
     if (getenv("LUE_GB300_VERBOSE"))
         fprintf(stderr, "%s: dataflow launch of %u stages, largest %lld cells, %zu B shared memory\n", what, blocks,
                 (long long)mc, smem);
-    if (int rc = steps == 1 ? launch_flow<R, true>(a, fa, rule, blocks, mc, smem, stream, what)
-                            : launch_flow<R, false>(a, fa, rule, blocks, mc, smem, stream, what))
+    if (int rc = steps == 1 ? launch_flow<R, true>(a, fa, rule, blocks, mc, smem, t->stage_threads, stream, what)
+                            : launch_flow<R, false>(a, fa, rule, blocks, mc, smem, t->stage_threads, stream, what))
         return rc;
     const int64_t n = core->n;
     k_invalidate_if<typename R::Out><<<grid_for(n, 256), 256, 0, stream>>>(error, rule.out_raster(), rule.rem_raster(),

@@ -84,6 +84,11 @@ namespace lue_gb300 {
 void stage_buffers_free(lue_gpu_topology* t);
 // Builds the stage topology of t now (lue_gpu_topology_prepare).
 int stage_prepare(lue_gpu_topology* t, cudaStream_t stream);
+// Schedule of the stage engine for handle t: the cap of the shared stage structures and the handle's
+// threads per stage CTA and steps per progress publication (lue_gpu_topology_{get,set}_stage_schedule).
+// Setting another cap frees the stage structures (rebuilt by the next call); refused while clones share them.
+void stage_schedule_get(const lue_gpu_topology* t, int* cap, int* threads, int* publish_every);
+int stage_schedule_set(lue_gpu_topology* t, int cap, int threads, int publish_every);
 int stage_route_f32(lue_gpu_topology* t, int rule, const float* a, float as, const float* b, float bs, float* out,
                     float* rem, cudaStream_t stream, bool* done);
 int stage_route_f64(lue_gpu_topology* t, int rule, const double* a, double as, const double* b, double bs,

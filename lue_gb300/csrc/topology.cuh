@@ -21,6 +21,7 @@ struct TopologyCore {
     int32_t* order = nullptr;   // valid cells sorted by downstream level (built on first multi-step call)
     std::vector<int32_t> level_offsets;  // [levels + 1] start of each level in `order`
     StageCore* stages = nullptr;         // stage engine (acyclic rasters; built on first use)
+    int stage_cap = 0;                   // most cells of one stage when built (0: LUE_GB300_STAGE_CAP or 128)
     bool stages_unavailable = false;     // the raster is beyond the stage engine's limits
     std::mutex stage_mutex;              // guards the first build (clones share the core)
     lue_gpu_topology_stats stats{};
@@ -44,6 +45,8 @@ struct lue_gpu_topology {
     int* stage_flow = nullptr;       // stage engine, dataflow mode: per-stage progress, ticket and error flag
     size_t stage_flow_bytes = 0;
     int* stage_flow_error = nullptr; // pinned: the error flag of the last dataflow launch, read by the next call
+    int stage_threads = 0;           // stage engine: threads per stage CTA (0: LUE_GB300_STAGE_THREADS or by size)
+    int publish_every = 0;           // stage engine: steps per progress publication (0: LUE_GB300_PUBLISH_EVERY or 4)
     int64_t scratch_bytes = 0;
 };
 

@@ -63,6 +63,15 @@ int main()
         } catch (const std::runtime_error&) {
             std::printf("shape mismatch rejected\n");
         }
+
+        // the stage schedule autotuned for this accu_threshold call; the result stays the same
+        auto tuned = fd.topology().autotune_stage_schedule(
+            [&] { flux = std::get<0>(value_policies::accu_threshold<float>(fd, in, Scalar<float>{1.5f})); }, nullptr);
+        flux.to_host(f.data());
+        for (float v : f) std::printf("%g ", v);
+        std::printf("\n");
+        std::printf("schedule cap %d threads %d publish_every %d ms %g\n", tuned.cap, tuned.threads,
+                    tuned.publish_every, tuned.ms);
     } catch (const std::exception& ex) {
         std::fprintf(stderr, "error: %s\n", ex.what());
         return 2;

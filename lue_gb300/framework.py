@@ -90,6 +90,22 @@ class Topology:
         _lib.check(_lib.lib().lue_gpu_topology_prepare(self.handle,
                                                        torch.cuda.current_stream(self.device).cuda_stream))
 
+    def stage_schedule(self):
+        """The stage engine's schedule for this handle: {cap, threads, publish_every} (threads 0: by the
+        largest stage)."""
+        s = _lib.StageSchedule()
+        _lib.check(_lib.lib().lue_gpu_topology_get_stage_schedule(self.handle, ctypes.byref(s)))
+        d = s.as_dict()
+        del d["ms"]
+        return d
+
+    def set_stage_schedule(self, cap=0, threads=0, publish_every=0):
+        """Sets the stage engine's schedule (0 keeps the cap / picks threads by stage size / default
+        publication interval).  Results do not depend on it.  Another cap is refused while clones share
+        the stage structures."""
+        s = _lib.StageSchedule(int(cap), int(threads), int(publish_every), 0.0)
+        _lib.check(_lib.lib().lue_gpu_topology_set_stage_schedule(self.handle, ctypes.byref(s)))
+
     def stats(self):
         s = _lib.TopologyStats()
         _lib.check(_lib.lib().lue_gpu_topology_get_stats(self.handle, ctypes.byref(s)))
@@ -335,3 +351,34 @@ def kinematic_wave_steps(flow_direction, current_outflow, inflow, alpha, beta, t
         out.data_ptr(), _stream(flow_direction.data)))
     del kq, kl, ka
     return PartitionedArray(out, flow_direction.partition_shape)
+
+
+def autotune_stage_schedule(flow_direction, call, repeats=1):
+    """Autotunes the stage engine's schedule of `flow_direction`'s topology for `call`, a callable without
+    arguments that issues one routing call over `flow_direction` (for example
+    ``lambda: accu_threshold(fd, material, threshold)``) on torch's current stream.  The native tuner
+    (lue_gpu_autotune_stage_schedule) times it with CUDA events for candidate stage caps, publication
+    intervals and CTA sizes, keeps the fastest schedule on the topology and returns it as
+    {cap, threads, publish_every, ms}.  Results do not depend on the schedule."""
+    t = flow_direction.topology()
+    errors = []
+
+    def trampoline(handle, user, stream):
+        try:
+            call()
+            return 0
+        except _lib.LueGpuError as e:
+            errors.append(e)
+            return e.status
+        except Exception as e:  # noqa: BLE001  (re-raised below, after the native tuner returns)
+            errors.append(e)
+            return 1
+
+    cb = _lib.STAGE_CALL(trampoline)
+    best = _lib.StageSchedule()
+    status = _lib.lib().lue_gpu_autotune_stage_schedule(t.handle, cb, None, int(repeats),
+                                                        _stream(flow_direction.data), ctypes.byref(best))
+    if errors and not isinstance(errors[0], _lib.LueGpuError):
+        raise errors[0]
+    _lib.check(status)
+    return best.as_dict()

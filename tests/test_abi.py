@@ -52,3 +52,13 @@ def test_bad_arguments_fail_without_touching_the_gpu():
     assert rc == 1
     assert L.lue_gpu_accu_f32(None, None, 1.0, None, None) == 1
     assert L.lue_gpu_topology_destroy(None) == 1
+
+
+def test_schedule_and_autotune_entry_points_reject_bad_arguments_without_a_gpu():
+    L = _lib.lib()
+    s = _lib.StageSchedule()
+    assert L.lue_gpu_topology_get_stage_schedule(None, ctypes.byref(s)) == 1
+    assert L.lue_gpu_topology_set_stage_schedule(None, ctypes.byref(s)) == 1
+    cb = _lib.STAGE_CALL(lambda handle, user, stream: 0)
+    assert L.lue_gpu_autotune_stage_schedule(None, cb, None, 1, None, ctypes.byref(s)) == 1
+    assert b"NULL" in L.lue_gpu_last_error()

@@ -39,3 +39,6 @@ def test_cpp_mirror_known_answers():
     # printed with %g: six significant digits
     np.testing.assert_allclose(rows[6], oracle.downstream_distance(fd, 2.0, np.float32), rtol=1e-5)
     assert lines[10] == "shape mismatch rejected"
+    # accu_threshold again after the stage schedule was autotuned for it: the same flux
+    assert lines[11].split() == lines[1].split()
+    assert lines[12].startswith("schedule cap ")
