@@ -424,31 +424,44 @@ def bench_threshold(args, dev, fd_d, m_d, inputs):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / 1000.0 / calls
 
-    default_schedule = fd_d.topology().stage_schedule()
-    s = s_default = timed()
-    tuned = None
-    if not args.no_autotune:
-        t0 = time.perf_counter()
-        best = lfr.autotune_stage_schedule(fd_d, lambda: lfr.accu_threshold(fd_d, m_d, thr))
-        tune_s = time.perf_counter() - t0
-        s = timed()
-        tuned = {"schedule": {k: best[k] for k in ("cap", "threads", "publish_every")},
-                 "tuner_ms_of_best": round(best["ms"], 3), "tuning_s": round(tune_s, 2),
-                 "ms_per_call": round(1000 * s, 3)}
+    s = timed()  # the path engine
     mask = outlet_mask(fd_d.data)
     total_in = float(m_d.data.double().sum())
     kept = float(state.data.double().sum())
     left = float(flux.data.double()[mask].sum())
+    # the stage engine on the same call, with its default and its autotuned schedule
+    stage = None
+    if args.stage_compare:
+        os.environ["LUE_GB300_ENGINE"] = "stage"
+        try:
+            t0 = time.perf_counter()
+            lfr.accu_threshold(fd_d, m_d, thr)  # builds the stages
+            torch.cuda.synchronize()
+            stage_first = time.perf_counter() - t0
+            default_schedule = fd_d.topology().stage_schedule()
+            s_default = timed()
+            tuned = None
+            if not args.no_autotune:
+                t0 = time.perf_counter()
+                best = lfr.autotune_stage_schedule(fd_d, lambda: lfr.accu_threshold(fd_d, m_d, thr))
+                tune_s = time.perf_counter() - t0
+                tuned = {"schedule": {k: best[k] for k in ("cap", "threads", "publish_every")},
+                         "tuner_ms_of_best": round(best["ms"], 3), "tuning_s": round(tune_s, 2),
+                         "ms_per_call": round(1000 * timed(), 3)}
+            stage = {"engine": "stage engine: 32 x 32 tiles cut into stages of at most `cap` cells by crossing "
+                               "depth, one dataflow launch", "first_call_ms": round(1000 * stage_first, 2),
+                     "default_schedule": {"schedule": default_schedule, "ms_per_call": round(1000 * s_default, 3)},
+                     "autotuned": tuned}
+        finally:
+            del os.environ["LUE_GB300_ENGINE"]
     return {"workload": f"accu_16k raster and material, threshold uniform [0, 0.5) float32 ({rows}x{cols})",
             "calls": calls, "ms_per_call": round(1000 * s, 3), "value": round(n / s / 1e6, 3), "unit": "Mcells/s",
             "roofline_frac_hbm": round(THRESHOLD_BYTES_PER_CELL * n / s / 1e9 / peaks()[0], 4),
             "bytes_per_cell": THRESHOLD_BYTES_PER_CELL,
             "first_call_ms": round(1000 * first_s, 2),
-            "default_schedule": {"schedule": default_schedule, "ms_per_call": round(1000 * s_default, 3)},
-            "autotuned": tuned,
-            "timed_schedule": "autotuned (lue_gpu_autotune_stage_schedule)" if tuned else "default",
-            "engine": "stage engine: 32 x 32 tiles cut into stages of at most `cap` cells by crossing depth, one "
-                      "dataflow launch (lue_gpu_accu_threshold_f32)",
+            "engine": "path engine: heavy paths of the flow forest, level by level, one float-float prefix scan "
+                      "of the cells' max-plus maps per level (lue_gpu_accu_threshold_f32)",
+            "stage_engine": stage,
             "mass_balance": {"material_in": total_in, "kept_plus_outlet_flux": kept + left,
                              "rel_err": abs(kept + left - total_in) / total_in}}
 
@@ -588,6 +601,8 @@ def main():
     ap.add_argument("--serve-sequential", type=int, default=32)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="time the stage legs with the default schedule only")
+    ap.add_argument("--no-stage-compare", dest="stage_compare", action="store_false",
+                    help="do not time accu_threshold on the stage engine beside the path engine")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -1,0 +1,746 @@
+// path_route.cu — the path engine (see path_route.cuh): heavy-path layout of the flow forest, built once
+// per raster, and accu_threshold / accu_capacity (float32) as one prefix scan per path level.
+#include <algorithm>
+#include <cmath>
+#include <string>
+
+#include "route_walk_visitors.cuh"
+#include "topology.cuh"
+
+namespace lue_gb300 {
+
+// ---------------------------------------------------------------------------------------------------
+// Build
+// ---------------------------------------------------------------------------------------------------
+
+// Upstream-first walk: per cell the cells upstream of it (itself included), its heavy upstream neighbour
+// (the one with most cells upstream, the first in neighbour order on ties; 8: none), the cells above it
+// on its path, and its path level (the largest number of light edges on a flow path ending at it).
+struct PathVisitor {
+    const uint8_t* upmask;
+    int32_t* size;
+    int32_t* dtop;
+    int32_t* plev;
+    int32_t* heavy;
+    int64_t cols;
+    __device__ void enter(int64_t c)
+    {
+        const unsigned m = __ldg(upmask + c);
+        int32_t sz = 1, best = -1;
+        int hk = 8;
+        for (unsigned mm = m; mm; mm &= mm - 1) {
+            const int k = __ffs(mm) - 1;
+            const int32_t s = load_cg(size + c + nb_dr(k) * cols + nb_dc(k));
+            sz += s;
+            if (s > best) {
+                best = s;
+                hk = k;
+            }
+        }
+        int32_t lv = 0, dt = 0;
+        for (unsigned mm = m; mm; mm &= mm - 1) {
+            const int k = __ffs(mm) - 1;
+            const int64_t u = c + nb_dr(k) * cols + nb_dc(k);
+            const int32_t l = load_cg(plev + u);
+            if (k == hk) {
+                lv = max(lv, l);
+                dt = load_cg(dtop + u) + 1;
+            } else {
+                lv = max(lv, l + 1);
+            }
+        }
+        size[c] = sz;
+        plev[c] = lv;
+        dtop[c] = dt;
+        heavy[c] = hk;
+    }
+    __device__ void no_data(int64_t) {}
+};
+
+// Neighbour slot k of a cell's upstream neighbour that drains into it with D8 code `code`.
+__device__ __forceinline__ int inflow_slot(uint8_t code)
+{
+    switch (code) {
+        case 3: return 0;
+        case 2: return 1;
+        case 1: return 2;
+        case 6: return 3;
+        case 4: return 4;
+        case 9: return 5;
+        case 8: return 6;
+        case 7: return 7;
+        default: return -1;
+    }
+}
+
+__global__ void k_fill(int32_t* p, int64_t n, int32_t v)
+{
+    for (int64_t i = grid_stride_begin(); i < n; i += grid_stride()) p[i] = v;
+}
+
+// next[c]: the cell below c on its path (c itself at the bottom), -1 for no-data.
+__global__ void k_path_next(const uint8_t* fd, const int32_t* heavy, int64_t rows, int64_t cols, int64_t n,
+                            int32_t* next)
+{
+    for (int64_t c = grid_stride_begin(); c < n; c += grid_stride()) {
+        const uint8_t code = __ldg(fd + c);
+        if (code == kNoData) {
+            next[c] = -1;
+            continue;
+        }
+        const int64_t r = c / cols, col = c - r * cols;
+        int64_t d = 0;
+        int32_t v = (int32_t)c;
+        if (downstream(code, r, col, rows, cols, d) && __ldg(fd + d) != kNoData && heavy[d] == inflow_slot(code))
+            v = (int32_t)d;
+        next[c] = v;
+    }
+}
+
+// One round of pointer jumping: next[c] = next[next[c]] (in place: a value read from a cell that has
+// already jumped this round is still a cell of the same path, at or above the bottom).
+__global__ void k_path_jump(int32_t* next, int64_t n)
+{
+    for (int64_t c = grid_stride_begin(); c < n; c += grid_stride()) {
+        const int32_t v = next[c];
+        if (v >= 0) next[c] = next[v];
+    }
+}
+
+// key[c] = path level of c if c is the bottom of its path, else 255; stats: [0] largest level,
+// [1] longest path, [2] cells whose next is not a bottom (must be 0).
+__global__ void k_path_keys(const int32_t* next, const int32_t* plev, const int32_t* dtop, int64_t n, uint8_t* key,
+                            int* stats)
+{
+    int lmax = -1, longest = 0, bad = 0;
+    for (int64_t c = grid_stride_begin(); c < n; c += grid_stride()) {
+        const int32_t v = next[c];
+        uint8_t k = 255;
+        if (v >= 0) {
+            if (next[v] != v) ++bad;
+            if (v == c) {
+                const int l = plev[c];
+                k = (uint8_t)min(l, 254);
+                lmax = max(lmax, l);
+                longest = max(longest, dtop[c] + 1);
+            }
+        }
+        key[c] = k;
+    }
+    if (lmax >= 0) atomicMax(stats, lmax);
+    if (longest) atomicMax(stats + 1, longest);
+    if (bad) atomicAdd(stats + 2, bad);
+}
+
+constexpr int kCompactPer = 32;                          // cells per thread
+constexpr int kCompactCells = 256 * kCompactPer;         // cells per CTA
+
+template <int NT>
+__device__ __forceinline__ long long block_excl_sum(long long v, long long* s_warp, long long& total)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    long long x = v;
+    for (int d = 1; d < 32; d <<= 1) {
+        const long long y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= d) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        long long w = lane < NT / 32 ? s_warp[lane] : 0;
+        for (int d = 1; d < 32; d <<= 1) {
+            const long long y = __shfl_up_sync(0xffffffffu, w, d);
+            if (lane >= d) w += y;
+        }
+        if (lane < NT / 32) s_warp[lane] = w;
+    }
+    __syncthreads();
+    total = s_warp[NT / 32 - 1];
+    const long long before = warp ? s_warp[warp - 1] : 0;
+    __syncthreads();
+    return before + x - v;
+}
+
+// Per CTA of cells: the positions taken by the paths of level `lvl` whose bottom lies in it.
+__global__ void __launch_bounds__(256) k_level_sums(const uint8_t* key, const int32_t* dtop, int lvl, int64_t n,
+                                                    long long* bsum)
+{
+    __shared__ long long s_warp[8];
+    const int64_t c0 = (int64_t)blockIdx.x * kCompactCells + (int64_t)threadIdx.x * kCompactPer;
+    long long s = 0;
+    for (int j = 0; j < kCompactPer; ++j) {
+        const int64_t c = c0 + j;
+        if (c < n && key[c] == lvl) s += dtop[c] + 1;
+    }
+    long long total = 0;
+    block_excl_sum<256>(s, s_warp, total);
+    if (threadIdx.x == 0) bsum[blockIdx.x] = total;
+}
+
+// Exclusive scan of the per-CTA sums of one level, after the positions of the lower levels
+// (running[0]); offsets[lvl + 1] = running[0] afterwards.
+__global__ void __launch_bounds__(1024) k_level_scan(long long* bsum, int64_t nblk, long long* running,
+                                                     long long* offsets, int lvl)
+{
+    __shared__ long long s_warp[32];
+    const int64_t per = (nblk + 1023) / 1024;
+    const int64_t b0 = (int64_t)threadIdx.x * per, b1 = min(nblk, b0 + per);
+    long long s = 0;
+    for (int64_t b = b0; b < b1; ++b) s += bsum[b];
+    long long total = 0;
+    long long x = block_excl_sum<1024>(s, s_warp, total) + running[0];
+    for (int64_t b = b0; b < b1; ++b) {
+        const long long v = bsum[b];
+        bsum[b] = x;
+        x += v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        offsets[lvl] = running[0];
+        running[0] += total;
+        offsets[lvl + 1] = running[0];
+    }
+}
+
+// base[b]: first position of the path whose bottom is b (paths of one level in cell order of bottoms).
+__global__ void __launch_bounds__(256) k_level_assign(const uint8_t* key, const int32_t* dtop, int lvl, int64_t n,
+                                                      const long long* bsum, int32_t* base)
+{
+    __shared__ long long s_warp[8];
+    const int64_t c0 = (int64_t)blockIdx.x * kCompactCells + (int64_t)threadIdx.x * kCompactPer;
+    long long s = 0;
+    for (int j = 0; j < kCompactPer; ++j) {
+        const int64_t c = c0 + j;
+        if (c < n && key[c] == lvl) s += dtop[c] + 1;
+    }
+    long long total = 0;
+    long long x = block_excl_sum<256>(s, s_warp, total) + bsum[blockIdx.x];
+    for (int j = 0; j < kCompactPer; ++j) {
+        const int64_t c = c0 + j;
+        if (c < n && key[c] == lvl) {
+            base[c] = (int32_t)x;
+            x += dtop[c] + 1;
+        }
+    }
+}
+
+// order / light by position (order starts as all ones: no cell).  bad counts positions outside
+// [0, npos) and positions written twice; the build then fails instead of handing on a wrong layout.
+__global__ void k_path_place(const int32_t* next, const int32_t* base, const int32_t* dtop, const int32_t* heavy,
+                             const uint8_t* upmask, int64_t n, int64_t npos, int32_t* order, uint8_t* light, int* bad)
+{
+    int nbad = 0;
+    for (int64_t c = grid_stride_begin(); c < n; c += grid_stride()) {
+        const int32_t b = next[c];
+        if (b < 0) continue;
+        const int32_t dt = dtop[c];
+        const int64_t pos = (int64_t)base[b] + dt;
+        if (pos < 0 || pos >= npos) {
+            ++nbad;
+            continue;
+        }
+        const int32_t old = atomicExch(order + pos, (int32_t)((uint32_t)c | (dt == 0 ? 0x80000000u : 0u)));
+        if (old != -1) ++nbad;
+        const int hk = heavy[c];
+        light[pos] = (uint8_t)(__ldg(upmask + c) & ~(hk < 8 ? 1u << hk : 0u));
+    }
+    if (nbad) atomicAdd(bad, nbad);
+}
+
+// Positions that no cell took.
+__global__ void k_path_unwritten(const int32_t* order, int64_t npos, int* bad)
+{
+    int nbad = 0;
+    for (int64_t i = grid_stride_begin(); i < npos; i += grid_stride()) nbad += order[i] == -1;
+    if (nbad) atomicAdd(bad, nbad);
+}
+
+void path_core_free(PathCore* pc)
+{
+    if (!pc) return;
+    cudaFree(pc->order);
+    cudaFree(pc->light);
+    delete pc;
+}
+
+int path_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stream, PathCore** out)
+{
+    *out = nullptr;
+    const int64_t n = core->n, rows = core->rows, cols = core->cols;
+    if (n >= (int64_t(1) << 31)) return fail(LUE_GPU_ERANGE, "path topology: 2^31 cells or more");
+    const int64_t npos = core->stats.valid_cells;
+    auto* pc = new (std::nothrow) PathCore();
+    if (!pc) return fail(LUE_GPU_ENOMEM, "path topology: host allocation");
+    pc->npos = npos;
+    int32_t *size = nullptr, *dtop = nullptr, *plev = nullptr, *heavy = nullptr, *next = nullptr;
+    uint8_t* key = nullptr;
+    long long* scan = nullptr;  // [0] running, [1..] offsets, then per-CTA sums
+    int* stats = nullptr;
+    const int64_t nblk = (n + kCompactCells - 1) / kCompactCells;
+    const int kMaxLevels = 255;
+    int rc = LUE_GPU_OK;
+    int hstats[3] = {0, 0, 0};
+    const char* what = "path topology";
+    auto cleanup = [&]() {
+        cudaFree(size);
+        cudaFree(dtop);
+        cudaFree(plev);
+        cudaFree(heavy);
+        cudaFree(next);
+        cudaFree(key);
+        cudaFree(scan);
+        cudaFree(stats);
+    };
+    if ((rc = cuda_status(cudaMalloc(&size, n * sizeof(int32_t)), what)) ||
+        (rc = cuda_status(cudaMalloc(&dtop, n * sizeof(int32_t)), what)) ||
+        (rc = cuda_status(cudaMalloc(&plev, n * sizeof(int32_t)), what)) ||
+        (rc = cuda_status(cudaMalloc(&heavy, n * sizeof(int32_t)), what)) ||
+        (rc = cuda_status(cudaMalloc(&next, n * sizeof(int32_t)), what)) ||
+        (rc = cuda_status(cudaMalloc(&key, n), what)) ||
+        (rc = cuda_status(cudaMalloc(&scan, (2 + kMaxLevels + 1 + nblk) * sizeof(long long)), what)) ||
+        (rc = cuda_status(cudaMalloc(&stats, 3 * sizeof(int)), what)) ||
+        (rc = cuda_status(cudaMalloc(&pc->order, std::max<int64_t>(npos, 1) * sizeof(int32_t)), what)) ||
+        (rc = cuda_status(cudaMalloc(&pc->light, std::max<int64_t>(npos, 1)), what))) {
+        cleanup();
+        path_core_free(pc);
+        return rc;
+    }
+    pc->bytes = std::max<int64_t>(npos, 1) * 5;
+    // 1. sizes, heavy neighbours, cells above on the path, path levels
+    k_fill<<<grid_for(n, 256), 256, 0, stream>>>(heavy, n, 8);
+    cudaMemcpyAsync(work, core->count, words_for(n) * 4, cudaMemcpyDeviceToDevice, stream);
+    {
+        WalkGrid g{core->fd, core->count, work, rows, cols, n};
+        PathVisitor v{core->upmask, size, dtop, plev, heavy, cols};
+        k_walk<<<grid_all(n, 256), 256, 0, stream>>>(g, v);
+    }
+    // 2. bottom of each cell's path: pointer jumping over the path links
+    k_path_next<<<grid_for(n, 256), 256, 0, stream>>>(core->fd, heavy, rows, cols, n, next);
+    int rounds = 1;
+    while ((int64_t(1) << rounds) < core->stats.max_level + 2) ++rounds;
+    for (int i = 0; i <= rounds; ++i) k_path_jump<<<grid_for(n, 256), 256, 0, stream>>>(next, n);
+    // 3. keys and level count
+    cudaMemsetAsync(stats, 0, 3 * sizeof(int), stream);
+    k_path_keys<<<grid_for(n, 256), 256, 0, stream>>>(next, plev, dtop, n, key, stats);
+    if ((rc = cuda_status(cudaMemcpyAsync(hstats, stats, sizeof hstats, cudaMemcpyDeviceToHost, stream), what)) ||
+        (rc = cuda_status(cudaStreamSynchronize(stream), what))) {
+        cleanup();
+        path_core_free(pc);
+        return rc;
+    }
+    if (hstats[2] != 0 || hstats[0] >= 254) {
+        cleanup();
+        path_core_free(pc);
+        return fail(LUE_GPU_ERANGE, "path topology: " + std::to_string(hstats[2]) + " cells without a bottom, " +
+                                        std::to_string(hstats[0] + 1) + " levels");
+    }
+    const int levels = npos > 0 ? hstats[0] + 1 : 0;
+    pc->longest_path = hstats[1];
+    // 4. positions: levels in order, paths of a level in cell order of their bottoms
+    int32_t* base = size;  // sizes are no longer needed
+    long long* running = scan;
+    long long* offsets = scan + 1;
+    long long* bsum = scan + 2 + kMaxLevels;
+    cudaMemsetAsync(scan, 0, (2 + kMaxLevels) * sizeof(long long), stream);
+    for (int l = 0; l < levels; ++l) {
+        k_level_sums<<<(unsigned)nblk, 256, 0, stream>>>(key, dtop, l, n, bsum);
+        k_level_scan<<<1, 1024, 0, stream>>>(bsum, nblk, running, offsets, l);
+        k_level_assign<<<(unsigned)nblk, 256, 0, stream>>>(key, dtop, l, n, bsum, base);
+    }
+    cudaMemsetAsync(pc->order, 0xFF, std::max<int64_t>(npos, 1) * sizeof(int32_t), stream);
+    cudaMemsetAsync(stats + 2, 0, sizeof(int), stream);
+    k_path_place<<<grid_for(n, 256), 256, 0, stream>>>(next, base, dtop, heavy, core->upmask, n, npos, pc->order,
+                                                       pc->light, stats + 2);
+    k_path_unwritten<<<grid_for(npos, 256), 256, 0, stream>>>(pc->order, npos, stats + 2);
+    std::vector<long long> hoff(levels + 1, 0);
+    if (levels > 0 &&
+        (rc = cuda_status(cudaMemcpyAsync(hoff.data(), offsets, (levels + 1) * sizeof(long long),
+                                          cudaMemcpyDeviceToHost, stream),
+                          what))) {
+        cleanup();
+        path_core_free(pc);
+        return rc;
+    }
+    int bad = 0;
+    rc = cuda_status(cudaMemcpyAsync(&bad, stats + 2, sizeof(int), cudaMemcpyDeviceToHost, stream), what);
+    if (!rc) rc = cuda_status(cudaStreamSynchronize(stream), what);
+    if (!rc) rc = cuda_status(cudaGetLastError(), what);
+    cleanup();
+    count_launches(8 + rounds + 3 * levels);
+    if (rc) {
+        path_core_free(pc);
+        return rc;
+    }
+    if ((levels > 0 && hoff[levels] != npos) || bad) {
+        path_core_free(pc);
+        return fail(LUE_GPU_ERANGE, "path topology: inconsistent layout (" + std::to_string(levels ? hoff[levels] : 0) +
+                                        " positions for " + std::to_string(npos) + " cells, " + std::to_string(bad) +
+                                        " misplaced)");
+    }
+    pc->level_offsets.assign(hoff.begin(), hoff.end());
+    pc->tiles = 0;
+    for (int l = 0; l < levels; ++l) pc->tiles += (hoff[l + 1] - hoff[l] + kPathTile - 1) / kPathTile;
+    if (getenv("LUE_GB300_VERBOSE")) {
+        fprintf(stderr, "path topology: %lld cells, %d levels, %lld tiles, longest path %lld cells; positions:",
+                (long long)npos, levels, (long long)pc->tiles, (long long)pc->longest_path);
+        for (int l = 0; l < levels; ++l) fprintf(stderr, " %lld", hoff[l + 1] - hoff[l]);
+        fprintf(stderr, "\n");
+    }
+    *out = pc;
+    return LUE_GPU_OK;
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Per call
+// ---------------------------------------------------------------------------------------------------
+
+// A map x -> op(x + a, b) with op = max (threshold) or min (capacity), a and b float-float.  flags bit 0:
+// the map of a path's top cell, which ignores its input (its value is b); bit 1: no-data (NaN) from the
+// cell itself or from upstream.
+struct PMap {
+    float ah, al, bh, bl;
+    int flags;
+};
+
+template <bool MIN>
+__device__ __forceinline__ PMap pm_identity()
+{
+    return PMap{0.0f, 0.0f, MIN ? INFINITY : -INFINITY, 0.0f, 0};
+}
+
+// x + y for float-float values; a sum that is not finite is kept with lo = 0 (two_sum's error terms would
+// turn an infinity into NaN).
+__device__ __forceinline__ void ff_sum(float xh, float xl, float yh, float yl, float& rh, float& rl)
+{
+    float s, e;
+    two_sum(xh, yh, s, e);
+    if (!isfinite(s)) {
+        rh = s;
+        rl = 0.0f;
+        return;
+    }
+    e = __fadd_rn(e, __fadd_rn(xl, yl));
+    rh = __fadd_rn(s, e);
+    rl = __fsub_rn(e, __fsub_rn(rh, s));
+}
+
+__device__ __forceinline__ bool ff_less(float xh, float xl, float yh, float yl)
+{
+    return xh < yh || (xh == yh && xl < yl);
+}
+
+// m1 first, then m2.
+template <bool MIN>
+__device__ __forceinline__ PMap compose(const PMap& m1, const PMap& m2)
+{
+    if (m2.flags & 1) return m2;
+    PMap r;
+    r.flags = (m1.flags & 1) | ((m1.flags | m2.flags) & 2);
+    ff_sum(m1.ah, m1.al, m2.ah, m2.al, r.ah, r.al);
+    float th, tl;
+    ff_sum(m1.bh, m1.bl, m2.ah, m2.al, th, tl);
+    const bool take = MIN ? ff_less(th, tl, m2.bh, m2.bl) : ff_less(m2.bh, m2.bl, th, tl);
+    r.bh = take ? th : m2.bh;
+    r.bl = take ? tl : m2.bl;
+    return r;
+}
+
+// The map of one cell: s = its material plus the outflow of its light upstream neighbours, b its
+// threshold or capacity.
+template <Rule R>
+__device__ __forceinline__ PMap cell_map(bool top, float sh, float sl, float b, bool nan)
+{
+    if (nan) return PMap{0.0f, 0.0f, 0.0f, 0.0f, 2 | (top ? 1 : 0)};
+    if (top) {
+        float oh = 0.0f, ol = 0.0f, rem = 0.0f;
+        rule_f32<R>(FF{sh, sl}, false, 0.0f, b, oh, ol, rem);
+        return PMap{0.0f, 0.0f, oh, ol, 1};
+    }
+    if (R == Rule::threshold) {  // max(x + (s - threshold), 0)
+        float dh, dl;
+        ff_sum(sh, sl, -b, 0.0f, dh, dl);
+        return PMap{dh, dl, 0.0f, 0.0f, 0};
+    }
+    return PMap{sh, sl, b, 0.0f, 0};  // capacity: min(x + s, capacity)
+}
+
+__device__ __forceinline__ PMap shfl_up(const PMap& m, int d)
+{
+    PMap r;
+    r.ah = __shfl_up_sync(0xffffffffu, m.ah, d);
+    r.al = __shfl_up_sync(0xffffffffu, m.al, d);
+    r.bh = __shfl_up_sync(0xffffffffu, m.bh, d);
+    r.bl = __shfl_up_sync(0xffffffffu, m.bl, d);
+    r.flags = __shfl_up_sync(0xffffffffu, m.flags, d);
+    return r;
+}
+
+// Exclusive scan of the threads' maps in thread order; `total` is the composition of all of them.
+template <bool MIN, int NT>
+__device__ __forceinline__ PMap block_excl_scan(const PMap& v, PMap* s_warp, PMap& total)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    PMap x = v;
+    for (int d = 1; d < 32; d <<= 1) {
+        const PMap y = shfl_up(x, d);
+        if (lane >= d) x = compose<MIN>(y, x);
+    }
+    PMap ex = shfl_up(x, 1);
+    if (lane == 0) ex = pm_identity<MIN>();
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        PMap w = lane < NT / 32 ? s_warp[lane] : pm_identity<MIN>();
+        for (int d = 1; d < 32; d <<= 1) {
+            const PMap y = shfl_up(w, d);
+            if (lane >= d) w = compose<MIN>(y, w);
+        }
+        if (lane < NT / 32) s_warp[lane] = w;
+    }
+    __syncthreads();
+    total = s_warp[NT / 32 - 1];
+    const PMap r = warp ? compose<MIN>(s_warp[warp - 1], ex) : ex;
+    __syncthreads();
+    return r;
+}
+
+struct PathCall {
+    const int32_t* order;
+    const uint8_t* light;
+    const float* a;  // material
+    float as;
+    const float* b;  // threshold / capacity
+    float bs;
+    float* out;
+    float* rem;
+    float* lo;       // float-float residual of the outflow (path bottoms: read as light inflow)
+    float2* s;       // per position: material plus light inflow
+    float* bv;       // per position: threshold / capacity
+    unsigned long long* flag;
+    int64_t cols;
+};
+
+// Pass 1 of a level: per position its map inputs (stored by position), per CTA the composition of its maps.
+template <Rule R, bool MIN>
+__global__ void __launch_bounds__(kPathThreads) k_path_maps(PathCall p, int64_t p0, int64_t p1, PMap* agg)
+{
+    __shared__ PMap s_warp[kPathThreads / 32];
+    const int64_t first = p0 + (int64_t)blockIdx.x * kPathTile + (int64_t)threadIdx.x * kPathPer;
+    PMap acc = pm_identity<MIN>();
+    bool odd = false;
+    for (int j = 0; j < kPathPer; ++j) {
+        const int64_t pos = first + j;
+        if (pos >= p1) break;
+        const int32_t w = __ldg(p.order + pos);
+        const int64_t c = (int64_t)(w & 0x7fffffff);
+        FF s{0.0f, 0.0f};
+        bool nan = false;
+        for (unsigned lm = __ldg(p.light + pos); lm; lm &= lm - 1) {
+            const int k = __ffs(lm) - 1;
+            const int64_t u = c + nb_dr(k) * p.cols + nb_dc(k);
+            const float vh = p.out[u];
+            nan |= isnan(vh);
+            s.add(vh, p.lo[u]);
+        }
+        const float e = value_at(p.a, p.as, c), b = value_at(p.b, p.bs, c);
+        nan |= isnan(e) || isnan(b) || !(e >= 0.0f && b >= 0.0f);
+        s.add(e);
+        s.normalise();
+        odd |= !nan && (isinf(e) || isinf(b) || isinf(s.hi));
+        p.s[pos] = make_float2(nan ? __int_as_float(0x7fc00000) : s.hi, nan ? 0.0f : s.lo);
+        p.bv[pos] = b;
+        acc = compose<MIN>(acc, cell_map<R>(w < 0, s.hi, s.lo, b, nan));
+    }
+    if (odd) p.flag[1] = 1;  // +-inf: the walk engine redoes the call
+    PMap total;
+    block_excl_scan<MIN, kPathThreads>(acc, s_warp, total);
+    if (threadIdx.x == 0) agg[blockIdx.x] = total;
+}
+
+// Pass 2 of a level: exclusive scan of the CTAs' maps.
+template <bool MIN>
+__global__ void __launch_bounds__(1024) k_path_carry(const PMap* agg, int64_t ntiles, PMap* carry)
+{
+    __shared__ PMap s_warp[32];
+    const int64_t per = (ntiles + 1023) / 1024;
+    const int64_t t0 = (int64_t)threadIdx.x * per, t1 = min(ntiles, t0 + per);
+    PMap acc = pm_identity<MIN>();
+    for (int64_t i = t0; i < t1; ++i) acc = compose<MIN>(acc, agg[i]);
+    PMap total;
+    PMap x = block_excl_scan<MIN, 1024>(acc, s_warp, total);
+    for (int64_t i = t0; i < t1; ++i) {
+        carry[i] = x;
+        x = compose<MIN>(x, agg[i]);
+    }
+}
+
+// Pass 3 of a level: each cell's outflow from the composed map of the cells above it on its path, the
+// cell rule (the walk engine's, route_walk_visitors.cuh) and its outputs.
+template <Rule R, bool MIN>
+__global__ void __launch_bounds__(kPathThreads) k_path_out(PathCall p, int64_t p0, int64_t p1, const PMap* carry)
+{
+    __shared__ PMap s_warp[kPathThreads / 32];
+    const int64_t first = p0 + (int64_t)blockIdx.x * kPathTile + (int64_t)threadIdx.x * kPathPer;
+    PMap acc = pm_identity<MIN>();
+    for (int j = 0; j < kPathPer; ++j) {
+        const int64_t pos = first + j;
+        if (pos >= p1) break;
+        const float2 s = p.s[pos];
+        acc = compose<MIN>(acc, cell_map<R>(__ldg(p.order + pos) < 0, s.x, s.y, p.bv[pos], isnan(s.x)));
+    }
+    PMap total;
+    PMap E = block_excl_scan<MIN, kPathThreads>(acc, s_warp, total);
+    if (carry) E = compose<MIN>(carry[blockIdx.x], E);
+    for (int j = 0; j < kPathPer; ++j) {
+        const int64_t pos = first + j;
+        if (pos >= p1) break;
+        const int32_t w = __ldg(p.order + pos);
+        const int64_t c = (int64_t)(w & 0x7fffffff);
+        const bool top = w < 0;
+        const float2 s = p.s[pos];
+        const float b = p.bv[pos];
+        const bool nan_own = isnan(s.x);
+        FF t{0.0f, 0.0f};
+        bool nan = nan_own;
+        if (!top) {
+            nan |= (E.flags & 2) != 0;
+            t = FF{E.bh, E.bl};
+        }
+        t.add(s.x, s.y);
+        float oh = 0.0f, ol = 0.0f, rem = 0.0f;
+        if (!rule_f32<R>(t, nan, 0.0f, b, oh, ol, rem)) {
+            oh = __int_as_float(0x7fc00000);
+            ol = 0.0f;
+            rem = oh;
+        }
+        p.out[c] = oh;
+        p.rem[c] = rem;
+        if (pos + 1 >= p1 || __ldg(p.order + pos + 1) < 0) p.lo[c] = ol;  // a path bottom
+        E = compose<MIN>(E, cell_map<R>(top, s.x, s.y, b, nan_own));
+    }
+}
+
+__global__ void k_path_no_data(const uint8_t* fd, int64_t n, float* out, float* rem)
+{
+    for (int64_t i = grid_stride_begin(); i < n; i += grid_stride())
+        if (__ldg(fd + i) == kNoData) {
+            out[i] = __int_as_float(0x7fc00000);
+            rem[i] = __int_as_float(0x7fc00000);
+        }
+}
+
+static bool path_engine_off()
+{
+    const char* e = getenv("LUE_GB300_ENGINE");
+    return e && (e[0] == 'w' || e[0] == 's');
+}
+
+static int path_core_get(lue_gpu_topology* t, cudaStream_t stream, const PathCore** out)
+{
+    *out = nullptr;
+    TopologyCore* core = t->core;
+    if (core->stats.cycle_cells > 0) return LUE_GPU_OK;
+    std::lock_guard<std::mutex> lock(core->stage_mutex);
+    if (!core->paths && !core->paths_unavailable) {
+        PathCore* pc = nullptr;
+        const int rc = path_core_build(core, t->work_count, stream, &pc);
+        if (rc == LUE_GPU_ERANGE) {
+            core->paths_unavailable = true;
+            return LUE_GPU_OK;
+        }
+        if (rc) return rc;
+        core->paths = pc;
+        core->bytes += pc->bytes;
+    }
+    *out = core->paths;
+    return LUE_GPU_OK;
+}
+
+void path_buffers_free(lue_gpu_topology* t)
+{
+    cudaFree(t->path_s);
+    cudaFree(t->path_b);
+    cudaFree(t->path_maps);
+    cudaFree(t->path_flag);
+    t->path_s = nullptr;
+    t->path_b = nullptr;
+    t->path_maps = nullptr;
+    t->path_flag = nullptr;
+}
+
+static int path_buffers(lue_gpu_topology* t, const PathCore* pc)
+{
+    if (t->path_s) return LUE_GPU_OK;
+    const char* what = "path engine buffers";
+    const int64_t np = std::max<int64_t>(pc->npos, 1), nt = std::max<int64_t>(pc->tiles, 1);
+    int rc = LUE_GPU_OK;
+    if ((rc = cuda_status(cudaMalloc(&t->path_s, np * sizeof(float2)), what)) ||
+        (rc = cuda_status(cudaMalloc(&t->path_b, np * sizeof(float)), what)) ||
+        (rc = cuda_status(cudaMalloc(&t->path_maps, 2 * nt * sizeof(PMap)), what)) ||
+        (rc = cuda_status(cudaMalloc(&t->path_flag, 2 * sizeof(unsigned long long)), what))) {
+        path_buffers_free(t);
+        return rc;
+    }
+    t->scratch_bytes += np * (int64_t)(sizeof(float2) + sizeof(float)) + 2 * nt * (int64_t)sizeof(PMap) + 16;
+    return LUE_GPU_OK;
+}
+
+int path_prepare(lue_gpu_topology* t, cudaStream_t stream)
+{
+    const PathCore* pc = nullptr;
+    return path_core_get(t, stream, &pc);
+}
+
+template <Rule R, bool MIN>
+static int path_run(lue_gpu_topology* t, const PathCore* pc, const float* a, float as, const float* b, float bs,
+                    float* out, float* rem, cudaStream_t stream, const char* what)
+{
+    const TopologyCore* core = t->core;
+    const int64_t n = core->n;
+    if (int rc = path_buffers(t, pc)) return rc;
+    if (int rc = cuda_status(cudaMemsetAsync(t->path_flag, 0, 2 * sizeof(unsigned long long), stream), what))
+        return rc;
+    k_path_no_data<<<grid_for(n, 256), 256, 0, stream>>>(core->fd, n, out, rem);
+    PathCall p{pc->order, pc->light, a, as, b, bs, out, rem, t->lo, t->path_s, t->path_b, t->path_flag, core->cols};
+    PMap* agg = static_cast<PMap*>(t->path_maps);
+    PMap* carry = agg + std::max<int64_t>(pc->tiles, 1);
+    int launches = 1;
+    int64_t tile = 0;
+    const int levels = (int)pc->level_offsets.size() - 1;
+    for (int l = 0; l < levels; ++l) {
+        const int64_t p0 = pc->level_offsets[l], p1 = pc->level_offsets[l + 1];
+        if (p1 <= p0) continue;
+        const int64_t nt = (p1 - p0 + kPathTile - 1) / kPathTile;
+        k_path_maps<R, MIN><<<(unsigned)nt, kPathThreads, 0, stream>>>(p, p0, p1, agg + tile);
+        if (nt > 1) k_path_carry<MIN><<<1, 1024, 0, stream>>>(agg + tile, nt, carry + tile);
+        k_path_out<R, MIN><<<(unsigned)nt, kPathThreads, 0, stream>>>(p, p0, p1, nt > 1 ? carry + tile : nullptr);
+        launches += nt > 1 ? 3 : 2;
+        tile += nt;
+    }
+    // +-inf inputs: the walk engine redoes the whole call (as behind the tile engine of accu)
+    const unsigned long long* flag = t->path_flag;
+    k_copy_words_if<<<grid_for(words_for(n), 256), 256, 0, stream>>>(reinterpret_cast<const uint32_t*>(core->count),
+                                                                     t->work_count, words_for(n), flag);
+    WalkGrid g{core->fd, core->count, t->work_count, core->rows, core->cols, n};
+    RouteF32<R> v{core->upmask, a, as, b, bs, out, rem, t->lo, core->cols};
+    k_walk_if<<<grid_for(n, 256), 256, 0, stream>>>(g, v, flag);
+    count_launches(launches + 2);
+    return cuda_status(cudaGetLastError(), what);
+}
+
+int path_route_f32(lue_gpu_topology* t, int rule, const float* a, float as, const float* b, float bs, float* out,
+                   float* rem, cudaStream_t stream, bool* done)
+{
+    *done = false;
+    if (path_engine_off()) return LUE_GPU_OK;
+    if (rule != (int)Rule::threshold && rule != (int)Rule::capacity) return LUE_GPU_OK;
+    const PathCore* pc = nullptr;
+    if (int rc = path_core_get(t, stream, &pc)) return rc;
+    if (!pc) return LUE_GPU_OK;
+    *done = true;
+    if (rule == (int)Rule::threshold)
+        return path_run<Rule::threshold, false>(t, pc, a, as, b, bs, out, rem, stream, "accu_threshold_f32 (paths)");
+    return path_run<Rule::capacity, true>(t, pc, a, as, b, bs, out, rem, stream, "accu_capacity_f32 (paths)");
+}
+
+}  // namespace lue_gb300

@@ -142,6 +142,8 @@ extern "C" int lue_gpu_accu_threshold_f32(lue_gpu_topology* t, const float* infl
 {
     if (int rc = check_topology(t, "accu_threshold_f32")) return rc;
     if (!flux || !state) return fail(LUE_GPU_EINVAL, "accu_threshold_f32: NULL output");
+    STAGE_OR_WALK(path_route_f32(t, (int)Rule::threshold, inflow, inflow_scalar, threshold, threshold_scalar, flux,
+                                 state, (cudaStream_t)stream, &done));
     STAGE_OR_WALK(stage_route_f32(t, (int)Rule::threshold, inflow, inflow_scalar, threshold, threshold_scalar, flux,
                                   state, (cudaStream_t)stream, &done));
     return route_f32<Rule::threshold>(t, inflow, inflow_scalar, threshold, threshold_scalar, flux, state, stream,
@@ -184,6 +186,19 @@ extern "C" int lue_gpu_accu_fraction_f64(lue_gpu_topology* t, const double* infl
                                      "accu_fraction_f64");
 }
 
+// The path engine (path_route.cuh) takes float32 accu_threshold and accu_capacity on acyclic rasters.
+static int path_first(lue_gpu_topology* t, int rule, const float* a, float as, const float* b, float bs, float* out,
+                      float* rem, cudaStream_t stream, bool* done)
+{
+    return path_route_f32(t, rule, a, as, b, bs, out, rem, stream, done);
+}
+static int path_first(lue_gpu_topology*, int, const double*, double, const double*, double, double*, double*,
+                      cudaStream_t, bool* done)
+{
+    *done = false;
+    return LUE_GPU_OK;
+}
+
 // accu_capacity / accu_trigger: the same routers with the cell rules of ALG/definition/accu_capacity.hpp
 // and ALG/definition/accu_trigger.hpp (enter_cell).
 #define TWO_OUTPUT_OP(NAME, RULE, T, ROUTE, STAGE)                                                           \
@@ -192,6 +207,8 @@ extern "C" int lue_gpu_accu_fraction_f64(lue_gpu_topology* t, const double* infl
     {                                                                                                         \
         if (int rc = check_topology(t, #NAME)) return rc;                                                     \
         if (!outflow || !remainder) return fail(LUE_GPU_EINVAL, #NAME ": NULL output");                       \
+        STAGE_OR_WALK(path_first(t, (int)RULE, inflow, inflow_scalar, other, other_scalar, outflow, remainder, \
+                                 (cudaStream_t)stream, &done));                                               \
         STAGE_OR_WALK(STAGE(t, (int)RULE, inflow, inflow_scalar, other, other_scalar, outflow, remainder,      \
                             (cudaStream_t)stream, &done));                                                    \
         return ROUTE<RULE>(t, inflow, inflow_scalar, other, other_scalar, outflow, remainder, stream, #NAME); \

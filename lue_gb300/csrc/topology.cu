@@ -161,6 +161,7 @@ static void free_core(TopologyCore* core)
     cudaFree(core->order);
     tile_core_free(core->tiles);
     stage_core_free(core->stages);
+    path_core_free(core->paths);
     delete core;
 }
 
@@ -172,6 +173,7 @@ static void free_handle(lue_gpu_topology* t)
     cudaFree(t->history);
     cudaFree(t->planes);
     stage_buffers_free(t);
+    path_buffers_free(t);
     cudaFreeHost(t->stage_flow_error);
     tile_scratch_free(&t->tile_scratch);
     if (t->core && --t->core->refs == 0) free_core(t->core);
@@ -303,6 +305,7 @@ extern "C" int lue_gpu_topology_clone(const lue_gpu_topology* topology, lue_gpu_
 extern "C" int lue_gpu_topology_prepare(lue_gpu_topology* topology, void* stream)
 {
     if (!topology) return fail(LUE_GPU_EINVAL, "topology_prepare: NULL topology");
+    if (int rc = path_prepare(topology, (cudaStream_t)stream)) return rc;
     return stage_prepare(topology, (cudaStream_t)stream);
 }
 

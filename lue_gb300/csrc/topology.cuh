@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "path_route.cuh"
 #include "stage_route.cuh"
 #include "tile_accu.cuh"
 
@@ -23,7 +24,9 @@ struct TopologyCore {
     StageCore* stages = nullptr;         // stage engine (acyclic rasters; built on first use)
     int stage_cap = 0;                   // most cells of one stage when built (0: LUE_GB300_STAGE_CAP or 128)
     bool stages_unavailable = false;     // the raster is beyond the stage engine's limits
-    std::mutex stage_mutex;              // guards the first build (clones share the core)
+    PathCore* paths = nullptr;           // path engine (acyclic rasters; built on first use)
+    bool paths_unavailable = false;      // the raster is beyond the path engine's limits
+    std::mutex stage_mutex;              // guards the first build of stages and paths (clones share the core)
     lue_gpu_topology_stats stats{};
     int64_t bytes = 0;
     std::atomic<int> refs{1};
@@ -47,6 +50,10 @@ struct lue_gpu_topology {
     int* stage_flow_error = nullptr; // pinned: the error flag of the last dataflow launch, read by the next call
     int stage_threads = 0;           // stage engine: threads per stage CTA (0: LUE_GB300_STAGE_THREADS or by size)
     int publish_every = 0;           // stage engine: steps per progress publication (0: LUE_GB300_PUBLISH_EVERY or 4)
+    float2* path_s = nullptr;        // path engine: per position the material plus light inflow (float-float)
+    float* path_b = nullptr;         // path engine: per position the threshold / capacity
+    void* path_maps = nullptr;       // path engine: per tile its composed map and its carry
+    unsigned long long* path_flag = nullptr;  // path engine: [2], [1] set when the walk engine must redo a call
     int64_t scratch_bytes = 0;
 };
 

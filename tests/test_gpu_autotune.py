@@ -10,6 +10,13 @@ from lue_gb300 import _lib, synthetic
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(autouse=True)
+def _stage_engine(monkeypatch):
+    """accu_threshold and accu_capacity (float32) run on the path engine by default; these tests are about
+    the stage engine."""
+    monkeypatch.setenv("LUE_GB300_ENGINE", "stage")
+
+
 @pytest.fixture(scope="module")
 def lfr():
     import torch
