@@ -161,20 +161,27 @@ __device__ __forceinline__ long long block_excl_sum(long long v, long long* s_wa
     return before + x - v;
 }
 
-// Per CTA of cells: the positions taken by the paths of level `lvl` whose bottom lies in it.
+// Per CTA of cells: the positions taken by the paths of level `lvl` whose bottom lies in it; longest[lvl]:
+// the longest path of the level.
 __global__ void __launch_bounds__(256) k_level_sums(const uint8_t* key, const int32_t* dtop, int lvl, int64_t n,
-                                                    long long* bsum)
+                                                    long long* bsum, int* longest)
 {
     __shared__ long long s_warp[8];
     const int64_t c0 = (int64_t)blockIdx.x * kCompactCells + (int64_t)threadIdx.x * kCompactPer;
     long long s = 0;
+    int lmax = 0;
     for (int j = 0; j < kCompactPer; ++j) {
         const int64_t c = c0 + j;
-        if (c < n && key[c] == lvl) s += dtop[c] + 1;
+        if (c < n && key[c] == lvl) {
+            s += dtop[c] + 1;
+            lmax = max(lmax, dtop[c] + 1);
+        }
     }
     long long total = 0;
     block_excl_sum<256>(s, s_warp, total);
     if (threadIdx.x == 0) bsum[blockIdx.x] = total;
+    for (int d = 16; d; d >>= 1) lmax = max(lmax, __shfl_xor_sync(0xffffffffu, lmax, d));
+    if ((threadIdx.x & 31) == 0 && lmax) atomicMax(longest + lvl, lmax);
 }
 
 // Exclusive scan of the per-CTA sums of one level, after the positions of the lower levels
@@ -255,6 +262,31 @@ __global__ void k_path_unwritten(const int32_t* order, int64_t npos, int* bad)
     if (nbad) atomicAdd(bad, nbad);
 }
 
+// Position arrays are padded to whole 8-position chunks plus one chunk, for the vector loads of the
+// per-call kernels.
+static int64_t path_padded(int64_t npos) { return ((npos + 7) / 8 + 1) * 8; }
+
+// Positions per thread of a level: LUE_GB300_PATH_PER (1, 2, 4 or 8; default 4, the fastest at 16384^2:
+// 8.7 ms against 9.8 ms for 8 and 9.3 ms for 2) for large levels, 1 for small ones (of long paths: short
+// chains of dependent loads per thread).
+constexpr int64_t kPathSmallLevel = 1 << 20;
+static int path_per_large()
+{
+    static const int per = [] {
+        const char* e = getenv("LUE_GB300_PATH_PER");
+        const int v = e ? atoi(e) : 4;
+        return v == 1 || v == 2 || v == 8 ? v : 4;
+    }();
+    return per;
+}
+static int path_per(int64_t p0, int64_t p1) { return p1 - p0 < kPathSmallLevel ? 1 : path_per_large(); }
+static int64_t path_level_tiles(int64_t p0, int64_t p1, int per)
+{
+    if (p1 <= p0) return 0;
+    const int64_t base = per > 1 ? (p0 & ~int64_t(per - 1)) : p0;
+    return (p1 - base + kPathThreads * per - 1) / (kPathThreads * per);
+}
+
 void path_core_free(PathCore* pc)
 {
     if (!pc) return;
@@ -298,14 +330,14 @@ int path_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t strea
         (rc = cuda_status(cudaMalloc(&next, n * sizeof(int32_t)), what)) ||
         (rc = cuda_status(cudaMalloc(&key, n), what)) ||
         (rc = cuda_status(cudaMalloc(&scan, (2 + kMaxLevels + 1 + nblk) * sizeof(long long)), what)) ||
-        (rc = cuda_status(cudaMalloc(&stats, 3 * sizeof(int)), what)) ||
-        (rc = cuda_status(cudaMalloc(&pc->order, std::max<int64_t>(npos, 1) * sizeof(int32_t)), what)) ||
-        (rc = cuda_status(cudaMalloc(&pc->light, std::max<int64_t>(npos, 1)), what))) {
+        (rc = cuda_status(cudaMalloc(&stats, (3 + kMaxLevels) * sizeof(int)), what)) ||
+        (rc = cuda_status(cudaMalloc(&pc->order, path_padded(npos) * sizeof(int32_t)), what)) ||
+        (rc = cuda_status(cudaMalloc(&pc->light, path_padded(npos)), what))) {
         cleanup();
         path_core_free(pc);
         return rc;
     }
-    pc->bytes = std::max<int64_t>(npos, 1) * 5;
+    pc->bytes = path_padded(npos) * 5;
     // 1. sizes, heavy neighbours, cells above on the path, path levels
     k_fill<<<grid_for(n, 256), 256, 0, stream>>>(heavy, n, 8);
     cudaMemcpyAsync(work, core->count, words_for(n) * 4, cudaMemcpyDeviceToDevice, stream);
@@ -342,21 +374,28 @@ int path_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t strea
     long long* offsets = scan + 1;
     long long* bsum = scan + 2 + kMaxLevels;
     cudaMemsetAsync(scan, 0, (2 + kMaxLevels) * sizeof(long long), stream);
+    int* longest = stats + 3;
+    cudaMemsetAsync(longest, 0, kMaxLevels * sizeof(int), stream);
     for (int l = 0; l < levels; ++l) {
-        k_level_sums<<<(unsigned)nblk, 256, 0, stream>>>(key, dtop, l, n, bsum);
+        k_level_sums<<<(unsigned)nblk, 256, 0, stream>>>(key, dtop, l, n, bsum, longest);
         k_level_scan<<<1, 1024, 0, stream>>>(bsum, nblk, running, offsets, l);
         k_level_assign<<<(unsigned)nblk, 256, 0, stream>>>(key, dtop, l, n, bsum, base);
     }
-    cudaMemsetAsync(pc->order, 0xFF, std::max<int64_t>(npos, 1) * sizeof(int32_t), stream);
+    cudaMemsetAsync(pc->order, 0xFF, path_padded(npos) * sizeof(int32_t), stream);
+    cudaMemsetAsync(pc->light, 0, path_padded(npos), stream);
     cudaMemsetAsync(stats + 2, 0, sizeof(int), stream);
     k_path_place<<<grid_for(n, 256), 256, 0, stream>>>(next, base, dtop, heavy, core->upmask, n, npos, pc->order,
                                                        pc->light, stats + 2);
     k_path_unwritten<<<grid_for(npos, 256), 256, 0, stream>>>(pc->order, npos, stats + 2);
     std::vector<long long> hoff(levels + 1, 0);
+    std::vector<int> hlong(std::max(levels, 1), 0);
     if (levels > 0 &&
-        (rc = cuda_status(cudaMemcpyAsync(hoff.data(), offsets, (levels + 1) * sizeof(long long),
-                                          cudaMemcpyDeviceToHost, stream),
-                          what))) {
+        ((rc = cuda_status(cudaMemcpyAsync(hoff.data(), offsets, (levels + 1) * sizeof(long long),
+                                           cudaMemcpyDeviceToHost, stream),
+                           what)) ||
+         (rc = cuda_status(cudaMemcpyAsync(hlong.data(), longest, levels * sizeof(int), cudaMemcpyDeviceToHost,
+                                           stream),
+                           what)))) {
         cleanup();
         path_core_free(pc);
         return rc;
@@ -378,12 +417,15 @@ int path_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t strea
                                         " misplaced)");
     }
     pc->level_offsets.assign(hoff.begin(), hoff.end());
+    pc->level_longest.assign(hlong.begin(), hlong.begin() + levels);
     pc->tiles = 0;
-    for (int l = 0; l < levels; ++l) pc->tiles += (hoff[l + 1] - hoff[l] + kPathTile - 1) / kPathTile;
+    for (int l = 0; l < levels; ++l)  // as many as one position per thread would need
+        pc->tiles = std::max(pc->tiles, path_level_tiles(hoff[l], hoff[l + 1], 1));
     if (getenv("LUE_GB300_VERBOSE")) {
-        fprintf(stderr, "path topology: %lld cells, %d levels, %lld tiles, longest path %lld cells; positions:",
+        fprintf(stderr, "path topology: %lld cells, %d levels, %lld tiles, longest path %lld cells; positions "
+                        "(longest path) by level:",
                 (long long)npos, levels, (long long)pc->tiles, (long long)pc->longest_path);
-        for (int l = 0; l < levels; ++l) fprintf(stderr, " %lld", hoff[l + 1] - hoff[l]);
+        for (int l = 0; l < levels; ++l) fprintf(stderr, " %lld (%d)", hoff[l + 1] - hoff[l], hlong[l]);
         fprintf(stderr, "\n");
     }
     *out = pc;
@@ -505,118 +547,318 @@ __device__ __forceinline__ PMap block_excl_scan(const PMap& v, PMap* s_warp, PMa
 }
 
 struct PathCall {
-    const int32_t* order;
-    const uint8_t* light;
-    const float* a;  // material
+    const int32_t* __restrict__ order;
+    const uint8_t* __restrict__ light;
+    const float* __restrict__ a;  // material
     float as;
-    const float* b;  // threshold / capacity
+    const float* __restrict__ b;  // threshold / capacity
     float bs;
     float* out;
     float* rem;
-    float* lo;       // float-float residual of the outflow (path bottoms: read as light inflow)
-    float2* s;       // per position: material plus light inflow
-    float* bv;       // per position: threshold / capacity
+    float* lo;                    // float-float residual of the outflow (path bottoms: read as light inflow)
     unsigned long long* flag;
     int64_t cols;
 };
 
-// Pass 1 of a level: per position its map inputs (stored by position), per CTA the composition of its maps.
-template <Rule R, bool MIN>
-__global__ void __launch_bounds__(kPathThreads) k_path_maps(PathCall p, int64_t p0, int64_t p1, PMap* agg)
+// The positions of one thread: PER consecutive positions from `first`; those outside [p0, p1) (the
+// 8-aligned chunks of PER = 8 may start before a level or end after it) are inactive.  PER = 8 loads
+// the position arrays with vector loads (the arrays are padded to whole chunks).
+template <int PER>
+__device__ __forceinline__ void load_order(const PathCall& p, int64_t first, int32_t (&w)[PER])
 {
-    __shared__ PMap s_warp[kPathThreads / 32];
-    const int64_t first = p0 + (int64_t)blockIdx.x * kPathTile + (int64_t)threadIdx.x * kPathPer;
-    PMap acc = pm_identity<MIN>();
-    bool odd = false;
-    for (int j = 0; j < kPathPer; ++j) {
-        const int64_t pos = first + j;
-        if (pos >= p1) break;
-        const int32_t w = __ldg(p.order + pos);
-        const int64_t c = (int64_t)(w & 0x7fffffff);
-        FF s{0.0f, 0.0f};
-        bool nan = false;
-        for (unsigned lm = __ldg(p.light + pos); lm; lm &= lm - 1) {
-            const int k = __ffs(lm) - 1;
-            const int64_t u = c + nb_dr(k) * p.cols + nb_dc(k);
-            const float vh = p.out[u];
-            nan |= isnan(vh);
-            s.add(vh, p.lo[u]);
-        }
-        const float e = value_at(p.a, p.as, c), b = value_at(p.b, p.bs, c);
-        nan |= isnan(e) || isnan(b) || !(e >= 0.0f && b >= 0.0f);
-        s.add(e);
-        s.normalise();
-        odd |= !nan && (isinf(e) || isinf(b) || isinf(s.hi));
-        p.s[pos] = make_float2(nan ? __int_as_float(0x7fc00000) : s.hi, nan ? 0.0f : s.lo);
-        p.bv[pos] = b;
-        acc = compose<MIN>(acc, cell_map<R>(w < 0, s.hi, s.lo, b, nan));
+    if (PER == 4) {
+        const int4 x = __ldg(reinterpret_cast<const int4*>(p.order + first));
+        w[0] = x.x; w[1 % PER] = x.y; w[2 % PER] = x.z; w[3 % PER] = x.w;
+    } else if (PER == 2) {
+        const int2 x = __ldg(reinterpret_cast<const int2*>(p.order + first));
+        w[0] = x.x; w[1 % PER] = x.y;
+    } else if (PER == 8) {
+        const int4 x = __ldg(reinterpret_cast<const int4*>(p.order + first));
+        const int4 y = __ldg(reinterpret_cast<const int4*>(p.order + first) + 1);
+        w[0] = x.x; w[1] = x.y; w[2] = x.z; w[3] = x.w;
+        w[4 % PER] = y.x; w[5 % PER] = y.y; w[6 % PER] = y.z; w[7 % PER] = y.w;
+    } else {
+#pragma unroll
+        for (int j = 0; j < PER; ++j) w[j] = __ldg(p.order + first + j);
     }
-    if (odd) p.flag[1] = 1;  // +-inf: the walk engine redoes the call
-    PMap total;
-    block_excl_scan<MIN, kPathThreads>(acc, s_warp, total);
-    if (threadIdx.x == 0) agg[blockIdx.x] = total;
 }
 
-// Pass 2 of a level: exclusive scan of the CTAs' maps.
+template <int PER>
+__device__ __forceinline__ int64_t chunk_base(int64_t p0)
+{
+    return PER > 1 ? (p0 & ~int64_t(PER - 1)) : p0;
+}
+
+__device__ __forceinline__ int ld_acquire_gpu(const int* p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(int* p, int v)
+{
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ PMap ld_map(const PMap* m)
+{
+    return PMap{__ldcg(&m->ah), __ldcg(&m->al), __ldcg(&m->bh), __ldcg(&m->bl), __ldcg(&m->flags)};
+}
+
+__device__ __forceinline__ PMap shfl_down(const PMap& m, int d)
+{
+    PMap r;
+    r.ah = __shfl_down_sync(0xffffffffu, m.ah, d);
+    r.al = __shfl_down_sync(0xffffffffu, m.al, d);
+    r.bh = __shfl_down_sync(0xffffffffu, m.bh, d);
+    r.bl = __shfl_down_sync(0xffffffffu, m.bl, d);
+    r.flags = __shfl_down_sync(0xffffffffu, m.flags, d);
+    return r;
+}
+
+// Decoupled look-back of one level's launch: CTAs take tiles in ticket order; each publishes the
+// composition of its tile's maps (state 1), then the composition of everything before and including its
+// tile (state 2).  Status words carry the launch's epoch, so the arrays need no clearing between launches.
+struct PathScan {
+    int* status;  // [tiles] epoch << 2 | state
+    PMap* aggm;   // [tiles] the tile's own composition
+    PMap* inclm;  // [tiles] the composition up to and including the tile
+    int* ticket;  // zeroed before the launch
+    int epoch;
+    int polls;    // poll limit of one wait
+};
+
+constexpr int kPathPolls = 1 << 20;
+
+// Warp 0: the composition of all tiles before `tile` (in every lane).  Lane i looks at tile j - i, 32 at
+// a time, until a tile with a published prefix is among them.  Every wait is bounded: a wait that gives
+// up (or finds that another one did) sets flag[1], after which the walk engine redoes the call.
 template <bool MIN>
-__global__ void __launch_bounds__(1024) k_path_carry(const PMap* agg, int64_t ntiles, PMap* carry)
+__device__ PMap look_back(const PathScan& q, int64_t tile, unsigned long long* flag)
 {
-    __shared__ PMap s_warp[32];
-    const int64_t per = (ntiles + 1023) / 1024;
-    const int64_t t0 = (int64_t)threadIdx.x * per, t1 = min(ntiles, t0 + per);
-    PMap acc = pm_identity<MIN>();
-    for (int64_t i = t0; i < t1; ++i) acc = compose<MIN>(acc, agg[i]);
-    PMap total;
-    PMap x = block_excl_scan<MIN, 1024>(acc, s_warp, total);
-    for (int64_t i = t0; i < t1; ++i) {
-        carry[i] = x;
-        x = compose<MIN>(x, agg[i]);
+    const int lane = threadIdx.x & 31;
+    PMap running = pm_identity<MIN>();
+    for (int64_t j = tile - 1;; j -= 32) {
+        const int64_t idx = j - lane;
+        int st = 2;
+        PMap m = pm_identity<MIN>();
+        if (idx >= 0) {
+            int v = 0, k = 0;
+            for (; k < q.polls; ++k) {
+                v = ld_acquire_gpu(q.status + idx);
+                if ((v >> 2) == q.epoch && (v & 3) != 0) break;
+                if (*reinterpret_cast<volatile unsigned long long*>(flag + 1)) k = q.polls - 1;
+                __nanosleep(32);
+            }
+            if (k >= q.polls) {
+                st = -1;
+            } else {
+                st = v & 3;
+                m = ld_map(st == 2 ? q.inclm + idx : q.aggm + idx);
+            }
+        }
+        if (__ballot_sync(0xffffffffu, st < 0)) {
+            if (lane == 0) flag[1] = 1;
+            return pm_identity<MIN>();
+        }
+        const unsigned incl = __ballot_sync(0xffffffffu, st == 2);
+        if (incl && lane > __ffs(incl) - 1) m = pm_identity<MIN>();
+        // lanes 31 .. 0 in this order (farther tiles come first)
+        for (int d = 1; d < 32; d <<= 1) {
+            const PMap o = shfl_down(m, d);
+            if (lane + d < 32) m = compose<MIN>(o, m);
+        }
+        const PMap window = PMap{__shfl_sync(0xffffffffu, m.ah, 0), __shfl_sync(0xffffffffu, m.al, 0),
+                                 __shfl_sync(0xffffffffu, m.bh, 0), __shfl_sync(0xffffffffu, m.bl, 0),
+                                 __shfl_sync(0xffffffffu, m.flags, 0)};
+        running = compose<MIN>(window, running);
+        if (incl) return running;
     }
 }
 
-// Pass 3 of a level: each cell's outflow from the composed map of the cells above it on its path, the
-// cell rule (the walk engine's, route_walk_visitors.cuh) and its outputs.
-template <Rule R, bool MIN>
-__global__ void __launch_bounds__(kPathThreads) k_path_out(PathCall p, int64_t p0, int64_t p1, const PMap* carry)
+// The positions of one thread in one chunk: PER consecutive positions from `first`, those in [lo, hi)
+// active.  load(): inputs, light inflow and the cells' maps, composed in order; store(): from the
+// composition E of everything before the first position, each cell's rule and outputs.  VEC: `first` is
+// a multiple of PER and the order array is read with vector loads.
+template <Rule R, bool MIN, int PER, bool LIGHT, bool VEC>
+struct Chunk {
+    int32_t w[PER];
+    bool on[PER];
+    float b[PER];
+    FF sum[PER];
+    bool nan[PER];
+
+    __device__ __forceinline__ PMap load(const PathCall& p, int64_t first, int64_t lo, int64_t hi)
+    {
+#pragma unroll
+        for (int j = 0; j < PER; ++j) on[j] = first + j >= lo && first + j < hi;
+        if (VEC && first < hi) {
+            load_order<PER>(p, first, w);
+        } else {
+#pragma unroll
+            for (int j = 0; j < PER; ++j) w[j] = on[j] ? __ldg(p.order + first + j) : 0;
+        }
+        float e[PER];
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+            const int64_t c = (int64_t)(w[j] & 0x7fffffff);
+            e[j] = on[j] ? value_at(p.a, p.as, c) : 0.0f;
+            b[j] = on[j] ? value_at(p.b, p.bs, c) : 0.0f;
+            sum[j] = FF{0.0f, 0.0f};
+            nan[j] = false;
+        }
+        if (LIGHT) {
+#pragma unroll
+            for (int j = 0; j < PER; ++j) {
+                if (!on[j]) continue;
+                const int64_t c = (int64_t)(w[j] & 0x7fffffff);
+                for (unsigned lm = __ldg(p.light + first + j); lm; lm &= lm - 1) {
+                    const int k = __ffs(lm) - 1;
+                    const int64_t u = c + nb_dr(k) * p.cols + nb_dc(k);
+                    const float vh = p.out[u];
+                    nan[j] |= isnan(vh);
+                    sum[j].add(vh, p.lo[u]);
+                }
+            }
+        }
+        PMap acc = pm_identity<MIN>();
+        bool odd = false;
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+            if (!on[j]) continue;
+            nan[j] |= isnan(e[j]) || isnan(b[j]) || !(e[j] >= 0.0f && b[j] >= 0.0f);
+            sum[j].add(e[j]);
+            sum[j].normalise();
+            odd |= !nan[j] && (isinf(e[j]) || isinf(b[j]) || isinf(sum[j].hi));
+            acc = compose<MIN>(acc, cell_map<R>(w[j] < 0, sum[j].hi, sum[j].lo, b[j], nan[j]));
+        }
+        if (odd) p.flag[1] = 1;  // +-inf: the walk engine redoes the call
+        return acc;
+    }
+
+    __device__ __forceinline__ void store(const PathCall& p, int64_t first, int64_t p1, PMap E)
+    {
+        // the position after this thread's last one: is it the top of a path (then the last one is a bottom)?
+        const int32_t after = first + PER < p1 ? __ldg(p.order + first + PER) : -1;
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+            if (!on[j]) continue;
+            const int64_t c = (int64_t)(w[j] & 0x7fffffff);
+            const bool top = w[j] < 0;
+            FF t{0.0f, 0.0f};
+            bool nn = nan[j];
+            if (!top) {
+                nn |= (E.flags & 2) != 0;
+                t = FF{E.bh, E.bl};
+            }
+            t.add(sum[j].hi, sum[j].lo);
+            float oh = 0.0f, ol = 0.0f, rem = 0.0f;
+            if (!rule_f32<R>(t, nn, 0.0f, b[j], oh, ol, rem)) {
+                oh = __int_as_float(0x7fc00000);
+                ol = 0.0f;
+                rem = oh;
+            }
+            p.out[c] = oh;
+            p.rem[c] = rem;
+            const int32_t next = j + 1 < PER ? w[(j + 1) % PER] : after;
+            if (first + j + 1 >= p1 || next < 0) p.lo[c] = ol;  // a path bottom
+            E = compose<MIN>(E, cell_map<R>(top, sum[j].hi, sum[j].lo, b[j], nan[j]));
+        }
+    }
+};
+
+#define PATH_BOUNDS(PER) __launch_bounds__(kPathThreads, PER >= 8 ? 2 : (PER == 4 ? 4 : (PER == 2 ? 5 : 6)))
+
+// One level in one pass, for levels with long paths: tiles in ticket order, the composition of the
+// tiles before each one by decoupled look-back.
+template <Rule R, bool MIN, int PER, bool LIGHT>
+__global__ void PATH_BOUNDS(PER) k_path_level(PathCall p, int64_t p0, int64_t p1, PathScan q)
 {
     __shared__ PMap s_warp[kPathThreads / 32];
-    const int64_t first = p0 + (int64_t)blockIdx.x * kPathTile + (int64_t)threadIdx.x * kPathPer;
-    PMap acc = pm_identity<MIN>();
-    for (int j = 0; j < kPathPer; ++j) {
-        const int64_t pos = first + j;
-        if (pos >= p1) break;
-        const float2 s = p.s[pos];
-        acc = compose<MIN>(acc, cell_map<R>(__ldg(p.order + pos) < 0, s.x, s.y, p.bv[pos], isnan(s.x)));
-    }
+    __shared__ PMap s_prefix;
+    __shared__ int64_t s_tile;
+    if (threadIdx.x == 0) s_tile = atomicAdd(q.ticket, 1);
+    __syncthreads();
+    const int64_t tile = s_tile;
+    const int64_t first = chunk_base<PER>(p0) + tile * (kPathThreads * PER) + (int64_t)threadIdx.x * PER;
+    Chunk<R, MIN, PER, LIGHT, true> ch;
+    const PMap acc = ch.load(p, first, p0, p1);
     PMap total;
     PMap E = block_excl_scan<MIN, kPathThreads>(acc, s_warp, total);
-    if (carry) E = compose<MIN>(carry[blockIdx.x], E);
-    for (int j = 0; j < kPathPer; ++j) {
-        const int64_t pos = first + j;
-        if (pos >= p1) break;
-        const int32_t w = __ldg(p.order + pos);
-        const int64_t c = (int64_t)(w & 0x7fffffff);
-        const bool top = w < 0;
-        const float2 s = p.s[pos];
-        const float b = p.bv[pos];
-        const bool nan_own = isnan(s.x);
-        FF t{0.0f, 0.0f};
-        bool nan = nan_own;
-        if (!top) {
-            nan |= (E.flags & 2) != 0;
-            t = FF{E.bh, E.bl};
+    if (threadIdx.x < 32) {
+        if (tile == 0) {
+            if (threadIdx.x == 0) {
+                q.inclm[0] = total;
+                __threadfence();
+                st_release_gpu(q.status, (q.epoch << 2) | 2);
+                s_prefix = pm_identity<MIN>();
+            }
+        } else {
+            if (threadIdx.x == 0) {
+                q.aggm[tile] = total;
+                __threadfence();
+                st_release_gpu(q.status + tile, (q.epoch << 2) | 1);
+            }
+            const PMap before = look_back<MIN>(q, tile, p.flag);
+            if (threadIdx.x == 0) {
+                q.inclm[tile] = compose<MIN>(before, total);
+                __threadfence();
+                st_release_gpu(q.status + tile, (q.epoch << 2) | 2);
+                s_prefix = before;
+            }
         }
-        t.add(s.x, s.y);
-        float oh = 0.0f, ol = 0.0f, rem = 0.0f;
-        if (!rule_f32<R>(t, nan, 0.0f, b, oh, ol, rem)) {
-            oh = __int_as_float(0x7fc00000);
-            ol = 0.0f;
-            rem = oh;
+    }
+    __syncthreads();
+    ch.store(p, first, p1, compose<MIN>(s_prefix, E));
+}
+
+// The first path top at or after position s (p1 if none), for every lane of a warp.
+__device__ __forceinline__ int64_t next_top(const int32_t* order, int64_t s, int64_t p1)
+{
+    const int lane = threadIdx.x & 31;
+    for (int64_t pos = s; pos < p1; pos += 32) {
+        const unsigned m = __ballot_sync(0xffffffffu, pos + lane < p1 && __ldg(order + pos + lane) < 0);
+        if (m) return pos + __ffs(m) - 1;
+    }
+    return p1;
+}
+
+// Levels whose paths are all short (at most kPathFreeLongest cells): each CTA's range of positions is
+// cut at path tops (its nominal range with both ends moved forward to the next top), so no path crosses
+// from one CTA to another and CTAs do not wait for one another; a range is processed in chunks of
+// kPathThreads * PER positions with the composition carried from chunk to chunk.
+constexpr int kPathFreeLongest = 2048;
+
+template <Rule R, bool MIN, int PER, bool LIGHT>
+__global__ void PATH_BOUNDS(PER) k_path_free(PathCall p, int64_t p0, int64_t p1)
+{
+    __shared__ PMap s_warp[kPathThreads / 32];
+    __shared__ PMap s_carry;
+    __shared__ int64_t s_range[2];
+    const int64_t T = (int64_t)kPathThreads * PER;
+    const int64_t s0 = p0 + (int64_t)blockIdx.x * T;
+    if (threadIdx.x < 32) {
+        const int64_t lo = blockIdx.x == 0 ? p0 : next_top(p.order, s0, p1);
+        const int64_t hi = next_top(p.order, min(s0 + T, p1), p1);
+        if (threadIdx.x == 0) {
+            s_range[0] = lo;
+            s_range[1] = hi;
+            s_carry = pm_identity<MIN>();
         }
-        p.out[c] = oh;
-        p.rem[c] = rem;
-        if (pos + 1 >= p1 || __ldg(p.order + pos + 1) < 0) p.lo[c] = ol;  // a path bottom
-        E = compose<MIN>(E, cell_map<R>(top, s.x, s.y, b, nan_own));
+    }
+    __syncthreads();
+    const int64_t lo = s_range[0], hi = s_range[1];
+    for (int64_t c0 = lo; c0 < hi; c0 += T) {
+        const int64_t first = c0 + (int64_t)threadIdx.x * PER;
+        Chunk<R, MIN, PER, LIGHT, false> ch;
+        const PMap acc = ch.load(p, first, c0, min(hi, c0 + T));
+        PMap total;
+        // the scan's barriers come after thread 0's update of s_carry for the previous chunk
+        const PMap ex = block_excl_scan<MIN, kPathThreads>(acc, s_warp, total);
+        const PMap E = compose<MIN>(s_carry, ex);
+        __syncthreads();  // every thread has read s_carry
+        if (threadIdx.x == 0) s_carry = compose<MIN>(s_carry, total);
+        ch.store(p, first, p1, E);
     }
 }
 
@@ -658,30 +900,31 @@ static int path_core_get(lue_gpu_topology* t, cudaStream_t stream, const PathCor
 
 void path_buffers_free(lue_gpu_topology* t)
 {
-    cudaFree(t->path_s);
-    cudaFree(t->path_b);
     cudaFree(t->path_maps);
+    cudaFree(t->path_status);
     cudaFree(t->path_flag);
-    t->path_s = nullptr;
-    t->path_b = nullptr;
     t->path_maps = nullptr;
+    t->path_status = nullptr;
     t->path_flag = nullptr;
 }
 
-static int path_buffers(lue_gpu_topology* t, const PathCore* pc)
+constexpr int kPathMaxLevels = 256;
+
+static int path_buffers(lue_gpu_topology* t, const PathCore* pc, cudaStream_t stream)
 {
-    if (t->path_s) return LUE_GPU_OK;
+    if (t->path_maps) return LUE_GPU_OK;
     const char* what = "path engine buffers";
-    const int64_t np = std::max<int64_t>(pc->npos, 1), nt = std::max<int64_t>(pc->tiles, 1);
+    const int64_t nt = std::max<int64_t>(pc->tiles, 1);
     int rc = LUE_GPU_OK;
-    if ((rc = cuda_status(cudaMalloc(&t->path_s, np * sizeof(float2)), what)) ||
-        (rc = cuda_status(cudaMalloc(&t->path_b, np * sizeof(float)), what)) ||
-        (rc = cuda_status(cudaMalloc(&t->path_maps, 2 * nt * sizeof(PMap)), what)) ||
-        (rc = cuda_status(cudaMalloc(&t->path_flag, 2 * sizeof(unsigned long long)), what))) {
+    if ((rc = cuda_status(cudaMalloc(&t->path_maps, 2 * nt * sizeof(PMap)), what)) ||
+        (rc = cuda_status(cudaMalloc(&t->path_status, (nt + kPathMaxLevels) * sizeof(int)), what)) ||
+        (rc = cuda_status(cudaMalloc(&t->path_flag, 2 * sizeof(unsigned long long)), what)) ||
+        (rc = cuda_status(cudaMemsetAsync(t->path_status, 0, (nt + kPathMaxLevels) * sizeof(int), stream), what))) {
         path_buffers_free(t);
         return rc;
     }
-    t->scratch_bytes += np * (int64_t)(sizeof(float2) + sizeof(float)) + 2 * nt * (int64_t)sizeof(PMap) + 16;
+    t->path_epoch = 0;
+    t->scratch_bytes += 2 * nt * (int64_t)sizeof(PMap) + (nt + kPathMaxLevels) * 4 + 16;
     return LUE_GPU_OK;
 }
 
@@ -697,27 +940,58 @@ static int path_run(lue_gpu_topology* t, const PathCore* pc, const float* a, flo
 {
     const TopologyCore* core = t->core;
     const int64_t n = core->n;
-    if (int rc = path_buffers(t, pc)) return rc;
+    const int levels = (int)pc->level_offsets.size() - 1;
+    if (levels > kPathMaxLevels) return fail(LUE_GPU_ERANGE, std::string(what) + ": too many path levels");
+    if (int rc = path_buffers(t, pc, stream)) return rc;
+    const int64_t nt_max = std::max<int64_t>(pc->tiles, 1);
+    int* tickets = t->path_status + nt_max;
     if (int rc = cuda_status(cudaMemsetAsync(t->path_flag, 0, 2 * sizeof(unsigned long long), stream), what))
         return rc;
+    if (int rc = cuda_status(cudaMemsetAsync(tickets, 0, kPathMaxLevels * sizeof(int), stream), what)) return rc;
     k_path_no_data<<<grid_for(n, 256), 256, 0, stream>>>(core->fd, n, out, rem);
-    PathCall p{pc->order, pc->light, a, as, b, bs, out, rem, t->lo, t->path_s, t->path_b, t->path_flag, core->cols};
-    PMap* agg = static_cast<PMap*>(t->path_maps);
-    PMap* carry = agg + std::max<int64_t>(pc->tiles, 1);
+    PathCall p{pc->order, pc->light, a, as, b, bs, out, rem, t->lo, t->path_flag, core->cols};
+    PMap* aggm = static_cast<PMap*>(t->path_maps);
     int launches = 1;
-    int64_t tile = 0;
-    const int levels = (int)pc->level_offsets.size() - 1;
     for (int l = 0; l < levels; ++l) {
         const int64_t p0 = pc->level_offsets[l], p1 = pc->level_offsets[l + 1];
-        if (p1 <= p0) continue;
-        const int64_t nt = (p1 - p0 + kPathTile - 1) / kPathTile;
-        k_path_maps<R, MIN><<<(unsigned)nt, kPathThreads, 0, stream>>>(p, p0, p1, agg + tile);
-        if (nt > 1) k_path_carry<MIN><<<1, 1024, 0, stream>>>(agg + tile, nt, carry + tile);
-        k_path_out<R, MIN><<<(unsigned)nt, kPathThreads, 0, stream>>>(p, p0, p1, nt > 1 ? carry + tile : nullptr);
-        launches += nt > 1 ? 3 : 2;
-        tile += nt;
+        const int per = path_per(p0, p1);
+        const int64_t nt = path_level_tiles(p0, p1, per);
+        if (nt == 0) continue;
+        if (++t->path_epoch >= (1 << 29)) {  // status words of old launches could match again: clear them
+            t->path_epoch = 1;
+            if (int rc = cuda_status(cudaMemsetAsync(t->path_status, 0, nt_max * sizeof(int), stream), what))
+                return rc;
+        }
+        const dim3 grid((unsigned)nt);
+        if (pc->level_longest[l] <= kPathFreeLongest) {  // CTAs cut at path tops: no waits
+            const int64_t nf = (p1 - p0 + kPathThreads * per - 1) / (kPathThreads * per);
+            const dim3 gf((unsigned)nf);
+            switch (per * 2 + (l > 0)) {
+                case 16: k_path_free<R, MIN, 8, false><<<gf, kPathThreads, 0, stream>>>(p, p0, p1); break;
+                case 17: k_path_free<R, MIN, 8, true><<<gf, kPathThreads, 0, stream>>>(p, p0, p1); break;
+                case 8: k_path_free<R, MIN, 4, false><<<gf, kPathThreads, 0, stream>>>(p, p0, p1); break;
+                case 9: k_path_free<R, MIN, 4, true><<<gf, kPathThreads, 0, stream>>>(p, p0, p1); break;
+                case 4: k_path_free<R, MIN, 2, false><<<gf, kPathThreads, 0, stream>>>(p, p0, p1); break;
+                case 5: k_path_free<R, MIN, 2, true><<<gf, kPathThreads, 0, stream>>>(p, p0, p1); break;
+                default: k_path_free<R, MIN, 1, true><<<gf, kPathThreads, 0, stream>>>(p, p0, p1); break;
+            }
+            ++launches;
+            continue;
+        }
+        PathScan q{t->path_status, aggm, aggm + nt_max, tickets + l, t->path_epoch, kPathPolls};
+        switch (per * 2 + (l > 0)) {
+            case 16: k_path_level<R, MIN, 8, false><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
+            case 17: k_path_level<R, MIN, 8, true><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
+            case 8: k_path_level<R, MIN, 4, false><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
+            case 9: k_path_level<R, MIN, 4, true><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
+            case 4: k_path_level<R, MIN, 2, false><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
+            case 5: k_path_level<R, MIN, 2, true><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
+            default: k_path_level<R, MIN, 1, true><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
+        }
+        ++launches;
     }
-    // +-inf inputs: the walk engine redoes the whole call (as behind the tile engine of accu)
+    // +-inf inputs, or a wait of the scan that gave up: the walk engine redoes the whole call (as behind
+    // the tile engine of accu)
     const unsigned long long* flag = t->path_flag;
     k_copy_words_if<<<grid_for(words_for(n), 256), 256, 0, stream>>>(reinterpret_cast<const uint32_t*>(core->count),
                                                                      t->work_count, words_for(n), flag);

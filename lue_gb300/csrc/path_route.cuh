@@ -28,16 +28,15 @@
 
 namespace lue_gb300 {
 
-constexpr int kPathThreads = 256;                    // CTA of the per-call kernels
-constexpr int kPathPer = 8;                          // positions per thread
-constexpr int kPathTile = kPathThreads * kPathPer;  // positions per CTA
+constexpr int kPathThreads = 256;  // CTA of the per-call kernels
 
 struct PathCore {
     int64_t npos = 0;                   // valid cells (positions)
     int32_t* order = nullptr;           // [npos] cell index, bit 31 set at the top cell of a path
     uint8_t* light = nullptr;           // [npos] light upstream neighbours (bit k: neighbour k, walk order)
     std::vector<int64_t> level_offsets; // [levels + 1] first position of each level
-    int64_t tiles = 0;                  // CTA tiles over all levels
+    std::vector<int> level_longest;     // [levels] cells of the longest path of each level
+    int64_t tiles = 0;                  // most CTAs of one level's scan
     int64_t longest_path = 0;           // cells of the longest path
     int64_t bytes = 0;
 };

@@ -50,9 +50,9 @@ struct lue_gpu_topology {
     int* stage_flow_error = nullptr; // pinned: the error flag of the last dataflow launch, read by the next call
     int stage_threads = 0;           // stage engine: threads per stage CTA (0: LUE_GB300_STAGE_THREADS or by size)
     int publish_every = 0;           // stage engine: steps per progress publication (0: LUE_GB300_PUBLISH_EVERY or 4)
-    float2* path_s = nullptr;        // path engine: per position the material plus light inflow (float-float)
-    float* path_b = nullptr;         // path engine: per position the threshold / capacity
-    void* path_maps = nullptr;       // path engine: per tile its composed map and its carry
+    void* path_maps = nullptr;       // path engine: per tile of a level's scan its own and its inclusive map
+    int* path_status = nullptr;      // path engine: per tile its published state, then one ticket per level
+    int path_epoch = 0;              // path engine: tag of the last launch's status words
     unsigned long long* path_flag = nullptr;  // path engine: [2], [1] set when the walk engine must redo a call
     int64_t scratch_bytes = 0;
 };
