@@ -19,7 +19,8 @@ Reported (one JSON line, rank 0):
              measured HBM copy bandwidth; traffic from the committed ncu summary when present.
   cpu_baseline  the CPU oracle (a restatement of the reference's partitioned ridge walk, threaded
              one task per partition) on a bounded sample, rank 0 only.
-  extra.accu_threshold  accu_threshold over the same raster and material (threshold uniform [0, 0.5)).
+  extra.accu_threshold  accu_threshold over the same raster and material (threshold uniform [0, 0.5)):
+             the path engine, and the stage engine with its default and its autotuned schedule.
   extra.kinematic_wave  kinematic_wave steps over the 8192 x 8192 workload (float64 discharge).
 
 --impl reference times the reference algorithm on the CPU (the oracle port, every host core), since
@@ -396,8 +397,9 @@ def bench_ours(args, world, rank, local):
 
 def bench_threshold(args, dev, fd_d, m_d, inputs):
     """C2's second operation: accu_threshold over the same raster and material, threshold float32
-    uniform [0, 0.5) (seeded); the stage engine (one dataflow launch).  Mass balance: what the cells keep
-    plus what leaves at outlets and sinks equals the material put in."""
+    uniform [0, 0.5) (seeded), on the path engine (one launch per path level), with the stage engine
+    (default and autotuned schedule) timed beside it.  Mass balance: what the cells keep plus what leaves
+    at outlets and sinks equals the material put in."""
     import torch
 
     from lue_gb300 import framework as lfr
@@ -454,7 +456,7 @@ def bench_threshold(args, dev, fd_d, m_d, inputs):
                      "autotuned": tuned}
         finally:
             del os.environ["LUE_GB300_ENGINE"]
-    return {"workload": f"accu_16k raster and material, threshold uniform [0, 0.5) float32 ({rows}x{cols})",
+    return {"workload": f"{args.workload} raster and material, threshold uniform [0, 0.5) float32 ({rows}x{cols})",
             "calls": calls, "ms_per_call": round(1000 * s, 3), "value": round(n / s / 1e6, 3), "unit": "Mcells/s",
             "roofline_frac_hbm": round(THRESHOLD_BYTES_PER_CELL * n / s / 1e9 / peaks()[0], 4),
             "bytes_per_cell": THRESHOLD_BYTES_PER_CELL,
