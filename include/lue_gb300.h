@@ -104,9 +104,10 @@ int lue_gpu_topology_create(const uint8_t* flow_direction, int64_t rows, int64_t
 int lue_gpu_topology_clone(const lue_gpu_topology* topology, lue_gpu_topology** clone);
 int lue_gpu_topology_destroy(lue_gpu_topology* topology);
 int lue_gpu_topology_get_stats(const lue_gpu_topology* topology, lue_gpu_topology_stats* stats);
-/* Builds now, on `stream`, what the first call of an operation would otherwise build: the stage
- * structures of accu_threshold / accu_fraction / accu_capacity / accu_trigger / float64 accu /
- * kinematic_wave (shared by the clones of the handle).  Returns when they are built.  A serving loop
+/* Builds now, on `stream`, what the first call of an operation would otherwise build: the path layout of
+ * float32 accu_threshold / accu_capacity and the stage structures of accu_threshold / accu_fraction /
+ * accu_capacity / accu_trigger / float64 accu / kinematic_wave (shared by the clones of the handle).
+ * Returns when they are built.  A serving loop
  * calls it when it loads a raster, so that no request pays for it.  (No reference counterpart: the
  * reference keeps no state between calls.) */
 int lue_gpu_topology_prepare(lue_gpu_topology* topology, void* stream);
