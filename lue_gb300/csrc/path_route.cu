@@ -1,5 +1,6 @@
 // path_route.cu — the path engine (see path_route.cuh): heavy-path layout of the flow forest, built once
-// per raster, and accu_threshold / accu_capacity (float32) as one prefix scan per path level.
+// per raster, and accu_threshold / accu_fraction / accu_capacity (float32) as one prefix scan per path
+// level.
 #include <algorithm>
 #include <cmath>
 #include <string>
@@ -436,7 +437,8 @@ int path_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t strea
 // Per call
 // ---------------------------------------------------------------------------------------------------
 
-// A map x -> op(x + a, b) with op = max (threshold) or min (capacity), a and b float-float.  flags bit 0:
+// A map x -> op(x + a, b) with op = max (threshold) or min (capacity), or x -> a * x + b (fraction); a and
+// b float-float.  flags bit 0:
 // the map of a path's top cell, which ignores its input (its value is b); bit 1: no-data (NaN) from the
 // cell itself or from upstream.
 struct PMap {
@@ -444,10 +446,14 @@ struct PMap {
     int flags;
 };
 
-template <bool MIN>
+// Kinds of maps: x -> max(x + a, b) (threshold), x -> min(x + a, b) (capacity), x -> a * x + b (fraction).
+constexpr int kMaxPlus = 0, kMinPlus = 1, kAffine = 2;
+
+template <int K>
 __device__ __forceinline__ PMap pm_identity()
 {
-    return PMap{0.0f, 0.0f, MIN ? INFINITY : -INFINITY, 0.0f, 0};
+    if (K == kAffine) return PMap{1.0f, 0.0f, 0.0f, 0.0f, 0};
+    return PMap{0.0f, 0.0f, K == kMinPlus ? INFINITY : -INFINITY, 0.0f, 0};
 }
 
 // x + y for float-float values; a sum that is not finite is kept with lo = 0 (two_sum's error terms would
@@ -471,17 +477,41 @@ __device__ __forceinline__ bool ff_less(float xh, float xl, float yh, float yl)
     return xh < yh || (xh == yh && xl < yl);
 }
 
+// x * y for float-float values: the exact product of the high parts by FMA (two-product), plus the cross
+// terms, renormalised.
+__device__ __forceinline__ void ff_mul(float xh, float xl, float yh, float yl, float& rh, float& rl)
+{
+    const float p = __fmul_rn(xh, yh);
+    float e = __fmaf_rn(xh, yh, -p);
+    e = __fmaf_rn(xh, yl, e);
+    e = __fmaf_rn(xl, yh, e);
+    if (!isfinite(p)) {
+        rh = p;
+        rl = 0.0f;
+        return;
+    }
+    rh = __fadd_rn(p, e);
+    rl = __fsub_rn(e, __fsub_rn(rh, p));
+}
+
 // m1 first, then m2.
-template <bool MIN>
+template <int K>
 __device__ __forceinline__ PMap compose(const PMap& m1, const PMap& m2)
 {
     if (m2.flags & 1) return m2;
     PMap r;
     r.flags = (m1.flags & 1) | ((m1.flags | m2.flags) & 2);
+    if (K == kAffine) {  // a2 * (a1 * x + b1) + b2
+        ff_mul(m1.ah, m1.al, m2.ah, m2.al, r.ah, r.al);
+        float th, tl;
+        ff_mul(m2.ah, m2.al, m1.bh, m1.bl, th, tl);
+        ff_sum(th, tl, m2.bh, m2.bl, r.bh, r.bl);
+        return r;
+    }
     ff_sum(m1.ah, m1.al, m2.ah, m2.al, r.ah, r.al);
     float th, tl;
     ff_sum(m1.bh, m1.bl, m2.ah, m2.al, th, tl);
-    const bool take = MIN ? ff_less(th, tl, m2.bh, m2.bl) : ff_less(m2.bh, m2.bl, th, tl);
+    const bool take = K == kMinPlus ? ff_less(th, tl, m2.bh, m2.bl) : ff_less(m2.bh, m2.bl, th, tl);
     r.bh = take ? th : m2.bh;
     r.bl = take ? tl : m2.bl;
     return r;
@@ -503,6 +533,11 @@ __device__ __forceinline__ PMap cell_map(bool top, float sh, float sl, float b, 
         ff_sum(sh, sl, -b, 0.0f, dh, dl);
         return PMap{dh, dl, 0.0f, 0.0f, 0};
     }
+    if (R == Rule::fraction) {  // fraction * x + fraction * s
+        float qh, ql;
+        ff_mul(b, 0.0f, sh, sl, qh, ql);
+        return PMap{b, 0.0f, qh, ql, 0};
+    }
     return PMap{sh, sl, b, 0.0f, 0};  // capacity: min(x + s, capacity)
 }
 
@@ -518,30 +553,30 @@ __device__ __forceinline__ PMap shfl_up(const PMap& m, int d)
 }
 
 // Exclusive scan of the threads' maps in thread order; `total` is the composition of all of them.
-template <bool MIN, int NT>
+template <int K, int NT>
 __device__ __forceinline__ PMap block_excl_scan(const PMap& v, PMap* s_warp, PMap& total)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     PMap x = v;
     for (int d = 1; d < 32; d <<= 1) {
         const PMap y = shfl_up(x, d);
-        if (lane >= d) x = compose<MIN>(y, x);
+        if (lane >= d) x = compose<K>(y, x);
     }
     PMap ex = shfl_up(x, 1);
-    if (lane == 0) ex = pm_identity<MIN>();
+    if (lane == 0) ex = pm_identity<K>();
     if (lane == 31) s_warp[warp] = x;
     __syncthreads();
     if (warp == 0) {
-        PMap w = lane < NT / 32 ? s_warp[lane] : pm_identity<MIN>();
+        PMap w = lane < NT / 32 ? s_warp[lane] : pm_identity<K>();
         for (int d = 1; d < 32; d <<= 1) {
             const PMap y = shfl_up(w, d);
-            if (lane >= d) w = compose<MIN>(y, w);
+            if (lane >= d) w = compose<K>(y, w);
         }
         if (lane < NT / 32) s_warp[lane] = w;
     }
     __syncthreads();
     total = s_warp[NT / 32 - 1];
-    const PMap r = warp ? compose<MIN>(s_warp[warp - 1], ex) : ex;
+    const PMap r = warp ? compose<K>(s_warp[warp - 1], ex) : ex;
     __syncthreads();
     return r;
 }
@@ -633,15 +668,15 @@ constexpr int kPathPolls = 1 << 20;
 // Warp 0: the composition of all tiles before `tile` (in every lane).  Lane i looks at tile j - i, 32 at
 // a time, until a tile with a published prefix is among them.  Every wait is bounded: a wait that gives
 // up (or finds that another one did) sets flag[1], after which the walk engine redoes the call.
-template <bool MIN>
+template <int K>
 __device__ PMap look_back(const PathScan& q, int64_t tile, unsigned long long* flag)
 {
     const int lane = threadIdx.x & 31;
-    PMap running = pm_identity<MIN>();
+    PMap running = pm_identity<K>();
     for (int64_t j = tile - 1;; j -= 32) {
         const int64_t idx = j - lane;
         int st = 2;
-        PMap m = pm_identity<MIN>();
+        PMap m = pm_identity<K>();
         if (idx >= 0) {
             int v = 0, k = 0;
             for (; k < q.polls; ++k) {
@@ -659,19 +694,19 @@ __device__ PMap look_back(const PathScan& q, int64_t tile, unsigned long long* f
         }
         if (__ballot_sync(0xffffffffu, st < 0)) {
             if (lane == 0) flag[1] = 1;
-            return pm_identity<MIN>();
+            return pm_identity<K>();
         }
         const unsigned incl = __ballot_sync(0xffffffffu, st == 2);
-        if (incl && lane > __ffs(incl) - 1) m = pm_identity<MIN>();
+        if (incl && lane > __ffs(incl) - 1) m = pm_identity<K>();
         // lanes 31 .. 0 in this order (farther tiles come first)
         for (int d = 1; d < 32; d <<= 1) {
             const PMap o = shfl_down(m, d);
-            if (lane + d < 32) m = compose<MIN>(o, m);
+            if (lane + d < 32) m = compose<K>(o, m);
         }
         const PMap window = PMap{__shfl_sync(0xffffffffu, m.ah, 0), __shfl_sync(0xffffffffu, m.al, 0),
                                  __shfl_sync(0xffffffffu, m.bh, 0), __shfl_sync(0xffffffffu, m.bl, 0),
                                  __shfl_sync(0xffffffffu, m.flags, 0)};
-        running = compose<MIN>(window, running);
+        running = compose<K>(window, running);
         if (incl) return running;
     }
 }
@@ -680,7 +715,7 @@ __device__ PMap look_back(const PathScan& q, int64_t tile, unsigned long long* f
 // active.  load(): inputs, light inflow and the cells' maps, composed in order; store(): from the
 // composition E of everything before the first position, each cell's rule and outputs.  VEC: `first` is
 // a multiple of PER and the order array is read with vector loads.
-template <Rule R, bool MIN, int PER, bool LIGHT, bool VEC>
+template <Rule R, int K, int PER, bool LIGHT, bool VEC>
 struct Chunk {
     int32_t w[PER];
     bool on[PER];
@@ -721,16 +756,17 @@ struct Chunk {
                 }
             }
         }
-        PMap acc = pm_identity<MIN>();
+        PMap acc = pm_identity<K>();
         bool odd = false;
 #pragma unroll
         for (int j = 0; j < PER; ++j) {
             if (!on[j]) continue;
-            nan[j] |= isnan(e[j]) || isnan(b[j]) || !(e[j] >= 0.0f && b[j] >= 0.0f);
+            nan[j] |= isnan(e[j]) || isnan(b[j]) || !(e[j] >= 0.0f && b[j] >= 0.0f) ||
+                      (R == Rule::fraction && !(b[j] <= 1.0f));
             sum[j].add(e[j]);
             sum[j].normalise();
             odd |= !nan[j] && (isinf(e[j]) || isinf(b[j]) || isinf(sum[j].hi));
-            acc = compose<MIN>(acc, cell_map<R>(w[j] < 0, sum[j].hi, sum[j].lo, b[j], nan[j]));
+            acc = compose<K>(acc, cell_map<R>(w[j] < 0, sum[j].hi, sum[j].lo, b[j], nan[j]));
         }
         if (odd) p.flag[1] = 1;  // +-inf: the walk engine redoes the call
         return acc;
@@ -762,7 +798,7 @@ struct Chunk {
             p.rem[c] = rem;
             const int32_t next = j + 1 < PER ? w[(j + 1) % PER] : after;
             if (first + j + 1 >= p1 || next < 0) p.lo[c] = ol;  // a path bottom
-            E = compose<MIN>(E, cell_map<R>(top, sum[j].hi, sum[j].lo, b[j], nan[j]));
+            E = compose<K>(E, cell_map<R>(top, sum[j].hi, sum[j].lo, b[j], nan[j]));
         }
     }
 };
@@ -771,7 +807,7 @@ struct Chunk {
 
 // One level in one pass, for levels with long paths: tiles in ticket order, the composition of the
 // tiles before each one by decoupled look-back.
-template <Rule R, bool MIN, int PER, bool LIGHT>
+template <Rule R, int K, int PER, bool LIGHT>
 __global__ void PATH_BOUNDS(PER) k_path_level(PathCall p, int64_t p0, int64_t p1, PathScan q)
 {
     __shared__ PMap s_warp[kPathThreads / 32];
@@ -781,17 +817,17 @@ __global__ void PATH_BOUNDS(PER) k_path_level(PathCall p, int64_t p0, int64_t p1
     __syncthreads();
     const int64_t tile = s_tile;
     const int64_t first = chunk_base<PER>(p0) + tile * (kPathThreads * PER) + (int64_t)threadIdx.x * PER;
-    Chunk<R, MIN, PER, LIGHT, true> ch;
+    Chunk<R, K, PER, LIGHT, true> ch;
     const PMap acc = ch.load(p, first, p0, p1);
     PMap total;
-    PMap E = block_excl_scan<MIN, kPathThreads>(acc, s_warp, total);
+    PMap E = block_excl_scan<K, kPathThreads>(acc, s_warp, total);
     if (threadIdx.x < 32) {
         if (tile == 0) {
             if (threadIdx.x == 0) {
                 q.inclm[0] = total;
                 __threadfence();
                 st_release_gpu(q.status, (q.epoch << 2) | 2);
-                s_prefix = pm_identity<MIN>();
+                s_prefix = pm_identity<K>();
             }
         } else {
             if (threadIdx.x == 0) {
@@ -799,9 +835,9 @@ __global__ void PATH_BOUNDS(PER) k_path_level(PathCall p, int64_t p0, int64_t p1
                 __threadfence();
                 st_release_gpu(q.status + tile, (q.epoch << 2) | 1);
             }
-            const PMap before = look_back<MIN>(q, tile, p.flag);
+            const PMap before = look_back<K>(q, tile, p.flag);
             if (threadIdx.x == 0) {
-                q.inclm[tile] = compose<MIN>(before, total);
+                q.inclm[tile] = compose<K>(before, total);
                 __threadfence();
                 st_release_gpu(q.status + tile, (q.epoch << 2) | 2);
                 s_prefix = before;
@@ -809,7 +845,7 @@ __global__ void PATH_BOUNDS(PER) k_path_level(PathCall p, int64_t p0, int64_t p1
         }
     }
     __syncthreads();
-    ch.store(p, first, p1, compose<MIN>(s_prefix, E));
+    ch.store(p, first, p1, compose<K>(s_prefix, E));
 }
 
 // The first path top at or after position s (p1 if none), for every lane of a warp.
@@ -829,7 +865,7 @@ __device__ __forceinline__ int64_t next_top(const int32_t* order, int64_t s, int
 // kPathThreads * PER positions with the composition carried from chunk to chunk.
 constexpr int kPathFreeLongest = 2048;
 
-template <Rule R, bool MIN, int PER, bool LIGHT>
+template <Rule R, int K, int PER, bool LIGHT>
 __global__ void PATH_BOUNDS(PER) k_path_free(PathCall p, int64_t p0, int64_t p1)
 {
     __shared__ PMap s_warp[kPathThreads / 32];
@@ -843,21 +879,21 @@ __global__ void PATH_BOUNDS(PER) k_path_free(PathCall p, int64_t p0, int64_t p1)
         if (threadIdx.x == 0) {
             s_range[0] = lo;
             s_range[1] = hi;
-            s_carry = pm_identity<MIN>();
+            s_carry = pm_identity<K>();
         }
     }
     __syncthreads();
     const int64_t lo = s_range[0], hi = s_range[1];
     for (int64_t c0 = lo; c0 < hi; c0 += T) {
         const int64_t first = c0 + (int64_t)threadIdx.x * PER;
-        Chunk<R, MIN, PER, LIGHT, false> ch;
+        Chunk<R, K, PER, LIGHT, false> ch;
         const PMap acc = ch.load(p, first, c0, min(hi, c0 + T));
         PMap total;
         // the scan's barriers come after thread 0's update of s_carry for the previous chunk
-        const PMap ex = block_excl_scan<MIN, kPathThreads>(acc, s_warp, total);
-        const PMap E = compose<MIN>(s_carry, ex);
+        const PMap ex = block_excl_scan<K, kPathThreads>(acc, s_warp, total);
+        const PMap E = compose<K>(s_carry, ex);
         __syncthreads();  // every thread has read s_carry
-        if (threadIdx.x == 0) s_carry = compose<MIN>(s_carry, total);
+        if (threadIdx.x == 0) s_carry = compose<K>(s_carry, total);
         ch.store(p, first, p1, E);
     }
 }
@@ -934,7 +970,7 @@ int path_prepare(lue_gpu_topology* t, cudaStream_t stream)
     return path_core_get(t, stream, &pc);
 }
 
-template <Rule R, bool MIN>
+template <Rule R, int K>
 static int path_run(lue_gpu_topology* t, const PathCore* pc, const float* a, float as, const float* b, float bs,
                     float* out, float* rem, cudaStream_t stream, const char* what)
 {
@@ -967,26 +1003,26 @@ static int path_run(lue_gpu_topology* t, const PathCore* pc, const float* a, flo
             const int64_t nf = (p1 - p0 + kPathThreads * per - 1) / (kPathThreads * per);
             const dim3 gf((unsigned)nf);
             switch (per * 2 + (l > 0)) {
-                case 16: k_path_free<R, MIN, 8, false><<<gf, kPathThreads, 0, stream>>>(p, p0, p1); break;
-                case 17: k_path_free<R, MIN, 8, true><<<gf, kPathThreads, 0, stream>>>(p, p0, p1); break;
-                case 8: k_path_free<R, MIN, 4, false><<<gf, kPathThreads, 0, stream>>>(p, p0, p1); break;
-                case 9: k_path_free<R, MIN, 4, true><<<gf, kPathThreads, 0, stream>>>(p, p0, p1); break;
-                case 4: k_path_free<R, MIN, 2, false><<<gf, kPathThreads, 0, stream>>>(p, p0, p1); break;
-                case 5: k_path_free<R, MIN, 2, true><<<gf, kPathThreads, 0, stream>>>(p, p0, p1); break;
-                default: k_path_free<R, MIN, 1, true><<<gf, kPathThreads, 0, stream>>>(p, p0, p1); break;
+                case 16: k_path_free<R, K, 8, false><<<gf, kPathThreads, 0, stream>>>(p, p0, p1); break;
+                case 17: k_path_free<R, K, 8, true><<<gf, kPathThreads, 0, stream>>>(p, p0, p1); break;
+                case 8: k_path_free<R, K, 4, false><<<gf, kPathThreads, 0, stream>>>(p, p0, p1); break;
+                case 9: k_path_free<R, K, 4, true><<<gf, kPathThreads, 0, stream>>>(p, p0, p1); break;
+                case 4: k_path_free<R, K, 2, false><<<gf, kPathThreads, 0, stream>>>(p, p0, p1); break;
+                case 5: k_path_free<R, K, 2, true><<<gf, kPathThreads, 0, stream>>>(p, p0, p1); break;
+                default: k_path_free<R, K, 1, true><<<gf, kPathThreads, 0, stream>>>(p, p0, p1); break;
             }
             ++launches;
             continue;
         }
         PathScan q{t->path_status, aggm, aggm + nt_max, tickets + l, t->path_epoch, kPathPolls};
         switch (per * 2 + (l > 0)) {
-            case 16: k_path_level<R, MIN, 8, false><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
-            case 17: k_path_level<R, MIN, 8, true><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
-            case 8: k_path_level<R, MIN, 4, false><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
-            case 9: k_path_level<R, MIN, 4, true><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
-            case 4: k_path_level<R, MIN, 2, false><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
-            case 5: k_path_level<R, MIN, 2, true><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
-            default: k_path_level<R, MIN, 1, true><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
+            case 16: k_path_level<R, K, 8, false><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
+            case 17: k_path_level<R, K, 8, true><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
+            case 8: k_path_level<R, K, 4, false><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
+            case 9: k_path_level<R, K, 4, true><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
+            case 4: k_path_level<R, K, 2, false><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
+            case 5: k_path_level<R, K, 2, true><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
+            default: k_path_level<R, K, 1, true><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
         }
         ++launches;
     }
@@ -1007,14 +1043,17 @@ int path_route_f32(lue_gpu_topology* t, int rule, const float* a, float as, cons
 {
     *done = false;
     if (path_engine_off()) return LUE_GPU_OK;
-    if (rule != (int)Rule::threshold && rule != (int)Rule::capacity) return LUE_GPU_OK;
+    if (rule != (int)Rule::threshold && rule != (int)Rule::capacity && rule != (int)Rule::fraction)
+        return LUE_GPU_OK;
     const PathCore* pc = nullptr;
     if (int rc = path_core_get(t, stream, &pc)) return rc;
     if (!pc) return LUE_GPU_OK;
     *done = true;
     if (rule == (int)Rule::threshold)
-        return path_run<Rule::threshold, false>(t, pc, a, as, b, bs, out, rem, stream, "accu_threshold_f32 (paths)");
-    return path_run<Rule::capacity, true>(t, pc, a, as, b, bs, out, rem, stream, "accu_capacity_f32 (paths)");
+        return path_run<Rule::threshold, kMaxPlus>(t, pc, a, as, b, bs, out, rem, stream, "accu_threshold_f32 (paths)");
+    if (rule == (int)Rule::fraction)
+        return path_run<Rule::fraction, kAffine>(t, pc, a, as, b, bs, out, rem, stream, "accu_fraction_f32 (paths)");
+    return path_run<Rule::capacity, kMinPlus>(t, pc, a, as, b, bs, out, rem, stream, "accu_capacity_f32 (paths)");
 }
 
 }  // namespace lue_gb300

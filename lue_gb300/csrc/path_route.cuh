@@ -1,12 +1,13 @@
-// path_route.cuh — the path engine: accu_threshold and accu_capacity (float32) as prefix scans along
-// the heavy paths of the flow forest.
+// path_route.cuh — the path engine: accu_threshold, accu_fraction and accu_capacity (float32) as prefix
+// scans along the heavy paths of the flow forest.
 //
 // Along one flow path the threshold rule maps the outflow x of the upstream cell to
-// max(x + s - threshold, 0), and the capacity rule to min(x + s, capacity), where s is the material of the
-// cell plus the outflow of its other upstream cells.  Maps x -> max(x + a, b) (and x -> min(x + a, b))
-// compose into maps of the same form, so the outflows of a whole path follow from a prefix scan of the
-// per-cell maps instead of a cell-by-cell walk (ALG/definition/accumulating_router.hpp:525-599 walks
-// them one cell after the other, ALG/definition/accu_threshold.hpp:124-169 and
+// max(x + s - threshold, 0), the fraction rule to fraction * (x + s) and the capacity rule to
+// min(x + s, capacity), where s is the material of the cell plus the outflow of its other upstream cells.
+// Maps x -> max(x + a, b), x -> a * x + b and x -> min(x + a, b) compose into maps of the same form, so the
+// outflows of a whole path follow from a prefix scan of the per-cell maps instead of a cell-by-cell walk
+// (ALG/definition/accumulating_router.hpp:525-599 walks them one cell after the other;
+// ALG/definition/accu_threshold.hpp:124-169, ALG/definition/accu_fraction.hpp:124-162 and
 // ALG/definition/accu_capacity.hpp enter_cell are the cell rules).
 //
 // The flow forest is cut into heavy paths: each cell continues the path of its upstream neighbour with
@@ -54,7 +55,7 @@ struct lue_gpu_topology;
 
 namespace lue_gb300 {
 
-// accu_threshold (rule 1) and accu_capacity (rule 3), float32.  *done is false when the engine does not
+// accu_threshold (rule 1), accu_fraction (rule 2) and accu_capacity (rule 3), float32.  *done is false when the engine does not
 // apply (flow cycles, a raster beyond its limits, LUE_GB300_ENGINE=walk or =stage): the caller then runs
 // another engine.
 int path_route_f32(lue_gpu_topology* t, int rule, const float* a, float as, const float* b, float bs, float* out,

@@ -168,6 +168,8 @@ extern "C" int lue_gpu_accu_fraction_f32(lue_gpu_topology* t, const float* inflo
 {
     if (int rc = check_topology(t, "accu_fraction_f32")) return rc;
     if (!flux || !state) return fail(LUE_GPU_EINVAL, "accu_fraction_f32: NULL output");
+    STAGE_OR_WALK(path_route_f32(t, (int)Rule::fraction, inflow, inflow_scalar, fraction, fraction_scalar, flux,
+                                 state, (cudaStream_t)stream, &done));
     STAGE_OR_WALK(stage_route_f32(t, (int)Rule::fraction, inflow, inflow_scalar, fraction, fraction_scalar, flux,
                                   state, (cudaStream_t)stream, &done));
     return route_f32<Rule::fraction>(t, inflow, inflow_scalar, fraction, fraction_scalar, flux, state, stream,
@@ -186,7 +188,8 @@ extern "C" int lue_gpu_accu_fraction_f64(lue_gpu_topology* t, const double* infl
                                      "accu_fraction_f64");
 }
 
-// The path engine (path_route.cuh) takes float32 accu_threshold and accu_capacity on acyclic rasters.
+// The path engine (path_route.cuh) takes float32 accu_threshold, accu_fraction and accu_capacity on acyclic
+// rasters.
 static int path_first(lue_gpu_topology* t, int rule, const float* a, float as, const float* b, float bs, float* out,
                       float* rem, cudaStream_t stream, bool* done)
 {

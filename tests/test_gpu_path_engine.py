@@ -1,7 +1,7 @@
-"""The path engine (float32 accu_threshold and accu_capacity on acyclic rasters): outflows along the heavy
-paths of the flow forest from prefix scans of the cell rules' maps, level by level.
+"""The path engine (float32 accu_threshold, accu_fraction and accu_capacity on acyclic rasters): outflows
+along the heavy paths of the flow forest from prefix scans of the cell rules' maps, level by level.
 
-It is the default engine of these two operations, so the reference's known-answer cases
+It is the default engine of these three operations, so the reference's known-answer cases
 (test_gpu_golden.py) and the synthetic parity tests (test_gpu_parity.py) run through it too.  Here:
 parity against the float64 oracle and against the walk engine on rasters with no-data holes, NaN and
 negative material, ragged shapes and long flow paths; scalar overloads; +inf material (the walk engine
@@ -16,7 +16,7 @@ from tests import parity
 
 pytestmark = pytest.mark.gpu
 
-OPS = ("threshold", "capacity")
+OPS = ("threshold", "fraction", "capacity")
 
 
 @pytest.fixture(scope="module")
@@ -38,7 +38,19 @@ def _raster(rows, cols, seed, amplitude=40.0, holes=0.0, wavelength=None):
 def _ops(lfr, op):
     if op == "threshold":
         return lfr.accu_threshold, oracle.accu_threshold
+    if op == "fraction":
+        return lfr.accu_fraction, oracle.accu_fraction
     return lfr.accu_capacity, oracle.accu_capacity
+
+
+def _other(rng, shape, op, scale=None):
+    """Threshold U[0, 0.5), fraction U[0, 1) with a few values above 1 (outside the domain), capacity
+    U[0, 3)."""
+    if op == "fraction":
+        b = rng.random(shape).astype(np.float32)
+        b[rng.random(shape) < 0.0005] = 1.5
+        return b
+    return (rng.random(shape) * (scale or (0.5 if op == "threshold" else 3.0))).astype(np.float32)
 
 
 def _run(lfr, op, fd, m, b, ps, engine=None, monkeypatch=None):
@@ -61,7 +73,7 @@ def test_path_engine_against_oracle_and_walk_engine(lfr, monkeypatch, shape, op)
     m = rng.lognormal(0.0, 1.0, shape).astype(np.float32)
     m[rng.random(shape) < 0.001] = np.nan
     m[rng.random(shape) < 0.001] = -1.0
-    b = (rng.random(shape) * (0.5 if op == "threshold" else 3.0)).astype(np.float32)
+    b = _other(rng, shape, op)
     b[rng.random(shape) < 0.0005] = np.nan
     ps = (min(256, shape[0]), min(256, shape[1]))
     got = _run(lfr, op, fd, m, b, ps)
@@ -80,7 +92,9 @@ def test_long_paths_and_mass_balance(lfr, op):
     and paths of thousands of cells, each cut across many CTAs of the scan."""
     fd, rng = _raster(2048, 2048, seed=73, amplitude=200.0, wavelength=2048)
     m = rng.lognormal(0.0, 1.0, fd.shape).astype(np.float32)
-    b = (rng.random(fd.shape) * (0.5 if op == "threshold" else 50.0)).astype(np.float32)
+    b = _other(rng, fd.shape, op, scale=0.5 if op == "threshold" else 50.0)
+    if op == "fraction":
+        b = np.minimum(b, 1.0).astype(np.float32)
     out, rem = _run(lfr, op, fd, m, b, (512, 512))
     _, cpu = _ops(lfr, op)
     wo, wr = cpu(fd, m.astype(np.float64), b.astype(np.float64), (512, 512), dtype=np.float64)
