@@ -546,6 +546,12 @@ def bench_ensemble(args, dev):
     steps = 48
     s_graph, atlas, _, stats = ensemble.run_batched(inst, steps, device=dev, graph=True)
     s_waves, _, _, _ = ensemble.run_batched(inst, steps, device=dev, waves=True)
+    tuned = None
+    if not args.no_autotune:
+        s_tuned, _, _, tstats = ensemble.run_batched(inst, steps, device=dev, waves=True, autotune_steps=4)
+        tuned = {"schedule": tstats["stage_schedule"], "tuned_on": "a 4-step call of the same atlas",
+                 "tuning_s": tstats["tuning_s"], "batched_waves_s": round(s_tuned, 3),
+                 "batched_waves_mcells_per_s": round(cells * steps / s_tuned / 1e6, 3)}
     sample = 8
     s_alone, cells_alone, _ = ensemble.run_unbatched(inst, steps, sample, device=dev)
     return {"workload": "64 catchments (sides log-uniform 512-4096, depression-filled D8) x 4 rain scenarios, "
@@ -555,6 +561,7 @@ def bench_ensemble(args, dev):
             "batched_graph_s": round(s_graph, 3),
             "batched_waves_mcells_per_s": round(cells * steps / s_waves / 1e6, 3),
             "batched_waves_s": round(s_waves, 3),
+            "batched_waves_autotuned": tuned,
             "one_launch_per_instance_mcells_per_s": round(cells_alone * steps / s_alone / 1e6, 3),
             "one_launch_per_instance_sample": f"first {sample} instances, topology built per instance"}
 

@@ -97,11 +97,13 @@ def ensemble_inputs(n_catchments=64, scenarios=4, lo=512, hi=4096, seed=11, devi
     return inst
 
 
-def run_batched(inst, steps, device="cuda", graph=True, partition=(1024, 1024), waves=False):
+def run_batched(inst, steps, device="cuda", graph=True, partition=(1024, 1024), waves=False, autotune_steps=0):
     """All instances in one atlas.  waves=False: one kinematic_wave launch per step, the steps captured
     in one CUDA graph (graph=True) or launched in a loop; waves=True: all steps in one
-    kinematic_wave_steps call (time-skewed level waves).
-    Returns (seconds for `steps` steps, atlas, final discharge atlas tensor, topology stats)."""
+    kinematic_wave_steps call (the stage engine's pipelined steps).  autotune_steps > 0 (waves=True):
+    first autotune the stage schedule of the atlas on a call of that many steps, then time `steps`.
+    Returns (seconds for `steps` steps, atlas, final discharge atlas tensor, topology stats); with
+    autotune_steps, the stats carry the schedule (`stage_schedule`) and the tuning time (`tuning_s`)."""
     import torch
 
     from . import framework as lfr
@@ -136,6 +138,21 @@ def run_batched(inst, steps, device="cuda", graph=True, partition=(1024, 1024), 
                                                             alpha.data_ptr(), 0.0, 0.6, 3600.0, 100.0, steps,
                                                             out.data_ptr(), stream.cuda_stream))
         torch.cuda.synchronize()
+        stats = topo.stats()
+        if autotune_steps > 0:
+            def short_call():
+                _lib.check(L.lue_gpu_kinematic_wave_steps_f64_f32in(
+                    topo.handle, q0.data_ptr(), lat.data_ptr(), 0.0, alpha.data_ptr(), 0.0, 0.6, 3600.0, 100.0,
+                    autotune_steps, out.data_ptr(), stream.cuda_stream))
+            t0 = time.perf_counter()
+            best = lfr.autotune_stage_schedule(fdA, short_call)
+            stats["tuning_s"] = round(time.perf_counter() - t0, 2)
+            stats["stage_schedule"] = {k: best[k] for k in ("cap", "threads", "publish_every")}
+            # the full call once with the chosen schedule (a new cap rebuilds the stages and the history)
+            _lib.check(L.lue_gpu_kinematic_wave_steps_f64_f32in(topo.handle, q0.data_ptr(), lat.data_ptr(), 0.0,
+                                                                alpha.data_ptr(), 0.0, 0.6, 3600.0, 100.0, steps,
+                                                                out.data_ptr(), stream.cuda_stream))
+            torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         _lib.check(L.lue_gpu_kinematic_wave_steps_f64_f32in(topo.handle, q0.data_ptr(), lat.data_ptr(), 0.0,
@@ -143,7 +160,7 @@ def run_batched(inst, steps, device="cuda", graph=True, partition=(1024, 1024), 
                                                             out.data_ptr(), stream.cuda_stream))
         e1.record()
         torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / 1000.0, atlas, out, topo.stats()
+        return e0.elapsed_time(e1) / 1000.0, atlas, out, stats
     if graph:
         s = torch.cuda.Stream(device)
         s.wait_stream(torch.cuda.current_stream(device))

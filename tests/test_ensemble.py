@@ -33,3 +33,16 @@ def test_batched_results_equal_each_instance_alone():
     for i, qa in enumerate(alone):
         got = atlas.view(q, i).cpu().numpy()
         assert np.array_equal(got, qa.cpu().numpy()), i  # same kernels, same inputs: bitwise equal
+
+
+@pytest.mark.gpu
+def test_autotuned_multi_step_atlas_equals_the_default_schedule():
+    """The batched multi-step call with the stage schedule autotuned on a shorter call gives the same bits
+    as with the default schedule."""
+    import torch
+    assert torch.cuda.is_available()
+    inst = ensemble.ensemble_inputs(n_catchments=3, scenarios=2, lo=64, hi=200, seed=7)
+    _, atlas, q_default, _ = ensemble.run_batched(inst, steps=6, waves=True)
+    _, _, q_tuned, stats = ensemble.run_batched(inst, steps=6, waves=True, autotune_steps=2)
+    assert stats["stage_schedule"]["cap"] in (64, 128, 256)
+    assert torch.equal(q_default, q_tuned)
