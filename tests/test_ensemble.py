@@ -45,4 +45,4 @@ def test_autotuned_multi_step_atlas_equals_the_default_schedule():
     _, atlas, q_default, _ = ensemble.run_batched(inst, steps=6, waves=True)
     _, _, q_tuned, stats = ensemble.run_batched(inst, steps=6, waves=True, autotune_steps=2)
     assert stats["stage_schedule"]["cap"] in (64, 128, 256)
-    assert torch.equal(q_default, q_tuned)
+    assert np.array_equal(q_default.cpu().numpy(), q_tuned.cpu().numpy(), equal_nan=True)  # NaN: atlas borders
