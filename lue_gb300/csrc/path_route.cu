@@ -986,6 +986,12 @@ static int path_run(lue_gpu_topology* t, const PathCore* pc, const float* a, flo
     if (int rc = cuda_status(cudaMemsetAsync(tickets, 0, kPathMaxLevels * sizeof(int), stream), what)) return rc;
     k_path_no_data<<<grid_for(n, 256), 256, 0, stream>>>(core->fd, n, out, rem);
     PathCall p{pc->order, pc->light, a, as, b, bs, out, rem, t->lo, t->path_flag, core->cols};
+    // test hooks: LUE_GB300_PATH_FREE_LONGEST (levels with longer paths use the look-back scan; 0: every
+    // level) and LUE_GB300_PATH_POLLS (poll limit of a look-back wait; 0: every wait gives up at once,
+    // and the walk engine redoes the call)
+    int free_longest = kPathFreeLongest, polls = kPathPolls;
+    if (const char* e = getenv("LUE_GB300_PATH_FREE_LONGEST")) free_longest = std::max(0, atoi(e));
+    if (const char* e = getenv("LUE_GB300_PATH_POLLS")) polls = std::max(0, atoi(e));
     PMap* aggm = static_cast<PMap*>(t->path_maps);
     int launches = 1;
     for (int l = 0; l < levels; ++l) {
@@ -999,7 +1005,7 @@ static int path_run(lue_gpu_topology* t, const PathCore* pc, const float* a, flo
                 return rc;
         }
         const dim3 grid((unsigned)nt);
-        if (pc->level_longest[l] <= kPathFreeLongest) {  // CTAs cut at path tops: no waits
+        if (pc->level_longest[l] <= free_longest) {  // CTAs cut at path tops: no waits
             const int64_t nf = (p1 - p0 + kPathThreads * per - 1) / (kPathThreads * per);
             const dim3 gf((unsigned)nf);
             switch (per * 2 + (l > 0)) {
@@ -1014,7 +1020,7 @@ static int path_run(lue_gpu_topology* t, const PathCore* pc, const float* a, flo
             ++launches;
             continue;
         }
-        PathScan q{t->path_status, aggm, aggm + nt_max, tickets + l, t->path_epoch, kPathPolls};
+        PathScan q{t->path_status, aggm, aggm + nt_max, tickets + l, t->path_epoch, polls};
         switch (per * 2 + (l > 0)) {
             case 16: k_path_level<R, K, 8, false><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;
             case 17: k_path_level<R, K, 8, true><<<grid, kPathThreads, 0, stream>>>(p, p0, p1, q); break;

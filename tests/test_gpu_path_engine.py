@@ -168,3 +168,38 @@ def test_prepare_builds_the_paths(lfr):
     wo, wr = oracle.accu_threshold(fd, m.astype(np.float64), 0.25, fd.shape, dtype=np.float64)
     parity.assert_close32(lfr.to_numpy(out), wo, "outflow after prepare")
     parity.assert_close32(lfr.to_numpy(rem), wr, "remainder after prepare")
+
+
+@pytest.mark.parametrize("op", OPS)
+def test_look_back_scan_on_every_level(lfr, monkeypatch, op):
+    """LUE_GB300_PATH_FREE_LONGEST=0 sends every level through the decoupled look-back scan (used on
+    levels of long paths), here on a raster of short ones with no-data holes and NaN material."""
+    monkeypatch.setenv("LUE_GB300_PATH_FREE_LONGEST", "0")
+    fd, rng = _raster(700, 900, seed=83, holes=0.001)
+    m = rng.lognormal(0.0, 1.0, fd.shape).astype(np.float32)
+    m[rng.random(fd.shape) < 0.001] = np.nan
+    b = _other(rng, fd.shape, op)
+    got = _run(lfr, op, fd, m, b, (256, 256))
+    _, cpu = _ops(lfr, op)
+    want = cpu(fd, m.astype(np.float64), b.astype(np.float64), (256, 256), dtype=np.float64)
+    for g, w, name in zip(got, want, ("outflow", "remainder")):
+        parity.assert_close32(g, w, f"{op} {name}, look-back on every level")
+
+
+def test_look_back_waits_that_give_up_are_redone_by_the_walk_engine(lfr, monkeypatch):
+    """Every wait of the look-back gives up at once (LUE_GB300_PATH_POLLS=0): the kernel sets the redo
+    flag, the walk engine redoes the call, and the results are the walk engine's bit for bit."""
+    fd, rng = _raster(500, 600, seed=85, holes=0.001)
+    m = rng.lognormal(0.0, 1.0, fd.shape).astype(np.float32)
+    b = _other(rng, fd.shape, "threshold")
+    monkeypatch.setenv("LUE_GB300_PATH_FREE_LONGEST", "0")
+    monkeypatch.setenv("LUE_GB300_PATH_POLLS", "0")
+    got = _run(lfr, "threshold", fd, m, b, fd.shape)
+    monkeypatch.delenv("LUE_GB300_PATH_FREE_LONGEST")
+    monkeypatch.delenv("LUE_GB300_PATH_POLLS")
+    walk = _run(lfr, "threshold", fd, m, b, fd.shape, engine="walk", monkeypatch=monkeypatch)
+    for g, w in zip(got, walk):
+        assert np.array_equal(g, w, equal_nan=True)
+    again = _run(lfr, "threshold", fd, m, b, fd.shape)  # the next call is a normal one
+    for g, w in zip(again, walk):
+        parity.assert_close32(g, w.astype(np.float64), "after a call that gave up")
