@@ -438,9 +438,8 @@ int path_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t strea
 // ---------------------------------------------------------------------------------------------------
 
 // A map x -> op(x + a, b) with op = max (threshold) or min (capacity), or x -> a * x + b (fraction); a and
-// b float-float.  flags bit 0:
-// the map of a path's top cell, which ignores its input (its value is b); bit 1: no-data (NaN) from the
-// cell itself or from upstream.
+// b float-float.  flags bit 0: the map of a path's top cell, which ignores its input (its value is b);
+// bit 1: no-data (NaN) from the cell itself or from upstream.
 struct PMap {
     float ah, al, bh, bl;
     int flags;
@@ -586,7 +585,7 @@ struct PathCall {
     const uint8_t* __restrict__ light;
     const float* __restrict__ a;  // material
     float as;
-    const float* __restrict__ b;  // threshold / capacity
+    const float* __restrict__ b;  // threshold / fraction / capacity
     float bs;
     float* out;
     float* rem;
@@ -595,9 +594,9 @@ struct PathCall {
     int64_t cols;
 };
 
-// The positions of one thread: PER consecutive positions from `first`; those outside [p0, p1) (the
-// 8-aligned chunks of PER = 8 may start before a level or end after it) are inactive.  PER = 8 loads
-// the position arrays with vector loads (the arrays are padded to whole chunks).
+// The order entries of PER consecutive positions from `first` (a multiple of PER), read with vector
+// loads; the position arrays are padded by one 8-position chunk, so a chunk that starts before the end
+// of the array stays inside it.
 template <int PER>
 __device__ __forceinline__ void load_order(const PathCall& p, int64_t first, int32_t (&w)[PER])
 {
