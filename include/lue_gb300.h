@@ -7,6 +7,7 @@
  *   LUE operation (C++ template, PartitionedArray in/out)        entry point here
  *   ----------------------------------------------------------   -----------------------------------
  *   inflow_count<uint8>(policies, fd)  inflow_count.hpp:29-42      lue_gpu_inflow_count_u8
+ *   value_policies::accu_info(fd)      value_policies/accu_info.hpp:18-26   lue_gpu_accu_info_u8
  *   value_policies::accu(fd, inflow)   value_policies/accu.hpp:33-55   lue_gpu_accu_f32 / _f64
  *   value_policies::accu_threshold(fd, inflow, threshold)
  *                                      value_policies/accu_threshold.hpp:33-90
@@ -152,6 +153,15 @@ int lue_gpu_autotune_stage_schedule(lue_gpu_topology* topology, lue_gpu_stage_ca
  * unknown code, i.e. a sink; definition/inflow_count.hpp:9-15). */
 int lue_gpu_inflow_count_u8(const lue_gpu_topology* topology, int value_policies, uint8_t* inflow_count,
                             void* stream);
+
+/* accu_info(fd) (value_policies/accu_info.hpp:18-26; classes accu_info.hpp:22-63): the class of every cell
+ * in the reference's partitioned flow accumulation, for the topology's partition shape: 11 ridge, 12
+ * intra-partition stream, 13 partition output, 14 partition input, 15 partition input-output, 16
+ * inter-partition stream, 17 sink; 255 where the flow direction is no-data.  A partition input cell whose
+ * upstream cells in its own partition also wait for other partitions is classed by the last arrival in
+ * the reference, which depends on the order its channels deliver; here it is classed as if material from
+ * another partition arrived last (14 or 15). */
+int lue_gpu_accu_info_u8(lue_gpu_topology* topology, uint8_t* cell_class, void* stream);
 
 /* Downstream level of each cell: 0 for cells without inflow, else 1 + the largest level upstream;
  * -1 for no-data and for cells on or below a cycle.  No reference counterpart: it exposes the

@@ -302,7 +302,23 @@ PartitionedArray<Count> inflow_count(const PartitionedArray<std::uint8_t>& flow_
     return out;
 }
 
+// The cell classes of accu_info (ALG/accu_info.hpp:22-63).
+using CellClass = std::uint8_t;
+constexpr CellClass ridge_cell = 11, intra_partition_stream_cell = 12, partition_output_cell = 13,
+                    partition_input_cell = 14, partition_input_output_cell = 15, inter_partition_stream_cell = 16,
+                    sink_cell = 17;
+
 namespace value_policies {
+
+// accu_info(flow_direction): the class of every cell in the partitioned flow accumulation
+// (ALG/value_policies/accu_info.hpp:18-26), for the array's partition shape.
+inline PartitionedArray<CellClass> accu_info(const PartitionedArray<std::uint8_t>& flow_direction,
+                                             cudaStream_t stream = nullptr)
+{
+    PartitionedArray<CellClass> out(flow_direction.shape(), flow_direction.partition_shape());
+    check(lue_gpu_accu_info_u8(flow_direction.topology(stream).handle(), out.data(), stream), "accu_info");
+    return out;
+}
 
 // accu(flow_direction, inflow): inflow is a PartitionedArray<F> or a Scalar<F>.
 template <typename F, typename Inflow>

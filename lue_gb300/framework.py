@@ -202,6 +202,16 @@ def inflow_count(flow_direction, value_policies=True):
     return PartitionedArray(out, flow_direction.partition_shape)
 
 
+def accu_info(flow_direction):
+    """value_policies::accu_info: the class of every cell in the reference's partitioned flow accumulation
+    (uint8: 11 ridge, 12 intra-partition stream, 13 partition output, 14 partition input, 15 partition
+    input-output, 16 inter-partition stream, 17 sink, 255 no-data) for the array's partition shape."""
+    t = flow_direction.topology()
+    out = _empty(flow_direction, torch.uint8)
+    _lib.check(_lib.lib().lue_gpu_accu_info_u8(t.handle, out.data_ptr(), _stream(flow_direction.data)))
+    return PartitionedArray(out, flow_direction.partition_shape)
+
+
 def downstream_level(flow_direction):
     t = flow_direction.topology()
     out = _empty(flow_direction, torch.int32)

@@ -500,3 +500,125 @@ static const uint8_t NB_INFLOW[8] = {3, 2, 1, 6, 4, 9, 8, 7};  /* code of a neig
 
 ONE_HOP(float, f32)
 ONE_HOP(double, f64)
+
+/* ------------------------------------------------------------------------------------------------ */
+/* accu_info                                                                                         */
+/* ------------------------------------------------------------------------------------------------ */
+
+/*
+ * accu_info (ALG/definition/accu_info.hpp:13-190; classes ALG/accu_info.hpp:22-63): the class of every
+ * cell after the router's own event sequence (ALG/definition/accumulating_router.hpp:525-599 walk,
+ * :866-882 intra-partition ridge scan, :984-1010 inter-partition arrivals), with the AccuInfo cell
+ * accumulator's hooks:
+ *   enter_intra_partition_stream -> intra stream; leave_intra_partition_stream -> ridge;
+ *   enter_inter_partition_stream -> inter stream; leave_inter_partition_stream -> partition input
+ *   (partition input-output if the cell is a partition output cell);
+ *   leave_cell copies the upstream class downstream (no-data wins); stop_at_sink -> sink;
+ *   stop_at_confluence -> confluence; stop_at_partition_output -> partition output; no-data 255.
+ * Result buffers start at 0.  Inter-partition arrivals are taken in FIFO order (one order HPX may
+ * deliver); at a partition input cell that also waits for upstream cells of its own partition which wait
+ * for other partitions, the class depends on that order.
+ */
+enum { CLS_RIDGE = 11, CLS_INTRA = 12, CLS_OUTPUT = 13, CLS_INPUT = 14, CLS_INPUT_OUTPUT = 15, CLS_INTER = 16,
+       CLS_SINK = 17, CLS_CONFLUENCE = 18, CLS_NO_DATA = 255 };
+
+typedef struct {
+    Grid g;
+    const uint8_t* fd;
+    int8_t* cnt;
+    uint8_t* cls;
+    int64_t* fifo;
+    int64_t fifo_size, fifo_cap;
+} InfoRouter;
+
+static void info_push(InfoRouter* R, int64_t j)
+{
+    if (R->fifo_size == R->fifo_cap) {
+        R->fifo_cap = R->fifo_cap ? 2 * R->fifo_cap : 64;
+        R->fifo = (int64_t*)realloc(R->fifo, (size_t)R->fifo_cap * sizeof(int64_t));
+    }
+    R->fifo[R->fifo_size++] = j;
+}
+
+static void info_walk(InfoRouter* R, int64_t r, int64_t c)
+{
+    const Grid* g = &R->g;
+    const int64_t cols = g->cols;
+    int64_t r0, r1, c0, c1;
+    part_rows(g, part_of_row(g, r), &r0, &r1);
+    part_cols(g, part_of_col(g, c), &c0, &c1);
+    for (;;) {
+        const int64_t i = r * cols + c;
+        int dr, dc;
+        d8_offset(R->fd[i], &dr, &dc);
+        if (dr == 0 && dc == 0) {
+            R->cls[i] = CLS_SINK;
+            return;
+        }
+        const int64_t rd = r + dr, cd = c + dc;
+        if (rd < r0 || rd >= r1 || cd < c0 || cd >= c1) {
+            R->cls[i] = CLS_OUTPUT;
+            if (rd >= 0 && rd < g->rows && cd >= 0 && cd < cols) info_push(R, rd * cols + cd);
+            return;
+        }
+        const int64_t j = rd * cols + cd;
+        if (R->cls[j] != CLS_NO_DATA) R->cls[j] = R->cls[i] == CLS_NO_DATA ? CLS_NO_DATA : R->cls[i];
+        r = rd;
+        c = cd;
+        if (--R->cnt[j] > 0) {
+            R->cls[j] = CLS_CONFLUENCE;
+            return;
+        }
+    }
+}
+
+int lue_oracle_accu_info(const uint8_t* fd, int64_t rows, int64_t cols, int64_t prow, int64_t pcol, uint8_t* cls)
+{
+    InfoRouter R;
+    memset(&R, 0, sizeof R);
+    if (grid_init(&R.g, rows, cols, prow, pcol)) return -1;
+    const int64_t n = rows * cols;
+    R.fd = fd;
+    R.cls = cls;
+    R.cnt = (int8_t*)malloc((size_t)n);
+    int8_t* orig = (int8_t*)malloc((size_t)n);
+    if (!R.cnt || !orig) {
+        free(R.cnt);
+        free(orig);
+        return -2;
+    }
+    router_counts(&R.g, fd, 1, orig);
+    memcpy(R.cnt, orig, (size_t)n);
+    memset(cls, 0, (size_t)n);
+    for (int64_t pr = 0; pr < R.g.nprow; ++pr) {
+        int64_t r0, r1;
+        part_rows(&R.g, pr, &r0, &r1);
+        for (int64_t pc = 0; pc < R.g.npcol; ++pc) {
+            int64_t c0, c1;
+            part_cols(&R.g, pc, &c0, &c1);
+            for (int64_t r = r0; r < r1; ++r)
+                for (int64_t c = c0; c < c1; ++c) {
+                    const int64_t i = r * cols + c;
+                    if (fd[i] == U8_NO_DATA) {
+                        cls[i] = CLS_NO_DATA;
+                    } else if (orig[i] == 0) {
+                        cls[i] = CLS_INTRA;
+                        info_walk(&R, r, c);
+                        cls[i] = CLS_RIDGE;
+                    }
+                }
+        }
+    }
+    for (int64_t k = 0; k < R.fifo_size; ++k) {
+        const int64_t j = R.fifo[k];
+        R.cls[j] = CLS_INTER;
+        if (--R.cnt[j] == 0) {
+            info_walk(&R, j / cols, j % cols);
+            R.cls[j] = R.cls[j] != CLS_OUTPUT ? CLS_INPUT : CLS_INPUT_OUTPUT;
+        }
+    }
+    free(R.fifo);
+    free(R.cnt);
+    free(orig);
+    return 0;
+}

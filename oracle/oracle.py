@@ -53,6 +53,7 @@ def lib():
             getattr(L, f"lue_oracle_downstream_{sfx}").argtypes = [p, i64, i64, p, p]
             getattr(L, f"lue_oracle_downstream_distance_{sfx}").argtypes = [p, i64, i64, real, p]
         L.lue_oracle_inflow_count.argtypes = [p, i64, i64, i64, i64, i32, p]
+        L.lue_oracle_accu_info.argtypes = [p, i64, i64, i64, i64, p]
         L.lue_oracle_downstream_level.argtypes = [p, i64, i64, p]
         L.lue_oracle_d8_flow_direction.argtypes = [p, i64, i64, p]
         d = ctypes.c_double
@@ -102,6 +103,16 @@ def inflow_count(fd, partition_shape=None, value_policies=True):
     out = np.empty(fd.shape, np.uint8)
     _check(lib().lue_oracle_inflow_count(fd.ctypes.data, fd.shape[0], fd.shape[1], pr, pc,
                                          int(value_policies), out.ctypes.data))
+    return out
+
+
+def accu_info(fd, partition_shape=None):
+    """accu_info: the class of every cell after the reference router's event sequence (uint8, 255 no-data;
+    inter-partition arrivals in FIFO order)."""
+    fd = _fd(fd)
+    pr, pc = _pshape(fd, partition_shape)
+    out = np.empty(fd.shape, np.uint8)
+    _check(lib().lue_oracle_accu_info(fd.ctypes.data, fd.shape[0], fd.shape[1], pr, pc, out.ctypes.data))
     return out
 
 

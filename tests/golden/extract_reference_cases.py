@@ -19,6 +19,7 @@ Sources read (paths within the reference project):
 - source/framework/algorithm/test/d8_flow_direction_test.cpp
 - source/framework/algorithm/test/accu_capacity_test.cpp, accu_trigger_test.cpp
 - source/framework/algorithm/test/upstream_test.cpp, downstream_test.cpp, downstream_distance_test.cpp
+- source/framework/algorithm/test/accu_info_test.cpp
 
 Each ``create_partitioned_array(shape, partition_shape, {{partition}, ...})`` literal lists its
 partitions in row-major partition order, each partition's cells row-major.  Partition extents follow
@@ -39,6 +40,10 @@ TEST_DIR = "source/framework/algorithm/test"
 # D8 keypad codes, source/framework/algorithm/include/lue/framework/algorithm/flow_direction.hpp:7-35
 D8 = {"nw": 7, "n": 8, "ne": 9, "w": 4, "p": 5, "e": 6, "sw": 1, "s": 2, "se": 3}
 U8_NO_DATA = 255
+# accu_info cell classes, source/framework/algorithm/include/lue/framework/algorithm/accu_info.hpp:22-63
+CELL_CLASSES = {"ridge_cell": 11, "intra_partition_stream_cell": 12, "partition_output_cell": 13,
+                "partition_input_cell": 14, "partition_input_output_cell": 15, "inter_partition_stream_cell": 16,
+                "sink_cell": 17, "confluence_cell": 18}
 
 
 def strip_comments(text):
@@ -156,7 +161,7 @@ class Env:
 def elem_kind(type_text):
     """'u8' for flow directions and counts, 'f' for material."""
     t = type_text
-    if "FlowDirection" in t or "CountElement" in t or "InflowCount" in t or "uint8" in t:
+    if "FlowDirection" in t or "CountElement" in t or "InflowCount" in t or "uint8" in t or "CellClass" in t:
         return "u8"
     return "f"
 
@@ -164,7 +169,7 @@ def elem_kind(type_text):
 def eval_scalar(expr, env, kind="f"):
     e = expr.strip()
     e = re.sub(r"^lue::test::", "", e)
-    m = re.fullmatch(r"lue::policy::no_data_value<(\w+)>", e)
+    m = re.fullmatch(r"lue::policy::no_data_value<([\w:]+)>", e)
     if m:
         return U8_NO_DATA if elem_kind(m.group(1)) == "u8" else math.nan
     m = re.fullmatch(r"(\w+)\{(.*)\}", e)  # MaterialElement{0}
@@ -275,9 +280,14 @@ def process_statements(stmts, env, fixtures, on_call):
             env.shapes[m.group(1)] = eval_shape(m.group(2) or m.group(3), env)
             continue
         # aliases: auto const n = lue::test::n / auto const x{no_data_value<...>}
-        m = re.match(r"auto const (\w+)\s*(?:=\s*|\{)(lue::test::\w+|lue::policy::no_data_value<\w+>)\}?$", s1)
+        m = re.match(r"auto const (\w+)\s*(?:=\s*|\{)(lue::test::\w+|lue::policy::no_data_value<[\w:]+>)\}?$", s1)
         if m:
-            env.values[m.group(1)] = eval_scalar(m.group(2), env)
+            env.values[m.group(1)] = eval_scalar(m.group(2), env, elem_kind(m.group(2)))
+            continue
+        # accu_info cell classes: auto const intra = lue::intra_partition_stream_cell
+        m = re.match(r"auto const (\w+)\s*=\s*lue::(\w+_cell)$", s1)
+        if m and m.group(2) in CELL_CLASSES:
+            env.values[m.group(1)] = CELL_CLASSES[m.group(2)]
             continue
         # scalars
         m = re.match(r"lue::Scalar<\w+> const (\w+)\s*(?:=\s*(.*)|\{(.*)\})$", s1)
@@ -286,7 +296,8 @@ def process_statements(stmts, env, fixtures, on_call):
             if text:  # default-constructed scalars (overload-only cases) carry no value
                 env.values[m.group(1)] = eval_scalar(text, env)
             continue
-        m = re.match(r"(?:auto const|auto|\w+ const) (\w+)\s*=\s*(lue::.*)$", s, flags=re.S)
+        m = re.match(r"(?:auto const|auto|\w+ const|lue::PartitionedArray<[^=]*?>(?: const)?) (\w+)\s*=\s*(lue::.*)$", s,
+                     flags=re.S)
         if m and ("create_partitioned_array" in m.group(2) or re.match(r"lue::test::\w+(<\w+>)?\(", m.group(2).strip())):
             env.arrays[m.group(1)] = eval_array(m.group(2), env, fixtures)
             continue
@@ -315,7 +326,7 @@ def parse_fixtures(text):
 
 
 OPS = ("accu_threshold", "accu_fraction", "kinematic_wave", "accu", "accu_capacity", "accu_trigger", "upstream",
-       "downstream")
+       "downstream", "accu_info")
 
 
 def extract_file(path, rel, fixtures, cases):
@@ -499,7 +510,7 @@ def main():
     cases = []
     for f in ("accu_test.cpp", "accu_threshold_test.cpp", "accu_fraction_test.cpp",
               "kinematic_wave_test.cpp", "inflow_count_test.cpp", "accu_capacity_test.cpp",
-              "accu_trigger_test.cpp", "upstream_test.cpp", "downstream_test.cpp"):
+              "accu_trigger_test.cpp", "upstream_test.cpp", "downstream_test.cpp", "accu_info_test.cpp"):
         extract_file(os.path.join(tdir, f), f"{TEST_DIR}/{f}", fixtures, cases)
     extract_downstream_distance(os.path.join(tdir, "downstream_distance_test.cpp"),
                                 f"{TEST_DIR}/downstream_distance_test.cpp", fixtures, cases)

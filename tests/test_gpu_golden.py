@@ -123,3 +123,14 @@ def test_downstream_distance_case(lfr, case, dtype):
                                                torch.float32 if dtype == np.float32 else torch.float64))
     assert got.dtype == dtype
     assert_matches(got, golden.f32(case["expected"]["distance"]), "close")
+
+
+INFO = golden.load("accu_info")
+
+
+@pytest.mark.parametrize("case", INFO, ids=[golden.case_id(c) for c in INFO])
+def test_accu_info_case(lfr, case):
+    fd = golden.u8(case["flow_direction"])
+    got = lfr.to_numpy(lfr.accu_info(lfr.from_numpy(fd, case["partition_shape"])))
+    want = golden.u8(case["expected"]["class_we_got"])
+    assert (got == want).all(), f"\n got {got}\n want {want}"

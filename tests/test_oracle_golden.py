@@ -147,3 +147,13 @@ DISTANCE = golden.load("downstream_distance")
 def test_downstream_distance_case(case, dtype):
     got = oracle.downstream_distance(golden.u8(case["flow_direction"]), case["cell_size"], dtype)
     assert_matches(got, golden.f32(case["expected"]["distance"]), "close")
+
+
+INFO = golden.load("accu_info")
+
+
+@pytest.mark.parametrize("case", INFO, ids=[golden.case_id(c) for c in INFO])
+def test_accu_info_case(case):
+    got = oracle.accu_info(golden.u8(case["flow_direction"]), case["partition_shape"])
+    want = golden.u8(case["expected"]["class_we_got"])
+    assert (got == want).all(), f"\n got {got}\n want {want}"
