@@ -186,6 +186,30 @@ def run_cpu_accu(fd, m, partition, nthreads):
     return time.perf_counter() - t0
 
 
+def accuracy_on_sample(fd, m, ps, nthreads, dev):
+    """The GPU's float32 results on the CPU sample against the float64 oracle: relative error
+    |gpu - oracle| / max(|oracle|, 1e-3) (tests/parity.py), max and mean, for accu and accu_threshold
+    (threshold uniform [0, 0.5), seed 17)."""
+    from lue_gb300 import framework as lfr
+    from oracle import oracle
+    from tests import parity
+    a = lfr.from_numpy(fd, ps, device=dev)
+    md = lfr.from_numpy(m, ps, device=dev)
+    m64 = m.astype(np.float64)
+    got = lfr.to_numpy(lfr.accu(a, md))
+    want = oracle.accu(fd, m64, ps, dtype=np.float64, nthreads=nthreads)
+    out = {"against": "oracle/lue_oracle.c in float64", "floor": parity.FLOOR32}
+    mx, mean = parity.rel_error(got, want, parity.FLOOR32)
+    out["accu"] = {"max_rel_err": mx, "mean_rel_err": mean}
+    thr = np.random.default_rng(17).random(fd.shape, dtype=np.float32) * np.float32(0.5)
+    flux, state = lfr.accu_threshold(a, md, lfr.from_numpy(thr, ps, device=dev))
+    wf, ws = oracle.accu_threshold(fd, m64, thr.astype(np.float64), ps, dtype=np.float64, nthreads=nthreads)
+    for name, g, w in (("accu_threshold_flux", flux, wf), ("accu_threshold_state", state, ws)):
+        mx, mean = parity.rel_error(lfr.to_numpy(g), w, parity.FLOOR32)
+        out[name] = {"max_rel_err": mx, "mean_rel_err": mean}
+    return out
+
+
 def workload_inputs(name):
     from lue_gb300 import synthetic
     w = synthetic.WORKLOADS[name]
@@ -364,6 +388,10 @@ def bench_ours(args, world, rank, local):
         cpu = {"value": round(fd_s.size / t_cpu / 1e6, 3), "unit": "Mcells/s", "cores": nthreads, "kind": "port",
                "sample": f"accu over rows 0-{fd_s.shape[0] - 1} of the raster ({fd_s.shape[0]}x{fd_s.shape[1]} "
                          f"cells, partitions {ps_s[0]}x{ps_s[1]}), one pass, oracle/lue_oracle.c threaded"}
+        try:  # the float32 error of the GPU results on the same sample, against the float64 oracle
+            cpu["accuracy"] = accuracy_on_sample(fd_s, m_s, ps_s, nthreads, dev)
+        except Exception as e:  # noqa: BLE001  (reported in the line, the bench itself goes on)
+            cpu["accuracy"] = {"error": f"{type(e).__name__}: {e}"}
     line = {
         "metric": METRIC, "value": round(value, 3),
         "unit": "Mcells/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
