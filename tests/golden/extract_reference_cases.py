@@ -36,6 +36,8 @@ import re
 import sys
 
 TEST_DIR = "source/framework/algorithm/test"
+# where the reference's sources are mounted when the fixture is regenerated (LUE_REFERENCE overrides)
+DEFAULT_REFERENCE = os.environ.get("LUE_REFERENCE", "/root/reference")
 
 # D8 keypad codes, source/framework/algorithm/include/lue/framework/algorithm/flow_direction.hpp:7-35
 D8 = {"nw": 7, "n": 8, "ne": 9, "w": 4, "p": 5, "e": 6, "sw": 1, "s": 2, "se": 3}
@@ -502,7 +504,7 @@ def extract_downstream_distance(path, rel, fixtures, cases):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=os.environ.get("LUE_REFERENCE", "/root/reference"))
+    ap.add_argument("--reference", default=DEFAULT_REFERENCE)
     ap.add_argument("--out", default=os.path.join(os.path.dirname(__file__), "reference_cases.json"))
     a = ap.parse_args()
     tdir = os.path.join(a.reference, TEST_DIR)

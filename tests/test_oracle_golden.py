@@ -2,7 +2,8 @@
 
 Every case in tests/golden/reference_cases.json was extracted from the reference's Boost.Test sources
 (source/framework/algorithm/test/{accu,accu_threshold,accu_fraction,accu_capacity,accu_trigger,
-kinematic_wave,inflow_count,upstream,downstream,downstream_distance,d8_flow_direction}_test.cpp) by tests/golden/extract_reference_cases.py.  The comparison rules restate the reference's
+kinematic_wave,inflow_count,upstream,downstream,downstream_distance,d8_flow_direction,accu_info}_test.cpp)
+by tests/golden/extract_reference_cases.py.  The comparison rules restate the reference's
 test helpers (source/framework/test/include/lue/framework/test/compare.hpp):
 
 - ``check_arrays_are_equal``: element-wise equality, NaN == NaN (compare.hpp:52-100);
@@ -157,3 +158,26 @@ def test_accu_info_case(case):
     got = oracle.accu_info(golden.u8(case["flow_direction"]), case["partition_shape"])
     want = golden.u8(case["expected"]["class_we_got"])
     assert (got == want).all(), f"\n got {got}\n want {want}"
+
+
+def test_fixture_is_what_the_extractor_reads_from_the_reference_sources(tmp_path):
+    """tests/golden/reference_cases.json is exactly what tests/golden/extract_reference_cases.py writes from
+    the reference's test sources (where they are mounted; the fixture travels without them)."""
+    import json
+    import os
+    import subprocess
+    import sys
+
+    from tests.golden import extract_reference_cases as extract
+    ref = extract.DEFAULT_REFERENCE
+    if not os.path.isdir(os.path.join(ref, extract.TEST_DIR)):
+        pytest.skip("reference sources not mounted")
+    here = os.path.dirname(os.path.abspath(__file__))
+    out = tmp_path / "cases.json"
+    subprocess.run([sys.executable, os.path.join(here, "golden", "extract_reference_cases.py"), "--reference", ref,
+                    "--out", str(out)], check=True, capture_output=True)
+    with open(out) as fh:
+        fresh = json.load(fh)
+    with open(os.path.join(here, "golden", "reference_cases.json")) as fh:
+        committed = json.load(fh)
+    assert fresh == committed
