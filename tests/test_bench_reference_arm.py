@@ -1,4 +1,4 @@
-"""bench.py --impl reference on the CPU: one JSON line with the keys the driver reads, the CPU port of the
+"""bench.py --impl reference on the CPU: one JSON line with the benchmark's keys, the CPU port of the
 reference's algorithm timed on a bounded sample, and no host-device bytes."""
 import json
 import os
