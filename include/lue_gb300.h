@@ -262,10 +262,18 @@ int lue_gpu_kinematic_wave_f64_f32in(lue_gpu_topology* topology, const double* c
                                      void* stream);
 
 /* `steps` kinematic-wave time steps in one call (the discharge of each step feeds the next, lateral
- * inflow and alpha constant), equal bit for bit to `steps` calls of lue_gpu_kinematic_wave_f64_f32in.
- * Replaces the caller's per-step loop (the reference's lue::simulate pattern, source/framework/model/
- * include/lue/framework/model/simulate.hpp) with time-skewed level waves: max level + steps waves
- * instead of steps full sweeps.  Needs steps x cells x 8 bytes of scratch (kept by the topology). */
+ * inflow and alpha constant).  Replaces the caller's per-step loop (the reference's lue::simulate
+ * pattern, source/framework/model/include/lue/framework/model/simulate.hpp).
+ * Engines:
+ *  - default, for a scalar beta that is a small rational p/m (0.6 = 3/5): the stage engine runs every
+ *    step in one dataflow launch, with the solve in y = Q^(1/m) (float32 Newton plus one float-float
+ *    step).  Results agree with `steps` calls of lue_gpu_kinematic_wave_f64_f32in within 1e-12
+ *    relative, not bit for bit.  Scratch (kept by the topology): 8 bytes per stage exit (about 40 % of
+ *    the cells at 128-cell stages) and step of a call; calls whose history would not fit 40 % of the
+ *    free device memory are cut into parts.
+ *  - LUE_GB300_KW_SOLVE=reference, another beta, or a network with flow cycles: time-skewed level waves
+ *    with the float64 solve, equal bit for bit to `steps` calls of lue_gpu_kinematic_wave_f64_f32in
+ *    (cycles: one single-step call per step); scratch steps x cells x 8 bytes. */
 int lue_gpu_kinematic_wave_steps_f64_f32in(lue_gpu_topology* topology, const double* current_outflow,
                                            const float* inflow, double inflow_scalar, const float* alpha,
                                            double alpha_scalar, double beta, double time_step_duration,
@@ -278,9 +286,15 @@ int lue_gpu_kinematic_wave_steps_f64_f32in(lue_gpu_topology* topology, const dou
  * file-scope device array of 7 * LUE_GPU_NOALLOC_MAX_CELLS bytes (about 29 MB) that every GPU which
  * loads the library holds until the process exits.  Rasters above LUE_GPU_NOALLOC_MAX_CELLS cells fail
  * with LUE_GPU_ERANGE.  The first call on each device resolves that array's device address
- * (cudaGetSymbolAddress, with the device current); make the first call before any stream capture.
+ * (cudaGetSymbolAddress, with the device current); make the first call before any stream capture.  The
+ * address is cached per device and context: after a device reset (or any other teardown of the
+ * context) the next call resolves it again, so that call too must come before any stream capture.
  * All calls share the array: calls that overlap on the GPU race and must be serialised by the caller.
- * Results equal lue_gpu_accu_f32's. */
+ * The partition shape is validated like the reference's domain decomposition, for the same errors; it
+ * does not change the result or the schedule.  Every call runs the walk engine (one thread per cell,
+ * float-float sums along paths) plus one pass over the cells on or below flow cycles; results agree
+ * with lue_gpu_accu_f32 within the float32 tolerance of the other accu entry points (at most 1e-5
+ * relative), not bit for bit. */
 #define LUE_GPU_NOALLOC_MAX_CELLS 4194304
 int lue_gpu_accu_f32_noalloc(const uint8_t* flow_direction, int64_t rows, int64_t cols, int64_t partition_rows,
                              int64_t partition_cols, const float* inflow, float inflow_scalar, float* outflow,

@@ -1,4 +1,10 @@
-// kinematic_wave_steps.cu — many kinematic-wave time steps in one call, as time-skewed level waves.
+// kinematic_wave_steps.cu — many kinematic-wave time steps in one call.
+//
+// Which engine runs: for a scalar beta that is a small rational p/m, the stage engine
+// (stage_route.cu: one dataflow launch over all stages and steps, float-float solve in y = Q^(1/m)),
+// whose results agree with single-step calls within 1e-12 relative and whose scratch is the stage
+// history (8 bytes per stage exit and step).  The time-skewed level waves below run for
+// LUE_GB300_KW_SOLVE=reference and other betas; they equal single-step calls bit for bit.
 //
 // The reference's caller runs one kinematic_wave call per time step (lue::simulate, source/framework/
 // model/include/lue/framework/model/simulate.hpp), each a full downstream sweep: T steps cost T times
@@ -8,8 +14,8 @@
 //
 // Each step's discharge is kept in a plane Q_t (t = 0 is the input, t = T the output); a wave reads
 // Q_t of the upstream cells and Q_{t-1} of the cell itself, in the same fixed neighbour order as the
-// single-step kernels, so the result equals T single calls bit for bit.  The planes for 1 <= t < T live
-// in the topology's scratch (grown on demand: steps * cells * 8 bytes).
+// single-step kernels, so the level-wave result equals T single calls bit for bit.  The planes for
+// 1 <= t < T live in the topology's scratch (grown on demand: steps * cells * 8 bytes).
 //
 // Cells are ordered by level (counting sort, row-major within a level); a wave covers one contiguous
 // range of that order.  Networks with cycles run single steps instead (cells on or below a cycle are

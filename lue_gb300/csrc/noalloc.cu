@@ -14,10 +14,14 @@
 // race on it and must be serialised by the caller.
 //
 // In host code `g_noalloc_scratch` names a host-side stand-in, not a device address: its device
-// address is resolved once per device with cudaGetSymbolAddress (with that device current) by the
-// first call on that device, and cached.
-#include <mutex>
+// address is resolved with cudaGetSymbolAddress (with the device current) by the first call on a
+// device and cached together with the identity of the device's current context (cuCtxGetId).  A device
+// reset or any other teardown of that context loads the module again, possibly at another address: the
+// next call sees a new context id and resolves the address again, so that call, like the first, must
+// not be made during stream capture.
+#include <cuda.h>
 
+#include <mutex>
 #include <string>
 
 #include "route_walk_visitors.cuh"
@@ -31,8 +35,40 @@ constexpr int64_t kNoallocBytes = kNoallocMaxCells * 7 + 1024;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
 constexpr int kMaxDevices = 64;
-static unsigned char* g_scratch_ptr[kMaxDevices] = {};
+struct ScratchAddress {
+    unsigned char* ptr = nullptr;
+    unsigned long long context_id = 0;  // cuCtxGetId of the context the address was resolved in
+};
+static ScratchAddress g_scratch_address[kMaxDevices];
 static std::mutex g_scratch_mutex;
+
+// The id of the calling thread's current context (0 when there is none or the driver cannot tell),
+// through driver entry points fetched from the runtime, so that the library does not link libcuda.
+static unsigned long long current_context_id()
+{
+    typedef CUresult (*GetCurrent)(CUcontext*);
+    typedef CUresult (*GetId)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrent>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(f);
+        cudaGetLastError();  // a missing entry point is not an error of the call
+    });
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
 
 static int noalloc_scratch(unsigned char** out)
 {
@@ -40,13 +76,16 @@ static int noalloc_scratch(unsigned char** out)
     if (int rc = cuda_status(cudaGetDevice(&dev), "accu_f32_noalloc: cudaGetDevice")) return rc;
     if (dev < 0 || dev >= kMaxDevices) return fail(LUE_GPU_ERANGE, "accu_f32_noalloc: device index out of range");
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_ptr[dev]) {
+    ScratchAddress& a = g_scratch_address[dev];
+    const unsigned long long id = current_context_id();
+    if (!a.ptr || id == 0 || id != a.context_id) {
         void* p = nullptr;
         if (int rc = cuda_status(cudaGetSymbolAddress(&p, g_noalloc_scratch), "accu_f32_noalloc: cudaGetSymbolAddress"))
             return rc;
-        g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
+        a.ptr = static_cast<unsigned char*>(p);
+        a.context_id = current_context_id();  // the symbol lookup made the device's primary context current
     }
-    *out = g_scratch_ptr[dev];
+    *out = a.ptr;
     return LUE_GPU_OK;
 }
 

@@ -5,7 +5,7 @@ This script reads the reference's Boost.Test sources as TEXT (nothing is compile
 writes ``reference_cases.json`` beside itself.  The JSON is committed; the tests only read the
 JSON, so the reference tree is needed only when regenerating it:
 
-    python tests/golden/extract_reference_cases.py --reference /root/reference
+    python tests/golden/extract_reference_cases.py --reference <root of the reference project>
 
 Sources read (paths within the reference project):
 
@@ -36,8 +36,8 @@ import re
 import sys
 
 TEST_DIR = "source/framework/algorithm/test"
-# where the reference's sources are mounted when the fixture is regenerated (LUE_REFERENCE overrides)
-DEFAULT_REFERENCE = os.environ.get("LUE_REFERENCE", "/root/reference")
+# where the reference's sources are mounted when the fixture is regenerated: --reference, or LUE_REFERENCE
+DEFAULT_REFERENCE = os.environ.get("LUE_REFERENCE")
 
 # D8 keypad codes, source/framework/algorithm/include/lue/framework/algorithm/flow_direction.hpp:7-35
 D8 = {"nw": 7, "n": 8, "ne": 9, "w": 4, "p": 5, "e": 6, "sw": 1, "s": 2, "se": 3}
@@ -504,9 +504,12 @@ def extract_downstream_distance(path, rel, fixtures, cases):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=DEFAULT_REFERENCE)
+    ap.add_argument("--reference", default=DEFAULT_REFERENCE,
+                    help="root of the reference project's sources (default: $LUE_REFERENCE)")
     ap.add_argument("--out", default=os.path.join(os.path.dirname(__file__), "reference_cases.json"))
     a = ap.parse_args()
+    if not a.reference:
+        ap.error("give the reference project's root with --reference or LUE_REFERENCE")
     tdir = os.path.join(a.reference, TEST_DIR)
     fixtures = parse_fixtures(strip_comments(open(os.path.join(tdir, "flow_accumulation.cpp.in")).read()))
     cases = []

@@ -162,7 +162,7 @@ def test_accu_info_case(case):
 
 def test_fixture_is_what_the_extractor_reads_from_the_reference_sources(tmp_path):
     """tests/golden/reference_cases.json is exactly what tests/golden/extract_reference_cases.py writes from
-    the reference's test sources (where they are mounted; the fixture travels without them)."""
+    the reference's test sources, where LUE_REFERENCE names their root (the fixture travels without them)."""
     import json
     import os
     import subprocess
@@ -170,8 +170,8 @@ def test_fixture_is_what_the_extractor_reads_from_the_reference_sources(tmp_path
 
     from tests.golden import extract_reference_cases as extract
     ref = extract.DEFAULT_REFERENCE
-    if not os.path.isdir(os.path.join(ref, extract.TEST_DIR)):
-        pytest.skip("reference sources not mounted")
+    if not ref or not os.path.isdir(os.path.join(ref, extract.TEST_DIR)):
+        pytest.skip("reference sources not given (LUE_REFERENCE)")
     here = os.path.dirname(os.path.abspath(__file__))
     out = tmp_path / "cases.json"
     subprocess.run([sys.executable, os.path.join(here, "golden", "extract_reference_cases.py"), "--reference", ref,
