@@ -18,14 +18,18 @@ Reported (one JSON line, rank 0):
   roofline   algorithmic bytes (fd 1 + material 4 + outflow 4 = 9 B/cell) / mean step time against the
              measured HBM copy bandwidth; traffic from the committed ncu summary when present.
   cpu_baseline  the CPU oracle (a restatement of the reference's partitioned ridge walk, threaded
-             one task per partition) on a bounded sample, rank 0 only.
+             one task per partition) on the whole raster, one pass, rank 0 only.
+  accuracy   the GPU results of the timed run against the float64 oracle on the same inputs: accu and
+             accu_threshold on the whole 16384^2 raster (float32 tolerance 1e-5), and the 100-step
+             kinematic wave on the whole 8192^2 raster against 100 single-step float64-solve calls and on
+             rows 0-1023 against 100 oracle steps (float64 tolerance 1e-9).
   extra.accu_threshold  accu_threshold over the same raster and material (threshold uniform [0, 0.5)):
              the path engine, and the stage engine with its default and its autotuned schedule.
   extra.kinematic_wave  kinematic_wave steps over the 8192 x 8192 workload (float64 discharge).
 
 --impl reference times the reference algorithm on the CPU (the oracle port, every host core), since
-the reference (HPX + Boost) cannot be built here; each step is the bounded sample described in
-``cpu_baseline.sample``.  Multi-GPU (torchrun): each rank routes its own replica of the workload; no
+the reference (HPX + Boost) cannot be built here; each step is one accu pass over the workload's whole
+raster.  Multi-GPU (torchrun): each rank routes its own replica of the workload; no
 collective is involved (replicas only; scaling "weak").
 """
 import argparse
@@ -45,7 +49,6 @@ sys.path.insert(0, ROOT)
 ACCU_BYTES_PER_CELL = 9      # fd 1 + material 4 + outflow 4
 KW_BYTES_PER_CELL = 25       # fd 1 + Q_cur 8 + lateral 4 + alpha 4 + Q_new 8
 THRESHOLD_BYTES_PER_CELL = 17  # fd 1 + material 4 + threshold 4 + flux 4 + state 4
-REF_SAMPLE_ROWS = 4096       # reference-arm / cpu_baseline sample: the top 4096 rows, all columns
 METRIC = "accu Mcells/s (16384^2 D8 raster, float32 material)"  # the headline metric, on accu_16k
 
 
@@ -172,10 +175,9 @@ def outlet_mask(fd):
 
 
 def cpu_sample(inputs, partition):
-    """The bounded CPU sample: the top REF_SAMPLE_ROWS rows (flow leaving the band is dropped, as at
-    the array edge), same partitioning."""
-    fd = np.ascontiguousarray(inputs["flow_direction"][:REF_SAMPLE_ROWS])
-    m = np.ascontiguousarray(inputs["material"][:REF_SAMPLE_ROWS])
+    """The CPU arm's workload: the whole raster and material of the GPU workload, same partitioning."""
+    fd = np.ascontiguousarray(inputs["flow_direction"])
+    m = np.ascontiguousarray(inputs["material"])
     return fd, m, (min(partition[0], fd.shape[0]), min(partition[1], fd.shape[1]))
 
 
@@ -187,38 +189,70 @@ def run_cpu_accu(fd, m, partition, nthreads):
 
 
 def best_cpu_partition(fd, m, nominal, nthreads):
-    """The partition shape at which the CPU port of the reference's algorithm runs fastest on the sample,
-    from a small sweep (one pass each) over the workload's partition shape and square shapes of 512, 1024
-    and 2048 cells, as a user of the reference would pick it.  Returns (shape, {shape: seconds})."""
+    """The partition shape at which the CPU port of the reference's algorithm runs fastest on the
+    raster, from a small sweep (one pass each) over the workload's partition shape and square shapes of
+    1024, 2048 and 4096 cells, as a user of the reference would pick it.  Returns (shape,
+    {shape: seconds})."""
     rows, cols = fd.shape
     cands = {(min(nominal[0], rows), min(nominal[1], cols))}
-    cands.update((min(s, rows), min(s, cols)) for s in (512, 1024, 2048))
+    cands.update((min(s, rows), min(s, cols)) for s in (1024, 2048, 4096))
     times = {c: run_cpu_accu(fd, m, c, nthreads) for c in sorted(cands)}
     best = min(times, key=times.get)
     return best, times
 
 
-def accuracy_on_sample(fd, m, ps, nthreads, dev):
-    """The GPU's float32 results on the CPU sample against the float64 oracle: relative error
-    |gpu - oracle| / max(|oracle|, 1e-3) (tests/parity.py), max and mean, for accu and accu_threshold
-    (threshold uniform [0, 0.5), seed 17)."""
-    from lue_gb300 import framework as lfr
+def rel_error_device(got, want, floor):
+    """Max and mean of |got - want| / max(|want|, floor) (tests/parity.py) over the cells where want is
+    not NaN, computed on the device in float64; `got` a device tensor, `want` a float64 numpy array of
+    the same shape.  NaN positions must be identical (else ValueError)."""
+    import torch
+    g = got.reshape(-1)
+    w_host = torch.from_numpy(np.ascontiguousarray(want).reshape(-1))
+    mx, total, count = 0.0, 0.0, 0
+    chunk = 1 << 26
+    for k in range(0, g.numel(), chunk):
+        gd = g[k:k + chunk].double()
+        wd = w_host[k:k + chunk].to(g.device, non_blocking=False)
+        nan_g, nan_w = torch.isnan(gd), torch.isnan(wd)
+        if not torch.equal(nan_g, nan_w):
+            raise ValueError(f"no-data positions differ ({int((nan_g != nan_w).sum())} cells)")
+        ok = ~nan_w
+        e = (gd[ok] - wd[ok]).abs() / wd[ok].abs().clamp_min(floor)
+        if e.numel():
+            mx = max(mx, float(e.max()))
+            total += float(e.sum())
+            count += e.numel()
+    return mx, (total / count if count else 0.0)
+
+
+def accuracy_full_raster(inputs, ps, accu_out, thr_holder, nthreads):
+    """C2's results on the whole raster against the float64 oracle (oracle/lue_oracle.c, threaded) on the
+    same inputs: the accu output of the last timed step, and the accu_threshold flux and state of the
+    threshold leg.  Relative error with the float32 floor of tests/parity.py; tolerance 1e-5."""
     from oracle import oracle
     from tests import parity
-    a = lfr.from_numpy(fd, ps, device=dev)
-    md = lfr.from_numpy(m, ps, device=dev)
+    fd, m = inputs["flow_direction"], inputs["material"]
     m64 = m.astype(np.float64)
-    got = lfr.to_numpy(lfr.accu(a, md))
+    out = {"against": "oracle/lue_oracle.c in float64, whole raster", "floor": parity.FLOOR32,
+           "tolerance": parity.RTOL32, "cores": nthreads}
+    t0 = time.perf_counter()
     want = oracle.accu(fd, m64, ps, dtype=np.float64, nthreads=nthreads)
-    out = {"against": "oracle/lue_oracle.c in float64", "floor": parity.FLOOR32}
-    mx, mean = parity.rel_error(got, want, parity.FLOOR32)
+    out["oracle_accu_s"] = round(time.perf_counter() - t0, 2)
+    mx, mean = rel_error_device(accu_out, want, parity.FLOOR32)
+    del want
     out["accu"] = {"max_rel_err": mx, "mean_rel_err": mean}
-    thr = np.random.default_rng(17).random(fd.shape, dtype=np.float32) * np.float32(0.5)
-    flux, state = lfr.accu_threshold(a, md, lfr.from_numpy(thr, ps, device=dev))
-    wf, ws = oracle.accu_threshold(fd, m64, thr.astype(np.float64), ps, dtype=np.float64, nthreads=nthreads)
-    for name, g, w in (("accu_threshold_flux", flux, wf), ("accu_threshold_state", state, ws)):
-        mx, mean = parity.rel_error(lfr.to_numpy(g), w, parity.FLOOR32)
-        out[name] = {"max_rel_err": mx, "mean_rel_err": mean}
+    if thr_holder.get("flux") is not None:
+        thr = thr_holder["threshold"]
+        t0 = time.perf_counter()
+        wf, ws = oracle.accu_threshold(fd, m64, thr.astype(np.float64), ps, dtype=np.float64, nthreads=nthreads)
+        out["oracle_accu_threshold_s"] = round(time.perf_counter() - t0, 2)
+        for name, g, w in (("accu_threshold_flux", thr_holder["flux"], wf),
+                           ("accu_threshold_state", thr_holder["state"], ws)):
+            mx, mean = rel_error_device(g, w, parity.FLOOR32)
+            out[name] = {"max_rel_err": mx, "mean_rel_err": mean}
+        del wf, ws
+    out["within_tolerance"] = all(v["max_rel_err"] <= parity.RTOL32 for k, v in out.items()
+                                  if isinstance(v, dict) and "max_rel_err" in v)
     return out
 
 
@@ -242,16 +276,17 @@ def bench_reference(args, world, rank):
     times = [run_cpu_accu(fd, m, ps, nthreads) for _ in range(args.steps)]
     total = sum(times)
     value = fd.size * args.steps / total / 1e6
-    sample = (f"accu over rows 0-{fd.shape[0] - 1} of the {w['rows']}x{w['cols']} raster "
-              f"({fd.shape[0]}x{fd.shape[1]} cells, partitions {ps[0]}x{ps[1]}, the fastest of a sweep: "
-              + ", ".join(f"{a}x{b} {t * 1000:.0f} ms" for (a, b), t in sweep.items()) + ") per step")
+    sample = (f"accu over the whole {w['rows']}x{w['cols']} raster per step (partitions {ps[0]}x{ps[1]}, the "
+              f"fastest of a sweep: " + ", ".join(f"{a}x{b} {t * 1000:.0f} ms" for (a, b), t in sweep.items())
+              + ")")
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3),
         "unit": "Mcells/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1000 * total / args.steps, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fBm DEM, lognormal material)",
         "config": {"workload": args.workload, "rows": w["rows"], "cols": w["cols"],
-                   "partition_shape": list(w["partition"]), "l2": "inputs larger than L2"},
+                   "partition_shape": list(w["partition"]), "cpu_partition_shape": list(ps),
+                   "l2": "inputs larger than L2"},
         "cpu_baseline": {"value": round(value, 3), "unit": "Mcells/s", "cores": nthreads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": round(value, 3), "unit": "Mcells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -360,10 +395,12 @@ def bench_ours(args, world, rank, local):
         torch.cuda.synchronize()
         return max_over_ranks(e0.elapsed_time(e1) / 1000.0, world)
 
-    # The host memory and its link are shared with the other jobs of the machine: best of three trials
-    e2e_trials = [e2e_trial() for _ in range(3)]
-    e2e_s = min(e2e_trials)
+    # The host memory and its link are shared with the other jobs of the machine: five trials, the
+    # median is the value, the fastest is reported beside it
+    e2e_trials = [e2e_trial() for _ in range(5)]
+    e2e_s = statistics.median(e2e_trials)
     e2e_value = world * n * e2e_steps / e2e_s / 1e6
+    e2e_best = world * n * e2e_steps / min(e2e_trials) / 1e6
     assert torch.equal(out_host[(e2e_steps - 1) % 2], out.data.cpu()), "end-to-end result differs"
 
     # roofline of the accu call (its kernels together; one call per step)
@@ -383,8 +420,9 @@ def bench_ours(args, world, rank, local):
         torch.cuda.synchronize()
         torch.cuda.empty_cache()
 
+    thr_holder = {}
     if args.threshold_calls > 0 and rank == 0:
-        leg("accu_threshold", lambda a, d: bench_threshold(a, d, fd_d, m_d, inputs))
+        leg("accu_threshold", lambda a, d: bench_threshold(a, d, fd_d, m_d, inputs, thr_holder))
     if args.kinematic_wave_steps > 0 and rank == 0:
         leg("kinematic_wave", bench_kinematic_wave)
     if not args.no_ensemble and rank == 0:
@@ -395,20 +433,26 @@ def bench_ours(args, world, rank, local):
     if rank != 0:
         return
     cpu = None
+    accuracy = None
     if world == 1 and not args.skip_cpu:
         fd_s, m_s, ps_s = cpu_sample(inputs, ps)
         nthreads = os.cpu_count() or 1
         ps_s, sweep = best_cpu_partition(fd_s, m_s, ps_s, nthreads)
         t_cpu = run_cpu_accu(fd_s, m_s, ps_s, nthreads)
         cpu = {"value": round(fd_s.size / t_cpu / 1e6, 3), "unit": "Mcells/s", "cores": nthreads, "kind": "port",
-               "sample": f"accu over rows 0-{fd_s.shape[0] - 1} of the raster ({fd_s.shape[0]}x{fd_s.shape[1]} "
-                         f"cells, partitions {ps_s[0]}x{ps_s[1]}, the fastest of a sweep: "
+               "sample": f"accu over the whole raster ({fd_s.shape[0]}x{fd_s.shape[1]} cells, partitions "
+                         f"{ps_s[0]}x{ps_s[1]}, the fastest of a sweep: "
                          + ", ".join(f"{a}x{b} {t * 1000:.0f} ms" for (a, b), t in sweep.items())
                          + "), one pass, oracle/lue_oracle.c threaded"}
-        try:  # the float32 error of the GPU results on the same sample, against the float64 oracle
-            cpu["accuracy"] = accuracy_on_sample(fd_s, m_s, ps_s, nthreads, dev)
+    if world == 1 and not args.skip_accuracy:
+        try:  # the float32 error of the GPU results on the whole raster, against the float64 oracle
+            accuracy = {"accu_16k": accuracy_full_raster(inputs, ps, out.data, thr_holder, os.cpu_count() or 1)}
         except Exception as e:  # noqa: BLE001  (reported in the line, the bench itself goes on)
-            cpu["accuracy"] = {"error": f"{type(e).__name__}: {e}"}
+            accuracy = {"accu_16k": {"error": f"{type(e).__name__}: {e}"}}
+        thr_holder.clear()
+        kw = extra.get("kinematic_wave", {})
+        if "accuracy" in kw:
+            accuracy["kw_8k"] = kw["accuracy"]
     line = {
         "metric": METRIC, "value": round(value, 3),
         "unit": "Mcells/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -421,7 +465,9 @@ def bench_ours(args, world, rank, local):
                    "tile_exits": stats.get("tile_exits", 0), "exit_forest_depth": stats.get("exit_forest_depth", 0)},
         "e2e": {"value": round(e2e_value, 3), "unit": "Mcells/s", "h2d_bytes_per_step": 4 * n,
                 "d2h_bytes_per_step": 4 * n, "steps": e2e_steps,
-                "trials_ms_per_step": [round(1000 * x / e2e_steps, 2) for x in e2e_trials], "timed": "best of 3 trials",
+                "best_of_trials": round(e2e_best, 3),
+                "trials_ms_per_step": [round(1000 * x / e2e_steps, 2) for x in e2e_trials],
+                "timed": "median of 5 trials (value), fastest beside it",
                 "overlap": "upload of step k+1 and download of step k-1 beside the routing of step k "
                            "(three streams, double buffers, pinned host memory)"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
@@ -431,6 +477,7 @@ def bench_ours(args, world, rank, local):
                      "timed": "whole call per step (all its kernels), CUDA events on the launching stream",
                      "peak_kind": peak_kind, "bytes_per_cell": ACCU_BYTES_PER_CELL},
         "cpu_baseline": cpu,
+        "accuracy": accuracy,
         "clocks": clocks,
         "gpu_launches": int(launches),
         "mass_balance": {"material_in": total_in, "outlet_outflow": total_out,
@@ -440,7 +487,7 @@ def bench_ours(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
-def bench_threshold(args, dev, fd_d, m_d, inputs):
+def bench_threshold(args, dev, fd_d, m_d, inputs, holder):
     """C2's second operation: accu_threshold over the same raster and material, threshold float32
     uniform [0, 0.5) (seeded), on the path engine (one launch per path level), with the stage engine
     (default and autotuned schedule) timed beside it.  Mass balance: what the cells keep plus what leaves
@@ -472,6 +519,7 @@ def bench_threshold(args, dev, fd_d, m_d, inputs):
         return e0.elapsed_time(e1) / 1000.0 / calls
 
     s = timed()  # the path engine
+    holder.update(flux=flux.data, state=state.data, threshold=thr.data.cpu().numpy())
     mask = outlet_mask(fd_d.data)
     total_in = float(m_d.data.double().sum())
     kept = float(state.data.double().sum())
@@ -564,7 +612,14 @@ def bench_kinematic_wave(args, dev):
                  "tuner_ms_of_best": round(best["ms"], 3), "tuning_s": round(tune_s, 2),
                  "ms_per_step": round(1000 * s_multi / T, 3)}
     finite = torch.isfinite(out.data)
+    accuracy = None
+    if not args.skip_accuracy:
+        try:
+            accuracy = kinematic_wave_accuracy(args, dev, d, ps, fd, q, lat, alpha, out, T)
+        except Exception as e:  # noqa: BLE001  (reported in the line, the bench itself goes on)
+            accuracy = {"error": f"{type(e).__name__}: {e}"}
     return {"workload": "kw_8k (8192x8192, float64 discharge, float32 rain and alpha, beta 0.6, dt 3600 s, dx 100 m)",
+            "accuracy": accuracy,
             "steps": T, "ms_per_step": round(1000 * s_multi / T, 3),
             "value": round(n * T / s_multi / 1e6, 3), "unit": "Mcells/s",
             "roofline_frac_hbm": round(KW_BYTES_PER_CELL * n * T / s_multi / 1e9 / peaks()[0], 4),
@@ -579,6 +634,56 @@ def bench_kinematic_wave(args, dev):
                              "the 25 B/cell-step HBM figure is the per-call drop-in's traffic, not this kernel's",
             "longest_flow_path_cells": fd.topology().stats()["max_level"] + 1,
             "outflow_finite_cells": int(finite.sum())}
+
+
+def kinematic_wave_accuracy(args, dev, d, ps, fd, q, lat, alpha, out, T, band_rows=1024):
+    """C3's result against float64 references, tolerance 1e-9 relative (floor 1e-12):
+    - the whole 8192^2 raster: the timed T-step call (stage engine, float-float solve) against T
+      single-step calls with the reference-faithful float64 solve (LUE_GB300_KW_SOLVE=reference);
+    - rows 0..band_rows-1 of the same inputs (flow leaving the band is dropped, as at the array edge):
+      one T-step call on the band's own topology against T sequential steps of the float64 oracle
+      (oracle/lue_oracle.c, threaded)."""
+    import torch
+
+    from lue_gb300 import framework as lfr
+    from oracle import oracle
+    from tests import parity
+    res = {"tolerance": parity.RTOL64, "floor": parity.FLOOR64, "steps": T}
+    os.environ["LUE_GB300_KW_SOLVE"] = "reference"
+    try:
+        qq = q
+        t0 = time.perf_counter()
+        for _ in range(T):
+            qq = lfr.kinematic_wave(fd, qq, lat, alpha, 0.6, 3600.0, 100.0)
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+    finally:
+        del os.environ["LUE_GB300_KW_SOLVE"]
+    mx, mean = rel_error_device(out.data, qq.data.cpu().numpy(), parity.FLOOR64)
+    res["whole_raster_vs_single_step_float64_calls"] = {"max_rel_err": mx, "mean_rel_err": mean,
+                                                        "reference_calls_s": round(secs, 2)}
+    del qq
+    band = {k: np.ascontiguousarray(d[k][:band_rows]) for k in ("flow_direction", "discharge", "lateral_inflow",
+                                                                "alpha")}
+    bps = (min(ps[0], band_rows), ps[1])
+    fdb = lfr.from_numpy(band["flow_direction"], bps, device=dev)
+    got = lfr.kinematic_wave_steps(fdb, lfr.from_numpy(band["discharge"], bps, device=dev),
+                                   lfr.from_numpy(band["lateral_inflow"], bps, device=dev),
+                                   lfr.from_numpy(band["alpha"], bps, device=dev), 0.6, 3600.0, 100.0, T)
+    want = band["discharge"]
+    lat64, al64 = band["lateral_inflow"].astype(np.float64), band["alpha"].astype(np.float64)
+    t0 = time.perf_counter()
+    nthreads = os.cpu_count() or 1
+    for _ in range(T):
+        want = oracle.kinematic_wave(band["flow_direction"], want, lat64, al64, 0.6, 3600.0, 100.0, bps,
+                                     dtype=np.float64, nthreads=nthreads)
+    mx, mean = rel_error_device(got.data, want, parity.FLOOR64)
+    res[f"rows_0_{band_rows - 1}_vs_oracle"] = {"max_rel_err": mx, "mean_rel_err": mean,
+                                                "oracle_s": round(time.perf_counter() - t0, 2)}
+    fdb.topology().close()
+    res["within_tolerance"] = all(v["max_rel_err"] <= parity.RTOL64 for v in res.values()
+                                  if isinstance(v, dict) and "max_rel_err" in v)
+    return res
 
 
 def bench_ensemble(args, dev):
@@ -597,6 +702,7 @@ def bench_ensemble(args, dev):
         tuned = {"schedule": tstats["stage_schedule"], "tuned_on": "a 4-step call of the same atlas",
                  "tuning_s": tstats["tuning_s"], "batched_waves_s": round(s_tuned, 3),
                  "batched_waves_mcells_per_s": round(cells * steps / s_tuned / 1e6, 3)}
+    s_plain, cells_plain, _ = ensemble.run_plain_resident(inst, steps, device=dev)
     sample = 8
     s_alone, cells_alone, _ = ensemble.run_unbatched(inst, steps, sample, device=dev)
     return {"workload": "64 catchments (sides log-uniform 512-4096, depression-filled D8) x 4 rain scenarios, "
@@ -607,6 +713,11 @@ def bench_ensemble(args, dev):
             "batched_waves_mcells_per_s": round(cells * steps / s_waves / 1e6, 3),
             "batched_waves_s": round(s_waves, 3),
             "batched_waves_autotuned": tuned,
+            "plain_resident_per_instance_mcells_per_s": round(cells_plain * steps / s_plain / 1e6, 3),
+            "plain_resident_per_instance_s": round(s_plain, 3),
+            "plain_resident_note": "every instance alone through the drop-in at its best: resident topology "
+                                   "per catchment, device-resident inputs, one kinematic_wave_steps call of all "
+                                   "48 steps per instance, CUDA events",
             "one_launch_per_instance_mcells_per_s": round(cells_alone * steps / s_alone / 1e6, 3),
             "one_launch_per_instance_sample": f"first {sample} instances, topology built per instance"}
 
@@ -630,6 +741,10 @@ def bench_serving(args, dev):
     for r in sub:
         r.arrival = 0.0
     seq = serving.run_sequential_plain(server, sub, keep_results=False)
+    sub3 = copy.deepcopy(reqs[:k])
+    for r in sub3:
+        r.arrival = 0.0
+    seq_resident = serving.run_sequential_resident(server, sub3, keep_results=False)
     sub2 = copy.deepcopy(reqs[:k])
     for r in sub2:
         r.arrival = 0.0
@@ -638,6 +753,7 @@ def bench_serving(args, dev):
                         "128-grid pool, sides log-uniform 256-8192", "seconds_of_arrivals": args.serve_seconds,
             "served": served,
             "same_requests_closed_loop": {"first_k": k, "continuous_batching": batched_sub,
+                                          "sequential_resident_calls": seq_resident,
                                           "sequential_plain_calls": seq}}
 
 
@@ -654,6 +770,8 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--serve-sequential", type=int, default=32)
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-accuracy", action="store_true",
+                    help="do not compare the results with the float64 oracle on the whole raster")
     ap.add_argument("--no-autotune", action="store_true", help="time the stage legs with the default schedule only")
     ap.add_argument("--no-stage-compare", dest="stage_compare", action="store_false",
                     help="do not time accu_threshold on the stage engine beside the path engine")

@@ -6,8 +6,11 @@ stay on the device.  The loop:
 
 - queues requests as they arrive (a Poisson stream in the benchmark);
 - admits the oldest waiting request as soon as a slot (CUDA stream) is free and its device memory
-  (inputs, outputs, per-request scratch) fits in the free-HBM budget, so requests that arrive while
-  others run start while those are still on the GPU, and their kernels overlap;
+  (inputs, outputs, per-request scratch) fits, so requests that arrive while others run start while
+  those are still on the GPU, and their kernels overlap.  "Fits" is checked against two figures at
+  every admission: the server's budget less the estimates of the admitted requests, and the HBM free
+  right now (cudaMemGetInfo plus what torch's caching allocator holds unused) less a reserve.  A request
+  whose estimate exceeds the whole budget is never admitted: it completes at once with an error;
 - runs each request on its own stream with its own topology handle (a clone that shares the grid's
   resident topology and has its own scratch), copies the result back to pinned host memory, and
   completes it when its event has fired.
@@ -34,6 +37,7 @@ class Request:
     result: object = None
     start: float = None
     done: float = None
+    error: str = None
 
     @property
     def latency(self):
@@ -76,6 +80,8 @@ def device_inputs(r, shape, device, stream=None):
 
 
 class Server:
+    RESERVE_BYTES = 256 << 20  # kept free for the stage buffers that grow inside a call
+
     def __init__(self, pool_fds, slots=8, hbm_fraction=0.5, device="cuda"):
         import torch
 
@@ -108,6 +114,23 @@ class Server:
         per_class = max(1, slots // 4)
         held = [torch.empty(s, dtype=torch.uint8, pin_memory=True) for s in sorted(sizes) for _ in range(per_class)]
         del held
+
+    def free_bytes(self):
+        """Device memory a new request can use now: free HBM plus torch's cached, unallocated blocks."""
+        torch = self.torch
+        free, _ = torch.cuda.mem_get_info(self.device)
+        cached = torch.cuda.memory_reserved(self.device) - torch.cuda.memory_allocated(self.device)
+        return free + max(0, cached)
+
+    def admissible(self, r, busy):
+        """None if request r may start now; else why not ("wait", or "never" when its estimate exceeds
+        the whole budget).  With nothing running (busy False) a request within the budget starts."""
+        need = self.bytes_needed(r)
+        if need > self.budget:
+            return "never"
+        if busy and (self.in_use + need > self.budget or need > self.free_bytes() - self.RESERVE_BYTES):
+            return "wait"
+        return None
 
     def cells(self, r):
         return int(np.prod(self.grids[r.grid].shape))
@@ -177,11 +200,17 @@ class Server:
             active = still
             while waiting and free_streams:
                 r = waiting[0]
-                need = self.bytes_needed(r)
-                if active and self.in_use + need > self.budget:
+                why = self.admissible(r, bool(active))
+                if why == "never":  # larger than the whole budget: completes at once, with an error
+                    waiting.popleft()
+                    r.start = r.done = time.perf_counter() - t0
+                    r.error = "request needs more device memory than the server's budget"
+                    done += 1
+                    continue
+                if why == "wait":
                     break  # admission by free HBM: wait for running requests to finish
                 waiting.popleft()
-                self.in_use += need
+                self.in_use += self.bytes_needed(r)
                 r.start = time.perf_counter() - t0
                 active.append(self._launch(r, free_streams.pop(), keep_results))
                 self.max_active = max(self.max_active, len(active))
@@ -195,9 +224,11 @@ class Server:
 
 
 def summarize(requests, wall, server):
-    lat = np.array([r.latency for r in requests])
-    cell_steps = sum(int(np.prod(server.grids[r.grid].shape)) * r.steps for r in requests)
-    return {"requests": len(requests), "max_concurrent": getattr(server, "max_active", 1),
+    served = [r for r in requests if r.error is None]
+    lat = np.array([r.latency for r in served]) if served else np.zeros(1)
+    cell_steps = sum(int(np.prod(server.grids[r.grid].shape)) * r.steps for r in served)
+    return {"requests": len(requests), "rejected": len(requests) - len(served),
+            "max_concurrent": getattr(server, "max_active", 1),
             "p50_ms": float(np.percentile(lat, 50) * 1e3),
             "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_ms": float(lat.mean() * 1e3),
             "wall_s": wall, "mcells_per_s": cell_steps / wall / 1e6,
@@ -231,6 +262,40 @@ def run_sequential_plain(server, requests, keep_results=True):
         if keep_results:
             r.result = res
         fd.topology().close()
+    return summarize(requests, time.perf_counter() - t0, server)
+
+
+def run_sequential_resident(server, requests, keep_results=True):
+    """The plain drop-in at its best: one request at a time, in arrival order, on the server's resident
+    topology of its grid (no build per call) with all kinematic-wave steps in one
+    kinematic_wave_steps call; one stream, no overlap; the result read back to host memory, as in
+    Server.run."""
+    torch = server.torch
+    from . import _lib
+    L = _lib.lib()
+    stream = torch.cuda.current_stream(server.device)
+    t0 = time.perf_counter()
+    for r in sorted(requests, key=lambda r: r.arrival):
+        now = time.perf_counter() - t0
+        if r.arrival > now:
+            time.sleep(r.arrival - now)
+        r.start = time.perf_counter() - t0
+        fd = server.grids[r.grid]
+        topo = server.topologies[r.grid]
+        x = device_inputs(r, fd.shape, server.device)
+        if r.kind == "accu":
+            out = torch.empty(fd.shape, dtype=torch.float32, device=server.device)
+            _lib.check(L.lue_gpu_accu_f32(topo.handle, x["material"].data_ptr(), 0.0, out.data_ptr(),
+                                          stream.cuda_stream))
+        else:
+            out = torch.empty(fd.shape, dtype=torch.float64, device=server.device)
+            _lib.check(L.lue_gpu_kinematic_wave_steps_f64_f32in(
+                topo.handle, x["discharge"].data_ptr(), x["lateral"].data_ptr(), 0.0, x["alpha"].data_ptr(), 0.0,
+                0.6, 3600.0, 100.0, r.steps, out.data_ptr(), stream.cuda_stream))
+        res = out.cpu().numpy()
+        r.done = time.perf_counter() - t0
+        if keep_results:
+            r.result = res
     return summarize(requests, time.perf_counter() - t0, server)
 
 

@@ -1,5 +1,5 @@
 """bench.py --impl reference on the CPU: one JSON line with the benchmark's keys, the CPU port of the
-reference's algorithm timed on a bounded sample, and no host-device bytes."""
+reference's algorithm timed on the workload's whole raster, and no host-device bytes."""
 import json
 import os
 import subprocess

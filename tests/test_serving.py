@@ -48,3 +48,31 @@ def test_results_in_the_mix_equal_results_alone():
         else:
             assert np.array_equal(np.isnan(m.result), np.isnan(p.result)), m.rid
             assert parity.rel_error(m.result, p.result, parity.FLOOR64)[0] <= 1e-12, m.rid
+
+
+@pytest.mark.gpu
+def test_admission_waits_for_memory_and_rejects_requests_above_the_budget():
+    """A request that does not fit beside the running ones waits until they finish; one that exceeds the
+    whole budget is never admitted; low free HBM (a fake of the free-memory query) holds requests back."""
+    import torch
+    assert torch.cuda.is_available()
+    shapes = [(64, 64), (256, 256)]
+    pool = serving.build_pool(shapes, seed=4)
+    server = serving.Server(pool, slots=4)
+    small = serving.Request(0, "accu", 0, 0.0, 1, dict(seed=1))
+    big = serving.Request(1, "kinematic_wave", 1, 0.0, 5, dict(seed=2))
+    server.budget = server.bytes_needed(small) + server.bytes_needed(big) - 1  # not both at once
+    assert server.admissible(big, busy=True) == "wait"
+    assert server.admissible(big, busy=False) is None
+    summary = server.run([small, big], realtime=False)
+    assert summary["rejected"] == 0 and summary["max_concurrent"] == 1
+    assert big.start >= small.done and big.result is not None
+    server.budget = 1 << 40
+    server.free_bytes = lambda: server.RESERVE_BYTES  # nothing free beyond the reserve
+    assert server.admissible(small, busy=True) == "wait"
+    assert server.admissible(small, busy=False) is None
+    del server.free_bytes
+    server.budget = server.bytes_needed(big) - 1
+    too_big = serving.Request(2, "kinematic_wave", 1, 0.0, 5, dict(seed=3))
+    summary = server.run([too_big], realtime=False)
+    assert summary["rejected"] == 1 and too_big.error and too_big.result is None
