@@ -472,7 +472,7 @@ def bench_ours(args, world, rank, local):
                            "(three streams, double buffers, pinned host memory)"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "kernel": ("accu_f32 call: k_tile_exits + exit-forest scan + k_tile_accu" if engine == "tiles"
+                     "kernel": ("accu_f32 call: k_tile_exit_sums + exit-forest scan + k_tile_accu" if engine == "tiles"
                                 else "k_walk<RouteF32<accu>>"),
                      "timed": "whole call per step (all its kernels), CUDA events on the launching stream",
                      "peak_kind": peak_kind, "bytes_per_cell": ACCU_BYTES_PER_CELL},

@@ -328,6 +328,7 @@ struct __align__(16) TileSmem {
     uint8_t up[kTileCells];        // in-tile upstream mask
     uint8_t fd[kHalo][kHalo + 2];  // flow direction with a one-cell halo (255 outside the array)
     uint8_t border[kBorderCells];  // per border cell: outside neighbours draining into it
+    uint8_t lab[kTileCells];       // exit label of each cell
     int round_count[3];            // cells queued for the next rounds (a ring of three counters)
 };
 
@@ -414,14 +415,6 @@ __device__ __forceinline__ int border_index(int rin, int cin)
     return cin == 0 ? 2 * kTile + rin - 1 : 3 * kTile - 2 + rin - 1;
 }
 
-// 1 when in-tile cell i is a border cell with inflow from outside the tile (sm.border filled).
-__device__ __forceinline__ int entry_of(const TileSmem& sm, int i)
-{
-    const int rin = i >> 6, cin = i & 63;
-    if (!(rin == 0 || rin == kTile - 1 || cin == 0 || cin == kTile - 1)) return 0;
-    return sm.border[border_index(rin, cin)] != 0;
-}
-
 // Exclusive prefix of one int per thread over the block; `total` gets the block sum.
 __device__ __forceinline__ int block_exclusive_int(int v, int* warp_tot, int& total)
 {
@@ -448,12 +441,12 @@ __device__ __forceinline__ int block_exclusive_int(int v, int* warp_tot, int& to
 // Build: the flow forest of one tile (CTA per tile), in post-order.  A cell's in-tile upstream cells
 // (its subtree) get the positions start .. pos - 1 and the cell itself pos, so that the accu of any cell
 // is the difference of two prefix sums over the material laid out in post-order.  Cells with a no-data
-// flow direction (or outside the array) take the positions after the valid cells, flagged kInvalidPos.
-// Also: each exit's (pos, start) and, per border cell, which outside neighbours drain into it.
+// flow direction (or outside the array) take the positions after the valid cells, flagged kNoValue.
+// Also: each cell's exit label, and, per border cell, which outside neighbours drain into it.
 __global__ void __launch_bounds__(kTileThreads)
     k_tile_forest(const uint8_t* __restrict__ fd, TileGeom g, const int32_t* __restrict__ exit_base,
-                  const uint16_t* __restrict__ exit_local, uint16_t* cell_at, uint16_t* prev_at,
-                  uint32_t* exit_span, uint8_t* border_in, int* error)
+                  const uint16_t* __restrict__ exit_local, uint16_t* cell_at, uint16_t* prev_at, uint8_t* label,
+                  uint8_t* border_in, int* error)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TileSmem& sm = *reinterpret_cast<TileSmem*>(smem_raw);
@@ -494,8 +487,13 @@ __global__ void __launch_bounds__(kTileThreads)
     }
     const int rounds = r, nvalid = head;
     if (t == 0) rstart[rounds] = (uint16_t)nvalid;
+    // labels: none (or no-data) everywhere, then each exit its index; the exits are roots of the forest
+    for (int i = t; i < kTileCells; i += kTileThreads)
+        sm.lab[i] = sm.fd[(i >> 6) + 1][(i & 63) + 1] == kNoData ? kLabelNoData : kLabelNone;
     __syncthreads();
-    // per border cell, the neighbours outside the tile that drain into it (the cell then gets an entry node)
+    const int32_t e0 = exit_base[tile], ne = exit_base[tile + 1] - e0;
+    for (int e = t; e < ne; e += kTileThreads) sm.lab[exit_local[e0 + e]] = (uint8_t)e;
+    // per border cell, the neighbours outside the tile that drain into it
     for (int b = t; b < kBorderCells; b += kTileThreads) {
         int rin, cin;
         border_cell(b, rin, cin);
@@ -508,16 +506,15 @@ __global__ void __launch_bounds__(kTileThreads)
                 if (sm.fd[hr + 1][hc + 1] == nb_inflow_code(q)) outside |= 1u << q;
             }
         }
-        sm.border[b] = (uint8_t)outside;
         border_in[tile * kBorderCells + b] = (uint8_t)outside;
     }
     __syncthreads();
-    // subtree sizes (entry nodes included), upstream first
+    // subtree sizes, upstream first
     for (int q = 0; q < rounds; ++q) {
         for (int k = rstart[q] + t; k < rstart[q + 1]; k += kTileThreads) {
             const int i = sm.queue[k];
             unsigned m = sm.up[i];
-            int size = 1 + entry_of(sm, i);
+            int size = 1;
             while (m) {
                 size += sz[i + tile_nb_offset(__ffs(m) - 1)];
                 m &= m - 1;
@@ -549,22 +546,24 @@ __global__ void __launch_bounds__(kTileThreads)
         }
     }
     __syncthreads();
-    // the other cells, downstream first: after the siblings that come before them
+    // the other cells, downstream first: after the siblings that come before them; a cell's label is
+    // its downstream cell's
     for (int q = rounds - 1; q >= 0; --q) {
         for (int k = rstart[q] + t; k < rstart[q + 1]; k += kTileThreads) {
             const int i = sm.queue[k], d = sm.dsl[i];
             if (d == kNoCell) continue;
             unsigned m = sm.up[d] & ((1u << nb_index_from(d, i)) - 1u);
-            int o = st[d] + entry_of(sm, d);  // after d's entry node and the siblings before i
+            int o = st[d];
             while (m) {
                 o += sz[d + tile_nb_offset(__ffs(m) - 1)];
                 m &= m - 1;
             }
             st[i] = (uint16_t)o;
+            sm.lab[i] = sm.lab[d];
         }
         __syncthreads();
     }
-    // positions, checked distinct, and the tables by position: cells, entry nodes, then padding
+    // positions, checked distinct (every position 0 .. 4095 once), and the tables by position
     const int64_t T = tile * kRunPositions;
     uint32_t* seen = reinterpret_cast<uint32_t*>(sm.queue);  // the queue is no longer read
     for (int w = t; w < kRunPositions / 32; w += kTileThreads) seen[w] = 0;
@@ -572,34 +571,20 @@ __global__ void __launch_bounds__(kTileThreads)
     for (int i = t; i < kTileCells; i += kTileThreads) {
         const int rin = i >> 6, cin = i & 63;
         const bool valid = sm.fd[rin + 1][cin + 1] != kNoData;
-        const bool entry = valid && entry_of(sm, i);
         const int s0 = st[i], p = s0 + sz[i] - 1;
         bool bad = p >= kRunPositions || s0 > p;
         if (!bad) bad = (atomicOr(&seen[p >> 5], 1u << (p & 31)) >> (p & 31)) & 1u;
-        if (!bad && entry) bad = (atomicOr(&seen[s0 >> 5], 1u << (s0 & 31)) >> (s0 & 31)) & 1u;
         if (bad) {
             *error = 1;
             continue;
         }
         cell_at[T + run_table_index(p)] = (uint16_t)(i | (valid ? 0u : kNoValue));
-        prev_at[T + run_table_index(p)] = (uint16_t)((s0 > 0 ? s0 - 1 : kZeroSlot) | (s0 == p ? kPrevRidge : 0u));
-        if (entry) {
-            cell_at[T + run_table_index(s0)] = (uint16_t)((kEntryBase + border_index(rin, cin)) | kNoOutput);
-            prev_at[T + run_table_index(s0)] = (uint16_t)kZeroSlot;
-        }
+        prev_at[T + run_table_index(p)] =
+            (uint16_t)((s0 > 0 ? scan_slot(s0 - 1) : kZeroSlot) | (s0 == p ? kPrevRidge : 0u));
+        label[tile * kTileCells + i] = sm.lab[i];
     }
     __syncthreads();
-    for (int p = t; p < kRunPositions; p += kTileThreads) {
-        if ((seen[p >> 5] >> (p & 31)) & 1u) continue;
-        cell_at[T + run_table_index(p)] = (uint16_t)(kNoValue | kNoOutput);
-        prev_at[T + run_table_index(p)] = (uint16_t)kZeroSlot;
-    }
-    const int32_t e0 = exit_base[tile], ne = exit_base[tile + 1] - e0;
-    for (int e = t; e < ne; e += kTileThreads) {
-        const int loc = exit_local[e0 + e];
-        const int s0 = st[loc], p = s0 + sz[loc] - 1;
-        exit_span[e0 + e] = (uint32_t)p | ((uint32_t)(s0 > 0 ? s0 - 1 : kZeroSlot) << 16);
-    }
+    if (t < kRunPositions / 32 && seen[t] != 0xFFFFFFFFu) *error = 1;
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -746,21 +731,21 @@ __device__ __forceinline__ void store_quad(float* __restrict__ p, const TileGeom
 struct TileForest {
     const uint16_t* cell_at;
     const uint16_t* prev_at;
+    const uint8_t* label;
     const uint8_t* border_in;
     const int32_t* halo_exit;
 };
 
-// Shared memory of a tile CTA (dynamic: 54 KB, four CTAs per SM).
+// Shared memory of a pass-3 tile CTA (dynamic: 53 KB, four CTAs per SM).
 struct __align__(16) TileCallSmem {
-    unsigned long long S[kScanSlotCount];  // inclusive prefix sums by position; S[kZeroSlot] = 0
-    float M[kTileCells + kTileThreads];    // material in cell order, then the entry sums (kEntryBase + b);
-                                           // pass 3 then puts the results there in cell order
-    float warp_sum[kTileThreads / 32];
+    unsigned long long S[kScanSlotCount];  // inclusive prefix sums by scan slot; S[kZeroSlot] = 0
+    float M[kTileCells];                   // material plus what enters, in cell order; then the results
     unsigned long long warp_tot[kTileThreads / 32];
     unsigned red[2][kTileThreads / 32];
+    float warp_sum[kTileThreads / 32];
 };
 
-// The thread's run of a per-position table (cell_at or prev_at): nine coalesced 4-byte loads.
+// The thread's run of a per-position table (cell_at or prev_at): eight coalesced 4-byte loads.
 __device__ __forceinline__ void load_run(const uint16_t* __restrict__ table, uint32_t (&w)[kRunWords])
 {
     const uint32_t* p = reinterpret_cast<const uint32_t*>(table) + threadIdx.x;
@@ -772,7 +757,7 @@ __device__ __forceinline__ unsigned run_at(const uint32_t (&w)[kRunWords], int j
     return (w[j >> 1] >> (16 * (j & 1))) & 0xFFFFu;
 }
 
-// Material of the tile in cell order (0 outside the array): the loads, then the stores to M.
+// Material of the tile in cell order (0 outside the array), by quads of 4 cells (quad_cell).
 __device__ __forceinline__ void load_material(float4 (&x)[4], const float* __restrict__ ext, float ext_s,
                                               const TileGeom& g, int64_t tr, int64_t tc, bool vec)
 {
@@ -783,214 +768,158 @@ __device__ __forceinline__ void load_material(float4 (&x)[4], const float* __res
                    : make_float4(ext_s, ext_s, ext_s, ext_s);
     }
 }
-__device__ __forceinline__ void store_material(TileCallSmem& sm, const float4 (&x)[4])
+
+__device__ __forceinline__ float quad_at(const float4& q, int k)
 {
-#pragma unroll
-    for (int j = 0; j < 4; ++j) *reinterpret_cast<float4*>(sm.M + quad_cell(j)) = x[j];
+    return k == 0 ? q.x : (k == 1 ? q.y : (k == 2 ? q.z : q.w));
 }
 
-// Block reductions: the largest bits, the smallest bits, and the float sum of one value per thread.
-__device__ __forceinline__ void tile_reduce(TileCallSmem& sm, unsigned& mx, unsigned& mn, float& sum)
+// Shared memory of a pass-1 tile CTA.
+struct __align__(16) ExitSumSmem {
+    unsigned long long bin[kBorderCells];        // fixed-point material total per exit label
+    unsigned poisoned[(kBorderCells + 31) / 32]; // exits with a NaN or negative term upstream
+    unsigned long long warp_tot[kTileThreads / 32];
+    unsigned red[3][kTileThreads / 32];
+};
+
+// Inclusive sums of v over runs of lanes with equal `key` (consecutive lanes), in the run's last lane.
+__device__ __forceinline__ unsigned long long run_sum(unsigned key, unsigned long long v, bool& last)
 {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    mx = __reduce_max_sync(0xffffffffu, mx);
-    mn = __reduce_min_sync(0xffffffffu, mn);
+    const int lane = threadIdx.x & 31;
+    const unsigned prev = __shfl_up_sync(0xffffffffu, key, 1);
+    const unsigned next = __shfl_down_sync(0xffffffffu, key, 1);
+    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || prev != key);
+    const int start = 31 - __clz(heads & (0xFFFFFFFFu >> (31 - lane)));  // first lane of this lane's run
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-    if (lane == 0) {
-        sm.red[0][warp] = mx;
-        sm.red[1][warp] = mn;
-        sm.warp_sum[warp] = sum;
+    for (int d = 1; d < 32; d <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, v, d);
+        if (lane - d >= start) v += y;
     }
-    __syncthreads();
-    sum = 0.0f;
-#pragma unroll
-    for (int w = 0; w < kTileThreads / 32; ++w) {  // the same order in every thread
-        mx = max(mx, sm.red[0][w]);
-        mn = min(mn, sm.red[1][w]);
-        sum += sm.warp_sum[w];
-    }
+    last = lane == 31 || next != key;
+    return v;
 }
 
-// The thread's terms in post-order (0 where flagged kNoValue), with the bits of its largest term, of its
-// smallest positive term minus one, and its float sum.
-__device__ __forceinline__ void gather_run(const TileCallSmem& sm, const uint32_t (&ca)[kRunWords], float (&x)[kRun],
-                                           unsigned& mx, unsigned& mn, float& sum)
-{
-    mx = 0;
-    mn = 0xFFFFFFFFu;
-    sum = 0.0f;
-#pragma unroll
-    for (int j = 0; j < kRun; ++j) {
-        const unsigned w = run_at(ca, j);
-        const float v = (w & kNoValue) ? 0.0f : sm.M[w & kIndexMask];
-        x[j] = v;
-        const unsigned b = __float_as_uint(v);
-        mx = max(mx, b);
-        mn = min(mn, b - 1u);
-        sum += v;
-    }
-}
-
-// NaN or negative terms (material, or a no-data exit upstream entering the tile): they become 0 and
-// are flagged in the returned mask; the reductions are redone on the cleaned run.
-__device__ __forceinline__ unsigned clean_run(const uint32_t (&ca)[kRunWords], float (&x)[kRun], unsigned& mx,
-                                              unsigned& mn, float& sum)
-{
-    unsigned bad = 0;
-    mx = 0;
-    mn = 0xFFFFFFFFu;
-    sum = 0.0f;
-#pragma unroll
-    for (int j = 0; j < kRun; ++j) {
-        const bool valid = !(run_at(ca, j) & kNoValue);
-        const float v = x[j];
-        if (valid && !(v >= 0.0f)) bad |= 1u << j;
-        x[j] = (valid && v >= 0.0f) ? fabsf(v) : 0.0f;  // fabsf: -0 counts as 0
-        const unsigned b = __float_as_uint(x[j]);
-        mx = max(mx, b);
-        mn = min(mn, b - 1u);
-        sum += x[j];
-    }
-    return bad;
-}
-
-// Poison counts: inclusive prefix sums over the post-order of the flagged terms, written as 32-bit
-// counts by position over S (free until the value scan).  Ends with a block barrier.
-__device__ __forceinline__ void poison_counts(TileCallSmem& sm, unsigned bad)
-{
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    unsigned c[kRun];
-    unsigned run = 0;
-#pragma unroll
-    for (int j = 0; j < kRun; ++j) {
-        run += (bad >> j) & 1u;
-        c[j] = run;
-    }
-    unsigned x = run;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    __syncthreads();  // warp_tot is free
-    if (lane == 31) sm.warp_tot[warp] = x;
-    __syncthreads();
-    unsigned off = x - run;
-    for (int w = 0; w < warp; ++w) off += (unsigned)sm.warp_tot[w];
-    unsigned* C = reinterpret_cast<unsigned*>(sm.S);
-#pragma unroll
-    for (int j = 0; j < kRun; ++j) C[kRun * t + j] = c[j] + off;
-    __syncthreads();
-}
-
-// The poison count up to a scan slot (0 for the zero slot).
-__device__ __forceinline__ unsigned count_at(const TileCallSmem& sm, int slot)
-{
-    return slot == kZeroSlot ? 0u : reinterpret_cast<const unsigned*>(sm.S)[slot];
-}
-
-// Inclusive prefix sums (modulo 2^64) of the thread runs a[0..17] over the whole tile, written to S.
-// Ends with a block barrier.
-__device__ __forceinline__ void tile_prefix(TileCallSmem& sm, unsigned long long (&a)[kRun])
-{
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-#pragma unroll
-    for (int j = 1; j < kRun; ++j) a[j] += a[j - 1];
-    unsigned long long x = a[kRun - 1];
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) sm.warp_tot[warp] = x;
-    __syncthreads();
-    unsigned long long off = x - a[kRun - 1];
-    for (int w = 0; w < warp; ++w) off += sm.warp_tot[w];
-    // 144-byte runs: 16-byte aligned, and the 16-byte stores of a quarter-warp fall on distinct banks
-    ulonglong2* run = reinterpret_cast<ulonglong2*>(sm.S + kRun * t);
-#pragma unroll
-    for (int i = 0; i < kRunWords; ++i) {
-        a[2 * i] += off;
-        a[2 * i + 1] += off;
-        run[i] = make_ulonglong2(a[2 * i], a[2 * i + 1]);
-    }
-    if (t == 0) sm.S[kZeroSlot] = 0ull;
-    __syncthreads();
-}
-
-// F for a tile from its float sum, and whether the tile must go to the walk engine: +inf, a total
-// beyond float range, or a smallest positive term with fewer than 19 bits at that scale.
-__device__ __forceinline__ bool tile_fixed_scale(unsigned mx, unsigned mn, float sum, int& F)
-{
-    const float bound = sum * 1.0009765625f;
-    F = tile_scale(bound);
-    return mx == 0x7F800000u || !(bound < 1.0e38f) ||
-           (mn != 0xFFFFFFFFu && __uint_as_float(mn + 1u) * pow2f(F) < kMinQuantum);
-}
-
-// Pass 1: the local value of every exit (the accu of its in-tile subtree) to P, in the exit forest's
-// post-order, and an upper bound of the tile's material total in 2^-16 units (from its exact fixed-point
-// total).  ~0 as the bound asks for the walk engine.
+// Pass 1: the local value of every exit (the material total of its in-tile catchment: the cells with
+// its label) to P, in the exit forest's post-order; per tile an upper bound of the material total in
+// 2^-16 units (~0 asks for the walk engine: +inf, a total beyond float range, or a dynamic range the
+// 64-bit fixed point cannot hold) and the statistics pass 3 needs.
+//
+// Fixed point: round(x * 2^F), F from 4096 times the tile's largest term, so that every sum stays below
+// 2^62 and is exact (integer addition), whatever the order of the shared-memory atomics.  Each thread
+// holds 4 quads of 4 cells; a quad whose 4 cells have one label takes part in a warp sum over runs of
+// lanes with equal labels (a run's last lane adds the run's total to the label's bin: one atomic per
+// run instead of one per cell, so a basin that covers the tile does not serialise on one address); the
+// other quads add their cells one by one.
 // vec: material rows can be read as float4 (16-byte aligned, columns a multiple of 4).
-__global__ void __launch_bounds__(kTileThreads, 4)
-    k_tile_exits(TileGeom g, const float* __restrict__ ext, float ext_s, bool vec, TileForest f,
-                 const int32_t* __restrict__ exit_base, const uint32_t* __restrict__ exit_span,
-                 const uint32_t* __restrict__ exit_pos, float2* __restrict__ P, unsigned long long* block_total)
+__global__ void __launch_bounds__(kTileThreads)
+    k_tile_exit_sums(TileGeom g, const float* __restrict__ ext, float ext_s, bool vec,
+                     const uint8_t* __restrict__ label, const int32_t* __restrict__ exit_base,
+                     const uint32_t* __restrict__ exit_pos, float2* __restrict__ P,
+                     unsigned long long* __restrict__ block_total, TileStat* __restrict__ stat)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    TileCallSmem& sm = *reinterpret_cast<TileCallSmem*>(smem_raw);
+    __shared__ ExitSumSmem sm;
     const int64_t tr = blockIdx.y, tc = blockIdx.x;  // grid = (tile columns, tile rows)
     const int64_t tile = tr * g.tcols + tc;
-    const int t = threadIdx.x;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     float4 xm[4];
     load_material(xm, ext, ext_s, g, tr, tc, vec);
-    uint32_t ca[kRunWords];
-    load_run(f.cell_at + tile * kRunPositions, ca);
-    const int32_t e0 = __ldg(exit_base + tile), ne = __ldg(exit_base + tile + 1) - e0;
-    uint32_t span = 0, epos = 0;
-    if (t < ne) {  // a tile has at most 252 exits (its border cells)
-        span = __ldg(exit_span + e0 + t);
-        epos = __ldg(exit_pos + e0 + t);
+    uint32_t lw[4];  // labels of the thread's quads (tile-major: quad j is word t + 256 j)
+    const uint32_t* lab = reinterpret_cast<const uint32_t*>(label + tile * kTileCells);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) lw[j] = __ldg(lab + t + kTileThreads * j);
+    if (t < kBorderCells) sm.bin[t] = 0ull;
+    if (t < (kBorderCells + 31) / 32) sm.poisoned[t] = 0u;
+    // over the valid cells: the largest raw bits (a sign bit or NaN sends pass 3 to its slow path), and
+    // the largest and smallest positive bits of the terms that are >= 0
+    unsigned raw = 0, mx = 0, mn = 0xFFFFFFFFu;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float v = quad_at(xm[j], k);
+            const unsigned b = __float_as_uint(v);
+            if (((lw[j] >> (8 * k)) & 0xFFu) != kLabelNoData) {
+                raw = max(raw, b);
+                if (v >= 0.0f) {
+                    mx = max(mx, b & 0x7FFFFFFFu);
+                    mn = min(mn, (b & 0x7FFFFFFFu) - 1u);
+                }
+            }
+        }
     }
-    store_material(sm, xm);
-    sm.M[kEntryBase + t] = 0.0f;  // nothing enters the tile in this pass
+    raw = __reduce_max_sync(0xffffffffu, raw);
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    mn = __reduce_min_sync(0xffffffffu, mn);
+    if (lane == 0) {
+        sm.red[0][warp] = raw;
+        sm.red[1][warp] = mx;
+        sm.red[2][warp] = mn;
+    }
     __syncthreads();
-    float x[kRun], sum;
-    unsigned mx, mn;
-    gather_run(sm, ca, x, mx, mn, sum);
-    tile_reduce(sm, mx, mn, sum);
-    unsigned poisoned_exit = 0;
-    if (mx > 0x7F800000u) {  // NaN or negative material (or -0): clean the run and count
-        const unsigned bad = clean_run(ca, x, mx, mn, sum);
-        __syncthreads();  // red is reused
-        tile_reduce(sm, mx, mn, sum);
-        poison_counts(sm, bad);
-        if (t < ne) poisoned_exit = count_at(sm, (int)(span & 0xFFFFu)) != count_at(sm, (int)(span >> 16));
-        __syncthreads();  // S and warp_tot are free for the value scan
+#pragma unroll
+    for (int w = 0; w < kTileThreads / 32; ++w) {
+        raw = max(raw, sm.red[0][w]);
+        mx = max(mx, sm.red[1][w]);
+        mn = min(mn, sm.red[2][w]);
     }
-    int F;
-    if (tile_fixed_scale(mx, mn, sum, F)) {
+    const float bound = tile_bound(mx, 0u);
+    const int F = tile_scale(bound);
+    if (mx >= 0x7F800000u || !(bound < 1.0e38f) ||
+        (mn != 0xFFFFFFFFu && __uint_as_float(mn + 1u) * pow2f(F) < kMinQuantum)) {
         if (t == 0) block_total[tile] = ~0ull;
         return;  // uniform: every thread has the same reductions
     }
-    unsigned long long a[kRun];
-    if (mn == 0xFFFFFFFFu || __uint_as_float(mn + 1u) * pow2f(F) >= 8388608.0f) {  // every term exact
+    const bool exact = mn == 0xFFFFFFFFu || __uint_as_float(mn + 1u) * pow2f(F) >= 8388608.0f;
+    const bool dirty = raw > 0x7F800000u;  // uniform
+    unsigned long long tile_sum = 0;
 #pragma unroll
-        for (int j = 0; j < kRun; ++j) a[j] = float_to_fixed64_exact(x[j], F);
-    } else {
+    for (int j = 0; j < 4; ++j) {
+        unsigned long long q[4];
+        unsigned l[4];
 #pragma unroll
-        for (int j = 0; j < kRun; ++j) a[j] = float_to_fixed64(x[j], F);
+        for (int k = 0; k < 4; ++k) {
+            l[k] = (lw[j] >> (8 * k)) & 0xFFu;
+            float v = quad_at(xm[j], k);
+            if (l[k] == kLabelNoData) v = 0.0f;
+            if (dirty) {
+                if (!(v >= 0.0f)) {  // NaN or negative: the exit downstream is NaN
+                    if (l[k] < kBorderCells) atomicOr(&sm.poisoned[l[k] >> 5], 1u << (l[k] & 31));
+                    v = 0.0f;
+                }
+                v = fabsf(v);  // -0 counts as 0
+            }
+            q[k] = exact ? float_to_fixed64_exact(v, F) : float_to_fixed64(v, F);
+        }
+        const unsigned long long qs = q[0] + q[1] + q[2] + q[3];
+        tile_sum += qs;
+        const bool uniform = lw[j] == (lw[j] & 0xFFu) * 0x01010101u;
+        if (!uniform) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (l[k] < kBorderCells && q[k]) atomicAdd(&sm.bin[l[k]], q[k]);
+        }
+        bool last;
+        const unsigned key = uniform ? l[0] : 0x100u + (unsigned)lane;  // mixed quads: a run of their own
+        const unsigned long long v = run_sum(key, uniform ? qs : 0ull, last);
+        if (last && key < kBorderCells && v) atomicAdd(&sm.bin[key], v);
     }
-    tile_prefix(sm, a);
-    if (t < ne) {
-        float2 value = fixed64_to_ff(sm.S[span & 0xFFFFu] - sm.S[span >> 16], F);
-        if (poisoned_exit) value.x = __int_as_float(0x7fc00000);
-        P[epos] = value;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) tile_sum += __shfl_xor_sync(0xffffffffu, tile_sum, o);
+    if (lane == 0) sm.warp_tot[warp] = tile_sum;
+    __syncthreads();
+    const int32_t e0 = __ldg(exit_base + tile), ne = __ldg(exit_base + tile + 1) - e0;
+    if (t < ne) {  // a tile has at most 252 exits (its border cells)
+        float2 value = fixed64_to_ff(sm.bin[t], F);
+        if ((sm.poisoned[t >> 5] >> (t & 31)) & 1u) value = make_float2(__int_as_float(0x7fc00000), 0.0f);
+        P[__ldg(exit_pos + e0 + t)] = value;
     }
-    if (t == kTileThreads - 1) {  // a[17] of the last thread: the tile's fixed-point total, exact
-        const double units = ldexp(((double)a[kRun - 1] + 8192.0) * (1.0 + 1e-12), 16 - F) + 64.0;
+    if (t == 0) {
+        unsigned long long total = 0;
+#pragma unroll
+        for (int w = 0; w < kTileThreads / 32; ++w) total += sm.warp_tot[w];
+        const double units = ldexp(((double)total + 8192.0) * (1.0 + 1e-12), 16 - F) + 64.0;
         block_total[tile] = units < 1.0e18 ? (unsigned long long)units : ~0ull;
+        stat[tile] = TileStat{bound, mn, dirty ? 1u : 0u, 0u};
     }
 }
 
@@ -1132,13 +1061,73 @@ __global__ void k_exit_sums(int64_t n, const uint32_t* __restrict__ pos, const u
     A[y] = from_u128(a);
 }
 
-// Pass 3: the result of every cell: the accu of its in-tile subtree, where the entry node of each border
-// cell carries the exact subtree sums of the exits draining into it (rounded to float), in one
-// fixed-point scan per tile.  A tile that cannot be scaled sets the fallback flag total[1]: the walk
-// engine redoes the call.
+// Inclusive prefix sums (modulo 2^64) of the thread runs a[0..15] over the whole tile, written to S by
+// scan slot.  Ends with a block barrier.
+__device__ __forceinline__ void tile_prefix(TileCallSmem& sm, unsigned long long (&a)[kRun])
+{
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+#pragma unroll
+    for (int j = 1; j < kRun; ++j) a[j] += a[j - 1];
+    unsigned long long x = a[kRun - 1];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sm.warp_tot[warp] = x;
+    __syncthreads();
+    unsigned long long off = x - a[kRun - 1];
+#pragma unroll
+    for (int w = 0; w < kTileThreads / 32; ++w) off += w < warp ? sm.warp_tot[w] : 0ull;
+    ulonglong2* run = reinterpret_cast<ulonglong2*>(sm.S + kRunSlots * t);  // 144-byte runs
+#pragma unroll
+    for (int i = 0; i < kRunWords; ++i) run[i] = make_ulonglong2(a[2 * i] + off, a[2 * i + 1] + off);
+    if (t == 0) sm.S[kZeroSlot] = 0ull;
+    __syncthreads();
+}
+
+// Poison counts (slow path): inclusive prefix counts over the post-order of the flagged terms, written as
+// 32-bit counts by scan slot over S (free until the value scan).  Ends with a block barrier.
+__device__ __forceinline__ void poison_counts(TileCallSmem& sm, unsigned bad)
+{
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    unsigned run = __popc(bad);
+    unsigned x = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sm.warp_tot[warp] = x;
+    __syncthreads();
+    unsigned off = x - run;
+    for (int w = 0; w < warp; ++w) off += (unsigned)sm.warp_tot[w];
+    unsigned* C = reinterpret_cast<unsigned*>(sm.S);
+    unsigned c = off;
+#pragma unroll
+    for (int j = 0; j < kRun; ++j) {
+        c += (bad >> j) & 1u;
+        C[kRunSlots * t + j] = c;
+    }
+    if (t == 0) C[kZeroSlot] = 0u;
+    __syncthreads();
+}
+
+// Pass 3: the result of every cell: the accu of its in-tile subtree, where each border cell's material
+// carries what enters it from other tiles (the exact subtree sums of the exits draining into it, rounded
+// to float once, added to the cell's material in float), in one fixed-point scan per tile.
+//
+// The scale F comes from pass 1's bound on the tile's material plus the float sum of what enters, so no
+// block reduction of the terms is needed; a tile whose smallest positive term would get fewer than 19
+// bits sets the fallback flag total[1], and the walk engine redoes the call.  Fast path (no NaN or
+// negative term and nothing NaN entering): gather, convert, scan, and for every cell with in-tile upstream
+// cells its prefix minus the prefix before its subtree; a cell without in-tile upstream cells keeps its
+// material (plus what enters) in M, which is its result.  Slow path: NaN / negative terms count as 0 and
+// are counted along the post-order; a cell whose subtree holds one is NaN.
 __global__ void __launch_bounds__(kTileThreads, 4)
     k_tile_accu(TileGeom g, const float* __restrict__ ext, float ext_s, bool vec, float* __restrict__ out,
-                TileForest f, const uint4* __restrict__ A, unsigned long long* total)
+                TileForest f, const uint4* __restrict__ A, const TileStat* __restrict__ stat,
+                unsigned long long* total)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TileCallSmem& sm = *reinterpret_cast<TileCallSmem*>(smem_raw);
@@ -1146,22 +1135,23 @@ __global__ void __launch_bounds__(kTileThreads, 4)
     const int Fg = fixed_point_bits(total[0]);
     const int64_t tr = blockIdx.y, tc = blockIdx.x;  // grid = (tile columns, tile rows)
     const int64_t tile = tr * g.tcols + tc;
-    const int t = threadIdx.x;
-    const uint16_t* pv_table = f.prev_at + tile * kRunPositions;
-    if (t < kRunPositions * 2 / 128)  // the run tables read at the end: into L2 now
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(reinterpret_cast<const char*>(pv_table) + 128 * t));
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     float4 xm[4];
     load_material(xm, ext, ext_s, g, tr, tc, vec);
-    uint32_t ca[kRunWords];
+    uint32_t ca[kRunWords], pv[kRunWords];
     load_run(f.cell_at + tile * kRunPositions, ca);
+    load_run(f.prev_at + tile * kRunPositions, pv);
+    const TileStat st = stat[tile];
     // what enters through border cell t: the exact subtree sums of the exits draining into it, as float
     // (NaN when one of them is no-data)
     float entering = 0.0f;
+    int ecell = -1;
     if (t < kBorderCells) {
         const unsigned in_mask = __ldg(f.border_in + tile * kBorderCells + t);
         if (in_mask) {
             int rin, cin;
             border_cell(t, rin, cin);
+            ecell = rin * kTile + cin;
             u128 src = 0;
             unsigned m = in_mask;
             while (m) {
@@ -1174,34 +1164,64 @@ __global__ void __launch_bounds__(kTileThreads, 4)
             entering = (src >> 96) ? __int_as_float(0x7fc00000) : fixed128_to_float(src & kValueMask, Fg);
         }
     }
-    store_material(sm, xm);
-    sm.M[kEntryBase + t] = entering;
+    // over what enters: NaN anywhere, the float sum, and the smallest positive bits minus one
+    const bool enan = isnan(entering);
+    const float eclean = enan ? 0.0f : entering;
+    float esum = eclean;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) esum += __shfl_xor_sync(0xffffffffu, esum, o);
+    const unsigned emn = __reduce_min_sync(0xffffffffu, __float_as_uint(eclean) - 1u);
+    const unsigned enan_any = __any_sync(0xffffffffu, enan);
+    if (lane == 0) {
+        sm.warp_sum[warp] = esum;
+        sm.red[0][warp] = emn;
+        sm.red[1][warp] = enan_any;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) *reinterpret_cast<float4*>(sm.M + quad_cell(j)) = xm[j];
     __syncthreads();
-    float x[kRun], sum;
-    unsigned mx, mn;
-    gather_run(sm, ca, x, mx, mn, sum);
-    tile_reduce(sm, mx, mn, sum);
-    unsigned poisoned = 0;  // bit j: the subtree of run entry j holds NaN / negative material or a no-data exit
-    uint32_t pv[kRunWords];
-    const bool clean = mx <= 0x7F800000u;  // uniform: no NaN, negative or -0 term in the tile
+    if (ecell >= 0) sm.M[ecell] += entering;
+    float in_total = 0.0f;
+    unsigned mn = st.min_bits, nan_in = 0;
+#pragma unroll
+    for (int w = 0; w < kTileThreads / 32; ++w) {  // the same order in every thread
+        in_total += sm.warp_sum[w];
+        mn = min(mn, sm.red[0][w]);
+        nan_in |= sm.red[1][w];
+    }
+    const float bound = (st.bound + in_total) * 1.0009765625f;
+    const int F = tile_scale(bound);
+    if (!(bound < 1.0e38f) || (mn != 0xFFFFFFFFu && __uint_as_float(mn + 1u) * pow2f(F) < kMinQuantum)) {
+        if (t == 0) total[1] = 1ull;  // the walk engine redoes the call
+        return;                       // uniform
+    }
+    const bool exact = mn == 0xFFFFFFFFu || __uint_as_float(mn + 1u) * pow2f(F) >= 8388608.0f;
+    const bool clean = !st.bad && !nan_in;  // uniform
+    __syncthreads();  // M holds what enters
+    float x[kRun];
+#pragma unroll
+    for (int j = 0; j < kRun; ++j) {
+        const unsigned w = run_at(ca, j);
+        const float v = sm.M[w & kIndexMask];
+        x[j] = (w & kNoValue) ? 0.0f : v;
+    }
+    unsigned poisoned = 0;  // bit j: the subtree of run entry j holds a NaN or negative term
     if (!clean) {
-        const unsigned bad = clean_run(ca, x, mx, mn, sum);
-        __syncthreads();  // red is reused
-        tile_reduce(sm, mx, mn, sum);
+        unsigned bad = 0;
+#pragma unroll
+        for (int j = 0; j < kRun; ++j) {
+            if (!(x[j] >= 0.0f)) bad |= 1u << j;
+            x[j] = x[j] >= 0.0f ? fabsf(x[j]) : 0.0f;  // fabsf: -0 counts as 0
+        }
         poison_counts(sm, bad);
-        load_run(pv_table, pv);
+        const unsigned* C = reinterpret_cast<const unsigned*>(sm.S);
 #pragma unroll
         for (int j = 0; j < kRun; ++j)
-            if (count_at(sm, kRun * t + j) != count_at(sm, (int)(run_at(pv, j) & kSlotMask))) poisoned |= 1u << j;
+            if (C[kRunSlots * t + j] != C[run_at(pv, j) & kSlotMask]) poisoned |= 1u << j;
         __syncthreads();  // S and warp_tot are free for the value scan
     }
-    int F;
-    if (tile_fixed_scale(mx, mn, sum, F)) {
-        if (t == 0) total[1] = 1ull;  // the walk engine redoes the call
-        return;
-    }
     unsigned long long a[kRun];
-    if (mn == 0xFFFFFFFFu || __uint_as_float(mn + 1u) * pow2f(F) >= 8388608.0f) {  // every term exact
+    if (exact) {
 #pragma unroll
         for (int j = 0; j < kRun; ++j) a[j] = float_to_fixed64_exact(x[j], F);
     } else {
@@ -1209,12 +1229,11 @@ __global__ void __launch_bounds__(kTileThreads, 4)
         for (int j = 0; j < kRun; ++j) a[j] = float_to_fixed64(x[j], F);
     }
     tile_prefix(sm, a);
-    load_run(pv_table, pv);
-    // results by position, put in cell order into M (its material was last read by the gather); a cell
-    // without in-tile upstream cells keeps its material there, which is its result
+    // results by position, put in cell order into M; a cell without in-tile upstream cells keeps its
+    // material (plus what enters) there on the fast path, which is its result
     const float nan = __int_as_float(0x7fc00000);
     const float unscale = pow2f(-F);
-    const ulonglong2* own = reinterpret_cast<const ulonglong2*>(sm.S + kRun * t);
+    const ulonglong2* own = reinterpret_cast<const ulonglong2*>(sm.S + kRunSlots * t);
 #pragma unroll
     for (int i = 0; i < kRunWords; ++i) {
         const ulonglong2 s2 = own[i];
@@ -1222,15 +1241,15 @@ __global__ void __launch_bounds__(kTileThreads, 4)
         for (int h = 0; h < 2; ++h) {
             const int j = 2 * i + h;
             const unsigned w = run_at(ca, j), p = run_at(pv, j);
-            const bool keep = (p & kPrevRidge) && clean && !(w & kNoValue);  // result already in M
-            const bool write = !(w & kNoOutput) && !keep;
-            const unsigned long long before = write ? sm.S[p & kSlotMask] : 0ull;
-            const unsigned long long v = (h ? s2.y : s2.x) - before;  // < 2^62
+            const bool none = (w & kNoValue) || ((poisoned >> j) & 1u);
+            const bool write = none || !clean || !(p & kPrevRidge);
+            if (!write) continue;
+            const unsigned long long v = (h ? s2.y : s2.x) - sm.S[p & kSlotMask];  // < 2^62
             // two 32-bit conversions, each rounded to nearest, and one fused rounding of their sum: within
             // about one unit in the last place, and exact when v has at most 24 significant bits
             const float r = __fmaf_rn(__uint2float_rn((unsigned)(v >> 32)), 4294967296.0f,
                                       __uint2float_rn((unsigned)v)) * unscale;
-            if (write) sm.M[w & kIndexMask] = ((w & kNoValue) || ((poisoned >> j) & 1u)) ? nan : r;
+            sm.M[w & kIndexMask] = none ? nan : r;
         }
     }
     __syncthreads();
@@ -1362,13 +1381,13 @@ int tile_core_build(TopologyCore* core, cudaStream_t stream)
     // per-tile flow forests in post-order
     TRY(cudaMalloc(&tc->cell_at, nt * kRunPositions * sizeof(uint16_t)), "tile forest");
     TRY(cudaMalloc(&tc->prev_at, nt * kRunPositions * sizeof(uint16_t)), "tile forest");
-    TRY(cudaMalloc(&tc->exit_span, std::max<int64_t>(E, 1) * sizeof(uint32_t)), "exit span");
+    TRY(cudaMalloc(&tc->label, nt * kTileCells), "tile labels");
     TRY(cudaMalloc(&tc->border_in, nt * kBorderCells), "tile border masks");
     TRY(cudaFuncSetAttribute(k_tile_forest, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TileSmem)),
         "tile forest");
     k_tile_forest<<<dim3((unsigned)g.tcols, (unsigned)g.trows), kTileThreads, sizeof(TileSmem), stream>>>(
-        core->fd, g, tc->exit_base, tc->exit_local, tc->cell_at, tc->prev_at, tc->exit_span, tc->border_in, flag);
-    tc->bytes += nt * kRunPositions * 4 + E * 4 + nt * kBorderCells;
+        core->fd, g, tc->exit_base, tc->exit_local, tc->cell_at, tc->prev_at, tc->label, tc->border_in, flag);
+    tc->bytes += nt * kRunPositions * 4 + nt * kTileCells + nt * kBorderCells;
     TRY(cudaGetLastError(), "tile build");
     TRY(cudaMemcpyAsync(&herr, flag, sizeof(int), cudaMemcpyDeviceToHost, stream), "tile flag");
     TRY(cudaStreamSynchronize(stream), "tile build");
@@ -1426,7 +1445,7 @@ void tile_core_free(TileCore* tc)
     cudaFree(tc->halo_exit);
     cudaFree(tc->cell_at);
     cudaFree(tc->prev_at);
-    cudaFree(tc->exit_span);
+    cudaFree(tc->label);
     cudaFree(tc->border_in);
     delete tc;
 }
@@ -1443,7 +1462,8 @@ int tile_scratch_alloc(const TileCore* tc, TileScratch* s)
     if ((rc = cuda_status(cudaMalloc(&s->total, 2 * sizeof(unsigned long long)), "tile scratch"))) return rc;
     if ((rc = cuda_status(cudaMalloc(&s->block_total, tc->ntiles * sizeof(unsigned long long)), "tile scratch")))
         return rc;
-    s->bytes = E * (8 + 16 + 16) + nb * 16 + 16 + tc->ntiles * 8;
+    if ((rc = cuda_status(cudaMalloc(&s->stat, tc->ntiles * sizeof(TileStat)), "tile scratch"))) return rc;
+    s->bytes = E * (8 + 16 + 16) + nb * 16 + 16 + tc->ntiles * (8 + sizeof(TileStat));
     return LUE_GPU_OK;
 }
 
@@ -1455,6 +1475,7 @@ void tile_scratch_free(TileScratch* s)
     cudaFree(s->block_sums);
     cudaFree(s->total);
     cudaFree(s->block_total);
+    cudaFree(s->stat);
     *s = TileScratch{};
 }
 
@@ -1466,20 +1487,17 @@ int tile_accu_f32(const TopologyCore* core, TileScratch* s, const float* ext, fl
 {
     const TileCore* tc = core->tiles;
     TileGeom g{core->rows, core->cols, tc->trows, tc->tcols};
-    const TileForest f{tc->cell_at, tc->prev_at, tc->border_in, tc->halo_exit};
+    const TileForest f{tc->cell_at, tc->prev_at, tc->label, tc->border_in, tc->halo_exit};
     // rows move as float4 when the columns are a multiple of 4 and the arrays 16-byte aligned
     const bool cols4 = (core->cols & 3) == 0;
     const bool vec_in = cols4 && (!ext || (reinterpret_cast<uintptr_t>(ext) & 15) == 0);
     const bool vec_out = cols4 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
-    static const bool smem_ok = cudaFuncSetAttribute(k_tile_exits, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     (int)sizeof(TileCallSmem)) == cudaSuccess &&
-                                cudaFuncSetAttribute(k_tile_accu, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    static const bool smem_ok = cudaFuncSetAttribute(k_tile_accu, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                      (int)sizeof(TileCallSmem)) == cudaSuccess;
     if (!smem_ok) return fail(LUE_GPU_ECUDA, "accu_f32 (tiles): shared memory attribute");
     const dim3 tile_grid((unsigned)tc->tcols, (unsigned)tc->trows);
-    k_tile_exits<<<tile_grid, kTileThreads, sizeof(TileCallSmem), stream>>>(g, ext, ext_s, vec_in, f, tc->exit_base,
-                                                                    tc->exit_span, tc->exit_pos, s->P,
-                                                                    s->block_total);
+    k_tile_exit_sums<<<tile_grid, kTileThreads, 0, stream>>>(g, ext, ext_s, vec_in, tc->label, tc->exit_base,
+                                                             tc->exit_pos, s->P, s->block_total, s->stat);
     k_total<<<1, 1024, 0, stream>>>(s->block_total, tc->ntiles, s->total);
     count_launches(2);
     const int64_t E = tc->nexit;
@@ -1491,8 +1509,8 @@ int tile_accu_f32(const TopologyCore* core, TileScratch* s, const float* ext, fl
         k_exit_sums<<<blocks_for(E, 256), 256, 0, stream>>>(E, tc->exit_pos, tc->exit_start, s->S, s->A, s->total);
         count_launches(4);
     }
-    k_tile_accu<<<tile_grid, kTileThreads, sizeof(TileCallSmem), stream>>>(g, ext, ext_s, vec_in && vec_out, out, f, s->A,
-                                                                   s->total);
+    k_tile_accu<<<tile_grid, kTileThreads, sizeof(TileCallSmem), stream>>>(g, ext, ext_s, vec_in && vec_out, out, f,
+                                                                           s->A, s->stat, s->total);
     count_launches(1);
     return cuda_status(cudaGetLastError(), "accu_f32 (tiles)");
 }

@@ -3,20 +3,21 @@
 // The raster is cut into 64 x 64 tiles (the GPU's partitions).  Inside a tile, the flow paths form a
 // forest; once, when the topology is built, it is laid out in post-order, so that the accu of a cell
 // (the material of its in-tile subtree) is the difference of two prefix sums of the material taken in
-// that order.  Per call:
-//   1. k_tile_exits: one CTA per tile gathers its material into post-order (each thread a run of 18
-//      positions), takes one exact 64-bit fixed-point prefix sum, and writes the local value of each
-//      exit cell (a cell whose flow leaves its tile but not the array) to P, in the post-order of the
-//      exit forest.
+// that order.  Each cell also gets a label: the exit of its tile that its in-tile path reaches (an exit
+// is a cell whose flow leaves its tile but not the array).  Per call:
+//   1. k_tile_exit_sums: one CTA per tile sums the material of each exit's in-tile catchment (the cells
+//      with that exit's label) in exact 64-bit fixed point, and writes each exit's local value to P, in
+//      the post-order of the exit forest, with per-tile statistics of the material.  It reads 5 bytes
+//      per cell: the material and the label.
 //   2. Exit forest: exit y's parent is the exit reached by following the flow from y's downstream
 //      cell through that cell's tile.  The final value of exit y is the sum of the local values over
 //      y's subtree of this forest, so an inclusive prefix sum over P in post-order gives every subtree
 //      sum as a difference of two prefix sums.  The sums are exact: 128-bit fixed point (96 value bits,
 //      32 bits counting no-data exits), so summation order cannot change the result.
-//   3. k_tile_accu: one CTA per tile puts, at each border cell's entry node, the subtree sums of the
-//      exits draining into it, takes the same prefix sum again and writes every cell's result.
-// Both tile passes read the material once (coalesced float4 rows) and 2-4 bytes of forest per cell; the
-// prefix sums stay in registers and shared memory.
+//   3. k_tile_accu: one CTA per tile adds to each border cell what enters it from other tiles (the
+//      exact subtree sums of the exits draining into it, rounded to float), takes one fixed-point prefix
+//      sum over the tile's post-order and writes every cell's result.  It reads the material, 4 bytes
+//      of post-order tables per cell and writes the result: 12 bytes per cell.
 // Reference counterpart: the per-partition intra/inter split of ALG/definition/accumulating_router.hpp
 // (intra :789-899, inter :902-1209), with the inter-partition channel hand-off replaced by the exit-forest
 // prefix sum.
@@ -33,33 +34,38 @@ constexpr int kHaloSlots = 4 * kTile + 4; // N row, S row, W column, E column, N
 constexpr int kTileThreads = 256;
 constexpr int kBorderCells = 4 * kTile - 4;  // cells on the tile's border ring
 
-// Per-tile post-order with virtual entry nodes.  The post-order of a tile's flow forest gets one extra
-// node per border cell that receives inflow from outside the tile (its "entry", placed first among that
-// cell's children), so that what enters the tile is just one more term of the prefix sum.  Cells
-// (4096) and entries (at most 252) fill positions 0 .. 4347; positions up to kRunPositions are padding.
-// Scan thread t owns the run of positions 18 t .. 18 t + 17; scan slot = position, and slot kZeroSlot
-// holds 0 (the prefix before position 0).  Per-position tables are stored word-transposed: the 16-bit
-// entries of positions 18 t + 2 i and 18 t + 2 i + 1 form word i of thread t, at word index 256 i + t,
-// so that each of a thread's nine table loads is one coalesced 128-byte line per warp.
-constexpr int kRun = 18;
+// Per-tile post-order: valid cells take positions 0 .. nvalid - 1, cells with a no-data flow direction
+// (or outside the array) the positions after them.  Scan thread t owns the run of positions 16 t ..
+// 16 t + 15.  Prefix sums are kept in shared memory by scan slot: position p has slot p + 2 (p / 16),
+// so that each thread's run is 144 bytes (16-byte stores of a quarter-warp fall on distinct banks);
+// slot kZeroSlot holds 0 (the prefix before position 0).  Per-position tables are stored
+// word-transposed: the 16-bit entries of positions 16 t + 2 i and 16 t + 2 i + 1 form word i of thread
+// t, at word index 256 i + t, so that each of a thread's eight table loads is one coalesced 128-byte
+// line per warp.
+constexpr int kRun = 16;
 constexpr int kRunWords = kRun / 2;
-constexpr int kRunPositions = kRun * kTileThreads;  // 4608
-constexpr int kZeroSlot = kRunPositions;
-constexpr int kScanSlotCount = kRunPositions + 2;
-constexpr int kEntryBase = kTileCells;             // material index of entry b: kEntryBase + b
+constexpr int kRunPositions = kRun * kTileThreads;  // 4096: every cell of the tile, nothing else
+constexpr int kRunSlots = kRun + 2;                 // scan slots per thread run (two pad slots)
+constexpr int kZeroSlot = kRunSlots * kTileThreads; // 4608
+constexpr int kScanSlotCount = kZeroSlot + 2;
 __host__ __device__ __forceinline__ int run_table_index(int p)
 {
     const int t = p / kRun, j = p - kRun * t;
     return ((j >> 1) * kTileThreads + t) * 2 + (j & 1);
 }
+__host__ __device__ __forceinline__ int scan_slot(int p) { return p + 2 * (p / kRun); }
 
-// cell_at entries: the material index (a cell 0..4095, or kEntryBase + border index) and two flags.
-constexpr unsigned kIndexMask = 0x1FFFu;
-constexpr unsigned kNoOutput = 0x4000u;  // an entry or padding: no result
-constexpr unsigned kNoValue = 0x8000u;   // no-data flow direction, outside the array, or padding: term 0
+// cell_at entries: the cell (0..4095) and a flag.
+constexpr unsigned kIndexMask = 0x0FFFu;
+constexpr unsigned kNoValue = 0x8000u;   // no-data flow direction or outside the array: result NaN / none
 // prev_at entries: the scan slot just before the node's subtree, and a flag.
 constexpr unsigned kSlotMask = 0x1FFFu;
 constexpr unsigned kPrevRidge = 0x8000u;  // the subtree is the cell alone
+
+// Exit labels (per cell, tile-major): the index (0 .. 251) among its tile's exits of the exit its
+// in-tile flow path reaches, or one of these.
+constexpr uint8_t kLabelNone = 0xFE;    // valid cell draining to a sink, the array edge or a no-data cell
+constexpr uint8_t kLabelNoData = 0xFF;  // no-data flow direction or outside the array
 
 struct TileCore {
     int64_t trows = 0, tcols = 0, ntiles = 0;  // tile grid
@@ -72,13 +78,20 @@ struct TileCore {
     int32_t* halo_exit = nullptr;              // [ntiles * kHaloSlots] exit id of the halo cell draining into
                                                // the tile, or -1
     // Per-tile flow forests in post-order (built once from the flow direction), by post-order position:
-    uint16_t* cell_at = nullptr;               // [ntiles * kRunPositions] material index at the position
-                                               // (| kNoOutput, kNoValue); no-data cells after the valid ones
+    uint16_t* cell_at = nullptr;               // [ntiles * kRunPositions] cell at the position (| kNoValue)
     uint16_t* prev_at = nullptr;               // [ntiles * kRunPositions] scan slot before the subtree
                                                // (kZeroSlot for a subtree at position 0) | kPrevRidge
-    uint32_t* exit_span = nullptr;             // [nexit] scan slots of each exit cell: own | before << 16
+    uint8_t* label = nullptr;                  // [ntiles * kTileCells] exit label of each cell (tile-major)
     uint8_t* border_in = nullptr;              // [ntiles * kBorderCells] per border cell: outside neighbours draining in
     int64_t bytes = 0;
+};
+
+// What pass 1 learns about a tile's material (valid cells only), for pass 3.
+struct TileStat {
+    float bound;          // upper bound of the tile's material total
+    unsigned min_bits;    // bits of the smallest positive term minus one (0xFFFFFFFF: none)
+    unsigned bad;         // a NaN or negative term
+    unsigned pad;
 };
 
 struct TileScratch {
@@ -88,6 +101,7 @@ struct TileScratch {
     uint4* block_sums = nullptr;               // [scan blocks]
     unsigned long long* total = nullptr;       // [2] material total bound (2^-16 units), fallback flag
     unsigned long long* block_total = nullptr; // [ntiles] per-tile bounds
+    TileStat* stat = nullptr;                  // [ntiles]
     int64_t bytes = 0;
 };
 
