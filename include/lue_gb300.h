@@ -8,6 +8,9 @@
  *   ----------------------------------------------------------   -----------------------------------
  *   inflow_count<uint8>(policies, fd)  inflow_count.hpp:29-42      lue_gpu_inflow_count_u8
  *   value_policies::accu_info(fd)      value_policies/accu_info.hpp:18-26   lue_gpu_accu_info_u8
+ *   value_policies::partial_accu(fd, inflow, nr_steps)
+ *                                      value_policies/partial_accu.hpp:17-28
+ *                                                                  lue_gpu_partial_accu_f32 / _f64
  *   value_policies::accu(fd, inflow)   value_policies/accu.hpp:33-55   lue_gpu_accu_f32 / _f64
  *   value_policies::accu_threshold(fd, inflow, threshold)
  *                                      value_policies/accu_threshold.hpp:33-90
@@ -162,6 +165,19 @@ int lue_gpu_inflow_count_u8(const lue_gpu_topology* topology, int value_policies
  * the reference, which depends on the order its channels deliver; here it is classed as if material from
  * another partition arrived last (14 or 15). */
 int lue_gpu_accu_info_u8(lue_gpu_topology* topology, uint8_t* cell_class, void* stream);
+
+/* partial_accu(fd, inflow, nr_steps) (value_policies/partial_accu.hpp:17-28, definition/partial_accu.hpp:
+ * 15-287): per cell, the number of the stream of the reference's partitioned walk that reached it last
+ * (ridge cells: their rank among their partition's ridge cells in row-major order; partition input cells:
+ * the largest arriving value plus one), NaN above nr_steps and for a no-data flow direction, for the
+ * topology's partition shape.  (The reference takes an inflow scalar that it does not use.)  Where the
+ * reference's result depends on the order its channels deliver (cells below a meeting of several walks
+ * that start at partition input cells of one partition), the value here is one of the possible ones and
+ * order_dependent (optional, uint8, may be NULL) is 1; elsewhere it is 0. */
+int lue_gpu_partial_accu_f32(lue_gpu_topology* topology, int64_t nr_steps, float* out, uint8_t* order_dependent,
+                             void* stream);
+int lue_gpu_partial_accu_f64(lue_gpu_topology* topology, int64_t nr_steps, double* out, uint8_t* order_dependent,
+                             void* stream);
 
 /* Downstream level of each cell: 0 for cells without inflow, else 1 + the largest level upstream;
  * -1 for no-data and for cells on or below a cycle.  No reference counterpart: it exposes the

@@ -35,14 +35,6 @@ enum : uint8_t {
     kSink = 17
 };
 
-struct PartitionGeom {
-    int64_t rows, cols, prow, pcol, nprow, npcol;
-    // partition row / column of a cell: the last partition of a row or column absorbs the remainder
-    // (source/framework/core/include/lue/framework/core/domain_decomposition.hpp:90-175)
-    __device__ __forceinline__ int64_t prow_of(int64_t r) const { return min(r / prow, nprow - 1); }
-    __device__ __forceinline__ int64_t pcol_of(int64_t c) const { return min(c / pcol, npcol - 1); }
-};
-
 // dep[c] = 1 when a partition input cell of c's partition lies upstream of c within the partition (c
 // itself included): c is finished only after material arrives from another partition.
 struct DependVisitor {

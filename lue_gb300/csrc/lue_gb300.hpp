@@ -320,6 +320,24 @@ inline PartitionedArray<CellClass> accu_info(const PartitionedArray<std::uint8_t
     return out;
 }
 
+// partial_accu(flow_direction, inflow, nr_steps) (ALG/value_policies/partial_accu.hpp:17-28): per cell the
+// number of the walk's stream that reached it last, NaN above nr_steps, for the array's partition shape.
+// The inflow scalar only picks the element type, as in the reference.
+template <typename F>
+PartitionedArray<F> partial_accu(const PartitionedArray<std::uint8_t>& flow_direction, const Scalar<F>& inflow,
+                                 std::int64_t nr_steps, cudaStream_t stream = nullptr)
+{
+    static_assert(std::is_same_v<F, float> || std::is_same_v<F, double>, "partial_accu: float or double");
+    (void)inflow;
+    PartitionedArray<F> out(flow_direction.shape(), flow_direction.partition_shape());
+    lue_gpu_topology* t = flow_direction.topology(stream).handle();
+    if constexpr (std::is_same_v<F, float>)
+        check(lue_gpu_partial_accu_f32(t, nr_steps, out.data(), nullptr, stream), "partial_accu");
+    else
+        check(lue_gpu_partial_accu_f64(t, nr_steps, out.data(), nullptr, stream), "partial_accu");
+    return out;
+}
+
 // accu(flow_direction, inflow): inflow is a PartitionedArray<F> or a Scalar<F>.
 template <typename F, typename Inflow>
 PartitionedArray<F> accu(const PartitionedArray<std::uint8_t>& flow_direction, const Inflow& inflow,

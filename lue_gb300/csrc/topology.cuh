@@ -61,6 +61,19 @@ namespace lue_gb300 {
 
 int allocate_scratch(lue_gpu_topology* t);
 
+// The reference's partitions of a raster: the last partition of a row or column absorbs the remainder
+// (source/framework/core/include/lue/framework/core/domain_decomposition.hpp:90-175).
+struct PartitionGeom {
+    int64_t rows, cols, prow, pcol, nprow, npcol;
+    __device__ __forceinline__ int64_t prow_of(int64_t r) const { return min(r / prow, nprow - 1); }
+    __device__ __forceinline__ int64_t pcol_of(int64_t c) const { return min(c / pcol, npcol - 1); }
+};
+inline PartitionGeom partition_geom(const TopologyCore* core)
+{
+    return PartitionGeom{core->rows, core->cols, core->prow, core->pcol, core->rows / core->prow,
+                         core->cols / core->pcol};
+}
+
 // accu (float32) on the tile engine; see tile_accu.cuh.
 int tile_accu_f32(const TopologyCore* core, TileScratch* s, const float* ext, float ext_s, float* out,
                   cudaStream_t stream);

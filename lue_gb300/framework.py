@@ -212,6 +212,25 @@ def accu_info(flow_direction):
     return PartitionedArray(out, flow_direction.partition_shape)
 
 
+def partial_accu(flow_direction, inflow, nr_steps, order_dependent=False):
+    """value_policies::partial_accu(flow_direction, inflow, nr_steps): per cell the number of the stream of
+    the partitioned walk that reached it last, NaN above nr_steps (float32 for a float or numpy.float32
+    inflow scalar, float64 for numpy.float64; the reference does not use the inflow's value).  With
+    order_dependent=True also returns a uint8 array that is 1 where the reference's result depends on
+    the order in which its inter-partition messages are delivered."""
+    if isinstance(inflow, PartitionedArray):
+        raise TypeError("partial_accu: inflow must be a scalar")
+    dtype = torch.float64 if isinstance(inflow, np.float64) else torch.float32
+    t = flow_direction.topology()
+    out = _empty(flow_direction, dtype)
+    od = _empty(flow_direction, torch.uint8) if order_dependent else None
+    fn = _lib.lib().lue_gpu_partial_accu_f64 if dtype == torch.float64 else _lib.lib().lue_gpu_partial_accu_f32
+    _lib.check(fn(t.handle, int(nr_steps), out.data_ptr(), None if od is None else od.data_ptr(),
+                  _stream(flow_direction.data)))
+    res = PartitionedArray(out, flow_direction.partition_shape)
+    return (res, PartitionedArray(od, flow_direction.partition_shape)) if order_dependent else res
+
+
 def downstream_level(flow_direction):
     t = flow_direction.topology()
     out = _empty(flow_direction, torch.int32)

@@ -622,3 +622,169 @@ int lue_oracle_accu_info(const uint8_t* fd, int64_t rows, int64_t cols, int64_t 
     free(orig);
     return 0;
 }
+
+/* ------------------------------------------------------------------------------------------------ */
+/* partial_accu                                                                                      */
+/* ------------------------------------------------------------------------------------------------ */
+
+/*
+ * partial_accu (ALG/definition/partial_accu.hpp:15-287, value policies ALG/value_policies/
+ * partial_accu.hpp): the router's event sequence (ALG/definition/accumulating_router.hpp:525-599 walk,
+ * :866-882 intra-partition ridge scan, :984-1010 inter-partition arrivals) with the PartialAccu cell
+ * accumulator's hooks, in double (the values are small integers):
+ *   enter_intra_partition_stream: the ridge's value is the partition's stream counter (:71-76);
+ *   leave_intra_partition_stream: the counter goes up by one (:79-83);
+ *   enter_inter_partition_stream: a value arriving from another partition: NaN wins, else the larger
+ *     of the cell's value and the arriving one; above nr_steps the cell becomes NaN (:86-109);
+ *   leave_inter_partition_stream: after the walk from a partition input cell its value goes up by one
+ *     unless it is NaN (:112-120);
+ *   leave_cell: the downstream cell takes the upstream value (it is not added), NaN wins; above
+ *     nr_steps the downstream cell becomes NaN (:129-165).
+ * Result buffers start at 0; a no-data flow direction gives NaN; nr_steps below 0 counts as 0.
+ * Inter-partition arrivals: order 0 takes them in one FIFO (one order HPX may deliver); order 1 takes
+ * the mail of the highest-numbered partition that has mail first (FIFO within a partition's mail),
+ * another valid order, used to find the cells whose value depends on the order.
+ */
+typedef struct {
+    int64_t idx;
+    double value;
+    int64_t part;
+} PartialMsg;
+
+typedef struct {
+    Grid g;
+    const uint8_t* fd;
+    int8_t* cnt;
+    double* out;
+    double nr_steps;
+    PartialMsg* msg;
+    int64_t nmsg, cap;
+} PartialRouter;
+
+static void partial_push(PartialRouter* R, int64_t j, double v)
+{
+    if (R->nmsg == R->cap) {
+        R->cap = R->cap ? 2 * R->cap : 64;
+        R->msg = (PartialMsg*)realloc(R->msg, (size_t)R->cap * sizeof(PartialMsg));
+    }
+    const int64_t r = j / R->g.cols, c = j % R->g.cols;
+    R->msg[R->nmsg].idx = j;
+    R->msg[R->nmsg].value = v;
+    R->msg[R->nmsg].part = part_of_row(&R->g, r) * R->g.npcol + part_of_col(&R->g, c);
+    R->nmsg++;
+}
+
+static void partial_walk(PartialRouter* R, int64_t r, int64_t c)
+{
+    const Grid* g = &R->g;
+    const int64_t cols = g->cols;
+    int64_t r0, r1, c0, c1;
+    part_rows(g, part_of_row(g, r), &r0, &r1);
+    part_cols(g, part_of_col(g, c), &c0, &c1);
+    for (;;) {
+        const int64_t i = r * cols + c;
+        int dr, dc;
+        d8_offset(R->fd[i], &dr, &dc);
+        if (dr == 0 && dc == 0) return; /* sink */
+        const int64_t rd = r + dr, cd = c + dc;
+        if (rd < r0 || rd >= r1 || cd < c0 || cd >= c1) {
+            if (rd >= 0 && rd < g->rows && cd >= 0 && cd < cols) partial_push(R, rd * cols + cd, R->out[i]);
+            return; /* partition output cell */
+        }
+        const int64_t j = rd * cols + cd;
+        if (!isnan(R->out[j])) R->out[j] = isnan(R->out[i]) ? (double)NAN : R->out[i]; /* leave_cell */
+        if (R->out[j] > R->nr_steps) R->out[j] = (double)NAN;
+        r = rd;
+        c = cd;
+        if (--R->cnt[j] > 0) return; /* confluence */
+    }
+}
+
+static void partial_arrive(PartialRouter* R, int64_t j, double v)
+{
+    double* o = &R->out[j];
+    if (!isnan(*o)) { /* enter_inter_partition_stream */
+        if (isnan(v)) *o = (double)NAN;
+        else *o = *o > v ? *o : v;
+        if (*o > R->nr_steps) *o = (double)NAN;
+    }
+    if (--R->cnt[j] == 0) {
+        partial_walk(R, j / R->g.cols, j % R->g.cols);
+        if (!isnan(*o)) *o += 1.0; /* leave_inter_partition_stream */
+    }
+}
+
+int lue_oracle_partial_accu(const uint8_t* fd, int64_t rows, int64_t cols, int64_t prow, int64_t pcol,
+                            int64_t nr_steps, int order, double* out)
+{
+    PartialRouter R;
+    memset(&R, 0, sizeof R);
+    if (grid_init(&R.g, rows, cols, prow, pcol)) return -1;
+    const int64_t n = rows * cols;
+    R.fd = fd;
+    R.out = out;
+    R.nr_steps = (double)(nr_steps > 0 ? nr_steps : 0);
+    R.cnt = (int8_t*)malloc((size_t)n);
+    int8_t* orig = (int8_t*)malloc((size_t)n);
+    if (!R.cnt || !orig) {
+        free(R.cnt);
+        free(orig);
+        return -2;
+    }
+    router_counts(&R.g, fd, 1, orig);
+    memcpy(R.cnt, orig, (size_t)n);
+    for (int64_t i = 0; i < n; ++i) out[i] = 0.0;
+    for (int64_t pr = 0; pr < R.g.nprow; ++pr) {
+        int64_t r0, r1;
+        part_rows(&R.g, pr, &r0, &r1);
+        for (int64_t pc = 0; pc < R.g.npcol; ++pc) {
+            int64_t c0, c1;
+            part_cols(&R.g, pc, &c0, &c1);
+            double step = 0.0; /* one cell accumulator, and so one counter, per partition */
+            for (int64_t r = r0; r < r1; ++r)
+                for (int64_t c = c0; c < c1; ++c) {
+                    const int64_t i = r * cols + c;
+                    if (fd[i] == U8_NO_DATA) {
+                        out[i] = (double)NAN;
+                    } else if (orig[i] == 0) {
+                        out[i] = step;
+                        partial_walk(&R, r, c);
+                        step += 1.0;
+                    }
+                }
+        }
+    }
+    if (order == 0) {
+        for (int64_t k = 0; k < R.nmsg; ++k) partial_arrive(&R, R.msg[k].idx, R.msg[k].value);
+    } else {
+        /* the mail of the highest-numbered partition with mail first; done[] marks delivered messages */
+        uint8_t* done = NULL;
+        int64_t delivered = 0;
+        for (;;) {
+            done = (uint8_t*)realloc(done, (size_t)(R.nmsg > 0 ? R.nmsg : 1));
+            for (int64_t k = delivered; k < R.nmsg; ++k) done[k] = 0;
+            delivered = R.nmsg;
+            int64_t best = -1;
+            for (int64_t k = 0; k < R.nmsg; ++k)
+                if (!done[k] && (best < 0 || R.msg[k].part > R.msg[best].part)) best = k;
+            if (best < 0) break;
+            const int64_t p = R.msg[best].part;
+            for (int64_t k = 0; k < R.nmsg; ++k) {
+                if (done[k] || R.msg[k].part != p) continue;
+                done[k] = 1;
+                const int64_t nbefore = R.nmsg;
+                partial_arrive(&R, R.msg[k].idx, R.msg[k].value);
+                if (R.nmsg != nbefore) {
+                    done = (uint8_t*)realloc(done, (size_t)R.nmsg);
+                    for (int64_t q = nbefore; q < R.nmsg; ++q) done[q] = 0;
+                    delivered = R.nmsg;
+                }
+            }
+        }
+        free(done);
+    }
+    free(R.msg);
+    free(R.cnt);
+    free(orig);
+    return 0;
+}

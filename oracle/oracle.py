@@ -54,6 +54,7 @@ def lib():
             getattr(L, f"lue_oracle_downstream_distance_{sfx}").argtypes = [p, i64, i64, real, p]
         L.lue_oracle_inflow_count.argtypes = [p, i64, i64, i64, i64, i32, p]
         L.lue_oracle_accu_info.argtypes = [p, i64, i64, i64, i64, p]
+        L.lue_oracle_partial_accu.argtypes = [p, i64, i64, i64, i64, i64, i32, p]
         L.lue_oracle_downstream_level.argtypes = [p, i64, i64, p]
         L.lue_oracle_d8_flow_direction.argtypes = [p, i64, i64, p]
         d = ctypes.c_double
@@ -113,6 +114,18 @@ def accu_info(fd, partition_shape=None):
     pr, pc = _pshape(fd, partition_shape)
     out = np.empty(fd.shape, np.uint8)
     _check(lib().lue_oracle_accu_info(fd.ctypes.data, fd.shape[0], fd.shape[1], pr, pc, out.ctypes.data))
+    return out
+
+
+def partial_accu(fd, nr_steps, partition_shape=None, order=0):
+    """partial_accu: the reference router's event sequence with the PartialAccu hooks (float64; NaN for
+    no-data).  order 0: inter-partition arrivals in one FIFO; order 1: the mail of the highest-numbered
+    partition first (another order HPX may deliver)."""
+    fd = _fd(fd)
+    pr, pc = _pshape(fd, partition_shape)
+    out = np.empty(fd.shape, np.float64)
+    _check(lib().lue_oracle_partial_accu(fd.ctypes.data, fd.shape[0], fd.shape[1], pr, pc, int(nr_steps), int(order),
+                                         out.ctypes.data))
     return out
 
 
