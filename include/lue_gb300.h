@@ -29,7 +29,7 @@
  *   value_policies::kinematic_wave(fd, current_outflow, inflow, alpha, beta,
  *                                  time_step_duration, channel_length)
  *                                      value_policies/kinematic_wave.hpp:43-91
- *                                                                  lue_gpu_kinematic_wave_f64
+ *                                                                  lue_gpu_kinematic_wave_f64 / _f32
  *                                                                  (+ _f64_f32in: float32 lateral
  *                                                                   inflow and alpha rasters)
  *
@@ -270,6 +270,14 @@ int lue_gpu_kinematic_wave_f64(lue_gpu_topology* topology, const double* current
                                const double* alpha, double alpha_scalar, const double* beta,
                                double beta_scalar, double time_step_duration, const double* channel_length,
                                double channel_length_scalar, double* outflow, void* stream);
+/* kinematic_wave for F = float (the reference's float instantiation, definition/kinematic_wave.hpp:
+ * 662-684): every raster float32, the Newton-Raphson solve of :145-254 in float with digits =
+ * int(24 * 0.6) = 14, FLT_MIN guess floor and bracket [0, FLT_MAX].  Same domain and no-data rules. */
+int lue_gpu_kinematic_wave_f32(lue_gpu_topology* topology, const float* current_outflow,
+                               float current_outflow_scalar, const float* inflow, float inflow_scalar,
+                               const float* alpha, float alpha_scalar, const float* beta, float beta_scalar,
+                               float time_step_duration, const float* channel_length, float channel_length_scalar,
+                               float* outflow, void* stream);
 /* Same with float32 lateral inflow and alpha rasters, promoted exactly to double per cell. */
 int lue_gpu_kinematic_wave_f64_f32in(lue_gpu_topology* topology, const double* current_outflow,
                                      double current_outflow_scalar, const float* inflow, double inflow_scalar,

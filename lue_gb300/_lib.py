@@ -73,6 +73,7 @@ def _declare(L):
         "lue_gpu_accu_fraction_f64": ([p, p, d, p, d, p, p, p], i32),
         "lue_gpu_kinematic_wave_f64": ([p, p, d, p, d, p, d, p, d, d, p, d, p, p], i32),
         "lue_gpu_kinematic_wave_f64_f32in": ([p, p, d, p, d, p, d, d, d, d, p, p], i32),
+        "lue_gpu_kinematic_wave_f32": ([p, p, f, p, f, p, f, p, f, f, p, f, p, p], i32),
         "lue_gpu_accu_f32_noalloc": ([p, i64, i64, i64, i64, p, f, p, p], i32),
         "lue_gpu_kinematic_wave_steps_f64_f32in": ([p, p, p, d, p, d, d, d, d, i32, p, p], i32),
         "lue_gpu_accu_capacity_f32": ([p, p, f, p, f, p, p, p], i32),

@@ -445,23 +445,29 @@ PartitionedArray<F> downstream(const PartitionedArray<std::uint8_t>& fd, const P
 }
 
 // kinematic_wave(flow_direction, current_outflow, inflow, alpha, beta, time_step_duration, channel_length):
-// one time step, double precision (the reference's double instantiation).
-template <typename Alpha, typename Beta, typename ChannelLength>
-PartitionedArray<double> kinematic_wave(const PartitionedArray<std::uint8_t>& fd,
-                                        const PartitionedArray<double>& current_outflow,
-                                        const PartitionedArray<double>& inflow, const Alpha& alpha, const Beta& beta,
-                                        Scalar<double> time_step_duration, const ChannelLength& channel_length,
-                                        cudaStream_t stream = nullptr)
+// one time step for F = float or double (the reference's two instantiations); alpha, beta and channel
+// length are PartitionedArray<F> or Scalar<F>.
+template <typename F, typename Alpha, typename Beta, typename ChannelLength>
+PartitionedArray<F> kinematic_wave(const PartitionedArray<std::uint8_t>& fd, const PartitionedArray<F>& current_outflow,
+                                   const PartitionedArray<F>& inflow, const Alpha& alpha, const Beta& beta,
+                                   Scalar<F> time_step_duration, const ChannelLength& channel_length,
+                                   cudaStream_t stream = nullptr)
 {
-    auto q = detail::arg<double>(fd, current_outflow);
-    auto l = detail::arg<double>(fd, inflow);
-    auto a = detail::arg<double>(fd, alpha);
-    auto b = detail::arg<double>(fd, beta);
-    auto d = detail::arg<double>(fd, channel_length);
-    PartitionedArray<double> out(fd.shape(), fd.partition_shape());
-    check(lue_gpu_kinematic_wave_f64(fd.topology(stream).handle(), q.ptr, q.value, l.ptr, l.value, a.ptr, a.value,
-                                     b.ptr, b.value, time_step_duration.value, d.ptr, d.value, out.data(), stream),
-          "kinematic_wave");
+    static_assert(std::is_same_v<F, float> || std::is_same_v<F, double>, "kinematic_wave: float or double");
+    auto q = detail::arg<F>(fd, current_outflow);
+    auto l = detail::arg<F>(fd, inflow);
+    auto a = detail::arg<F>(fd, alpha);
+    auto b = detail::arg<F>(fd, beta);
+    auto d = detail::arg<F>(fd, channel_length);
+    PartitionedArray<F> out(fd.shape(), fd.partition_shape());
+    if constexpr (std::is_same_v<F, float>)
+        check(lue_gpu_kinematic_wave_f32(fd.topology(stream).handle(), q.ptr, q.value, l.ptr, l.value, a.ptr, a.value,
+                                         b.ptr, b.value, time_step_duration.value, d.ptr, d.value, out.data(), stream),
+              "kinematic_wave");
+    else
+        check(lue_gpu_kinematic_wave_f64(fd.topology(stream).handle(), q.ptr, q.value, l.ptr, l.value, a.ptr, a.value,
+                                         b.ptr, b.value, time_step_duration.value, d.ptr, d.value, out.data(), stream),
+              "kinematic_wave");
     return out;
 }
 

@@ -241,6 +241,23 @@ extern "C" int lue_gpu_kinematic_wave_f64(lue_gpu_topology* t, const double* cur
     return run(t, v, outflow, (double*)nullptr, false, (cudaStream_t)stream, "kinematic_wave_f64");
 }
 
+extern "C" int lue_gpu_kinematic_wave_f32(lue_gpu_topology* t, const float* current_outflow,
+                                          float current_outflow_scalar, const float* inflow, float inflow_scalar,
+                                          const float* alpha, float alpha_scalar, const float* beta, float beta_scalar,
+                                          float time_step_duration, const float* channel_length,
+                                          float channel_length_scalar, float* outflow, void* stream)
+{
+    if (int rc = check_topology(t, "kinematic_wave_f32")) return rc;
+    if (!outflow) return fail(LUE_GPU_EINVAL, "kinematic_wave_f32: NULL output");
+    STAGE_OR_WALK(stage_kinematic_wave_f32(t, current_outflow, current_outflow_scalar, inflow, inflow_scalar, alpha,
+                                           alpha_scalar, beta, beta_scalar, time_step_duration, channel_length,
+                                           channel_length_scalar, outflow, (cudaStream_t)stream, &done));
+    RouteKW32 v{t->core->upmask, current_outflow, current_outflow_scalar, inflow, inflow_scalar, alpha, alpha_scalar,
+                beta, beta_scalar, time_step_duration, channel_length, channel_length_scalar, outflow,
+                t->core->cols};
+    return run(t, v, outflow, (float*)nullptr, false, (cudaStream_t)stream, "kinematic_wave_f32");
+}
+
 extern "C" int lue_gpu_kinematic_wave_f64_f32in(lue_gpu_topology* t, const double* current_outflow,
                                                 double current_outflow_scalar, const float* inflow,
                                                 double inflow_scalar, const float* alpha, double alpha_scalar,

@@ -325,4 +325,53 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// --- kinematic wave, float instantiation (every raster float32) --------------------------------------
+
+// The cell rule of kinematic_wave.hpp:416-456 with F = float: NaN outside the domain, else the new
+// discharge from the float sum of the upstream discharges (fixed neighbour order).
+__device__ __forceinline__ float rule_kw32(float up, bool nan, float qc, float q, float al, float be, float dt,
+                                           float len)
+{
+    if (nan || isnan(qc) || isnan(q) || isnan(al) || isnan(be) || isnan(dt) || isnan(len) ||
+        !(qc >= 0.0f && q >= 0.0f && len > 0.0f))
+        return qnan<float>();
+    return iterate_to_new_discharge_f32(up, qc, q, al, be, dt, len);
+}
+
+struct RouteKW32 {
+    const uint8_t* upmask;
+    const float* qcur;
+    float qcur_s;
+    const float* lateral;
+    float lateral_s;
+    const float* alpha;
+    float alpha_s;
+    const float* beta;
+    float beta_s;
+    float dt;
+    const float* dx;
+    float dx_s;
+    float* out;
+    int64_t cols;
+
+    __device__ void no_data(int64_t c) { out[c] = qnan<float>(); }
+
+    __device__ void enter(int64_t c)
+    {
+        unsigned m = __ldg(upmask + c);
+        float up = 0.0f;
+        bool nan = false;
+        while (m) {
+            const int k = __ffs(m) - 1;
+            m &= m - 1;
+            const float h = load_cg(out + c + nb_dr(k) * cols + nb_dc(k));
+            if (isnan(h)) nan = true;
+            else up += h;
+        }
+        out[c] = rule_kw32(up, nan, qcur ? __ldg(qcur + c) : qcur_s, lateral ? __ldg(lateral + c) : lateral_s,
+                           alpha ? __ldg(alpha + c) : alpha_s, beta ? __ldg(beta + c) : beta_s, dt,
+                           dx ? __ldg(dx + c) : dx_s);
+    }
+};
+
 }  // namespace lue_gb300

@@ -1146,6 +1146,44 @@ struct StageKW64 {
     __device__ void store(Cell&, int64_t) const {}
 };
 
+// kinematic wave, float instantiation (every raster float32): the float solve, float upstream sums in the
+// walk engine's neighbour order, so results equal the walk engine's bit for bit.
+struct StageKW32 {
+    RouteKW32 v;  // inputs and constants (its out is the result raster)
+    using Out = float;
+    __host__ __device__ float* out_raster() const { return v.out; }
+    __host__ __device__ float* rem_raster() const { return nullptr; }
+    struct Cell {
+        float qc, q, al, be, len;  // the cell's inputs, loaded with the stage
+    };
+    struct Acc {
+        float up;
+        bool nan;
+    };
+    __device__ void load(Cell& cl, int64_t c) const
+    {
+        cl.qc = v.qcur ? __ldg(v.qcur + c) : v.qcur_s;
+        cl.q = v.lateral ? __ldg(v.lateral + c) : v.lateral_s;
+        cl.al = v.alpha ? __ldg(v.alpha + c) : v.alpha_s;
+        cl.be = v.beta ? __ldg(v.beta + c) : v.beta_s;
+        cl.len = v.dx ? __ldg(v.dx + c) : v.dx_s;
+    }
+    __device__ Acc begin() const { return Acc{0.0f, false}; }
+    __device__ void add(Acc& acc, uint2 x) const
+    {
+        const float h = __uint_as_float(x.x);
+        if (isnan(h)) acc.nan = true;
+        else acc.up += h;
+    }
+    __device__ uint2 step(Cell& cl, const Acc& acc, int64_t c, int) const
+    {
+        const float o = rule_kw32(acc.up, acc.nan, cl.qc, cl.q, cl.al, cl.be, v.dt, cl.len);
+        v.out[c] = o;
+        return make_uint2(__float_as_uint(o), 0u);
+    }
+    __device__ void store(Cell&, int64_t) const {}
+};
+
 // kinematic wave, many steps, in float-float and the variable y = Q^(1/m) (kinematic_wave_ff.cuh).
 template <int P, int M>
 struct StageKWPoly {
@@ -1571,6 +1609,24 @@ int stage_kinematic_wave_f64(lue_gpu_topology* t, const double* qcur, double qcu
     StageKW64<double> rule{RouteKW<double>{t->core->upmask, qcur, qcur_s, lateral, lateral_s, alpha, alpha_s, beta,
                                            beta_s, dt, dx, dx_s, out, t->core->cols, br}};
     return stage_run(t, sc, rule, 1, stream, "kinematic_wave_f64 (stages)");
+}
+
+int stage_kinematic_wave_f32(lue_gpu_topology* t, const float* qcur, float qcur_s, const float* lateral,
+                             float lateral_s, const float* alpha, float alpha_s, const float* beta, float beta_s,
+                             float dt, const float* dx, float dx_s, float* out, cudaStream_t stream, bool* done)
+{
+    *done = false;
+    if (stage_engine_off()) return LUE_GPU_OK;
+    const StageCore* sc = nullptr;
+    if (int rc = stage_core_get(t, stream, &sc)) return rc;
+    if (!sc) return LUE_GPU_OK;
+    *done = true;
+    const int64_t n = t->core->n;
+    k_stage_no_data<float><<<grid_for(n, 256), 256, 0, stream>>>(t->core->fd, n, out, (float*)nullptr);
+    count_launches(1);
+    StageKW32 rule{RouteKW32{t->core->upmask, qcur, qcur_s, lateral, lateral_s, alpha, alpha_s, beta, beta_s, dt, dx,
+                             dx_s, out, t->core->cols}};
+    return stage_run(t, sc, rule, 1, stream, "kinematic_wave_f32 (stages)");
 }
 
 static ffloat ff_split(double v);

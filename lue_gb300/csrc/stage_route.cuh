@@ -97,6 +97,9 @@ int stage_kinematic_wave_f64(lue_gpu_topology* t, const double* qcur, double qcu
                              double lateral_s, const double* alpha, double alpha_s, const double* beta, double beta_s,
                              double dt, const double* dx, double dx_s, double* out, const BetaRational& br,
                              cudaStream_t stream, bool* done);
+int stage_kinematic_wave_f32(lue_gpu_topology* t, const float* qcur, float qcur_s, const float* lateral,
+                             float lateral_s, const float* alpha, float alpha_s, const float* beta, float beta_s,
+                             float dt, const float* dx, float dx_s, float* out, cudaStream_t stream, bool* done);
 int stage_kinematic_wave_f32in(lue_gpu_topology* t, const double* qcur, double qcur_s, const float* lateral,
                                double lateral_s, const float* alpha, double alpha_s, double beta, double dt, double dx,
                                double* out, const BetaRational& br, cudaStream_t stream, bool* done);

@@ -1,7 +1,7 @@
 // accu_example.cpp — the reference's back_and_forth accu case (accu_test.cpp:1248-1308) and the
 // pcraster manual example of accu_threshold (accu_threshold_test.cpp:65-132), with accu_capacity,
-// accu_trigger, upstream, downstream and downstream_distance on the same rasters, through the C++ mirror
-// of lue::value_policies.  Prints the results row-major, one raster per line; exit status 0 on success.
+// accu_trigger, upstream, downstream, downstream_distance, partial_accu and float kinematic_wave on the
+// same rasters, through the C++ mirror of lue::value_policies.  Prints the results row-major, one raster per line; exit status 0 on success.
 #include <cstdio>
 #include <vector>
 
@@ -72,6 +72,26 @@ int main()
         std::printf("\n");
         std::printf("schedule cap %d threads %d publish_every %d ms %g\n", tuned.cap, tuned.threads,
                     tuned.publish_every, tuned.ms);
+
+        // partial_accu on back_and_forth (its 3 x 5 partitions) and the float instantiation of
+        // kinematic_wave on the pcraster rasters (current outflow = inflow / 10, lateral inflow = inflow /
+        // 1000, alpha 1.5, beta 0.6, dt 15 s, channel length 10 m)
+        auto partial = value_policies::partial_accu(flow_direction, Scalar<float>{0.0f}, 1000);
+        partial.to_host(out.data());
+        for (float v : out) std::printf("%g ", v);
+        std::printf("\n");
+        std::vector<float> q0(25), lat(25);
+        for (int i = 0; i < 25; ++i) {
+            q0[i] = inflow[i] / 10.0f;
+            lat[i] = inflow[i] / 1000.0f;
+        }
+        auto q = PartitionedArray<float>::from_host(q0.data(), {5, 5}, {5, 5});
+        auto l = PartitionedArray<float>::from_host(lat.data(), {5, 5}, {5, 5});
+        auto q1 = value_policies::kinematic_wave(fd, q, l, Scalar<float>{1.5f}, Scalar<float>{0.6f},
+                                                 Scalar<float>{15.0f}, Scalar<float>{10.0f});
+        q1.to_host(f.data());
+        for (float v : f) std::printf("%.9g ", v);
+        std::printf("\n");
     } catch (const std::exception& ex) {
         std::fprintf(stderr, "error: %s\n", ex.what());
         return 2;

@@ -331,11 +331,25 @@ def downstream_distance(flow_direction, cell_size, dtype=torch.float32):
 
 
 def kinematic_wave(flow_direction, current_outflow, inflow, alpha, beta, time_step_duration, channel_length):
-    """One time step; float64 discharge.  Float32 inflow/alpha rasters with scalar beta and channel
-    length take the mixed-precision entry point (exact float32 -> float64 promotion per cell)."""
+    """One time step.  A float32 current outflow raster (or a numpy.float32 scalar one) selects the
+    reference's float instantiation: every input as float32, float32 discharge out.  Otherwise the
+    discharge is float64; float32 inflow/alpha rasters with scalar beta and channel length then take the
+    mixed-precision entry point (exact float32 -> float64 promotion per cell)."""
     _check_partitioning(flow_direction, current_outflow, inflow, alpha, beta, channel_length)
     t = flow_direction.topology()
     shape = flow_direction.shape
+    if ((isinstance(current_outflow, PartitionedArray) and current_outflow.dtype == torch.float32) or
+            isinstance(current_outflow, np.float32)):
+        out = _empty(flow_direction, torch.float32)
+        args = [_raster_or_scalar(x, shape, torch.float32, name) for x, name in (
+            (current_outflow, "current_outflow"), (inflow, "inflow"), (alpha, "alpha"), (beta, "beta"),
+            (channel_length, "channel_length"))]
+        (pq, sq, _), (pl, sl, _), (pa, sa, _), (pb, sb, _), (pd, sd, _) = args
+        _lib.check(_lib.lib().lue_gpu_kinematic_wave_f32(t.handle, pq, sq, pl, sl, pa, sa, pb, sb,
+                                                         float(time_step_duration), pd, sd, out.data_ptr(),
+                                                         _stream(flow_direction.data)))
+        del args
+        return PartitionedArray(out, flow_direction.partition_shape)
     out = _empty(flow_direction, torch.float64)
     L = _lib.lib()
     stream = _stream(flow_direction.data)

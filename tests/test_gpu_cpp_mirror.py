@@ -42,3 +42,15 @@ def test_cpp_mirror_known_answers():
     # accu_threshold again after the stage schedule was autotuned for it: the same flux
     assert lines[11].split() == lines[1].split()
     assert lines[12].startswith("schedule cap ")
+    # partial_accu on back_and_forth against the oracle (one partition row per 3 rows: one inter-partition
+    # hand-off per column, no order dependence)
+    bf = [c for c in golden.load("accu") if c["name"] == "back_and_forth"][0]
+    fd_bf = golden.u8(bf["flow_direction"])
+    partial = np.array([float(v) for v in lines[13].split()]).reshape(6, 5)
+    assert np.array_equal(partial, oracle.partial_accu(fd_bf, 1000, (3, 5)), equal_nan=True)
+    # kinematic_wave<float> against the oracle's float instantiation
+    q1 = np.array([float(v) for v in lines[14].split()], np.float32).reshape(5, 5)
+    want = oracle.kinematic_wave(fd, inflow / np.float32(10), inflow / np.float32(1000), np.float32(1.5),
+                                 np.float32(0.6), np.float32(15.0), np.float32(10.0), (5, 5), dtype=np.float32)
+    from tests import parity
+    parity.assert_close32(q1, want, "kinematic_wave<float>")

@@ -75,6 +75,18 @@ def test_kinematic_wave_case(lfr, case):
         assert_matches(got, golden.f32(case["expected"]["outflow_we_got"]), case["compare"])
 
 
+@pytest.mark.parametrize("case", KW, ids=[golden.case_id(c) for c in KW])
+def test_kinematic_wave_case_float_instantiation(lfr, case):
+    """The same cases through the float instantiation (every raster float32, float Newton with 14-bit
+    stopping): float32 out, within the cases' own relative tolerance of the reference's values."""
+    got = run_case(lfr, case, np.float32)["outflow_we_got"]
+    assert got.dtype == np.float32
+    if case["compare"] == "all_positive":
+        assert (got > 0).all()
+    else:
+        assert_matches(got, golden.f32(case["expected"]["outflow_we_got"]), case["compare"])
+
+
 COUNTS = golden.load("inflow_count")
 
 

@@ -4,6 +4,7 @@ All calls go through liblue_gb300.so's C ABI (lue_gb300.framework).  Tolerances:
 """
 import numpy as np
 import pytest
+import torch
 
 from lue_gb300 import synthetic
 from oracle import oracle
@@ -95,6 +96,29 @@ def test_accu_threshold_and_fraction(lfr, dtype):
 def kw_inputs(rows, cols, seed):
     d = synthetic.kinematic_wave_inputs(rows, cols, seed, 100.0, cached=False)
     return d
+
+
+def test_kinematic_wave_float_instantiation_three_steps(lfr):
+    """kinematic_wave for F = float: float32 discharge, lateral inflow, alpha (raster), beta and channel
+    length (scalars) in, float32 out, against the oracle's float instantiation within the float32
+    tolerance, three steps, with a no-data cell and negative lateral inflow (extraction)."""
+    d = kw_inputs(512, 640, 6)
+    fd, ps = d["flow_direction"].copy(), (128, 160)
+    fd[100, 100] = 255
+    lat = d["lateral_inflow"].copy()
+    lat[::97, ::89] = np.float32(-2e-5)
+    q = d["discharge"].astype(np.float32)
+    a = lfr.from_numpy(fd, ps)
+    lat_d, alpha_d = lfr.from_numpy(lat, ps), lfr.from_numpy(d["alpha"], ps)
+    q_gpu = lfr.from_numpy(q, ps)
+    q_cpu = q
+    for step in range(3):
+        q_gpu = lfr.kinematic_wave(a, q_gpu, lat_d, alpha_d, np.float32(0.6), np.float32(3600.0), np.float32(100.0))
+        assert q_gpu.dtype == torch.float32
+        q_cpu = oracle.kinematic_wave(fd, q_cpu, lat, d["alpha"], np.float32(0.6), np.float32(3600.0),
+                                      np.float32(100.0), ps, dtype=np.float32)
+        parity.assert_close32(lfr.to_numpy(q_gpu), q_cpu, f"kinematic_wave float step {step}")
+        q_cpu = lfr.to_numpy(q_gpu)  # each step from the same inputs
 
 
 @pytest.mark.parametrize("f32_inputs", [True, False], ids=["f32in", "f64in"])
