@@ -12,9 +12,9 @@ for a model that routes many inputs over one flow-direction raster.
 Reported (one JSON line, rank 0):
   value      Mcells/s of the device-resident step (inputs in HBM), K steps timed with CUDA events on
              the launching stream between barriers + synchronize; max over ranks.
-  e2e        the same metric through the public API (lue_gb300.framework) with host buffers: per step
-             the float32 material goes host->device from pinned memory and the outflow comes back
-             device->host.
+  e2e        the same metric through the public API (lue_gb300.framework.from_numpy -> accu, which calls
+             the C ABI -> to_numpy_async) with host buffers: per step the float32 material goes
+             host->device from a pinned numpy array and the outflow comes back device->host into one.
   roofline   algorithmic bytes (fd 1 + material 4 + outflow 4 = 9 B/cell) / mean step time against the
              measured HBM copy bandwidth; traffic from the committed ncu summary when present.
   cpu_baseline  the CPU oracle (a restatement of the reference's partitioned ridge walk, threaded
@@ -310,8 +310,7 @@ def bench_ours(args, world, rank, local):
 
     # resident inputs
     fd_d = lfr.from_numpy(inputs["flow_direction"], ps, device=dev)
-    m_host = torch.from_numpy(inputs["material"]).pin_memory()
-    m_d = lfr.PartitionedArray(m_host.to(dev, non_blocking=True), ps)
+    m_d = lfr.from_numpy(inputs["material"], ps, device=dev)
     torch.cuda.synchronize()
 
     t0 = time.perf_counter()
@@ -353,18 +352,16 @@ def bench_ours(args, world, rank, local):
     total_out = float(out.data.double()[mask].sum())
     del mask
 
-    # end to end through the public C ABI with host buffers: every step the material goes host->device
-    # (pinned), accu runs, and the outflow comes back device->host (pinned).  Three streams overlap the
-    # upload of step k+1 and the download of step k-1 with the routing of step k (double buffers).
-    L = _lib.lib()
+    # end to end through the public API with host buffers (lue_gb300.framework: from_numpy -> accu ->
+    # to_numpy_async; accu is the C ABI's lue_gpu_accu_f32): every step the float32 material goes
+    # host->device from a pinned numpy array, accu runs, and the outflow comes back device->host into a
+    # pinned numpy array.  Three streams overlap the upload of step k+1 and the download of step k-1 with
+    # the routing of step k; arrays made on one stream and used on another are recorded on it.
     e2e_steps = max(3, min(args.steps, 8))
-    in_d = [torch.empty((rows, cols), dtype=torch.float32, device=dev) for _ in range(2)]
-    out_d = [torch.empty((rows, cols), dtype=torch.float32, device=dev) for _ in range(2)]
-    out_host = [torch.empty((rows, cols), dtype=torch.float32).pin_memory() for _ in range(2)]
+    m_np = lfr.pinned_empty((rows, cols), np.float32)
+    m_np[...] = inputs["material"]
+    out_np = [lfr.pinned_empty((rows, cols), np.float32) for _ in range(2)]
     s_in, s_c, s_out = (torch.cuda.Stream(dev) for _ in range(3))
-    ev_in = [torch.cuda.Event() for _ in range(e2e_steps)]
-    ev_c = [torch.cuda.Event() for _ in range(e2e_steps)]
-    ev_out = [torch.cuda.Event() for _ in range(e2e_steps)]
 
     def e2e_trial():
         torch.cuda.synchronize()
@@ -375,22 +372,20 @@ def bench_ours(args, world, rank, local):
         s_c.wait_event(e0)
         s_out.wait_event(e0)
         for k in range(e2e_steps):
-            b = k % 2
-            if k >= 2:
-                s_in.wait_event(ev_c[k - 2])  # in_d[b] is free once step k-2 has routed
             with torch.cuda.stream(s_in):
-                in_d[b].copy_(m_host.view(rows, cols), non_blocking=True)
-            ev_in[k].record(s_in)
-            s_c.wait_event(ev_in[k])
-            if k >= 2:
-                s_c.wait_event(ev_out[k - 2])  # out_d[b] is free once step k-2 is downloaded
-            _lib.check(L.lue_gpu_accu_f32(topo.handle, in_d[b].data_ptr(), 0.0, out_d[b].data_ptr(),
-                                          s_c.cuda_stream))
-            ev_c[k].record(s_c)
-            s_out.wait_event(ev_c[k])
+                md = lfr.from_numpy(m_np, ps, device=dev)
+                ev_in = torch.cuda.Event()
+                ev_in.record(s_in)
+            s_c.wait_event(ev_in)
+            with torch.cuda.stream(s_c):
+                md.data.record_stream(s_c)
+                o = lfr.accu(fd_d, md)
+                ev_c = torch.cuda.Event()
+                ev_c.record(s_c)
+            s_out.wait_event(ev_c)
             with torch.cuda.stream(s_out):
-                out_host[b].copy_(out_d[b], non_blocking=True)
-            ev_out[k].record(s_out)
+                o.data.record_stream(s_out)
+                lfr.to_numpy_async(o, out_np[k % 2])
         e1.record(s_out)
         torch.cuda.synchronize()
         return max_over_ranks(e0.elapsed_time(e1) / 1000.0, world)
@@ -401,7 +396,7 @@ def bench_ours(args, world, rank, local):
     e2e_s = statistics.median(e2e_trials)
     e2e_value = world * n * e2e_steps / e2e_s / 1e6
     e2e_best = world * n * e2e_steps / min(e2e_trials) / 1e6
-    assert torch.equal(out_host[(e2e_steps - 1) % 2], out.data.cpu()), "end-to-end result differs"
+    assert np.array_equal(out_np[(e2e_steps - 1) % 2], out.data.cpu().numpy()), "end-to-end result differs"
 
     # roofline of the accu call (its kernels together; one call per step)
     peak, peak_kind = peaks()
@@ -468,8 +463,10 @@ def bench_ours(args, world, rank, local):
                 "best_of_trials": round(e2e_best, 3),
                 "trials_ms_per_step": [round(1000 * x / e2e_steps, 2) for x in e2e_trials],
                 "timed": "median of 5 trials (value), fastest beside it",
+                "path": "lue_gb300.framework.from_numpy -> accu (C ABI lue_gpu_accu_f32) -> to_numpy_async, "
+                        "pinned numpy arrays",
                 "overlap": "upload of step k+1 and download of step k-1 beside the routing of step k "
-                           "(three streams, double buffers, pinned host memory)"},
+                           "(three streams, pinned host memory)"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "kernel": ("accu_f32 call: k_tile_exit_sums + exit-forest scan + k_tile_accu" if engine == "tiles"

@@ -179,6 +179,30 @@ int lue_gpu_partial_accu_f32(lue_gpu_topology* topology, int64_t nr_steps, float
 int lue_gpu_partial_accu_f64(lue_gpu_topology* topology, int64_t nr_steps, double* out, uint8_t* order_dependent,
                              void* stream);
 
+/* Element types of the numpy boundary (LUE's element types). */
+enum lue_gpu_element_type {
+    LUE_GPU_ELEMENT_U8 = 1,
+    LUE_GPU_ELEMENT_I32 = 2,
+    LUE_GPU_ELEMENT_U32 = 3,
+    LUE_GPU_ELEMENT_I64 = 4,
+    LUE_GPU_ELEMENT_U64 = 5,
+    LUE_GPU_ELEMENT_F32 = 6,
+    LUE_GPU_ELEMENT_F64 = 7
+};
+
+/* from_numpy(array, partition_shape, no_data_value) (source/framework/python/source/numpy/
+ * from_numpy.cpp:44-133), the no-data part: every element of the device buffer equal to *value (a host
+ * value of the element type) becomes the element type's no-data value (NaN for float and double, the
+ * minimum for signed and the maximum for unsigned integers; policy/detect_no_data_by_value.hpp:33-54),
+ * in place, on the stream.  The buffer must be 16-byte aligned. */
+int lue_gpu_mark_no_data(void* data, int64_t n, int element_type, const void* value, void* stream);
+
+/* to_numpy(array, no_data_value) (source/framework/python/source/numpy/to_numpy.cpp), the no-data part:
+ * src copied to dst (device buffers, 16-byte aligned, may be the same) with every no-data element
+ * replaced by *value. */
+int lue_gpu_replace_no_data(const void* src, void* dst, int64_t n, int element_type, const void* value,
+                            void* stream);
+
 /* Downstream level of each cell: 0 for cells without inflow, else 1 + the largest level upstream;
  * -1 for no-data and for cells on or below a cycle.  No reference counterpart: it exposes the
  * downstream ordering the routing kernels use. */

@@ -62,6 +62,8 @@ def _declare(L):
         "lue_gpu_topology_prepare": ([p, p], i32),
         "lue_gpu_inflow_count_u8": ([p, i32, p, p], i32),
         "lue_gpu_accu_info_u8": ([p, p, p], i32),
+        "lue_gpu_mark_no_data": ([p, i64, i32, p, p], i32),
+        "lue_gpu_replace_no_data": ([p, p, i64, i32, p, p], i32),
         "lue_gpu_partial_accu_f32": ([p, i64, p, p, p], i32),
         "lue_gpu_partial_accu_f64": ([p, i64, p, p, p], i32),
         "lue_gpu_downstream_level_i32": ([p, p, p], i32),

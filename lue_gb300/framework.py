@@ -123,22 +123,97 @@ class Topology:
             pass
 
 
+_ELEMENT_TYPES = {np.dtype(np.uint8): 1, np.dtype(np.int32): 2, np.dtype(np.uint32): 3, np.dtype(np.int64): 4,
+                  np.dtype(np.uint64): 5, np.dtype(np.float32): 6, np.dtype(np.float64): 7}
+_TORCH_DTYPES = {np.dtype(np.uint8): torch.uint8, np.dtype(np.int32): torch.int32, np.dtype(np.int64): torch.int64,
+                 np.dtype(np.float32): torch.float32, np.dtype(np.float64): torch.float64}
+
+
+def _element_type(dtype):
+    try:
+        return _ELEMENT_TYPES[np.dtype(dtype)]
+    except KeyError:
+        raise TypeError(f"element type {np.dtype(dtype)} is not one of LUE's") from None
+
+
+def pinned_empty(shape, dtype):
+    """An uninitialised numpy array in pinned (page-locked) host memory.  from_numpy reads such an array,
+    and to_numpy / to_numpy_async write one, with asynchronous copies and no staging copy."""
+    return torch.empty(tuple(shape), dtype=_TORCH_DTYPES[np.dtype(dtype)], pin_memory=True).numpy()
+
+
+def _host_tensor(a):
+    t = torch.from_numpy(a)
+    return t, t.is_pinned()
+
+
 def from_numpy(array, partition_shape=None, no_data_value=None, device="cuda"):
-    """Copy a 2-D numpy array to the GPU.  For floats, ``no_data_value`` cells become NaN; for
-    integers they become the element type's no-data value (255 for uint8)."""
+    """lue.framework.from_numpy (source/framework/python/source/numpy/from_numpy.cpp:44-133): a 2-D
+    numpy array to a PartitionedArray on the GPU; elements equal to ``no_data_value`` become the element
+    type's no-data value (NaN for floats, the minimum for signed and the maximum for unsigned integers).
+
+    The copy runs on torch's current stream and the call returns before it completes: an array in pinned
+    memory (pinned_empty) is copied directly, and must not be changed until the stream has passed the
+    copy; any other array is first copied into pinned memory from torch's host allocator, which keeps
+    that memory until the copy is done.  The no-data mapping runs on the device, on the same stream."""
     a = np.ascontiguousarray(array)
+    if a.ndim != 2:
+        raise RuntimeError("Currently only arrays of rank 2 are supported")
+    et = _element_type(a.dtype)
+    host, pinned = _host_tensor(a)
+    if not pinned:
+        host = host.pin_memory()
+    dev = torch.empty(a.shape, dtype=host.dtype, device=device)
+    dev.copy_(host, non_blocking=True)
     if no_data_value is not None:
-        a = a.copy()
-        mask = a == no_data_value
-        if np.issubdtype(a.dtype, np.floating):
-            a[mask] = np.nan
-        else:
-            a[mask] = np.iinfo(a.dtype).max
-    return PartitionedArray(torch.from_numpy(a).to(device), partition_shape)
+        v = np.array(no_data_value, dtype=a.dtype)
+        _lib.check(_lib.lib().lue_gpu_mark_no_data(dev.data_ptr(), dev.numel(), et, v.ctypes.data, _stream(dev)))
+    return PartitionedArray(dev, partition_shape)
 
 
-def to_numpy(array):
-    return array.data.cpu().numpy()
+def to_numpy_async(array, out, no_data_value=None):
+    """Starts the copy of a PartitionedArray into ``out`` (a numpy array of the same shape and element
+    type, in pinned memory: pinned_empty) on torch's current stream; no-data elements come out as
+    ``no_data_value`` when it is given (mapped on the device).  Returns a torch.cuda.Event that has
+    completed once ``out`` holds the result."""
+    d = array.data
+    if tuple(out.shape) != tuple(d.shape) or _TORCH_DTYPES.get(np.dtype(out.dtype)) != d.dtype:
+        raise ValueError("to_numpy: out must have the array's shape and element type")
+    host, pinned = _host_tensor(out)
+    if not pinned:
+        raise ValueError("to_numpy_async: out must be in pinned memory (pinned_empty)")
+    src = d
+    if no_data_value is not None:
+        src = torch.empty_like(d)
+        v = np.array(no_data_value, dtype=out.dtype)
+        _lib.check(_lib.lib().lue_gpu_replace_no_data(d.data_ptr(), src.data_ptr(), d.numel(),
+                                                      _element_type(out.dtype), v.ctypes.data, _stream(d)))
+    host.copy_(src, non_blocking=True)
+    ev = torch.cuda.Event()
+    ev.record(torch.cuda.current_stream(d.device))
+    return ev
+
+
+def to_numpy(array, no_data_value=None, out=None):
+    """lue.framework.to_numpy (source/framework/python/source/numpy/to_numpy.cpp): the array as a numpy
+    array (into ``out`` when given), no-data elements as ``no_data_value`` when it is given.  The copy
+    goes to pinned memory on torch's current stream; the call returns once it is complete."""
+    d = array.data
+    if out is None:
+        out = pinned_empty(d.shape, _numpy_dtype(d.dtype))
+    if _host_tensor(out)[1]:
+        to_numpy_async(array, out, no_data_value).synchronize()
+        return out
+    tmp = to_numpy(array, no_data_value)  # pageable out: through a pinned buffer
+    np.copyto(out, tmp)
+    return out
+
+
+def _numpy_dtype(torch_dtype):
+    for k, v in _TORCH_DTYPES.items():
+        if v == torch_dtype:
+            return k
+    raise TypeError(f"element type {torch_dtype} is not one of LUE's")
 
 
 def _stream(t):

@@ -62,8 +62,10 @@ def test_admission_waits_for_memory_and_rejects_requests_above_the_budget():
     small = serving.Request(0, "accu", 0, 0.0, 1, dict(seed=1))
     big = serving.Request(1, "kinematic_wave", 1, 0.0, 5, dict(seed=2))
     server.budget = server.bytes_needed(small) + server.bytes_needed(big) - 1  # not both at once
+    server.in_use = server.bytes_needed(small)  # as if the small request were running
     assert server.admissible(big, busy=True) == "wait"
     assert server.admissible(big, busy=False) is None
+    server.in_use = 0
     summary = server.run([small, big], realtime=False)
     assert summary["rejected"] == 0 and summary["max_concurrent"] == 1
     assert big.start >= small.done and big.result is not None
