@@ -328,7 +328,6 @@ struct __align__(16) TileSmem {
     uint8_t up[kTileCells];        // in-tile upstream mask
     uint8_t fd[kHalo][kHalo + 2];  // flow direction with a one-cell halo (255 outside the array)
     uint8_t border[kBorderCells];  // per border cell: outside neighbours draining into it
-    uint8_t lab[kTileCells];       // exit label of each cell
     int round_count[3];            // cells queued for the next rounds (a ring of three counters)
 };
 
@@ -442,11 +441,12 @@ __device__ __forceinline__ int block_exclusive_int(int v, int* warp_tot, int& to
 // (its subtree) get the positions start .. pos - 1 and the cell itself pos, so that the accu of any cell
 // is the difference of two prefix sums over the material laid out in post-order.  Cells with a no-data
 // flow direction (or outside the array) take the positions after the valid cells, flagged kNoValue.
-// Also: each cell's exit label, and, per border cell, which outside neighbours drain into it.
+// Also: each exit's scan slots (its own, and the one before its subtree), and, per border cell, which
+// outside neighbours drain into it.
 __global__ void __launch_bounds__(kTileThreads)
     k_tile_forest(const uint8_t* __restrict__ fd, TileGeom g, const int32_t* __restrict__ exit_base,
-                  const uint16_t* __restrict__ exit_local, uint16_t* cell_at, uint16_t* prev_at, uint8_t* label,
-                  uint8_t* border_in, int* error)
+                  const uint16_t* __restrict__ exit_local, uint16_t* cell_at, uint16_t* prev_at,
+                  uint32_t* exit_span, uint8_t* border_in, int* error)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TileSmem& sm = *reinterpret_cast<TileSmem*>(smem_raw);
@@ -487,12 +487,6 @@ __global__ void __launch_bounds__(kTileThreads)
     }
     const int rounds = r, nvalid = head;
     if (t == 0) rstart[rounds] = (uint16_t)nvalid;
-    // labels: none (or no-data) everywhere, then each exit its index; the exits are roots of the forest
-    for (int i = t; i < kTileCells; i += kTileThreads)
-        sm.lab[i] = sm.fd[(i >> 6) + 1][(i & 63) + 1] == kNoData ? kLabelNoData : kLabelNone;
-    __syncthreads();
-    const int32_t e0 = exit_base[tile], ne = exit_base[tile + 1] - e0;
-    for (int e = t; e < ne; e += kTileThreads) sm.lab[exit_local[e0 + e]] = (uint8_t)e;
     // per border cell, the neighbours outside the tile that drain into it
     for (int b = t; b < kBorderCells; b += kTileThreads) {
         int rin, cin;
@@ -546,8 +540,7 @@ __global__ void __launch_bounds__(kTileThreads)
         }
     }
     __syncthreads();
-    // the other cells, downstream first: after the siblings that come before them; a cell's label is
-    // its downstream cell's
+    // the other cells, downstream first: after the siblings that come before them
     for (int q = rounds - 1; q >= 0; --q) {
         for (int k = rstart[q] + t; k < rstart[q + 1]; k += kTileThreads) {
             const int i = sm.queue[k], d = sm.dsl[i];
@@ -559,7 +552,6 @@ __global__ void __launch_bounds__(kTileThreads)
                 m &= m - 1;
             }
             st[i] = (uint16_t)o;
-            sm.lab[i] = sm.lab[d];
         }
         __syncthreads();
     }
@@ -581,10 +573,15 @@ __global__ void __launch_bounds__(kTileThreads)
         cell_at[T + run_table_index(p)] = (uint16_t)(i | (valid ? 0u : kNoValue));
         prev_at[T + run_table_index(p)] =
             (uint16_t)((s0 > 0 ? scan_slot(s0 - 1) : kZeroSlot) | (s0 == p ? kPrevRidge : 0u));
-        label[tile * kTileCells + i] = sm.lab[i];
     }
     __syncthreads();
     if (t < kRunPositions / 32 && seen[t] != 0xFFFFFFFFu) *error = 1;
+    const int32_t e0 = exit_base[tile], ne = exit_base[tile + 1] - e0;
+    for (int e = t; e < ne; e += kTileThreads) {
+        const int loc = exit_local[e0 + e];
+        const int s0 = st[loc], p = s0 + sz[loc] - 1;
+        exit_span[e0 + e] = (uint32_t)scan_slot(p) | ((uint32_t)(s0 > 0 ? scan_slot(s0 - 1) : kZeroSlot) << 16);
+    }
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -731,7 +728,6 @@ __device__ __forceinline__ void store_quad(float* __restrict__ p, const TileGeom
 struct TileForest {
     const uint16_t* cell_at;
     const uint16_t* prev_at;
-    const uint8_t* label;
     const uint8_t* border_in;
     const int32_t* halo_exit;
 };
@@ -742,6 +738,7 @@ struct __align__(16) TileCallSmem {
     float M[kTileCells];                   // material plus what enters, in cell order; then the results
     unsigned long long warp_tot[kTileThreads / 32];
     unsigned red[2][kTileThreads / 32];
+    unsigned warp_mn[kTileThreads / 32];
     float warp_sum[kTileThreads / 32];
 };
 
@@ -772,155 +769,6 @@ __device__ __forceinline__ void load_material(float4 (&x)[4], const float* __res
 __device__ __forceinline__ float quad_at(const float4& q, int k)
 {
     return k == 0 ? q.x : (k == 1 ? q.y : (k == 2 ? q.z : q.w));
-}
-
-// Shared memory of a pass-1 tile CTA.
-struct __align__(16) ExitSumSmem {
-    unsigned long long bin[kBorderCells];        // fixed-point material total per exit label
-    unsigned poisoned[(kBorderCells + 31) / 32]; // exits with a NaN or negative term upstream
-    unsigned long long warp_tot[kTileThreads / 32];
-    unsigned red[3][kTileThreads / 32];
-};
-
-// Inclusive sums of v over runs of lanes with equal `key` (consecutive lanes), in the run's last lane.
-__device__ __forceinline__ unsigned long long run_sum(unsigned key, unsigned long long v, bool& last)
-{
-    const int lane = threadIdx.x & 31;
-    const unsigned prev = __shfl_up_sync(0xffffffffu, key, 1);
-    const unsigned next = __shfl_down_sync(0xffffffffu, key, 1);
-    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || prev != key);
-    const int start = 31 - __clz(heads & (0xFFFFFFFFu >> (31 - lane)));  // first lane of this lane's run
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const unsigned long long y = __shfl_up_sync(0xffffffffu, v, d);
-        if (lane - d >= start) v += y;
-    }
-    last = lane == 31 || next != key;
-    return v;
-}
-
-// Pass 1: the local value of every exit (the material total of its in-tile catchment: the cells with
-// its label) to P, in the exit forest's post-order; per tile an upper bound of the material total in
-// 2^-16 units (~0 asks for the walk engine: +inf, a total beyond float range, or a dynamic range the
-// 64-bit fixed point cannot hold) and the statistics pass 3 needs.
-//
-// Fixed point: round(x * 2^F), F from 4096 times the tile's largest term, so that every sum stays below
-// 2^62 and is exact (integer addition), whatever the order of the shared-memory atomics.  Each thread
-// holds 4 quads of 4 cells; a quad whose 4 cells have one label takes part in a warp sum over runs of
-// lanes with equal labels (a run's last lane adds the run's total to the label's bin: one atomic per
-// run instead of one per cell, so a basin that covers the tile does not serialise on one address); the
-// other quads add their cells one by one.
-// vec: material rows can be read as float4 (16-byte aligned, columns a multiple of 4).
-__global__ void __launch_bounds__(kTileThreads)
-    k_tile_exit_sums(TileGeom g, const float* __restrict__ ext, float ext_s, bool vec,
-                     const uint8_t* __restrict__ label, const int32_t* __restrict__ exit_base,
-                     const uint32_t* __restrict__ exit_pos, float2* __restrict__ P,
-                     unsigned long long* __restrict__ block_total, TileStat* __restrict__ stat)
-{
-    __shared__ ExitSumSmem sm;
-    const int64_t tr = blockIdx.y, tc = blockIdx.x;  // grid = (tile columns, tile rows)
-    const int64_t tile = tr * g.tcols + tc;
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    float4 xm[4];
-    load_material(xm, ext, ext_s, g, tr, tc, vec);
-    uint32_t lw[4];  // labels of the thread's quads (tile-major: quad j is word t + 256 j)
-    const uint32_t* lab = reinterpret_cast<const uint32_t*>(label + tile * kTileCells);
-#pragma unroll
-    for (int j = 0; j < 4; ++j) lw[j] = __ldg(lab + t + kTileThreads * j);
-    if (t < kBorderCells) sm.bin[t] = 0ull;
-    if (t < (kBorderCells + 31) / 32) sm.poisoned[t] = 0u;
-    // over the valid cells: the largest raw bits (a sign bit or NaN sends pass 3 to its slow path), and
-    // the largest and smallest positive bits of the terms that are >= 0
-    unsigned raw = 0, mx = 0, mn = 0xFFFFFFFFu;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const float v = quad_at(xm[j], k);
-            const unsigned b = __float_as_uint(v);
-            if (((lw[j] >> (8 * k)) & 0xFFu) != kLabelNoData) {
-                raw = max(raw, b);
-                if (v >= 0.0f) {
-                    mx = max(mx, b & 0x7FFFFFFFu);
-                    mn = min(mn, (b & 0x7FFFFFFFu) - 1u);
-                }
-            }
-        }
-    }
-    raw = __reduce_max_sync(0xffffffffu, raw);
-    mx = __reduce_max_sync(0xffffffffu, mx);
-    mn = __reduce_min_sync(0xffffffffu, mn);
-    if (lane == 0) {
-        sm.red[0][warp] = raw;
-        sm.red[1][warp] = mx;
-        sm.red[2][warp] = mn;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int w = 0; w < kTileThreads / 32; ++w) {
-        raw = max(raw, sm.red[0][w]);
-        mx = max(mx, sm.red[1][w]);
-        mn = min(mn, sm.red[2][w]);
-    }
-    const float bound = tile_bound(mx, 0u);
-    const int F = tile_scale(bound);
-    if (mx >= 0x7F800000u || !(bound < 1.0e38f) ||
-        (mn != 0xFFFFFFFFu && __uint_as_float(mn + 1u) * pow2f(F) < kMinQuantum)) {
-        if (t == 0) block_total[tile] = ~0ull;
-        return;  // uniform: every thread has the same reductions
-    }
-    const bool exact = mn == 0xFFFFFFFFu || __uint_as_float(mn + 1u) * pow2f(F) >= 8388608.0f;
-    const bool dirty = raw > 0x7F800000u;  // uniform
-    unsigned long long tile_sum = 0;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        unsigned long long q[4];
-        unsigned l[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            l[k] = (lw[j] >> (8 * k)) & 0xFFu;
-            float v = quad_at(xm[j], k);
-            if (l[k] == kLabelNoData) v = 0.0f;
-            if (dirty) {
-                if (!(v >= 0.0f)) {  // NaN or negative: the exit downstream is NaN
-                    if (l[k] < kBorderCells) atomicOr(&sm.poisoned[l[k] >> 5], 1u << (l[k] & 31));
-                    v = 0.0f;
-                }
-                v = fabsf(v);  // -0 counts as 0
-            }
-            q[k] = exact ? float_to_fixed64_exact(v, F) : float_to_fixed64(v, F);
-        }
-        const unsigned long long qs = q[0] + q[1] + q[2] + q[3];
-        tile_sum += qs;
-        const bool uniform = lw[j] == (lw[j] & 0xFFu) * 0x01010101u;
-        if (!uniform) {
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                if (l[k] < kBorderCells && q[k]) atomicAdd(&sm.bin[l[k]], q[k]);
-        }
-        bool last;
-        const unsigned key = uniform ? l[0] : 0x100u + (unsigned)lane;  // mixed quads: a run of their own
-        const unsigned long long v = run_sum(key, uniform ? qs : 0ull, last);
-        if (last && key < kBorderCells && v) atomicAdd(&sm.bin[key], v);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) tile_sum += __shfl_xor_sync(0xffffffffu, tile_sum, o);
-    if (lane == 0) sm.warp_tot[warp] = tile_sum;
-    __syncthreads();
-    const int32_t e0 = __ldg(exit_base + tile), ne = __ldg(exit_base + tile + 1) - e0;
-    if (t < ne) {  // a tile has at most 252 exits (its border cells)
-        float2 value = fixed64_to_ff(sm.bin[t], F);
-        if ((sm.poisoned[t >> 5] >> (t & 31)) & 1u) value = make_float2(__int_as_float(0x7fc00000), 0.0f);
-        P[__ldg(exit_pos + e0 + t)] = value;
-    }
-    if (t == 0) {
-        unsigned long long total = 0;
-#pragma unroll
-        for (int w = 0; w < kTileThreads / 32; ++w) total += sm.warp_tot[w];
-        const double units = ldexp(((double)total + 8192.0) * (1.0 + 1e-12), 16 - F) + 64.0;
-        block_total[tile] = units < 1.0e18 ? (unsigned long long)units : ~0ull;
-        stat[tile] = TileStat{bound, mn, dirty ? 1u : 0u, 0u};
-    }
 }
 
 // Sum of the per-tile bounds: total[0] = bound in 2^-16 units, total[1] != 0 when the tile engine must
@@ -1113,6 +961,127 @@ __device__ __forceinline__ void poison_counts(TileCallSmem& sm, unsigned bad)
     __syncthreads();
 }
 
+// The thread's run in post-order: the material of each position (0 for no-data cells and cells outside
+// the array), after a block barrier that follows the stores to M.
+__device__ __forceinline__ void gather_run(const TileCallSmem& sm, const uint32_t (&ca)[kRunWords], float (&x)[kRun])
+{
+#pragma unroll
+    for (int j = 0; j < kRun; ++j) {
+        const unsigned w = run_at(ca, j);
+        const float v = sm.M[w & kIndexMask];
+        x[j] = (w & kNoValue) ? 0.0f : v;
+    }
+}
+
+// NaN or negative terms of a run (slow path): flagged in the returned mask, then 0 (-0 counts as 0).
+__device__ __forceinline__ unsigned clean_run(float (&x)[kRun])
+{
+    unsigned bad = 0;
+#pragma unroll
+    for (int j = 0; j < kRun; ++j) {
+        if (!(x[j] >= 0.0f)) bad |= 1u << j;
+        x[j] = x[j] >= 0.0f ? fabsf(x[j]) : 0.0f;
+    }
+    return bad;
+}
+
+// Pass 1: the local value of every exit (the accu of its in-tile subtree) to P, in the exit forest's
+// post-order; per tile an upper bound of the material total in 2^-16 units (~0 asks for the walk
+// engine: +inf, a total beyond float range, or a dynamic range the 64-bit fixed point cannot hold), and
+// the statistics pass 3 takes its fixed-point scale from (so that it needs no reduction of its own).
+// Fixed point: round(x * 2^F), F from 4096 times the tile's largest term, so that every prefix sum stays
+// below 2^62 and every subtree sum (a difference of two of them) is exact.
+// vec: material rows can be read as float4 (16-byte aligned, columns a multiple of 4).
+__global__ void __launch_bounds__(kTileThreads, 4)
+    k_tile_exits(TileGeom g, const float* __restrict__ ext, float ext_s, bool vec, TileForest f,
+                 const int32_t* __restrict__ exit_base, const uint32_t* __restrict__ exit_span,
+                 const uint32_t* __restrict__ exit_pos, float2* __restrict__ P,
+                 unsigned long long* __restrict__ block_total, TileStat* __restrict__ stat)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TileCallSmem& sm = *reinterpret_cast<TileCallSmem*>(smem_raw);
+    const int64_t tr = blockIdx.y, tc = blockIdx.x;  // grid = (tile columns, tile rows)
+    const int64_t tile = tr * g.tcols + tc;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    float4 xm[4];
+    load_material(xm, ext, ext_s, g, tr, tc, vec);
+    uint32_t ca[kRunWords];
+    load_run(f.cell_at + tile * kRunPositions, ca);
+    const int32_t e0 = __ldg(exit_base + tile), ne = __ldg(exit_base + tile + 1) - e0;
+    uint32_t span = 0, epos = 0;
+    if (t < ne) {  // a tile has at most 252 exits (its border cells)
+        span = __ldg(exit_span + e0 + t);
+        epos = __ldg(exit_pos + e0 + t);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) *reinterpret_cast<float4*>(sm.M + quad_cell(j)) = xm[j];
+    __syncthreads();
+    float x[kRun];
+    gather_run(sm, ca, x);
+    // over the valid positions: the largest raw bits (a sign bit or NaN: the slow path, here and in pass
+    // 3), and the largest and smallest positive bits of the terms that are >= 0
+    unsigned raw = 0, mx = 0, mn = 0xFFFFFFFFu;
+#pragma unroll
+    for (int j = 0; j < kRun; ++j) {
+        const unsigned b = __float_as_uint(x[j]);
+        raw = max(raw, b);
+        const unsigned a = x[j] >= 0.0f ? (b & 0x7FFFFFFFu) : 0u;
+        mx = max(mx, a);
+        mn = min(mn, a - 1u);
+    }
+    raw = __reduce_max_sync(0xffffffffu, raw);
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    mn = __reduce_min_sync(0xffffffffu, mn);
+    if (lane == 0) {
+        sm.red[0][warp] = raw;
+        sm.red[1][warp] = mx;
+        sm.warp_mn[warp] = mn;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int w = 0; w < kTileThreads / 32; ++w) {  // the same order in every thread
+        raw = max(raw, sm.red[0][w]);
+        mx = max(mx, sm.red[1][w]);
+        mn = min(mn, sm.warp_mn[w]);
+    }
+    const float bound = tile_bound(mx, 0u);
+    const int F = tile_scale(bound);
+    if (mx >= 0x7F800000u || !(bound < 1.0e38f) ||
+        (mn != 0xFFFFFFFFu && __uint_as_float(mn + 1u) * pow2f(F) < kMinQuantum)) {
+        if (t == 0) block_total[tile] = ~0ull;
+        return;  // uniform: every thread has the same reductions
+    }
+    const bool dirty = raw > 0x7F800000u;  // uniform
+    unsigned poisoned_exit = 0;
+    if (dirty) {
+        poison_counts(sm, clean_run(x));
+        if (t < ne) {
+            const unsigned* C = reinterpret_cast<const unsigned*>(sm.S);
+            poisoned_exit = C[span & 0xFFFFu] != C[span >> 16];
+        }
+        __syncthreads();  // S and warp_tot are free for the value scan
+    }
+    unsigned long long a[kRun];
+    if (mn == 0xFFFFFFFFu || __uint_as_float(mn + 1u) * pow2f(F) >= 8388608.0f) {  // every term exact
+#pragma unroll
+        for (int j = 0; j < kRun; ++j) a[j] = float_to_fixed64_exact(x[j], F);
+    } else {
+#pragma unroll
+        for (int j = 0; j < kRun; ++j) a[j] = float_to_fixed64(x[j], F);
+    }
+    tile_prefix(sm, a);
+    if (t < ne) {
+        float2 value = fixed64_to_ff(sm.S[span & 0xFFFFu] - sm.S[span >> 16], F);
+        if (poisoned_exit) value = make_float2(__int_as_float(0x7fc00000), 0.0f);
+        P[epos] = value;
+    }
+    if (t == kTileThreads - 1) {  // a[15] of the last thread after the scan: the tile's exact total
+        const double units = ldexp(((double)sm.S[kRunSlots * t + kRun - 1] + 8192.0) * (1.0 + 1e-12), 16 - F) + 64.0;
+        block_total[tile] = units < 1.0e18 ? (unsigned long long)units : ~0ull;
+        stat[tile] = TileStat{bound, mn, dirty ? 1u : 0u, 0u};
+    }
+}
+
 // Pass 3: the result of every cell: the accu of its in-tile subtree, where each border cell's material
 // carries what enters it from other tiles (the exact subtree sums of the exits draining into it, rounded
 // to float once, added to the cell's material in float), in one fixed-point scan per tile.
@@ -1180,7 +1149,10 @@ __global__ void __launch_bounds__(kTileThreads, 4)
 #pragma unroll
     for (int j = 0; j < 4; ++j) *reinterpret_cast<float4*>(sm.M + quad_cell(j)) = xm[j];
     __syncthreads();
-    if (ecell >= 0) sm.M[ecell] += entering;
+    if (ecell >= 0) {  // material out of the domain stays visible as NaN (the cell and all below are NaN)
+        const float mat = sm.M[ecell];
+        sm.M[ecell] = mat >= 0.0f ? mat + entering : __int_as_float(0x7fc00000);
+    }
     float in_total = 0.0f;
     unsigned mn = st.min_bits, nan_in = 0;
 #pragma unroll
@@ -1199,21 +1171,10 @@ __global__ void __launch_bounds__(kTileThreads, 4)
     const bool clean = !st.bad && !nan_in;  // uniform
     __syncthreads();  // M holds what enters
     float x[kRun];
-#pragma unroll
-    for (int j = 0; j < kRun; ++j) {
-        const unsigned w = run_at(ca, j);
-        const float v = sm.M[w & kIndexMask];
-        x[j] = (w & kNoValue) ? 0.0f : v;
-    }
+    gather_run(sm, ca, x);
     unsigned poisoned = 0;  // bit j: the subtree of run entry j holds a NaN or negative term
     if (!clean) {
-        unsigned bad = 0;
-#pragma unroll
-        for (int j = 0; j < kRun; ++j) {
-            if (!(x[j] >= 0.0f)) bad |= 1u << j;
-            x[j] = x[j] >= 0.0f ? fabsf(x[j]) : 0.0f;  // fabsf: -0 counts as 0
-        }
-        poison_counts(sm, bad);
+        poison_counts(sm, clean_run(x));
         const unsigned* C = reinterpret_cast<const unsigned*>(sm.S);
 #pragma unroll
         for (int j = 0; j < kRun; ++j)
@@ -1381,13 +1342,13 @@ int tile_core_build(TopologyCore* core, cudaStream_t stream)
     // per-tile flow forests in post-order
     TRY(cudaMalloc(&tc->cell_at, nt * kRunPositions * sizeof(uint16_t)), "tile forest");
     TRY(cudaMalloc(&tc->prev_at, nt * kRunPositions * sizeof(uint16_t)), "tile forest");
-    TRY(cudaMalloc(&tc->label, nt * kTileCells), "tile labels");
+    TRY(cudaMalloc(&tc->exit_span, std::max<int64_t>(E, 1) * sizeof(uint32_t)), "exit span");
     TRY(cudaMalloc(&tc->border_in, nt * kBorderCells), "tile border masks");
     TRY(cudaFuncSetAttribute(k_tile_forest, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TileSmem)),
         "tile forest");
     k_tile_forest<<<dim3((unsigned)g.tcols, (unsigned)g.trows), kTileThreads, sizeof(TileSmem), stream>>>(
-        core->fd, g, tc->exit_base, tc->exit_local, tc->cell_at, tc->prev_at, tc->label, tc->border_in, flag);
-    tc->bytes += nt * kRunPositions * 4 + nt * kTileCells + nt * kBorderCells;
+        core->fd, g, tc->exit_base, tc->exit_local, tc->cell_at, tc->prev_at, tc->exit_span, tc->border_in, flag);
+    tc->bytes += nt * kRunPositions * 4 + E * 4 + nt * kBorderCells;
     TRY(cudaGetLastError(), "tile build");
     TRY(cudaMemcpyAsync(&herr, flag, sizeof(int), cudaMemcpyDeviceToHost, stream), "tile flag");
     TRY(cudaStreamSynchronize(stream), "tile build");
@@ -1445,7 +1406,7 @@ void tile_core_free(TileCore* tc)
     cudaFree(tc->halo_exit);
     cudaFree(tc->cell_at);
     cudaFree(tc->prev_at);
-    cudaFree(tc->label);
+    cudaFree(tc->exit_span);
     cudaFree(tc->border_in);
     delete tc;
 }
@@ -1487,17 +1448,20 @@ int tile_accu_f32(const TopologyCore* core, TileScratch* s, const float* ext, fl
 {
     const TileCore* tc = core->tiles;
     TileGeom g{core->rows, core->cols, tc->trows, tc->tcols};
-    const TileForest f{tc->cell_at, tc->prev_at, tc->label, tc->border_in, tc->halo_exit};
+    const TileForest f{tc->cell_at, tc->prev_at, tc->border_in, tc->halo_exit};
     // rows move as float4 when the columns are a multiple of 4 and the arrays 16-byte aligned
     const bool cols4 = (core->cols & 3) == 0;
     const bool vec_in = cols4 && (!ext || (reinterpret_cast<uintptr_t>(ext) & 15) == 0);
     const bool vec_out = cols4 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
-    static const bool smem_ok = cudaFuncSetAttribute(k_tile_accu, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    static const bool smem_ok = cudaFuncSetAttribute(k_tile_exits, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)sizeof(TileCallSmem)) == cudaSuccess &&
+                                cudaFuncSetAttribute(k_tile_accu, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                      (int)sizeof(TileCallSmem)) == cudaSuccess;
     if (!smem_ok) return fail(LUE_GPU_ECUDA, "accu_f32 (tiles): shared memory attribute");
     const dim3 tile_grid((unsigned)tc->tcols, (unsigned)tc->trows);
-    k_tile_exit_sums<<<tile_grid, kTileThreads, 0, stream>>>(g, ext, ext_s, vec_in, tc->label, tc->exit_base,
-                                                             tc->exit_pos, s->P, s->block_total, s->stat);
+    k_tile_exits<<<tile_grid, kTileThreads, sizeof(TileCallSmem), stream>>>(g, ext, ext_s, vec_in, f, tc->exit_base,
+                                                                            tc->exit_span, tc->exit_pos, s->P,
+                                                                            s->block_total, s->stat);
     k_total<<<1, 1024, 0, stream>>>(s->block_total, tc->ntiles, s->total);
     count_launches(2);
     const int64_t E = tc->nexit;

@@ -3,21 +3,21 @@
 // The raster is cut into 64 x 64 tiles (the GPU's partitions).  Inside a tile, the flow paths form a
 // forest; once, when the topology is built, it is laid out in post-order, so that the accu of a cell
 // (the material of its in-tile subtree) is the difference of two prefix sums of the material taken in
-// that order.  Each cell also gets a label: the exit of its tile that its in-tile path reaches (an exit
-// is a cell whose flow leaves its tile but not the array).  Per call:
-//   1. k_tile_exit_sums: one CTA per tile sums the material of each exit's in-tile catchment (the cells
-//      with that exit's label) in exact 64-bit fixed point, and writes each exit's local value to P, in
-//      the post-order of the exit forest, with per-tile statistics of the material.  It reads 5 bytes
-//      per cell: the material and the label.
+// that order.  Per call:
+//   1. k_tile_exits: one CTA per tile gathers its material into post-order, takes one exact 64-bit
+//      fixed-point prefix sum, and writes the local value of each exit cell (a cell whose flow leaves its
+//      tile but not the array: the material of its in-tile subtree) to P, in the post-order of the exit
+//      forest, with per-tile statistics of the material for pass 3.
 //   2. Exit forest: exit y's parent is the exit reached by following the flow from y's downstream
 //      cell through that cell's tile.  The final value of exit y is the sum of the local values over
 //      y's subtree of this forest, so an inclusive prefix sum over P in post-order gives every subtree
 //      sum as a difference of two prefix sums.  The sums are exact: 128-bit fixed point (96 value bits,
 //      32 bits counting no-data exits), so summation order cannot change the result.
 //   3. k_tile_accu: one CTA per tile adds to each border cell what enters it from other tiles (the
-//      exact subtree sums of the exits draining into it, rounded to float), takes one fixed-point prefix
-//      sum over the tile's post-order and writes every cell's result.  It reads the material, 4 bytes
-//      of post-order tables per cell and writes the result: 12 bytes per cell.
+//      exact subtree sums of the exits draining into it, rounded to float), takes the same prefix sum
+//      over the tile's post-order and writes every cell's result.
+// Pass 1 reads the material and 2 bytes of post-order table per cell; pass 3 the material and 4 bytes of
+// tables, and writes the result.  The prefix sums stay in registers and shared memory.
 // Reference counterpart: the per-partition intra/inter split of ALG/definition/accumulating_router.hpp
 // (intra :789-899, inter :902-1209), with the inter-partition channel hand-off replaced by the exit-forest
 // prefix sum.
@@ -62,11 +62,6 @@ constexpr unsigned kNoValue = 0x8000u;   // no-data flow direction or outside th
 constexpr unsigned kSlotMask = 0x1FFFu;
 constexpr unsigned kPrevRidge = 0x8000u;  // the subtree is the cell alone
 
-// Exit labels (per cell, tile-major): the index (0 .. 251) among its tile's exits of the exit its
-// in-tile flow path reaches, or one of these.
-constexpr uint8_t kLabelNone = 0xFE;    // valid cell draining to a sink, the array edge or a no-data cell
-constexpr uint8_t kLabelNoData = 0xFF;  // no-data flow direction or outside the array
-
 struct TileCore {
     int64_t trows = 0, tcols = 0, ntiles = 0;  // tile grid
     int64_t nexit = 0;                         // exits (coarse nodes)
@@ -81,7 +76,7 @@ struct TileCore {
     uint16_t* cell_at = nullptr;               // [ntiles * kRunPositions] cell at the position (| kNoValue)
     uint16_t* prev_at = nullptr;               // [ntiles * kRunPositions] scan slot before the subtree
                                                // (kZeroSlot for a subtree at position 0) | kPrevRidge
-    uint8_t* label = nullptr;                  // [ntiles * kTileCells] exit label of each cell (tile-major)
+    uint32_t* exit_span = nullptr;             // [nexit] scan slots of each exit cell: own | before << 16
     uint8_t* border_in = nullptr;              // [ntiles * kBorderCells] per border cell: outside neighbours draining in
     int64_t bytes = 0;
 };
