@@ -3,8 +3,9 @@ that the stage-engine profiles are taken on.
 
     python -m lue_gb300.examples.stage_workload SIDE OPERATION [CALLS]
 
-SIDE: raster side (cells); OPERATION: ``threshold`` (accu_threshold, float32 lognormal(0, 1)
-material, uniform [0, 0.5) thresholds) or ``kwN`` (kinematic_wave_steps with N steps, beta 0.6,
+SIDE: raster side (cells); OPERATION: ``accu`` (the tile engine, float32 lognormal(0, 1) material),
+``threshold`` (accu_threshold, float32 lognormal(0, 1) material, uniform [0, 0.5) thresholds) or ``kwN``
+(kinematic_wave_steps with N steps; ``kw1`` is one kinematic_wave call), beta 0.6,
 dt 3600 s, dx 100 m, float64 discharge, float32 rain and alpha); CALLS: calls, the last one timed
 (default 4).  Inputs come from ``lue_gb300.synthetic.kinematic_wave_inputs(SIDE, SIDE, 5, 200.0)``.
 """
@@ -26,9 +27,15 @@ def main(argv):
     rng = np.random.default_rng(1)
     material = lfr.from_numpy(rng.lognormal(0.0, 1.0, d["flow_direction"].shape).astype(np.float32))
     threshold = lfr.from_numpy((rng.random(d["flow_direction"].shape) * 0.5).astype(np.float32))
-    if op == "threshold":
+    if op == "accu":
+        def fn():
+            return lfr.accu(fd, material)
+    elif op == "threshold":
         def fn():
             return lfr.accu_threshold(fd, material, threshold)
+    elif op == "kw1":
+        def fn():
+            return lfr.kinematic_wave(fd, q, lat, alpha, 0.6, 3600.0, 100.0)
     elif op.startswith("kw"):
         steps = int(op[2:])
 
