@@ -897,6 +897,80 @@ __global__ void PATH_BOUNDS(PER) k_path_free(PathCall p, int64_t p0, int64_t p1)
     }
 }
 
+// Levels whose paths are all short (at most kPathSeqLongest cells; level 0, which holds most cells, at the
+// benchmark sizes): one thread per path, cell after cell from its top to its bottom, with the walk
+// engine's float32 cell rule (rule_f32) on the float-float sum of the upstream outflows (the previous cell
+// of the path, then the light upstream neighbours, which are bottoms of paths of lower levels, in
+// neighbour order), so that every cell gets the walk engine's result bit for bit and no map is composed.
+// A warp takes a range of kPathSeqSpan positions whose ends are moved forward to the next path top, and
+// walks its paths 32 at a time: the paths whose tops lie in the next 32 positions, one per lane; the next
+// group starts where the last of them ends.  Paths stay in the layout's order (by bottom cell), so the
+// cells a warp touches are close together.
+constexpr int kPathSeqLongest = 1024;
+constexpr int64_t kPathSeqSpan = 4096;
+
+template <Rule R, bool LIGHT>
+__global__ void __launch_bounds__(256) k_path_seq(PathCall p, int64_t p0, int64_t p1)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t s0 = p0 + warp * kPathSeqSpan;
+    if (s0 >= p1) return;
+    const int64_t lo = warp == 0 ? p0 : next_top(p.order, s0, p1);
+    const int64_t hi = next_top(p.order, min(s0 + kPathSeqSpan, p1), p1);
+    for (int64_t g = lo; g < hi;) {
+        // the paths whose tops lie in positions g .. g + 31: lane l takes the one at g + l, if any
+        const int64_t q0 = g + lane;
+        const bool mine = q0 < hi && __ldg(p.order + q0) < 0;
+        int64_t end = g;  // one past the last position of this lane's path
+        if (mine) {
+            FF x{0.0f, 0.0f};
+            bool nan_in = false;
+            int64_t q = q0;
+            int32_t w = __ldg(p.order + q);
+            for (;;) {
+                const int64_t c = (int64_t)(w & 0x7fffffff);
+                const int64_t qn = q + 1;
+                const int32_t wn = qn < hi ? __ldg(p.order + qn) : -1;  // -1: as if a top followed
+                const float e = value_at(p.a, p.as, c), b = value_at(p.b, p.bs, c);
+                FF t = x;
+                bool nan = nan_in;
+                if (LIGHT) {
+                    for (unsigned lm = __ldg(p.light + q); lm; lm &= lm - 1) {
+                        const int k = __ffs(lm) - 1;
+                        const int64_t u = c + nb_dr(k) * p.cols + nb_dc(k);
+                        const float vh = load_cg(p.out + u);
+                        if (isnan(vh)) nan = true;
+                        else t.add(vh, load_cg(p.lo + u));
+                    }
+                }
+                float oh = 0.0f, ol = 0.0f, rem = 0.0f;
+                if (!rule_f32<R>(t, nan, e, b, oh, ol, rem)) {
+                    oh = __int_as_float(0x7fc00000);
+                    ol = 0.0f;
+                    rem = oh;
+                }
+                p.out[c] = oh;
+                p.rem[c] = rem;
+                if (wn < 0) {  // a path bottom: its residual is read as light inflow by higher levels
+                    p.lo[c] = ol;
+                    end = qn;
+                    break;
+                }
+                x = FF{oh, ol};
+                nan_in = isnan(oh);
+                q = qn;
+                w = wn;
+            }
+        }
+        // the next group starts after the last path that started in this one (none: the next top)
+        int64_t next = end;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) next = max(next, __shfl_xor_sync(0xffffffffu, next, o));
+        g = next > g ? next : next_top(p.order, g + 32, hi);
+    }
+}
+
 __global__ void k_path_no_data(const uint8_t* fd, int64_t n, float* out, float* rem)
 {
     for (int64_t i = grid_stride_begin(); i < n; i += grid_stride())
@@ -985,10 +1059,12 @@ static int path_run(lue_gpu_topology* t, const PathCore* pc, const float* a, flo
     if (int rc = cuda_status(cudaMemsetAsync(tickets, 0, kPathMaxLevels * sizeof(int), stream), what)) return rc;
     k_path_no_data<<<grid_for(n, 256), 256, 0, stream>>>(core->fd, n, out, rem);
     PathCall p{pc->order, pc->light, a, as, b, bs, out, rem, t->lo, t->path_flag, core->cols};
-    // test hooks: LUE_GB300_PATH_FREE_LONGEST (levels with longer paths use the look-back scan; 0: every
+    // test hooks: LUE_GB300_PATH_SEQ_LONGEST (levels with longer paths are scanned; 0: every level),
+    // LUE_GB300_PATH_FREE_LONGEST (levels with longer paths use the look-back scan; 0: every
     // level) and LUE_GB300_PATH_POLLS (poll limit of a look-back wait; 0: every wait gives up at once,
     // and the walk engine redoes the call)
-    int free_longest = kPathFreeLongest, polls = kPathPolls;
+    int free_longest = kPathFreeLongest, polls = kPathPolls, seq_longest = kPathSeqLongest;
+    if (const char* e = getenv("LUE_GB300_PATH_SEQ_LONGEST")) seq_longest = std::max(0, atoi(e));
     if (const char* e = getenv("LUE_GB300_PATH_FREE_LONGEST")) free_longest = std::max(0, atoi(e));
     if (const char* e = getenv("LUE_GB300_PATH_POLLS")) polls = std::max(0, atoi(e));
     PMap* aggm = static_cast<PMap*>(t->path_maps);
@@ -1004,6 +1080,14 @@ static int path_run(lue_gpu_topology* t, const PathCore* pc, const float* a, flo
                 return rc;
         }
         const dim3 grid((unsigned)nt);
+        if (pc->level_longest[l] <= seq_longest) {  // one thread per path
+            const int64_t warps = (p1 - p0 + kPathSeqSpan - 1) / kPathSeqSpan;
+            const dim3 gs((unsigned)((warps + 7) / 8));
+            if (l > 0) k_path_seq<R, true><<<gs, 256, 0, stream>>>(p, p0, p1);
+            else k_path_seq<R, false><<<gs, 256, 0, stream>>>(p, p0, p1);
+            ++launches;
+            continue;
+        }
         if (pc->level_longest[l] <= free_longest) {  // CTAs cut at path tops: no waits
             const int64_t nf = (p1 - p0 + kPathThreads * per - 1) / (kPathThreads * per);
             const dim3 gf((unsigned)nf);
