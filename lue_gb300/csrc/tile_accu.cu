@@ -728,8 +728,7 @@ __device__ __forceinline__ void store_quad(float* __restrict__ p, const TileGeom
 struct TileForest {
     const uint16_t* cell_at;
     const uint16_t* prev_at;
-    const uint8_t* border_in;
-    const int32_t* halo_exit;
+    const float* inflow;
 };
 
 // Shared memory of a pass-3 tile CTA (dynamic: 53 KB, four CTAs per SM).
@@ -899,14 +898,64 @@ __global__ void __launch_bounds__(kTileThreads)
     }
 }
 
-__global__ void k_exit_sums(int64_t n, const uint32_t* __restrict__ pos, const uint32_t* __restrict__ start,
-                            const uint4* __restrict__ S, uint4* __restrict__ A, const unsigned long long* total)
+// What enters each inflow slot (a border cell receiving flow from other tiles): the exact sum of the subtree
+// sums of the exits draining into it (each a difference of two inclusive prefix sums of the exit
+// forest), rounded to float once; NaN when one of them holds a no-data exit.
+__global__ void k_slot_inflow(int64_t nslot, const int32_t* __restrict__ slot_at,
+                              const int32_t* __restrict__ slot_first, const int32_t* __restrict__ slot_exit,
+                              const uint32_t* __restrict__ pos, const uint32_t* __restrict__ start,
+                              const uint4* __restrict__ S, float* __restrict__ inflow,
+                              const unsigned long long* total)
 {
-    int64_t y = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (y >= n || total[1]) return;
-    uint32_t st = start[y];
-    u128 a = to_u128(S[pos[y]]) - (st ? to_u128(S[st - 1]) : (u128)0);
-    A[y] = from_u128(a);
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nslot || total[1]) return;
+    const int F = fixed_point_bits(total[0]);
+    u128 src = 0;
+    for (int32_t k = __ldg(slot_first + i), k1 = __ldg(slot_first + i + 1); k < k1; ++k) {
+        const int32_t y = __ldg(slot_exit + k);
+        const uint32_t st = __ldg(start + y);
+        src += to_u128(S[__ldg(pos + y)]) - (st ? to_u128(S[st - 1]) : (u128)0);
+    }
+    inflow[__ldg(slot_at + i)] = (src >> 96) ? __int_as_float(0x7fc00000) : fixed128_to_float(src & kValueMask, F);
+}
+
+// Build: per tile, its inflow slots and their upstream exits (one thread per tile, border order).
+__global__ void k_slot_count(int64_t ntiles, const uint8_t* __restrict__ border_in, int32_t* nslot, int32_t* nexit)
+{
+    const int64_t tile = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tile >= ntiles) return;
+    int a = 0, b = 0;
+    for (int k = 0; k < kBorderCells; ++k) {
+        const unsigned m = border_in[tile * kBorderCells + k];
+        a += m != 0;
+        b += __popc(m);
+    }
+    nslot[tile] = a;
+    nexit[tile] = b;
+}
+
+__global__ void k_slot_fill(int64_t ntiles, const uint8_t* __restrict__ border_in, const int32_t* __restrict__ halo_exit,
+                            const int32_t* __restrict__ slot_base, const int32_t* __restrict__ exit_base,
+                            int32_t* slot_at, int32_t* slot_first, int32_t* slot_exit, int* error)
+{
+    const int64_t tile = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tile >= ntiles) return;
+    int32_t s = slot_base[tile], e = exit_base[tile];
+    for (int b = 0; b < kBorderCells; ++b) {
+        const unsigned m0 = border_in[tile * kBorderCells + b];
+        if (!m0) continue;
+        int rin, cin;
+        border_cell(b, rin, cin);
+        slot_at[s] = (int32_t)(tile * kSlotStride + b);
+        slot_first[s] = e;
+        for (unsigned m = m0; m; m &= m - 1) {
+            const int q = __ffs(m) - 1;
+            const int32_t id = halo_exit[tile * kHaloSlots + halo_slot_of(rin + nb_dr(q), cin + nb_dc(q))];
+            if (id < 0) atomicExch(error, 1);  // a neighbour draining in must be an exit of its tile
+            slot_exit[e++] = id < 0 ? 0 : id;
+        }
+        ++s;
+    }
 }
 
 // Inclusive prefix sums (modulo 2^64) of the thread runs a[0..15] over the whole tile, written to S by
@@ -1095,13 +1144,11 @@ __global__ void __launch_bounds__(kTileThreads, 4)
 // are counted along the post-order; a cell whose subtree holds one is NaN.
 __global__ void __launch_bounds__(kTileThreads, 4)
     k_tile_accu(TileGeom g, const float* __restrict__ ext, float ext_s, bool vec, float* __restrict__ out,
-                TileForest f, const uint4* __restrict__ A, const TileStat* __restrict__ stat,
-                unsigned long long* total)
+                TileForest f, const TileStat* __restrict__ stat, unsigned long long* total)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TileCallSmem& sm = *reinterpret_cast<TileCallSmem*>(smem_raw);
     if (total[1]) return;
-    const int Fg = fixed_point_bits(total[0]);
     const int64_t tr = blockIdx.y, tc = blockIdx.x;  // grid = (tile columns, tile rows)
     const int64_t tile = tr * g.tcols + tc;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -1111,27 +1158,14 @@ __global__ void __launch_bounds__(kTileThreads, 4)
     load_run(f.cell_at + tile * kRunPositions, ca);
     load_run(f.prev_at + tile * kRunPositions, pv);
     const TileStat st = stat[tile];
-    // what enters through border cell t: the exact subtree sums of the exits draining into it, as float
-    // (NaN when one of them is no-data)
+    // what enters through border cell t (0 where nothing does; NaN when no-data enters)
     float entering = 0.0f;
     int ecell = -1;
     if (t < kBorderCells) {
-        const unsigned in_mask = __ldg(f.border_in + tile * kBorderCells + t);
-        if (in_mask) {
-            int rin, cin;
-            border_cell(t, rin, cin);
-            ecell = rin * kTile + cin;
-            u128 src = 0;
-            unsigned m = in_mask;
-            while (m) {
-                const int q = __ffs(m) - 1;
-                m &= m - 1;
-                const int32_t id =
-                    __ldg(f.halo_exit + tile * kHaloSlots + halo_slot_of(rin + nb_dr(q), cin + nb_dc(q)));
-                if (id >= 0) src += to_u128(A[id]);
-            }
-            entering = (src >> 96) ? __int_as_float(0x7fc00000) : fixed128_to_float(src & kValueMask, Fg);
-        }
+        entering = __ldg(f.inflow + tile * kSlotStride + t);
+        int rin, cin;
+        border_cell(t, rin, cin);
+        ecell = rin * kTile + cin;
     }
     // over what enters: NaN anywhere, the float sum, and the smallest positive bits minus one
     const bool enan = isnan(entering);
@@ -1245,6 +1279,7 @@ int tile_core_build(TopologyCore* core, cudaStream_t stream)
     uint32_t *size = nullptr, *acc = nullptr;
     int64_t *D = nullptr, *D2 = nullptr;
     unsigned long long* root_acc = nullptr;
+    int32_t *sc = nullptr, *ec = nullptr;
     int* flag = nullptr;
     std::vector<int32_t> hcount(nt), hbase(nt + 1);
     int rc = 0, herr = 0;
@@ -1356,6 +1391,50 @@ int tile_core_build(TopologyCore* core, cudaStream_t stream)
         rc = fail(LUE_GPU_EINVAL, "tile topology: cycle inside a tile or inconsistent exit forest");
         goto error;
     }
+    // inflow slots: per tile the border cells receiving flow from other tiles, and their upstream exits
+    {
+        std::vector<int32_t> hs(nt), he(nt), sbase(nt + 1), ebase(nt + 1);
+        TRY(cudaMalloc(&sc, nt * sizeof(int32_t)), "slot count");
+        TRY(cudaMalloc(&ec, nt * sizeof(int32_t)), "slot count");
+        k_slot_count<<<blocks_for(nt, 256), 256, 0, stream>>>(nt, tc->border_in, sc, ec);
+        TRY(cudaGetLastError(), "slot count");
+        TRY(cudaMemcpyAsync(hs.data(), sc, nt * sizeof(int32_t), cudaMemcpyDeviceToHost, stream), "slot count");
+        TRY(cudaMemcpyAsync(he.data(), ec, nt * sizeof(int32_t), cudaMemcpyDeviceToHost, stream), "slot count");
+        TRY(cudaStreamSynchronize(stream), "slot count");
+        int64_t a = 0, b = 0;
+        for (int64_t i = 0; i < nt; ++i) {
+            sbase[i] = (int32_t)a;
+            ebase[i] = (int32_t)b;
+            a += hs[i];
+            b += he[i];
+            if (a > INT32_MAX || b > INT32_MAX) {
+                rc = fail(LUE_GPU_ERANGE, "tile topology: too many inflow slots");
+                goto error;
+            }
+        }
+        sbase[nt] = (int32_t)a;
+        ebase[nt] = (int32_t)b;
+        tc->nslot = a;
+        TRY(cudaMemcpyAsync(sc, sbase.data(), nt * sizeof(int32_t), cudaMemcpyHostToDevice, stream), "slot base");
+        TRY(cudaMemcpyAsync(ec, ebase.data(), nt * sizeof(int32_t), cudaMemcpyHostToDevice, stream), "slot base");
+        TRY(cudaMalloc(&tc->slot_at, std::max<int64_t>(a, 1) * sizeof(int32_t)), "slots");
+        TRY(cudaMalloc(&tc->slot_first, (a + 1) * sizeof(int32_t)), "slots");
+        TRY(cudaMalloc(&tc->slot_exit, std::max<int64_t>(b, 1) * sizeof(int32_t)), "slots");
+        TRY(cudaMemcpyAsync(tc->slot_first + a, &ebase[nt], sizeof(int32_t), cudaMemcpyHostToDevice, stream),
+            "slot end");
+        k_slot_fill<<<blocks_for(nt, 256), 256, 0, stream>>>(nt, tc->border_in, tc->halo_exit, sc, ec, tc->slot_at,
+                                                             tc->slot_first, tc->slot_exit, flag);
+        TRY(cudaGetLastError(), "slot fill");
+        TRY(cudaMemcpyAsync(&herr, flag, sizeof(int), cudaMemcpyDeviceToHost, stream), "tile flag");
+        TRY(cudaStreamSynchronize(stream), "slot fill");  // the host vectors must outlive the copies
+        if (herr) {
+            rc = fail(LUE_GPU_EINVAL, "tile topology: an inflow without an upstream exit");
+            goto error;
+        }
+        tc->bytes += a * 8 + 4 + b * 4;
+    }
+    cudaFree(sc);
+    cudaFree(ec);
     cudaFree(bitmap);
     cudaFree(rowpref);
     cudaFree(count);
@@ -1375,6 +1454,8 @@ int tile_core_build(TopologyCore* core, cudaStream_t stream)
     core->tiles = tc;
     return LUE_GPU_OK;
 error:
+    cudaFree(sc);
+    cudaFree(ec);
     cudaFree(bitmap);
     cudaFree(rowpref);
     cudaFree(count);
@@ -1408,6 +1489,9 @@ void tile_core_free(TileCore* tc)
     cudaFree(tc->prev_at);
     cudaFree(tc->exit_span);
     cudaFree(tc->border_in);
+    cudaFree(tc->slot_at);
+    cudaFree(tc->slot_first);
+    cudaFree(tc->slot_exit);
     delete tc;
 }
 
@@ -1418,13 +1502,17 @@ int tile_scratch_alloc(const TileCore* tc, TileScratch* s)
     int rc = 0;
     if ((rc = cuda_status(cudaMalloc(&s->P, E * sizeof(float2)), "tile scratch"))) return rc;
     if ((rc = cuda_status(cudaMalloc(&s->S, E * sizeof(uint4)), "tile scratch"))) return rc;
-    if ((rc = cuda_status(cudaMalloc(&s->A, E * sizeof(uint4)), "tile scratch"))) return rc;
+    if ((rc = cuda_status(cudaMalloc(&s->inflow, tc->ntiles * kSlotStride * sizeof(float)), "tile scratch")))
+        return rc;
+    // slots without inflow are never written: they stay 0
+    if ((rc = cuda_status(cudaMemset(s->inflow, 0, tc->ntiles * kSlotStride * sizeof(float)), "tile scratch")))
+        return rc;
     if ((rc = cuda_status(cudaMalloc(&s->block_sums, nb * sizeof(uint4)), "tile scratch"))) return rc;
     if ((rc = cuda_status(cudaMalloc(&s->total, 2 * sizeof(unsigned long long)), "tile scratch"))) return rc;
     if ((rc = cuda_status(cudaMalloc(&s->block_total, tc->ntiles * sizeof(unsigned long long)), "tile scratch")))
         return rc;
     if ((rc = cuda_status(cudaMalloc(&s->stat, tc->ntiles * sizeof(TileStat)), "tile scratch"))) return rc;
-    s->bytes = E * (8 + 16 + 16) + nb * 16 + 16 + tc->ntiles * (8 + sizeof(TileStat));
+    s->bytes = E * (8 + 16) + nb * 16 + 16 + tc->ntiles * (8 + sizeof(TileStat) + kSlotStride * 4);
     return LUE_GPU_OK;
 }
 
@@ -1432,7 +1520,7 @@ void tile_scratch_free(TileScratch* s)
 {
     cudaFree(s->P);
     cudaFree(s->S);
-    cudaFree(s->A);
+    cudaFree(s->inflow);
     cudaFree(s->block_sums);
     cudaFree(s->total);
     cudaFree(s->block_total);
@@ -1448,7 +1536,7 @@ int tile_accu_f32(const TopologyCore* core, TileScratch* s, const float* ext, fl
 {
     const TileCore* tc = core->tiles;
     TileGeom g{core->rows, core->cols, tc->trows, tc->tcols};
-    const TileForest f{tc->cell_at, tc->prev_at, tc->border_in, tc->halo_exit};
+    const TileForest f{tc->cell_at, tc->prev_at, s->inflow};
     // rows move as float4 when the columns are a multiple of 4 and the arrays 16-byte aligned
     const bool cols4 = (core->cols & 3) == 0;
     const bool vec_in = cols4 && (!ext || (reinterpret_cast<uintptr_t>(ext) & 15) == 0);
@@ -1470,11 +1558,14 @@ int tile_accu_f32(const TopologyCore* core, TileScratch* s, const float* ext, fl
         k_scan_reduce<<<(unsigned)nb, kTileThreads, 0, stream>>>(s->P, E, s->total, s->block_sums);
         k_scan_blocks<<<1, kTileThreads, 0, stream>>>(s->block_sums, nb, s->total);
         k_scan_final<<<(unsigned)nb, kTileThreads, 0, stream>>>(s->P, E, s->total, s->block_sums, s->S);
-        k_exit_sums<<<blocks_for(E, 256), 256, 0, stream>>>(E, tc->exit_pos, tc->exit_start, s->S, s->A, s->total);
+        if (tc->nslot > 0)
+            k_slot_inflow<<<blocks_for(tc->nslot, 256), 256, 0, stream>>>(tc->nslot, tc->slot_at, tc->slot_first,
+                                                                          tc->slot_exit, tc->exit_pos, tc->exit_start,
+                                                                          s->S, s->inflow, s->total);
         count_launches(4);
     }
     k_tile_accu<<<tile_grid, kTileThreads, sizeof(TileCallSmem), stream>>>(g, ext, ext_s, vec_in && vec_out, out, f,
-                                                                           s->A, s->stat, s->total);
+                                                                           s->stat, s->total);
     count_launches(1);
     return cuda_status(cudaGetLastError(), "accu_f32 (tiles)");
 }

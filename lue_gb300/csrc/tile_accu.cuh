@@ -13,8 +13,9 @@
 //      y's subtree of this forest, so an inclusive prefix sum over P in post-order gives every subtree
 //      sum as a difference of two prefix sums.  The sums are exact: 128-bit fixed point (96 value bits,
 //      32 bits counting no-data exits), so summation order cannot change the result.
-//   3. k_tile_accu: one CTA per tile adds to each border cell what enters it from other tiles (the
-//      exact subtree sums of the exits draining into it, rounded to float), takes the same prefix sum
+//   3. k_slot_inflow: per border cell that receives flow from other tiles, the exact sum of the subtree
+//      sums of the exits draining into it, rounded to float once.
+//   4. k_tile_accu: one CTA per tile adds to each border cell what enters it, takes the same prefix sum
 //      over the tile's post-order and writes every cell's result.
 // Pass 1 reads the material and 2 bytes of post-order table per cell; pass 3 the material and 4 bytes of
 // tables, and writes the result.  The prefix sums stay in registers and shared memory.
@@ -78,8 +79,15 @@ struct TileCore {
                                                // (kZeroSlot for a subtree at position 0) | kPrevRidge
     uint32_t* exit_span = nullptr;             // [nexit] scan slots of each exit cell: own | before << 16
     uint8_t* border_in = nullptr;              // [ntiles * kBorderCells] per border cell: outside neighbours draining in
+    // Inflow slots (border cells that receive flow from other tiles), per tile in border order:
+    int64_t nslot = 0;
+    int32_t* slot_at = nullptr;                // [nslot] tile * kSlotStride + border index
+    int32_t* slot_first = nullptr;             // [nslot + 1] first of the slot's upstream exits in slot_exit
+    int32_t* slot_exit = nullptr;              // [slot_first[nslot]] exit ids draining into the slot
     int64_t bytes = 0;
 };
+
+constexpr int kSlotStride = 256;  // inflow values per tile (252 border cells, padded)
 
 // What pass 1 learns about a tile's material (valid cells only), for pass 3.
 struct TileStat {
@@ -92,7 +100,8 @@ struct TileStat {
 struct TileScratch {
     float2* P = nullptr;                       // [nexit] local exit values (hi, lo), post-order
     uint4* S = nullptr;                        // [nexit] inclusive prefix sums (128-bit), post-order
-    uint4* A = nullptr;                        // [nexit] subtree sums (128-bit), exit-id order
+    float* inflow = nullptr;                   // [ntiles * kSlotStride] what enters each border cell (0 where
+                                               // nothing does), float, NaN when no-data enters
     uint4* block_sums = nullptr;               // [scan blocks]
     unsigned long long* total = nullptr;       // [2] material total bound (2^-16 units), fallback flag
     unsigned long long* block_total = nullptr; // [ntiles] per-tile bounds
