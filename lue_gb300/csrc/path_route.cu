@@ -898,76 +898,108 @@ __global__ void PATH_BOUNDS(PER) k_path_free(PathCall p, int64_t p0, int64_t p1)
 }
 
 // Levels whose paths are all short (at most kPathSeqLongest cells; level 0, which holds most cells, at the
-// benchmark sizes): one thread per path, cell after cell from its top to its bottom, with the walk
-// engine's float32 cell rule (rule_f32) on the float-float sum of the upstream outflows (the previous cell
-// of the path, then the light upstream neighbours, which are bottoms of paths of lower levels, in
-// neighbour order), so that every cell gets the walk engine's result bit for bit and no map is composed.
-// A warp takes a range of kPathSeqSpan positions whose ends are moved forward to the next path top, and
-// walks its paths 32 at a time: the paths whose tops lie in the next 32 positions, one per lane; the next
-// group starts where the last of them ends.  Paths stay in the layout's order (by bottom cell), so the
-// cells a warp touches are close together.
+// benchmark sizes): each path is evaluated by one thread, cell after cell from its top to its bottom, with
+// the walk engine's float32 cell rule (rule_f32) on the float-float sum of the upstream outflows (the
+// previous cell of the path, then the light upstream neighbours, which are bottoms of paths of lower
+// levels, in neighbour order), so every cell gets the walk engine's result bit for bit and no map is
+// composed.  A CTA takes a range of positions whose ends are moved forward to the next path top and works
+// through it in windows of at least kPathSeqWindow positions, each ending at a path top: the CTA loads a
+// window's cell indices, inputs and light inflow into shared memory (all loads in flight at once), then
+// every thread walks the paths whose tops fall on its positions of the window in shared memory.  Paths
+// stay in the layout's order (by bottom cell), so the cells a CTA touches are close together.
 constexpr int kPathSeqLongest = 1024;
-constexpr int64_t kPathSeqSpan = 4096;
+constexpr int kPathSeqWindow = 1024;
+constexpr int kPathSeqCap = kPathSeqWindow + kPathSeqLongest;  // positions of the largest window
+constexpr int64_t kPathSeqSpan = 16 * kPathSeqWindow;
+
+template <bool LIGHT>
+struct SeqSmem {
+    int32_t ord[kPathSeqCap];
+    float e[kPathSeqCap], b[kPathSeqCap];
+    float lh[LIGHT ? kPathSeqCap : 1], ll[LIGHT ? kPathSeqCap : 1];
+    uint8_t lnan[LIGHT ? kPathSeqCap : 1];
+    int64_t range[2];
+};
 
 template <Rule R, bool LIGHT>
-__global__ void __launch_bounds__(256) k_path_seq(PathCall p, int64_t p0, int64_t p1)
+__global__ void __launch_bounds__(kPathThreads) k_path_seq(PathCall p, int64_t p0, int64_t p1)
 {
-    const int lane = threadIdx.x & 31;
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t s0 = p0 + warp * kPathSeqSpan;
-    if (s0 >= p1) return;
-    const int64_t lo = warp == 0 ? p0 : next_top(p.order, s0, p1);
-    const int64_t hi = next_top(p.order, min(s0 + kPathSeqSpan, p1), p1);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SeqSmem<LIGHT>& sm = *reinterpret_cast<SeqSmem<LIGHT>*>(smem_raw);
+    const int t = threadIdx.x;
+    const int64_t s0 = p0 + (int64_t)blockIdx.x * kPathSeqSpan;
+    if (t < 32) {
+        const int64_t lo = blockIdx.x == 0 ? p0 : next_top(p.order, s0, p1);
+        const int64_t hi = next_top(p.order, min(s0 + kPathSeqSpan, p1), p1);
+        if (t == 0) {
+            sm.range[0] = lo;
+            sm.range[1] = hi;
+        }
+    }
+    __syncthreads();
+    const int64_t lo = sm.range[0], hi = sm.range[1];
+    __syncthreads();
     for (int64_t g = lo; g < hi;) {
-        // the paths whose tops lie in positions g .. g + 31: lane l takes the one at g + l, if any
-        const int64_t q0 = g + lane;
-        const bool mine = q0 < hi && __ldg(p.order + q0) < 0;
-        int64_t end = g;  // one past the last position of this lane's path
-        if (mine) {
+        if (t < 32) {  // the window ends at the first path top at least kPathSeqWindow positions on
+            const int64_t w = next_top(p.order, min(g + kPathSeqWindow, hi), hi);
+            if (t == 0) sm.range[1] = w;
+        }
+        __syncthreads();
+        const int64_t wend = sm.range[1];
+        const int n = (int)(wend - g);  // <= kPathSeqCap: paths of these levels are short
+        for (int i = t; i < n; i += kPathThreads) {
+            const int32_t w = __ldg(p.order + g + i);
+            const int64_t c = (int64_t)(w & 0x7fffffff);
+            sm.ord[i] = w;
+            sm.e[i] = value_at(p.a, p.as, c);
+            sm.b[i] = value_at(p.b, p.bs, c);
+            if (LIGHT) {
+                FF s{0.0f, 0.0f};
+                bool nan = false;
+                for (unsigned lm = __ldg(p.light + g + i); lm; lm &= lm - 1) {
+                    const int k = __ffs(lm) - 1;
+                    const int64_t u = c + nb_dr(k) * p.cols + nb_dc(k);
+                    const float vh = p.out[u];
+                    if (isnan(vh)) nan = true;
+                    else s.add(vh, p.lo[u]);
+                }
+                sm.lh[i] = s.hi;
+                sm.ll[i] = s.lo;
+                sm.lnan[i] = nan;
+            }
+        }
+        __syncthreads();
+        for (int i0 = t; i0 < n; i0 += kPathThreads) {
+            if (sm.ord[i0] >= 0) continue;  // not a path top
             FF x{0.0f, 0.0f};
             bool nan_in = false;
-            int64_t q = q0;
-            int32_t w = __ldg(p.order + q);
-            for (;;) {
-                const int64_t c = (int64_t)(w & 0x7fffffff);
-                const int64_t qn = q + 1;
-                const int32_t wn = qn < hi ? __ldg(p.order + qn) : -1;  // -1: as if a top followed
-                const float e = value_at(p.a, p.as, c), b = value_at(p.b, p.bs, c);
-                FF t = x;
+            for (int i = i0;;) {
+                const int64_t c = (int64_t)(sm.ord[i] & 0x7fffffff);
+                FF tt = x;
                 bool nan = nan_in;
                 if (LIGHT) {
-                    for (unsigned lm = __ldg(p.light + q); lm; lm &= lm - 1) {
-                        const int k = __ffs(lm) - 1;
-                        const int64_t u = c + nb_dr(k) * p.cols + nb_dc(k);
-                        const float vh = load_cg(p.out + u);
-                        if (isnan(vh)) nan = true;
-                        else t.add(vh, load_cg(p.lo + u));
-                    }
+                    if (sm.lnan[i]) nan = true;
+                    else if (sm.lh[i] != 0.0f || sm.ll[i] != 0.0f) tt.add(sm.lh[i], sm.ll[i]);
                 }
                 float oh = 0.0f, ol = 0.0f, rem = 0.0f;
-                if (!rule_f32<R>(t, nan, e, b, oh, ol, rem)) {
+                if (!rule_f32<R>(tt, nan, sm.e[i], sm.b[i], oh, ol, rem)) {
                     oh = __int_as_float(0x7fc00000);
                     ol = 0.0f;
                     rem = oh;
                 }
                 p.out[c] = oh;
                 p.rem[c] = rem;
-                if (wn < 0) {  // a path bottom: its residual is read as light inflow by higher levels
+                if (i + 1 >= n || sm.ord[i + 1] < 0) {  // a path bottom: its residual is read as light inflow
                     p.lo[c] = ol;
-                    end = qn;
                     break;
                 }
                 x = FF{oh, ol};
                 nan_in = isnan(oh);
-                q = qn;
-                w = wn;
+                ++i;
             }
         }
-        // the next group starts after the last path that started in this one (none: the next top)
-        int64_t next = end;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) next = max(next, __shfl_xor_sync(0xffffffffu, next, o));
-        g = next > g ? next : next_top(p.order, g + 32, hi);
+        __syncthreads();
+        g = wend;
     }
 }
 
@@ -1043,6 +1075,17 @@ int path_prepare(lue_gpu_topology* t, cudaStream_t stream)
     return path_core_get(t, stream, &pc);
 }
 
+template <Rule R>
+static bool path_seq_smem_ok()
+{
+    static const bool ok =
+        cudaFuncSetAttribute(k_path_seq<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(SeqSmem<true>)) == cudaSuccess &&
+        cudaFuncSetAttribute(k_path_seq<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(SeqSmem<false>)) == cudaSuccess;
+    return ok;
+}
+
 template <Rule R, int K>
 static int path_run(lue_gpu_topology* t, const PathCore* pc, const float* a, float as, const float* b, float bs,
                     float* out, float* rem, cudaStream_t stream, const char* what)
@@ -1068,6 +1111,7 @@ static int path_run(lue_gpu_topology* t, const PathCore* pc, const float* a, flo
     if (const char* e = getenv("LUE_GB300_PATH_FREE_LONGEST")) free_longest = std::max(0, atoi(e));
     if (const char* e = getenv("LUE_GB300_PATH_POLLS")) polls = std::max(0, atoi(e));
     PMap* aggm = static_cast<PMap*>(t->path_maps);
+    if (!path_seq_smem_ok<R>()) return fail(LUE_GPU_ECUDA, std::string(what) + ": shared memory attribute");
     int launches = 1;
     for (int l = 0; l < levels; ++l) {
         const int64_t p0 = pc->level_offsets[l], p1 = pc->level_offsets[l + 1];
@@ -1080,11 +1124,10 @@ static int path_run(lue_gpu_topology* t, const PathCore* pc, const float* a, flo
                 return rc;
         }
         const dim3 grid((unsigned)nt);
-        if (pc->level_longest[l] <= seq_longest) {  // one thread per path
-            const int64_t warps = (p1 - p0 + kPathSeqSpan - 1) / kPathSeqSpan;
-            const dim3 gs((unsigned)((warps + 7) / 8));
-            if (l > 0) k_path_seq<R, true><<<gs, 256, 0, stream>>>(p, p0, p1);
-            else k_path_seq<R, false><<<gs, 256, 0, stream>>>(p, p0, p1);
+        if (pc->level_longest[l] <= std::min(seq_longest, kPathSeqLongest)) {  // one thread per path
+            const dim3 gs((unsigned)((p1 - p0 + kPathSeqSpan - 1) / kPathSeqSpan));
+            if (l > 0) k_path_seq<R, true><<<gs, kPathThreads, sizeof(SeqSmem<true>), stream>>>(p, p0, p1);
+            else k_path_seq<R, false><<<gs, kPathThreads, sizeof(SeqSmem<false>), stream>>>(p, p0, p1);
             ++launches;
             continue;
         }
