@@ -61,6 +61,21 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def profile_value(key, kernel):
+    """The numbers of a committed ncu summary line '<key> <kernel> <v1> <v2> ...' (None if absent)."""
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return None
+    for name in sorted(os.listdir(d)):
+        if not name.endswith((".md", ".txt")):
+            continue
+        for line in open(os.path.join(d, name)):
+            parts = line.strip().strip("`").split()
+            if len(parts) >= 3 and parts[0] == key and parts[1] == kernel:
+                return [float(x) for x in parts[2:]], name
+    return None
+
+
 def profile_traffic(kernel):
     """Per-launch DRAM bytes of `kernel` from a committed ncu summary line
     'traffic_per_launch <kernel> <bytes> <units_per_launch>'; scaled to a launch of this workload."""
@@ -609,6 +624,27 @@ def bench_kinematic_wave(args, dev):
                  "tuner_ms_of_best": round(best["ms"], 3), "tuning_s": round(tune_s, 2),
                  "ms_per_step": round(1000 * s_multi / T, 3)}
     finite = torch.isfinite(out.data)
+    # compute roofline of the multi-step kernel: warp instructions per cell step (ncu, the same 8192^2 x
+    # 100-step call) x cell steps per second, against the SM issue peak (4 warp instructions per cycle per
+    # SM) at the maximum SM clock
+    compute = None
+    ipcs = profile_value("warp_instructions_per_cell_step", "k_stage_flow_kw")
+    if ipcs is not None:
+        props = torch.cuda.get_device_properties(dev)
+        mhz = 2070.0
+        path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+        if os.path.exists(path):
+            mhz = float(json.load(open(path)).get("sm_max_mhz", mhz))
+        peak_issue = props.multi_processor_count * 4 * mhz * 1e6
+        achieved_issue = ipcs[0][0] * n * T / s_multi
+        fma = profile_value("fma_pipe_pct", "k_stage_flow_kw")
+        compute = {"bound": "instruction issue", "unit": "warp instructions/s",
+                   "achieved": round(achieved_issue, 1), "peak": round(peak_issue, 1),
+                   "frac": round(achieved_issue / peak_issue, 4),
+                   "warp_instructions_per_cell_step": ipcs[0][0],
+                   "fma_pipe_pct_of_active": fma[0][0] if fma else None,
+                   "peak_note": f"{props.multi_processor_count} SMs x 4 warp instructions per cycle at {mhz:g} MHz",
+                   "source": ipcs[1]}
     accuracy = None
     if not args.skip_accuracy:
         try:
@@ -619,7 +655,7 @@ def bench_kinematic_wave(args, dev):
             "accuracy": accuracy,
             "steps": T, "ms_per_step": round(1000 * s_multi / T, 3),
             "value": round(n * T / s_multi / 1e6, 3), "unit": "Mcells/s",
-            "roofline_frac_hbm": round(KW_BYTES_PER_CELL * n * T / s_multi / 1e9 / peaks()[0], 4),
+            "compute_roofline": compute,
             "default_schedule": {"schedule": default_schedule, "ms_per_step": round(1000 * s_default / T, 3)},
             "autotuned": tuned,
             "timed_schedule": "autotuned (lue_gpu_autotune_stage_schedule)" if tuned else "default",
@@ -627,8 +663,9 @@ def bench_kinematic_wave(args, dev):
             "single_step_call_mcells_per_s": round(n / s_single / 1e6, 3),
             "engine": "stage engine, pipelined steps, float-float solve in y = Q^(1/5) "
                       "(lue_gpu_kinematic_wave_steps_f64_f32in)",
-            "roofline_note": "all steps run in one call: the discharge stays in shared memory between steps, so "
-                             "the 25 B/cell-step HBM figure is the per-call drop-in's traffic, not this kernel's",
+            "roofline_note": "all steps run in one call with the discharge in shared memory between steps: the "
+                             "kernel is bound by instruction issue, not HBM, so its roofline is the issue rate",
+            "single_step_roofline_frac_hbm": round(KW_BYTES_PER_CELL * n / s_single / 1e9 / peaks()[0], 4),
             "longest_flow_path_cells": fd.topology().stats()["max_level"] + 1,
             "outflow_finite_cells": int(finite.sum())}
 

@@ -897,112 +897,6 @@ __global__ void PATH_BOUNDS(PER) k_path_free(PathCall p, int64_t p0, int64_t p1)
     }
 }
 
-// Levels whose paths are all short (at most kPathSeqLongest cells; level 0, which holds most cells, at the
-// benchmark sizes): each path is evaluated by one thread, cell after cell from its top to its bottom, with
-// the walk engine's float32 cell rule (rule_f32) on the float-float sum of the upstream outflows (the
-// previous cell of the path, then the light upstream neighbours, which are bottoms of paths of lower
-// levels, in neighbour order), so every cell gets the walk engine's result bit for bit and no map is
-// composed.  A CTA takes a range of positions whose ends are moved forward to the next path top and works
-// through it in windows of at least kPathSeqWindow positions, each ending at a path top: the CTA loads a
-// window's cell indices, inputs and light inflow into shared memory (all loads in flight at once), then
-// every thread walks the paths whose tops fall on its positions of the window in shared memory.  Paths
-// stay in the layout's order (by bottom cell), so the cells a CTA touches are close together.
-constexpr int kPathSeqLongest = 1024;
-constexpr int kPathSeqWindow = 1024;
-constexpr int kPathSeqCap = kPathSeqWindow + kPathSeqLongest;  // positions of the largest window
-constexpr int64_t kPathSeqSpan = 16 * kPathSeqWindow;
-
-template <bool LIGHT>
-struct SeqSmem {
-    int32_t ord[kPathSeqCap];
-    float e[kPathSeqCap], b[kPathSeqCap];
-    float lh[LIGHT ? kPathSeqCap : 1], ll[LIGHT ? kPathSeqCap : 1];
-    uint8_t lnan[LIGHT ? kPathSeqCap : 1];
-    int64_t range[2];
-};
-
-template <Rule R, bool LIGHT>
-__global__ void __launch_bounds__(kPathThreads) k_path_seq(PathCall p, int64_t p0, int64_t p1)
-{
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    SeqSmem<LIGHT>& sm = *reinterpret_cast<SeqSmem<LIGHT>*>(smem_raw);
-    const int t = threadIdx.x;
-    const int64_t s0 = p0 + (int64_t)blockIdx.x * kPathSeqSpan;
-    if (t < 32) {
-        const int64_t lo = blockIdx.x == 0 ? p0 : next_top(p.order, s0, p1);
-        const int64_t hi = next_top(p.order, min(s0 + kPathSeqSpan, p1), p1);
-        if (t == 0) {
-            sm.range[0] = lo;
-            sm.range[1] = hi;
-        }
-    }
-    __syncthreads();
-    const int64_t lo = sm.range[0], hi = sm.range[1];
-    __syncthreads();
-    for (int64_t g = lo; g < hi;) {
-        if (t < 32) {  // the window ends at the first path top at least kPathSeqWindow positions on
-            const int64_t w = next_top(p.order, min(g + kPathSeqWindow, hi), hi);
-            if (t == 0) sm.range[1] = w;
-        }
-        __syncthreads();
-        const int64_t wend = sm.range[1];
-        const int n = (int)(wend - g);  // <= kPathSeqCap: paths of these levels are short
-        for (int i = t; i < n; i += kPathThreads) {
-            const int32_t w = __ldg(p.order + g + i);
-            const int64_t c = (int64_t)(w & 0x7fffffff);
-            sm.ord[i] = w;
-            sm.e[i] = value_at(p.a, p.as, c);
-            sm.b[i] = value_at(p.b, p.bs, c);
-            if (LIGHT) {
-                FF s{0.0f, 0.0f};
-                bool nan = false;
-                for (unsigned lm = __ldg(p.light + g + i); lm; lm &= lm - 1) {
-                    const int k = __ffs(lm) - 1;
-                    const int64_t u = c + nb_dr(k) * p.cols + nb_dc(k);
-                    const float vh = p.out[u];
-                    if (isnan(vh)) nan = true;
-                    else s.add(vh, p.lo[u]);
-                }
-                sm.lh[i] = s.hi;
-                sm.ll[i] = s.lo;
-                sm.lnan[i] = nan;
-            }
-        }
-        __syncthreads();
-        for (int i0 = t; i0 < n; i0 += kPathThreads) {
-            if (sm.ord[i0] >= 0) continue;  // not a path top
-            FF x{0.0f, 0.0f};
-            bool nan_in = false;
-            for (int i = i0;;) {
-                const int64_t c = (int64_t)(sm.ord[i] & 0x7fffffff);
-                FF tt = x;
-                bool nan = nan_in;
-                if (LIGHT) {
-                    if (sm.lnan[i]) nan = true;
-                    else if (sm.lh[i] != 0.0f || sm.ll[i] != 0.0f) tt.add(sm.lh[i], sm.ll[i]);
-                }
-                float oh = 0.0f, ol = 0.0f, rem = 0.0f;
-                if (!rule_f32<R>(tt, nan, sm.e[i], sm.b[i], oh, ol, rem)) {
-                    oh = __int_as_float(0x7fc00000);
-                    ol = 0.0f;
-                    rem = oh;
-                }
-                p.out[c] = oh;
-                p.rem[c] = rem;
-                if (i + 1 >= n || sm.ord[i + 1] < 0) {  // a path bottom: its residual is read as light inflow
-                    p.lo[c] = ol;
-                    break;
-                }
-                x = FF{oh, ol};
-                nan_in = isnan(oh);
-                ++i;
-            }
-        }
-        __syncthreads();
-        g = wend;
-    }
-}
-
 __global__ void k_path_no_data(const uint8_t* fd, int64_t n, float* out, float* rem)
 {
     for (int64_t i = grid_stride_begin(); i < n; i += grid_stride())
@@ -1075,17 +969,6 @@ int path_prepare(lue_gpu_topology* t, cudaStream_t stream)
     return path_core_get(t, stream, &pc);
 }
 
-template <Rule R>
-static bool path_seq_smem_ok()
-{
-    static const bool ok =
-        cudaFuncSetAttribute(k_path_seq<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)sizeof(SeqSmem<true>)) == cudaSuccess &&
-        cudaFuncSetAttribute(k_path_seq<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)sizeof(SeqSmem<false>)) == cudaSuccess;
-    return ok;
-}
-
 template <Rule R, int K>
 static int path_run(lue_gpu_topology* t, const PathCore* pc, const float* a, float as, const float* b, float bs,
                     float* out, float* rem, cudaStream_t stream, const char* what)
@@ -1102,16 +985,13 @@ static int path_run(lue_gpu_topology* t, const PathCore* pc, const float* a, flo
     if (int rc = cuda_status(cudaMemsetAsync(tickets, 0, kPathMaxLevels * sizeof(int), stream), what)) return rc;
     k_path_no_data<<<grid_for(n, 256), 256, 0, stream>>>(core->fd, n, out, rem);
     PathCall p{pc->order, pc->light, a, as, b, bs, out, rem, t->lo, t->path_flag, core->cols};
-    // test hooks: LUE_GB300_PATH_SEQ_LONGEST (levels with longer paths are scanned; 0: every level),
-    // LUE_GB300_PATH_FREE_LONGEST (levels with longer paths use the look-back scan; 0: every
+    // test hooks: LUE_GB300_PATH_FREE_LONGEST (levels with longer paths use the look-back scan; 0: every
     // level) and LUE_GB300_PATH_POLLS (poll limit of a look-back wait; 0: every wait gives up at once,
     // and the walk engine redoes the call)
-    int free_longest = kPathFreeLongest, polls = kPathPolls, seq_longest = kPathSeqLongest;
-    if (const char* e = getenv("LUE_GB300_PATH_SEQ_LONGEST")) seq_longest = std::max(0, atoi(e));
+    int free_longest = kPathFreeLongest, polls = kPathPolls;
     if (const char* e = getenv("LUE_GB300_PATH_FREE_LONGEST")) free_longest = std::max(0, atoi(e));
     if (const char* e = getenv("LUE_GB300_PATH_POLLS")) polls = std::max(0, atoi(e));
     PMap* aggm = static_cast<PMap*>(t->path_maps);
-    if (!path_seq_smem_ok<R>()) return fail(LUE_GPU_ECUDA, std::string(what) + ": shared memory attribute");
     int launches = 1;
     for (int l = 0; l < levels; ++l) {
         const int64_t p0 = pc->level_offsets[l], p1 = pc->level_offsets[l + 1];
@@ -1124,13 +1004,6 @@ static int path_run(lue_gpu_topology* t, const PathCore* pc, const float* a, flo
                 return rc;
         }
         const dim3 grid((unsigned)nt);
-        if (pc->level_longest[l] <= std::min(seq_longest, kPathSeqLongest)) {  // one thread per path
-            const dim3 gs((unsigned)((p1 - p0 + kPathSeqSpan - 1) / kPathSeqSpan));
-            if (l > 0) k_path_seq<R, true><<<gs, kPathThreads, sizeof(SeqSmem<true>), stream>>>(p, p0, p1);
-            else k_path_seq<R, false><<<gs, kPathThreads, sizeof(SeqSmem<false>), stream>>>(p, p0, p1);
-            ++launches;
-            continue;
-        }
         if (pc->level_longest[l] <= free_longest) {  // CTAs cut at path tops: no waits
             const int64_t nf = (p1 - p0 + kPathThreads * per - 1) / (kPathThreads * per);
             const dim3 gf((unsigned)nf);

@@ -856,42 +856,6 @@ static size_t flow_smem(int64_t cells, int64_t inputs, int64_t producers)
            producers * (sizeof(int2) + sizeof(int)) + 32;  // + alignment
 }
 
-// One-step calls: a history entry still holding kHistUnset has not been written.  The history is set to
-// it before the launch; an exit's 8-byte value is its own ready flag (written once, read whole), so a stage
-// waits for exactly the inputs of its next round instead of for its producers' last rounds.
-constexpr unsigned long long kHistUnset = ~0ull;
-
-__device__ __forceinline__ unsigned long long ld_relaxed_u64(const uint2* p)
-{
-    unsigned long long v;
-    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ void st_relaxed_u64(uint2* p, unsigned long long v)
-{
-    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-__device__ __forceinline__ uint2 u64_to_uint2(unsigned long long v)
-{
-    return make_uint2((unsigned)v, (unsigned)(v >> 32));
-}
-
-// The input at p once written (`v`: a value read before, kHistUnset if not yet); gives up after `polls`
-// polls (setting *error) or once another wait has given up.
-__device__ __forceinline__ uint2 hist_wait(const uint2* p, unsigned long long v, int* error, int polls)
-{
-    for (int it = 0; v == kHistUnset && it < polls; ++it) {
-        if (*((volatile int*)error)) return make_uint2(0u, 0u);
-        __nanosleep(32);
-        v = ld_relaxed_u64(p);
-    }
-    if (v == kHistUnset) {
-        atomicExch(error, 1);
-        return make_uint2(0u, 0u);
-    }
-    return u64_to_uint2(v);
-}
-
 // Waits until every producer has published the steps that round r consumes (round r consumes step
 // r - round(c) at cell c): each thread waits for its share of the producers.
 template <int NT>
@@ -908,12 +872,11 @@ __device__ __forceinline__ void flow_wait_round(const StageFlowArgs& f, const in
 constexpr int kFlowPrefetch = 2;  // inputs per thread loaded one round ahead into registers
 
 // A Rule supplies the per-cell state (Cell, kept in shared memory by position), the accumulator of the
-// upstream outflows (Acc), the cell step and the final store.  ONE (a call of one step): the inputs of
-// round r + 1 are read while round r computes, and only those not yet written are waited for (each history
-// entry is its own ready flag), so a stage follows its producers' exits, not their last rounds.  With
-// many steps, round r waits for the producers' published progress of the steps round r + 1 reads and
-// loads those inputs into registers before its own cells, and puts them into shared memory after them, so
-// that their load overlaps the round's arithmetic.
+// upstream outflows (Acc), the cell step and the final store.  ONE (a call of one step): the stage first
+// waits for all its producers and loads all its inputs into shared memory at once, so that its rounds
+// read shared memory only.  With many steps, round r waits for the inputs of round r + 1 and loads them
+// into registers before its own cells, and puts them into shared memory after them, so that their load
+// overlaps the round's arithmetic.
 template <class R, int NT, bool ONE>
 __global__ void __launch_bounds__(NT) k_stage_flow(StageRunArgs a, StageFlowArgs f, R rule)
 {
@@ -963,35 +926,22 @@ __global__ void __launch_bounds__(NT) k_stage_flow(StageRunArgs a, StageFlowArgs
     if (threadIdx.x == 0) L.rstart[rounds] = (uint16_t)count;
     const int max_exit = __ldg(f.max_exit_round + k);
     if (f.trace && threadIdx.x == 0) f.trace[4 * k + 1] = global_ns();
-    // the inputs of round 0
-    if (!ONE) flow_wait_round<NT>(f, L.prod, L.have, np, ns, 0);
+    // the inputs of round 0 (ONE: of every round)
+    flow_wait_round<NT>(f, L.prod, L.have, np, ns, ONE ? ns + rounds : 0);
     if (k == f.stuck && threadIdx.x == 0) flow_wait(f.progress + k, ns + 1, f.error, f.polls);
     __syncthreads();
-    {
-        const int s_hi = rounds > 1 ? (int)(L.meta[L.rstart[1]].y >> 16) : nin;
-        for (int s = threadIdx.x; s < s_hi; s += NT) {
-            const uint2* src = a.hist + (int64_t)L.in_rows[s] * ns;
-            L.in_vals[s] = ONE ? hist_wait(src, ld_relaxed_u64(src), f.error, f.polls) : __ldcg(src);
-        }
-    }
     if (f.trace && threadIdx.x == 0) s_wait += global_ns() - f.trace[4 * k + 1];
+    {
+        const int s_hi = ONE ? nin : (rounds > 1 ? (int)(L.meta[L.rstart[1]].y >> 16) : nin);
+        for (int s = threadIdx.x; s < s_hi; s += NT) L.in_vals[s] = __ldcg(a.hist + (int64_t)L.in_rows[s] * ns);
+    }
     const int nrounds = rounds + ns - 1;
     int published = 0;
     for (int r = 0; r < nrounds; ++r) {
         // the inputs of round r + 1: wait, then load into registers
         uint2 pv[kFlowPrefetch];
         int s_lo = 0, s_hi = 0;
-        if (ONE && r + 1 < nrounds) {  // the inputs of round r + 1, as they are now (kHistUnset: not yet)
-            __syncthreads();
-            const int lo = L.rstart[r + 1], hi = L.rstart[min(rounds, r + 2)];
-            s_lo = (int)(L.meta[lo].y >> 16);
-            s_hi = hi < count ? (int)(L.meta[hi].y >> 16) : nin;
-#pragma unroll
-            for (int j = 0; j < kFlowPrefetch; ++j) {
-                const int s = s_lo + (int)threadIdx.x + j * NT;
-                if (s < s_hi) pv[j] = u64_to_uint2(ld_relaxed_u64(a.hist + L.in_rows[s]));
-            }
-        } else if (!ONE && r + 1 < nrounds) {
+        if (!ONE && r + 1 < nrounds) {
             if (f.trace && threadIdx.x == 0) s_wait -= global_ns();
             flow_wait_round<NT>(f, L.prod, L.have, np, ns, r + 1);
             __syncthreads();
@@ -1027,17 +977,10 @@ __global__ void __launch_bounds__(NT) k_stage_flow(StageRunArgs a, StageFlowArgs
                                                   : Qt[L.local[p + nb_dr(q) * kStageSide + nb_dc(q)]];
                 rule.add(acc, v);
             }
-            uint2 o = rule.step(L.cells[i], acc, (row0 + (p >> 5)) * a.cols + col0 + (p & 31), t);
+            const uint2 o = rule.step(L.cells[i], acc, (row0 + (p >> 5)) * a.cols + col0 + (p & 31), t);
             Qt[i] = o;
             const int32_t e = L.ex[i];
-            if (e >= 0) {
-                if (ONE) {
-                    if (o.x == 0xFFFFFFFFu && o.y == 0xFFFFFFFFu) o = make_uint2(0u, 0x7ff80000u);  // a NaN, not unset
-                    st_relaxed_u64(a.hist + e, ((unsigned long long)o.y << 32) | o.x);
-                } else {
-                    __stcg(a.hist + (int64_t)e * ns + t, o);
-                }
-            }
+            if (e >= 0) __stcg(a.hist + (int64_t)e * ns + t, o);
         }
         // The barrier orders every thread's history writes before thread 0's release, which makes them
         // visible at GPU scope before the progress that announces them (the pattern of a grid barrier).
@@ -1048,21 +991,6 @@ __global__ void __launch_bounds__(NT) k_stage_flow(StageRunArgs a, StageFlowArgs
             if (prog > published && (prog - published >= f.publish_every || prog == ns)) {
                 st_release(f.progress + k, prog);
                 published = prog;
-            }
-        }
-        if (ONE && r + 1 < nrounds) {  // round r + 1's inputs: those read as unset are waited for
-#pragma unroll
-            for (int j = 0; j < kFlowPrefetch; ++j) {
-                const int s = s_lo + (int)threadIdx.x + j * NT;
-                if (s < s_hi) {
-                    const uint2* src = a.hist + L.in_rows[s];
-                    const unsigned long long v = ((unsigned long long)pv[j].y << 32) | pv[j].x;
-                    L.in_vals[s] = hist_wait(src, v, f.error, f.polls);
-                }
-            }
-            for (int s = s_lo + (int)threadIdx.x + kFlowPrefetch * NT; s < s_hi; s += NT) {
-                const uint2* src = a.hist + L.in_rows[s];
-                L.in_vals[s] = hist_wait(src, ld_relaxed_u64(src), f.error, f.polls);
             }
         }
         if (!ONE && r + 1 < nrounds) {
@@ -1563,12 +1491,6 @@ static int stage_run(lue_gpu_topology* t, const StageCore* sc, const R& rule, in
     int* ticket = progress + sc->nstages;
     int* error = ticket + 1;
     if (int rc = cuda_status(cudaMemsetAsync(progress, 0, flow, stream), what)) return rc;
-    if (steps == 1) {  // one step: every exit's entry starts unset (kHistUnset)
-        if (int rc = cuda_status(cudaMemsetAsync(t->stage_hist, 0xFF, (size_t)std::max<int64_t>(sc->nexits, 1) *
-                                                                         sizeof(uint2), stream),
-                                 what))
-            return rc;
-    }
     StageRunArgs a{sc->stage, sc->wave_stage, sc->meta, sc->exit_id, sc->inputs, core->rows, core->cols, sc->tcols,
                    steps, t->stage_hist};
     StageFlowArgs fa{sc->prod_offsets, sc->prod, sc->max_exit_round, progress, ticket, error, sc->nstages,

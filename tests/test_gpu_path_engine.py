@@ -172,10 +172,8 @@ def test_prepare_builds_the_paths(lfr):
 
 @pytest.mark.parametrize("op", OPS)
 def test_look_back_scan_on_every_level(lfr, monkeypatch, op):
-    """LUE_GB300_PATH_SEQ_LONGEST=0 and LUE_GB300_PATH_FREE_LONGEST=0 send every level through the
-    decoupled look-back scan (used on levels of long paths), here on a raster of short ones with no-data
-    holes and NaN material."""
-    monkeypatch.setenv("LUE_GB300_PATH_SEQ_LONGEST", "0")
+    """LUE_GB300_PATH_FREE_LONGEST=0 sends every level through the decoupled look-back scan (used on
+    levels of long paths), here on a raster of short ones with no-data holes and NaN material."""
     monkeypatch.setenv("LUE_GB300_PATH_FREE_LONGEST", "0")
     fd, rng = _raster(700, 900, seed=83, holes=0.001)
     m = rng.lognormal(0.0, 1.0, fd.shape).astype(np.float32)
@@ -194,11 +192,9 @@ def test_look_back_waits_that_give_up_are_redone_by_the_walk_engine(lfr, monkeyp
     fd, rng = _raster(500, 600, seed=85, holes=0.001)
     m = rng.lognormal(0.0, 1.0, fd.shape).astype(np.float32)
     b = _other(rng, fd.shape, "threshold")
-    monkeypatch.setenv("LUE_GB300_PATH_SEQ_LONGEST", "0")
     monkeypatch.setenv("LUE_GB300_PATH_FREE_LONGEST", "0")
     monkeypatch.setenv("LUE_GB300_PATH_POLLS", "0")
     got = _run(lfr, "threshold", fd, m, b, fd.shape)
-    monkeypatch.delenv("LUE_GB300_PATH_SEQ_LONGEST")
     monkeypatch.delenv("LUE_GB300_PATH_FREE_LONGEST")
     monkeypatch.delenv("LUE_GB300_PATH_POLLS")
     walk = _run(lfr, "threshold", fd, m, b, fd.shape, engine="walk", monkeypatch=monkeypatch)
@@ -207,33 +203,3 @@ def test_look_back_waits_that_give_up_are_redone_by_the_walk_engine(lfr, monkeyp
     again = _run(lfr, "threshold", fd, m, b, fd.shape)  # the next call is a normal one
     for g, w in zip(again, walk):
         parity.assert_close32(g, w.astype(np.float64), "after a call that gave up")
-
-
-@pytest.mark.parametrize("op", OPS)
-def test_one_thread_per_path_agrees_with_the_walk_engine(lfr, monkeypatch, op):
-    """Levels of short paths run one thread per path with the walk engine's float32 cell rule on
-    float-float sums (the light inflow of a cell summed before the heavy one is added, so not bit for bit
-    where a cell has light upstream neighbours): with every level of short paths sent there
-    (LUE_GB300_PATH_SEQ_LONGEST large) the results agree with the walk engine to float-float rounding, on a
-    raster with no-data holes, NaN and negative material; with none sent there (0), the scans agree with
-    the oracle."""
-    fd, rng = _raster(300, 400, seed=87, holes=0.001)
-    m = rng.lognormal(0.0, 1.0, fd.shape).astype(np.float32)
-    m[rng.random(fd.shape) < 0.001] = np.nan
-    m[rng.random(fd.shape) < 0.001] = -1.0
-    b = _other(rng, fd.shape, op)
-    walk = _run(lfr, op, fd, m, b, (100, 200), engine="walk", monkeypatch=monkeypatch)
-    monkeypatch.setenv("LUE_GB300_PATH_SEQ_LONGEST", "1000000000")
-    seq = _run(lfr, op, fd, m, b, (100, 200))
-    monkeypatch.setenv("LUE_GB300_PATH_SEQ_LONGEST", "0")
-    scan = _run(lfr, op, fd, m, b, (100, 200))
-    monkeypatch.delenv("LUE_GB300_PATH_SEQ_LONGEST")
-    _, cpu = _ops(lfr, op)
-    want = cpu(fd, m.astype(np.float64), b.astype(np.float64), (100, 200), dtype=np.float64)
-    for g, w, name in zip(seq, walk, ("outflow", "remainder")):
-        assert np.array_equal(np.isnan(g), np.isnan(w))
-        assert parity.rel_error(g, w.astype(np.float64), parity.FLOOR32)[0] <= 1e-6, f"{op} {name}"
-    for g, w, name in zip(seq, want, ("outflow", "remainder")):
-        parity.assert_close32(g, w, f"{op} {name}, one thread per path")
-    for g, w, name in zip(scan, want, ("outflow", "remainder")):
-        parity.assert_close32(g, w, f"{op} {name}, scans on every level")
