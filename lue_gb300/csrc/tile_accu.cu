@@ -555,14 +555,18 @@ __global__ void __launch_bounds__(kTileThreads)
         }
         __syncthreads();
     }
-    // positions, checked distinct (every position 0 .. 4095 once), and the tables by position
+    // positions, checked distinct (every position 0 .. 4095 once), the first positions of the roots'
+    // subtrees (segment heads), then the tables by position
     const int64_t T = tile * kRunPositions;
     uint32_t* seen = reinterpret_cast<uint32_t*>(sm.queue);  // the queue is no longer read
-    for (int w = t; w < kRunPositions / 32; w += kTileThreads) seen[w] = 0;
+    uint32_t* heads = seen + kRunPositions / 32;
+    for (int w = t; w < kRunPositions / 32; w += kTileThreads) {
+        seen[w] = 0;
+        heads[w] = 0;
+    }
     __syncthreads();
     for (int i = t; i < kTileCells; i += kTileThreads) {
-        const int rin = i >> 6, cin = i & 63;
-        const bool valid = sm.fd[rin + 1][cin + 1] != kNoData;
+        const bool valid = sm.fd[(i >> 6) + 1][(i & 63) + 1] != kNoData;
         const int s0 = st[i], p = s0 + sz[i] - 1;
         bool bad = p >= kRunPositions || s0 > p;
         if (!bad) bad = (atomicOr(&seen[p >> 5], 1u << (p & 31)) >> (p & 31)) & 1u;
@@ -570,7 +574,15 @@ __global__ void __launch_bounds__(kTileThreads)
             *error = 1;
             continue;
         }
-        cell_at[T + run_table_index(p)] = (uint16_t)(i | (valid ? 0u : kNoValue));
+        if (!valid || sm.dsl[i] == kNoCell) atomicOr(&heads[s0 >> 5], 1u << (s0 & 31));
+    }
+    __syncthreads();
+    for (int i = t; i < kTileCells; i += kTileThreads) {
+        const bool valid = sm.fd[(i >> 6) + 1][(i & 63) + 1] != kNoData;
+        const int s0 = st[i], p = s0 + sz[i] - 1;
+        if (p >= kRunPositions || s0 > p) continue;  // reported above
+        const bool head = (heads[p >> 5] >> (p & 31)) & 1u;
+        cell_at[T + run_table_index(p)] = (uint16_t)(i | (valid ? 0u : kNoValue) | (head ? kSegHead : 0u));
         prev_at[T + run_table_index(p)] =
             (uint16_t)((s0 > 0 ? scan_slot(s0 - 1) : kZeroSlot) | (s0 == p ? kPrevRidge : 0u));
     }
@@ -739,6 +751,10 @@ struct __align__(16) TileCallSmem {
     unsigned red[2][kTileThreads / 32];
     unsigned warp_mn[kTileThreads / 32];
     float warp_sum[kTileThreads / 32];
+    float seg_hi[kTileThreads / 32], seg_lo[kTileThreads / 32];  // pass 1: warp totals of the segmented scan
+    int seg_head[kTileThreads / 32];
+    float carry_hi[kTileThreads], carry_lo[kTileThreads];        // pass 1: what each run's first segment carries in
+    uint8_t run_first[kTileThreads];                             // pass 1: first segment head of each run (16: none)
 };
 
 // The thread's run of a per-position table (cell_at or prev_at): eight coalesced 4-byte loads.
@@ -1034,12 +1050,43 @@ __device__ __forceinline__ unsigned clean_run(float (&x)[kRun])
     return bad;
 }
 
+// Float-float pieces of pass 1: x + y with the rounding error of the high parts kept in lo (no
+// renormalisation), and the segmented-scan combination of (sum since the last segment head, has a head).
+struct SegSum {
+    float hi, lo;
+    bool head;
+};
+__device__ __forceinline__ void ff_acc(float& hi, float& lo, float x)
+{
+    const float s = __fadd_rn(hi, x);
+    const float bp = __fsub_rn(s, hi);
+    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(x, bp));
+    hi = s;
+    lo = __fadd_rn(lo, e);
+}
+// a, then b
+__device__ __forceinline__ SegSum seg_combine(const SegSum& a, const SegSum& b)
+{
+    if (b.head) return b;
+    SegSum r{a.hi, __fadd_rn(a.lo, b.lo), a.head};
+    ff_acc(r.hi, r.lo, b.hi);
+    return r;
+}
+__device__ __forceinline__ SegSum seg_shfl_up(const SegSum& v, int d)
+{
+    return SegSum{__shfl_up_sync(0xffffffffu, v.hi, d), __shfl_up_sync(0xffffffffu, v.lo, d),
+                  __shfl_up_sync(0xffffffffu, (int)v.head, d) != 0};
+}
+
 // Pass 1: the local value of every exit (the accu of its in-tile subtree) to P, in the exit forest's
 // post-order; per tile an upper bound of the material total in 2^-16 units (~0 asks for the walk
-// engine: +inf, a total beyond float range, or a dynamic range the 64-bit fixed point cannot hold), and
-// the statistics pass 3 takes its fixed-point scale from (so that it needs no reduction of its own).
-// Fixed point: round(x * 2^F), F from 4096 times the tile's largest term, so that every prefix sum stays
-// below 2^62 and every subtree sum (a difference of two of them) is exact.
+// engine: +inf, a total beyond float range, or a dynamic range the 64-bit fixed point of pass 3 cannot
+// hold), and the statistics pass 3 takes its fixed-point scale from (so that it needs no reduction of its
+// own).  Exits are roots of the tile's forest; the subtrees of the roots are consecutive runs of
+// positions (segments, each starting at a flagged head), so an exit's value is the sum of its segment: a
+// segmented prefix sum in float-float (relative error about 2^-35 of the segment's total in the worst
+// case, no cancellation), computed on the float pipes.  A NaN or negative term makes its segment NaN,
+// and with it the exit: no-data flows on from there through the exit forest.
 // vec: material rows can be read as float4 (16-byte aligned, columns a multiple of 4).
 __global__ void __launch_bounds__(kTileThreads, 4)
     k_tile_exits(TileGeom g, const float* __restrict__ ext, float ext_s, bool vec, TileForest f,
@@ -1065,34 +1112,76 @@ __global__ void __launch_bounds__(kTileThreads, 4)
 #pragma unroll
     for (int j = 0; j < 4; ++j) *reinterpret_cast<float4*>(sm.M + quad_cell(j)) = xm[j];
     __syncthreads();
-    float x[kRun];
-    gather_run(sm, ca, x);
-    // over the valid positions: the largest raw bits (a sign bit or NaN: the slow path, here and in pass
-    // 3), and the largest and smallest positive bits of the terms that are >= 0
+    // over the valid positions: the largest raw bits (a sign bit or NaN: pass 3's slow path), the largest
+    // and smallest positive bits of the terms that are >= 0, and their float sum; and the segmented sums of
+    // the run, with the run's summary for the scan across threads
     unsigned raw = 0, mx = 0, mn = 0xFFFFFFFFu;
+    float sum = 0.0f;
+    SegSum run{0.0f, 0.0f, false};
+    int first_head = kRun;
+    float2* L = reinterpret_cast<float2*>(sm.S);
 #pragma unroll
     for (int j = 0; j < kRun; ++j) {
-        const unsigned b = __float_as_uint(x[j]);
+        const unsigned w = run_at(ca, j);
+        const float m = sm.M[w & kIndexMask];
+        const float x = (w & kNoValue) ? 0.0f : m;
+        const unsigned b = __float_as_uint(x);
         raw = max(raw, b);
-        const unsigned a = x[j] >= 0.0f ? (b & 0x7FFFFFFFu) : 0u;
+        const bool ok = x >= 0.0f;
+        const unsigned a = ok ? (b & 0x7FFFFFFFu) : 0u;
         mx = max(mx, a);
         mn = min(mn, a - 1u);
+        sum += ok ? x : 0.0f;
+        const float v = ok || isnan(x) ? x : __int_as_float(0x7fc00000);  // negative: NaN
+        if (w & kSegHead) {
+            if (!run.head) first_head = j;
+            run = SegSum{v, 0.0f, true};
+        } else {
+            ff_acc(run.hi, run.lo, v);
+        }
+        L[kRunSlots * t + j] = make_float2(run.hi, run.lo);
     }
     raw = __reduce_max_sync(0xffffffffu, raw);
     mx = __reduce_max_sync(0xffffffffu, mx);
     mn = __reduce_min_sync(0xffffffffu, mn);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    // exclusive segmented scan of the run summaries across the tile: what a segment that starts before
+    // this run carries into it
+    SegSum inc = run;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const SegSum y = seg_shfl_up(inc, d);
+        if (lane >= d) inc = seg_combine(y, inc);
+    }
+    SegSum exc = seg_shfl_up(inc, 1);
+    if (lane == 0) exc = SegSum{0.0f, 0.0f, false};
     if (lane == 0) {
         sm.red[0][warp] = raw;
         sm.red[1][warp] = mx;
         sm.warp_mn[warp] = mn;
+        sm.warp_sum[warp] = sum;
+    }
+    if (lane == 31) {
+        sm.seg_hi[warp] = inc.hi;
+        sm.seg_lo[warp] = inc.lo;
+        sm.seg_head[warp] = inc.head;
     }
     __syncthreads();
+    SegSum before{0.0f, 0.0f, false};
+    sum = 0.0f;
 #pragma unroll
     for (int w = 0; w < kTileThreads / 32; ++w) {  // the same order in every thread
         raw = max(raw, sm.red[0][w]);
         mx = max(mx, sm.red[1][w]);
         mn = min(mn, sm.warp_mn[w]);
+        sum += sm.warp_sum[w];
+        if (w < warp) before = seg_combine(before, SegSum{sm.seg_hi[w], sm.seg_lo[w], sm.seg_head[w] != 0});
     }
+    const SegSum carry = seg_combine(before, exc);
+    sm.run_first[t] = (uint8_t)first_head;
+    sm.carry_hi[t] = carry.hi;
+    sm.carry_lo[t] = carry.lo;
     const float bound = tile_bound(mx, 0u);
     const int F = tile_scale(bound);
     if (mx >= 0x7F800000u || !(bound < 1.0e38f) ||
@@ -1100,34 +1189,23 @@ __global__ void __launch_bounds__(kTileThreads, 4)
         if (t == 0) block_total[tile] = ~0ull;
         return;  // uniform: every thread has the same reductions
     }
-    const bool dirty = raw > 0x7F800000u;  // uniform
-    unsigned poisoned_exit = 0;
-    if (dirty) {
-        poison_counts(sm, clean_run(x));
-        if (t < ne) {
-            const unsigned* C = reinterpret_cast<const unsigned*>(sm.S);
-            poisoned_exit = C[span & 0xFFFFu] != C[span >> 16];
-        }
-        __syncthreads();  // S and warp_tot are free for the value scan
-    }
-    unsigned long long a[kRun];
-    if (mn == 0xFFFFFFFFu || __uint_as_float(mn + 1u) * pow2f(F) >= 8388608.0f) {  // every term exact
-#pragma unroll
-        for (int j = 0; j < kRun; ++j) a[j] = float_to_fixed64_exact(x[j], F);
-    } else {
-#pragma unroll
-        for (int j = 0; j < kRun; ++j) a[j] = float_to_fixed64(x[j], F);
-    }
-    tile_prefix(sm, a);
+    __syncthreads();
     if (t < ne) {
-        float2 value = fixed64_to_ff(sm.S[span & 0xFFFFu] - sm.S[span >> 16], F);
-        if (poisoned_exit) value = make_float2(__int_as_float(0x7fc00000), 0.0f);
-        P[epos] = value;
+        // the exit's position is the end of its segment; a segment that starts in an earlier run also
+        // holds what that run's carry brings
+        const int slot = (int)(span & 0xFFFFu), r = slot / kRunSlots, j = slot - kRunSlots * r;
+        float hi = L[slot].x, lo = L[slot].y;
+        if (j < sm.run_first[r]) {
+            lo = __fadd_rn(lo, sm.carry_lo[r]);
+            ff_acc(hi, lo, sm.carry_hi[r]);
+        }
+        const float h = __fadd_rn(hi, lo);
+        P[epos] = isnan(h) ? make_float2(__int_as_float(0x7fc00000), 0.0f) : make_float2(h, __fsub_rn(lo, __fsub_rn(h, hi)));
     }
-    if (t == kTileThreads - 1) {  // a[15] of the last thread after the scan: the tile's exact total
-        const double units = ldexp(((double)sm.S[kRunSlots * t + kRun - 1] + 8192.0) * (1.0 + 1e-12), 16 - F) + 64.0;
+    if (t == 0) {
+        const double units = ldexp((double)sum * (1.0 + 1.0 / 1024.0) + ldexp(1.0, -100), 16) + 64.0;
         block_total[tile] = units < 1.0e18 ? (unsigned long long)units : ~0ull;
-        stat[tile] = TileStat{bound, mn, dirty ? 1u : 0u, 0u};
+        stat[tile] = TileStat{bound, mn, raw > 0x7F800000u ? 1u : 0u, 0u};
     }
 }
 

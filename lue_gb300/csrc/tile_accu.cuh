@@ -4,10 +4,11 @@
 // forest; once, when the topology is built, it is laid out in post-order, so that the accu of a cell
 // (the material of its in-tile subtree) is the difference of two prefix sums of the material taken in
 // that order.  Per call:
-//   1. k_tile_exits: one CTA per tile gathers its material into post-order, takes one exact 64-bit
-//      fixed-point prefix sum, and writes the local value of each exit cell (a cell whose flow leaves its
-//      tile but not the array: the material of its in-tile subtree) to P, in the post-order of the exit
-//      forest, with per-tile statistics of the material for pass 3.
+//   1. k_tile_exits: one CTA per tile gathers its material into post-order and writes the local value of
+//      each exit cell (a cell whose flow leaves its tile but not the array: the material of its in-tile
+//      subtree) to P, in the post-order of the exit forest, with per-tile statistics of the material for
+//      pass 3.  An exit is a root of the tile's forest, and the subtrees of the roots are consecutive runs
+//      of positions, so its value is a segmented sum (float-float, no cancellation).
 //   2. Exit forest: exit y's parent is the exit reached by following the flow from y's downstream
 //      cell through that cell's tile.  The final value of exit y is the sum of the local values over
 //      y's subtree of this forest, so an inclusive prefix sum over P in post-order gives every subtree
@@ -56,8 +57,9 @@ __host__ __device__ __forceinline__ int run_table_index(int p)
 }
 __host__ __device__ __forceinline__ int scan_slot(int p) { return p + 2 * (p / kRun); }
 
-// cell_at entries: the cell (0..4095) and a flag.
+// cell_at entries: the cell (0..4095) and two flags.
 constexpr unsigned kIndexMask = 0x0FFFu;
+constexpr unsigned kSegHead = 0x4000u;   // the first position of a root's subtree (a no-data cell is its own)
 constexpr unsigned kNoValue = 0x8000u;   // no-data flow direction or outside the array: result NaN / none
 // prev_at entries: the scan slot just before the node's subtree, and a flag.
 constexpr unsigned kSlotMask = 0x1FFFu;
