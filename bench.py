@@ -405,9 +405,30 @@ def bench_ours(args, world, rank, local):
         torch.cuda.synchronize()
         return max_over_ranks(e0.elapsed_time(e1) / 1000.0, world)
 
+    def link_trial():
+        """The same bytes moved without the routing: per step the material host->device on one stream and
+        an outflow-sized buffer device->host on another, at the same time (the host link's capacity for
+        this step's traffic)."""
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(s_in)
+        s_out.wait_event(e0)
+        for k in range(e2e_steps):
+            with torch.cuda.stream(s_in):
+                md = lfr.from_numpy(m_np, ps, device=dev)
+            with torch.cuda.stream(s_out):
+                torch.from_numpy(out_np[k % 2]).copy_(out.data, non_blocking=True)
+            del md
+        s_in.wait_stream(s_out)
+        e1.record(s_in)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1000.0
+
     # The host memory and its link are shared with the other jobs of the machine: five trials, the
     # median is the value, the fastest is reported beside it
     e2e_trials = [e2e_trial() for _ in range(5)]
+    link_s = min(link_trial() for _ in range(3))
     e2e_s = statistics.median(e2e_trials)
     e2e_value = world * n * e2e_steps / e2e_s / 1e6
     e2e_best = world * n * e2e_steps / min(e2e_trials) / 1e6
@@ -476,6 +497,10 @@ def bench_ours(args, world, rank, local):
         "e2e": {"value": round(e2e_value, 3), "unit": "Mcells/s", "h2d_bytes_per_step": 4 * n,
                 "d2h_bytes_per_step": 4 * n, "steps": e2e_steps,
                 "best_of_trials": round(e2e_best, 3),
+                "link_only_ms_per_step": round(1000 * link_s / e2e_steps, 3),
+                "link_frac": round(link_s / e2e_s, 3),
+                "link_note": "the step's host->device and device->host bytes moved at the same time without the "
+                             "routing (best of 3); link_frac = that time / the e2e time",
                 "trials_ms_per_step": [round(1000 * x / e2e_steps, 2) for x in e2e_trials],
                 "timed": "median of 5 trials (value), fastest beside it",
                 "path": "lue_gb300.framework.from_numpy -> accu (C ABI lue_gpu_accu_f32) -> to_numpy_async, "
@@ -484,7 +509,7 @@ def bench_ours(args, world, rank, local):
                            "(three streams, pinned host memory)"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "kernel": ("accu_f32 call: k_tile_exit_sums + exit-forest scan + k_tile_accu" if engine == "tiles"
+                     "kernel": ("accu_f32 call: k_tile_exits + exit-forest scan + k_slot_inflow + k_tile_accu" if engine == "tiles"
                                 else "k_walk<RouteF32<accu>>"),
                      "timed": "whole call per step (all its kernels), CUDA events on the launching stream",
                      "peak_kind": peak_kind, "bytes_per_cell": ACCU_BYTES_PER_CELL},
