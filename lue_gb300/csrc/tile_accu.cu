@@ -48,24 +48,34 @@ __device__ __forceinline__ int fixed_point_bits(unsigned long long total_units)
     return f > 100 ? 100 : (f < -100 ? -100 : f);
 }
 
-// |x| * 2^F rounded to nearest, as a 128-bit two's-complement integer with the sign of x.
+// |x| * 2^F rounded to nearest (ties up; 0 below 2^-40, 0 from 2^128 up), as a 128-bit two's-complement
+// integer with the sign of x.  Built from 32-bit words: the 24-bit mantissa shifted by s & 31 spans two
+// words, placed at word s >> 5, so no 128-bit variable shift is needed.
 __device__ __forceinline__ u128 float_to_fixed(float x, int F)
 {
-    unsigned bits = __float_as_uint(x);
-    unsigned e8 = (bits >> 23) & 0xFFu;
-    unsigned mant = (bits & 0x7FFFFFu) | (e8 ? 0x800000u : 0u);
-    if (mant == 0) return 0;
-    int s = (int)(e8 ? e8 : 1u) - 150 + F;  // value = mant * 2^(e - 150) * 2^F
-    u128 m;
+    const unsigned bits = __float_as_uint(x);
+    const unsigned e8 = (bits >> 23) & 0xFFu;
+    const unsigned mant = (bits & 0x7FFFFFu) | (e8 ? 0x800000u : 0u);
+    const int s = (int)(e8 ? e8 : 1u) - 150 + F;  // value = mant * 2^(e - 150) * 2^F
+    unsigned long long lo = 0, hi = 0;
     if (s >= 0) {
-        m = s >= 104 ? (u128)0 : ((u128)mant << s);
+        if (s < 104) {
+            const int k = s >> 5;
+            const unsigned b = (unsigned)s & 31u;
+            const unsigned w0 = mant << b, w1 = __funnelshift_l(mant, 0u, b);
+            const unsigned long long pair = ((unsigned long long)w1 << 32) | w0;
+            const unsigned long long up = (unsigned long long)w0 << 32;
+            lo = k == 0 ? pair : (k == 1 ? up : 0ull);
+            hi = k == 1 ? (unsigned long long)w1 : (k == 2 ? pair : (k == 3 ? up : 0ull));
+        }
     } else if (s > -40) {
-        unsigned long long mm = mant;
-        m = (u128)((mm + (1ull << (-s - 1))) >> (-s));
-    } else {
-        m = 0;
+        lo = ((unsigned long long)mant + (1ull << (-s - 1))) >> (-s);
     }
-    return (bits >> 31) ? (u128)0 - m : m;
+    if (bits >> 31) {  // two's complement
+        hi = ~hi + (lo == 0 ? 1ull : 0ull);
+        lo = 0ull - lo;
+    }
+    return ((u128)hi << 64) | lo;
 }
 
 __device__ __forceinline__ u128 exit_value_fixed(float2 v, int F)
@@ -755,6 +765,7 @@ struct __align__(16) TileCallSmem {
     int seg_head[kTileThreads / 32];
     float carry_hi[kTileThreads], carry_lo[kTileThreads];        // pass 1: what each run's first segment carries in
     uint8_t run_first[kTileThreads];                             // pass 1: first segment head of each run (16: none)
+    int quit;                                                    // pass 3: the walk engine redoes the call
 };
 
 // The thread's run of a per-position table (cell_at or prev_at): eight coalesced 4-byte loads.
@@ -786,54 +797,20 @@ __device__ __forceinline__ float quad_at(const float4& q, int k)
     return k == 0 ? q.x : (k == 1 ? q.y : (k == 2 ? q.z : q.w));
 }
 
-// Sum of the per-tile bounds: total[0] = bound in 2^-16 units, total[1] != 0 when the tile engine must
-// hand the call to the walk engine (+inf material, or a total beyond the fixed-point range).
-__global__ void __launch_bounds__(1024) k_total(const unsigned long long* block_total, int64_t ntiles,
-                                                unsigned long long* total)
+// The material total in 2^-16 units at or beyond this makes the tile engine hand the call to the walk
+// engine (the 128-bit fixed point of the exit forest keeps 96 value bits).
+constexpr unsigned long long kTotalLimit = 1000000000000000000ull;
+
+// total[0], summed by pass 1 with 64-bit atomics (exact, so the order does not matter), and total[1]: the
+// tile engine's result stands when neither says otherwise.
+__device__ __forceinline__ bool tile_fallback(const unsigned long long* total)
 {
-    __shared__ unsigned long long part[32];
-    __shared__ int badw[32];
-    unsigned long long s = 0;
-    double chk = 0.0;  // the same sum in double: detects a total beyond the fixed-point range
-    int bad = 0;
-    for (int64_t i = threadIdx.x; i < ntiles; i += blockDim.x) {
-        unsigned long long v = block_total[i];
-        if (v == ~0ull) {
-            bad = 1;
-        } else {
-            s += v;
-            chk += (double)v;
-        }
-    }
-    if (chk >= 1.0e18) bad = 1;
-    for (int off = 16; off > 0; off >>= 1) {
-        s += __shfl_down_sync(0xffffffffu, s, off);
-        chk += __shfl_down_sync(0xffffffffu, chk, off);
-        bad |= __shfl_down_sync(0xffffffffu, bad, off);
-    }
-    if (chk >= 1.0e18) bad = 1;
-    if ((threadIdx.x & 31) == 0) {
-        part[threadIdx.x >> 5] = s;
-        badw[threadIdx.x >> 5] = bad;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned long long tot = 0;
-        double check = 0.0;
-        for (int w = 0; w < (int)(blockDim.x / 32); ++w) {
-            tot += part[w];
-            check += (double)part[w];
-            bad |= badw[w];
-        }
-        // parts that wrapped cannot pass here: every part is < 1e18 or already flagged
-        if (check >= 1.0e18) bad = 1;
-        total[0] = tot;
-        total[1] = bad ? 1ull : 0ull;
-    }
+    return *reinterpret_cast<const volatile unsigned long long*>(total + 1) != 0 || total[0] >= kTotalLimit;
 }
 
 constexpr int kScanItems = 16;
 constexpr int kScanBlock = kTileThreads * kScanItems;
+constexpr int kScanPolls = 1 << 20;  // poll limit of one look-back wait (about 0.1 s)
 
 __device__ __forceinline__ u128 block_exclusive_u128(u128 v, u128* warp_tot, u128& block_total)
 {
@@ -860,57 +837,126 @@ __device__ __forceinline__ u128 block_exclusive_u128(u128 v, u128* warp_tot, u12
     return before + x - v;
 }
 
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v)
+{
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// The exit forest's 128-bit inclusive scan, one chunk of consecutive scan blocks (kScanBlock exits each)
+// per CTA, with as many CTAs as fit on the GPU at once.  CTAs take chunks in ticket order; each sums its
+// chunk, publishes the sum (flag 1), then warp 0 adds up the sums of the chunks before it, 32 at a time,
+// until it meets a chunk that has published the sum up to and including itself (flag 2); the CTA
+// publishes its own (flag 2) and scans its chunk again, block by block, from that prefix.  A CTA waits
+// only for chunks with smaller tickets, held by CTAs that started earlier, and those publish their own
+// sums before they wait for anything: no chain of waits forms.  Every wait is bounded: a wait that gives
+// up (or sees that one did) sets total[1] = 2, after which the walk engine redoes the call.
+// ctl = the ticket, then the chunk flags, zeroed before the call.
 __global__ void __launch_bounds__(kTileThreads)
-    k_scan_reduce(const float2* __restrict__ P, int64_t n, const unsigned long long* total, uint4* block_sums)
+    k_scan_exits(const float2* __restrict__ P, int64_t n, int64_t chunk_blocks, unsigned long long* total,
+                 unsigned* ctl, uint4* look_aggr, uint4* look_incl, uint4* __restrict__ S)
 {
     __shared__ u128 warp_tot[kTileThreads / 32];
-    if (total[1]) return;
+    __shared__ u128 prefix_sh;
+    __shared__ unsigned ticket_sh;
+    __shared__ int abort_sh;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // one thread decides, so that the whole CTA leaves or stays
+    if (threadIdx.x == 0) ticket_sh = tile_fallback(total) ? ~0u : atomicAdd(ctl, 1u);
+    __syncthreads();
+    if (ticket_sh == ~0u) return;
+    const int64_t g = ticket_sh;
+    unsigned* flag = ctl + 1;
     const int F = fixed_point_bits(total[0]);
-    int64_t base = (int64_t)blockIdx.x * kScanBlock + (int64_t)threadIdx.x * kScanItems;
+    const int64_t first = g * chunk_blocks * kScanBlock;
+    const int64_t last = min(n, first + chunk_blocks * kScanBlock);
+    // the chunk's sum
     u128 s = 0;
-    for (int k = 0; k < kScanItems; ++k)
-        if (base + k < n) s += exit_value_fixed(P[base + k], F);
+    for (int64_t b0 = first; b0 < last; b0 += kScanBlock) {
+        const int64_t base = b0 + (int64_t)threadIdx.x * kScanItems;
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k)
+            if (base + k < last) s += exit_value_fixed(__ldg(P + base + k), F);
+    }
     u128 bt;
     block_exclusive_u128(s, warp_tot, bt);
-    if (threadIdx.x == 0) block_sums[blockIdx.x] = from_u128(bt);
-}
-
-__global__ void __launch_bounds__(kTileThreads) k_scan_blocks(uint4* block_sums, int64_t nblocks, const unsigned long long* total)
-{
-    __shared__ u128 warp_tot[kTileThreads / 32];
-    if (total[1]) return;
-    u128 carry = 0;
-    for (int64_t b0 = 0; b0 < nblocks; b0 += kTileThreads) {
-        int64_t b = b0 + threadIdx.x;
-        u128 v = b < nblocks ? to_u128(block_sums[b]) : (u128)0;
-        u128 bt;
-        u128 ex = block_exclusive_u128(v, warp_tot, bt);
-        if (b < nblocks) block_sums[b] = from_u128(carry + ex);
-        carry += bt;
+    if (warp == 0) {
+        if (g == 0) {
+            if (lane == 0) {
+                look_incl[0] = from_u128(bt);
+                st_release_u32(flag, 2u);
+                prefix_sh = 0;
+                abort_sh = 0;
+            }
+        } else {
+            if (lane == 0) {
+                look_aggr[g] = from_u128(bt);
+                st_release_u32(flag + g, 1u);
+            }
+            u128 prefix = 0;
+            bool failed = false;
+            for (int64_t top = g - 1;; top -= 32) {
+                const int64_t j = top - lane;
+                unsigned f = 2u;  // before chunk 0: nothing (never reached: chunk 0 publishes flag 2)
+                u128 x = 0;
+                if (j >= 0) {
+                    int k = 0;
+                    for (; k < kScanPolls; ++k) {
+                        f = ld_acquire_u32(flag + j);
+                        if (f != 0u) break;
+                        if (*reinterpret_cast<volatile unsigned long long*>(total + 1)) k = kScanPolls - 1;
+                        __nanosleep(64);
+                    }
+                    if (k >= kScanPolls) f = 0u;
+                }
+                if (__ballot_sync(0xffffffffu, f == 0u)) {
+                    failed = true;
+                    break;
+                }
+                const unsigned incl = __ballot_sync(0xffffffffu, f == 2u);
+                const int stop = incl ? __ffs(incl) - 1 : 31;  // lanes 0..stop count
+                if (j >= 0 && lane <= stop) x = to_u128(__ldcg(f == 2u ? look_incl + j : look_aggr + j));
+                for (int d = 16; d > 0; d >>= 1) x += shfl_down_u128(x, d);
+                prefix += x;  // lane 0 holds the window's sum
+                if (incl) break;
+            }
+            if (lane == 0) {
+                if (failed) {
+                    total[1] = 2ull;
+                } else {
+                    look_incl[g] = from_u128(prefix + bt);
+                    st_release_u32(flag + g, 2u);
+                }
+                prefix_sh = prefix;
+                abort_sh = failed ? 1 : 0;
+            }
+        }
     }
-}
-
-__global__ void __launch_bounds__(kTileThreads)
-    k_scan_final(const float2* __restrict__ P, int64_t n, const unsigned long long* total,
-                 const uint4* __restrict__ block_sums, uint4* __restrict__ S)
-{
-    __shared__ u128 warp_tot[kTileThreads / 32];
-    if (total[1]) return;
-    const int F = fixed_point_bits(total[0]);
-    int64_t base = (int64_t)blockIdx.x * kScanBlock + (int64_t)threadIdx.x * kScanItems;
-    u128 v[kScanItems];
-    u128 s = 0;
+    __syncthreads();
+    if (abort_sh) return;
+    u128 carry = prefix_sh;
+    for (int64_t b0 = first; b0 < last; b0 += kScanBlock) {
+        const int64_t base = b0 + (int64_t)threadIdx.x * kScanItems;
+        u128 v[kScanItems];
+        u128 t = 0;
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        v[k] = base + k < n ? exit_value_fixed(P[base + k], F) : (u128)0;
-        s += v[k];
-    }
-    u128 bt;
-    u128 run = to_u128(block_sums[blockIdx.x]) + block_exclusive_u128(s, warp_tot, bt);
+        for (int k = 0; k < kScanItems; ++k) {
+            v[k] = base + k < last ? exit_value_fixed(__ldg(P + base + k), F) : (u128)0;
+            t += v[k];
+        }
+        u128 blk;
+        u128 run = carry + block_exclusive_u128(t, warp_tot, blk);
+        carry += blk;
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        run += v[k];
-        if (base + k < n) S[base + k] = from_u128(run);
+        for (int k = 0; k < kScanItems; ++k) {
+            run += v[k];
+            if (base + k < last) S[base + k] = from_u128(run);
+        }
     }
 }
 
@@ -918,19 +964,17 @@ __global__ void __launch_bounds__(kTileThreads)
 // sums of the exits draining into it (each a difference of two inclusive prefix sums of the exit
 // forest), rounded to float once; NaN when one of them holds a no-data exit.
 __global__ void k_slot_inflow(int64_t nslot, const int32_t* __restrict__ slot_at,
-                              const int32_t* __restrict__ slot_first, const int32_t* __restrict__ slot_exit,
-                              const uint32_t* __restrict__ pos, const uint32_t* __restrict__ start,
+                              const int32_t* __restrict__ slot_first, const int2* __restrict__ slot_edge,
                               const uint4* __restrict__ S, float* __restrict__ inflow,
                               const unsigned long long* total)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nslot || total[1]) return;
+    if (i >= nslot || tile_fallback(total)) return;
     const int F = fixed_point_bits(total[0]);
     u128 src = 0;
     for (int32_t k = __ldg(slot_first + i), k1 = __ldg(slot_first + i + 1); k < k1; ++k) {
-        const int32_t y = __ldg(slot_exit + k);
-        const uint32_t st = __ldg(start + y);
-        src += to_u128(S[__ldg(pos + y)]) - (st ? to_u128(S[st - 1]) : (u128)0);
+        const int2 e = __ldg(slot_edge + k);
+        src += to_u128(__ldcg(S + e.x)) - (e.y >= 0 ? to_u128(__ldcg(S + e.y)) : (u128)0);
     }
     inflow[__ldg(slot_at + i)] = (src >> 96) ? __int_as_float(0x7fc00000) : fixed128_to_float(src & kValueMask, F);
 }
@@ -952,7 +996,8 @@ __global__ void k_slot_count(int64_t ntiles, const uint8_t* __restrict__ border_
 
 __global__ void k_slot_fill(int64_t ntiles, const uint8_t* __restrict__ border_in, const int32_t* __restrict__ halo_exit,
                             const int32_t* __restrict__ slot_base, const int32_t* __restrict__ exit_base,
-                            int32_t* slot_at, int32_t* slot_first, int32_t* slot_exit, int* error)
+                            const uint32_t* __restrict__ exit_pos, const uint32_t* __restrict__ exit_start,
+                            int32_t* slot_at, int32_t* slot_first, int2* slot_edge, int* error)
 {
     const int64_t tile = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (tile >= ntiles) return;
@@ -968,7 +1013,9 @@ __global__ void k_slot_fill(int64_t ntiles, const uint8_t* __restrict__ border_i
             const int q = __ffs(m) - 1;
             const int32_t id = halo_exit[tile * kHaloSlots + halo_slot_of(rin + nb_dr(q), cin + nb_dc(q))];
             if (id < 0) atomicExch(error, 1);  // a neighbour draining in must be an exit of its tile
-            slot_exit[e++] = id < 0 ? 0 : id;
+            const int32_t y = id < 0 ? 0 : id;
+            const uint32_t st = exit_start[y];
+            slot_edge[e++] = make_int2((int)exit_pos[y], st ? (int)(st - 1u) : -1);
         }
         ++s;
     }
@@ -1079,9 +1126,10 @@ __device__ __forceinline__ SegSum seg_shfl_up(const SegSum& v, int d)
 }
 
 // Pass 1: the local value of every exit (the accu of its in-tile subtree) to P, in the exit forest's
-// post-order; per tile an upper bound of the material total in 2^-16 units (~0 asks for the walk
-// engine: +inf, a total beyond float range, or a dynamic range the 64-bit fixed point of pass 3 cannot
-// hold), and the statistics pass 3 takes its fixed-point scale from (so that it needs no reduction of its
+// post-order; an upper bound of the tile's material total in 2^-16 units added to total[0] (64-bit
+// atomics: exact, whatever the order; total[1] is set instead, asking for the walk engine, on +inf, a
+// total beyond float range, a dynamic range the 64-bit fixed point of pass 3 cannot hold, or a sum that
+// wraps), and the statistics pass 3 takes its fixed-point scale from (so that it needs no reduction of its
 // own).  Exits are roots of the tile's forest; the subtrees of the roots are consecutive runs of
 // positions (segments, each starting at a flagged head), so an exit's value is the sum of its segment: a
 // segmented prefix sum in float-float (relative error about 2^-35 of the segment's total in the worst
@@ -1092,7 +1140,7 @@ __global__ void __launch_bounds__(kTileThreads, 4)
     k_tile_exits(TileGeom g, const float* __restrict__ ext, float ext_s, bool vec, TileForest f,
                  const int32_t* __restrict__ exit_base, const uint32_t* __restrict__ exit_span,
                  const uint32_t* __restrict__ exit_pos, float2* __restrict__ P,
-                 unsigned long long* __restrict__ block_total, TileStat* __restrict__ stat)
+                 unsigned long long* total, TileStat* __restrict__ stat)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TileCallSmem& sm = *reinterpret_cast<TileCallSmem*>(smem_raw);
@@ -1168,16 +1216,26 @@ __global__ void __launch_bounds__(kTileThreads, 4)
         sm.seg_head[warp] = inc.head;
     }
     __syncthreads();
-    SegSum before{0.0f, 0.0f, false};
-    sum = 0.0f;
+    // the warps' summaries: lane i of every warp takes warp (i & 7)'s; the block's largest and smallest bits
+    // by warp reductions, the sum (thread 0's is used) and a segmented scan over each group of eight lanes
+    // by three shuffle steps; the carry into this warp is lane warp - 1's inclusive scan
+    static_assert(kTileThreads == 256, "eight warps per tile CTA");
+    const int w8 = lane & 7;
+    raw = __reduce_max_sync(0xffffffffu, sm.red[0][w8]);
+    mx = __reduce_max_sync(0xffffffffu, sm.red[1][w8]);
+    mn = __reduce_min_sync(0xffffffffu, sm.warp_mn[w8]);
+    sum = sm.warp_sum[w8];
+    SegSum ws{sm.seg_hi[w8], sm.seg_lo[w8], sm.seg_head[w8] != 0};
 #pragma unroll
-    for (int w = 0; w < kTileThreads / 32; ++w) {  // the same order in every thread
-        raw = max(raw, sm.red[0][w]);
-        mx = max(mx, sm.red[1][w]);
-        mn = min(mn, sm.warp_mn[w]);
-        sum += sm.warp_sum[w];
-        if (w < warp) before = seg_combine(before, SegSum{sm.seg_hi[w], sm.seg_lo[w], sm.seg_head[w] != 0});
+    for (int o = 1; o < 8; o <<= 1) {
+        sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        const SegSum y = seg_shfl_up(ws, o);
+        if (w8 >= o) ws = seg_combine(y, ws);
     }
+    const int src = warp > 0 ? warp - 1 : 0;
+    SegSum before{__shfl_sync(0xffffffffu, ws.hi, src), __shfl_sync(0xffffffffu, ws.lo, src),
+                  __shfl_sync(0xffffffffu, (int)ws.head, src) != 0};
+    if (warp == 0) before = SegSum{0.0f, 0.0f, false};
     const SegSum carry = seg_combine(before, exc);
     sm.run_first[t] = (uint8_t)first_head;
     sm.carry_hi[t] = carry.hi;
@@ -1186,7 +1244,7 @@ __global__ void __launch_bounds__(kTileThreads, 4)
     const int F = tile_scale(bound);
     if (mx >= 0x7F800000u || !(bound < 1.0e38f) ||
         (mn != 0xFFFFFFFFu && __uint_as_float(mn + 1u) * pow2f(F) < kMinQuantum)) {
-        if (t == 0) block_total[tile] = ~0ull;
+        if (t == 0) atomicOr(total + 1, 1ull);
         return;  // uniform: every thread has the same reductions
     }
     __syncthreads();
@@ -1204,7 +1262,12 @@ __global__ void __launch_bounds__(kTileThreads, 4)
     }
     if (t == 0) {
         const double units = ldexp((double)sum * (1.0 + 1.0 / 1024.0) + ldexp(1.0, -100), 16) + 64.0;
-        block_total[tile] = units < 1.0e18 ? (unsigned long long)units : ~0ull;
+        if (units < (double)kTotalLimit) {
+            const unsigned long long u = (unsigned long long)units;
+            if (atomicAdd(total, u) + u < u) atomicOr(total + 1, 1ull);  // the sum wrapped
+        } else {
+            atomicOr(total + 1, 1ull);
+        }
         stat[tile] = TileStat{bound, mn, raw > 0x7F800000u ? 1u : 0u, 0u};
     }
 }
@@ -1226,10 +1289,14 @@ __global__ void __launch_bounds__(kTileThreads, 4)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TileCallSmem& sm = *reinterpret_cast<TileCallSmem*>(smem_raw);
-    if (total[1]) return;
     const int64_t tr = blockIdx.y, tc = blockIdx.x;  // grid = (tile columns, tile rows)
     const int64_t tile = tr * g.tcols + tc;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    if (t == 0) {  // one thread decides (other CTAs may set the flag meanwhile), read after the barrier below
+        const bool fb = tile_fallback(total);
+        if (fb && *reinterpret_cast<volatile unsigned long long*>(total + 1) == 0) total[1] = 1ull;
+        sm.quit = fb;
+    }
     float4 xm[4];
     load_material(xm, ext, ext_s, g, tr, tc, vec);
     uint32_t ca[kRunWords], pv[kRunWords];
@@ -1261,6 +1328,7 @@ __global__ void __launch_bounds__(kTileThreads, 4)
 #pragma unroll
     for (int j = 0; j < 4; ++j) *reinterpret_cast<float4*>(sm.M + quad_cell(j)) = xm[j];
     __syncthreads();
+    if (sm.quit) return;  // uniform
     if (ecell >= 0) {  // material out of the domain stays visible as NaN (the cell and all below are NaN)
         const float mat = sm.M[ecell];
         sm.M[ecell] = mat >= 0.0f ? mat + entering : __int_as_float(0x7fc00000);
@@ -1497,11 +1565,12 @@ int tile_core_build(TopologyCore* core, cudaStream_t stream)
         TRY(cudaMemcpyAsync(ec, ebase.data(), nt * sizeof(int32_t), cudaMemcpyHostToDevice, stream), "slot base");
         TRY(cudaMalloc(&tc->slot_at, std::max<int64_t>(a, 1) * sizeof(int32_t)), "slots");
         TRY(cudaMalloc(&tc->slot_first, (a + 1) * sizeof(int32_t)), "slots");
-        TRY(cudaMalloc(&tc->slot_exit, std::max<int64_t>(b, 1) * sizeof(int32_t)), "slots");
+        TRY(cudaMalloc(&tc->slot_edge, std::max<int64_t>(b, 1) * sizeof(int2)), "slots");
         TRY(cudaMemcpyAsync(tc->slot_first + a, &ebase[nt], sizeof(int32_t), cudaMemcpyHostToDevice, stream),
             "slot end");
-        k_slot_fill<<<blocks_for(nt, 256), 256, 0, stream>>>(nt, tc->border_in, tc->halo_exit, sc, ec, tc->slot_at,
-                                                             tc->slot_first, tc->slot_exit, flag);
+        k_slot_fill<<<blocks_for(nt, 256), 256, 0, stream>>>(nt, tc->border_in, tc->halo_exit, sc, ec,
+                                                             tc->exit_pos, tc->exit_start, tc->slot_at,
+                                                             tc->slot_first, tc->slot_edge, flag);
         TRY(cudaGetLastError(), "slot fill");
         TRY(cudaMemcpyAsync(&herr, flag, sizeof(int), cudaMemcpyDeviceToHost, stream), "tile flag");
         TRY(cudaStreamSynchronize(stream), "slot fill");  // the host vectors must outlive the copies
@@ -1509,7 +1578,7 @@ int tile_core_build(TopologyCore* core, cudaStream_t stream)
             rc = fail(LUE_GPU_EINVAL, "tile topology: an inflow without an upstream exit");
             goto error;
         }
-        tc->bytes += a * 8 + 4 + b * 4;
+        tc->bytes += a * 8 + 4 + b * 8;
     }
     cudaFree(sc);
     cudaFree(ec);
@@ -1569,7 +1638,7 @@ void tile_core_free(TileCore* tc)
     cudaFree(tc->border_in);
     cudaFree(tc->slot_at);
     cudaFree(tc->slot_first);
-    cudaFree(tc->slot_exit);
+    cudaFree(tc->slot_edge);
     delete tc;
 }
 
@@ -1585,12 +1654,14 @@ int tile_scratch_alloc(const TileCore* tc, TileScratch* s)
     // slots without inflow are never written: they stay 0
     if ((rc = cuda_status(cudaMemset(s->inflow, 0, tc->ntiles * kSlotStride * sizeof(float)), "tile scratch")))
         return rc;
-    if ((rc = cuda_status(cudaMalloc(&s->block_sums, nb * sizeof(uint4)), "tile scratch"))) return rc;
-    if ((rc = cuda_status(cudaMalloc(&s->total, 2 * sizeof(unsigned long long)), "tile scratch"))) return rc;
-    if ((rc = cuda_status(cudaMalloc(&s->block_total, tc->ntiles * sizeof(unsigned long long)), "tile scratch")))
-        return rc;
+    if ((rc = cuda_status(cudaMalloc(&s->look_aggr, nb * sizeof(uint4)), "tile scratch"))) return rc;
+    if ((rc = cuda_status(cudaMalloc(&s->look_incl, nb * sizeof(uint4)), "tile scratch"))) return rc;
+    // total[2], the scan's ticket, its block flags
+    s->ctl_bytes = 2 * sizeof(unsigned long long) + (1 + nb) * sizeof(unsigned);
+    if ((rc = cuda_status(cudaMalloc(&s->total, s->ctl_bytes), "tile scratch"))) return rc;
+    if ((rc = cuda_status(cudaMemset(s->total, 0, s->ctl_bytes), "tile scratch"))) return rc;
     if ((rc = cuda_status(cudaMalloc(&s->stat, tc->ntiles * sizeof(TileStat)), "tile scratch"))) return rc;
-    s->bytes = E * (8 + 16) + nb * 16 + 16 + tc->ntiles * (8 + sizeof(TileStat) + kSlotStride * 4);
+    s->bytes = E * (8 + 16) + nb * 32 + s->ctl_bytes + tc->ntiles * (sizeof(TileStat) + kSlotStride * 4);
     return LUE_GPU_OK;
 }
 
@@ -1599,11 +1670,29 @@ void tile_scratch_free(TileScratch* s)
     cudaFree(s->P);
     cudaFree(s->S);
     cudaFree(s->inflow);
-    cudaFree(s->block_sums);
+    cudaFree(s->look_aggr);
+    cudaFree(s->look_incl);
     cudaFree(s->total);
-    cudaFree(s->block_total);
     cudaFree(s->stat);
     *s = TileScratch{};
+}
+
+// CTAs of k_scan_exits that fit on the device at once (chunks of the exit-forest scan).  The result does
+// not depend on it: the chunks' sums are exact.
+static int64_t scan_ctas()
+{
+    static const int64_t n = [] {
+        int dev = 0, sms = 0, per_sm = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scan_exits, kTileThreads, 0) != cudaSuccess ||
+            sms <= 0 || per_sm <= 0) {
+            cudaGetLastError();
+            return (int64_t)152;
+        }
+        return (int64_t)sms * per_sm;
+    }();
+    return n;
 }
 
 // accu (float32) on the tile engine.  Returns LUE_GPU_OK with `fallback` set on the device when the
@@ -1625,22 +1714,25 @@ int tile_accu_f32(const TopologyCore* core, TileScratch* s, const float* ext, fl
                                                      (int)sizeof(TileCallSmem)) == cudaSuccess;
     if (!smem_ok) return fail(LUE_GPU_ECUDA, "accu_f32 (tiles): shared memory attribute");
     const dim3 tile_grid((unsigned)tc->tcols, (unsigned)tc->trows);
+    if (int rc = cuda_status(cudaMemsetAsync(s->total, 0, s->ctl_bytes, stream), "accu_f32 (tiles)")) return rc;
     k_tile_exits<<<tile_grid, kTileThreads, sizeof(TileCallSmem), stream>>>(g, ext, ext_s, vec_in, f, tc->exit_base,
                                                                             tc->exit_span, tc->exit_pos, s->P,
-                                                                            s->block_total, s->stat);
-    k_total<<<1, 1024, 0, stream>>>(s->block_total, tc->ntiles, s->total);
-    count_launches(2);
+                                                                            s->total, s->stat);
+    count_launches(1);
     const int64_t E = tc->nexit;
     if (E > 0) {
         const int64_t nb = (E + kScanBlock - 1) / kScanBlock;
-        k_scan_reduce<<<(unsigned)nb, kTileThreads, 0, stream>>>(s->P, E, s->total, s->block_sums);
-        k_scan_blocks<<<1, kTileThreads, 0, stream>>>(s->block_sums, nb, s->total);
-        k_scan_final<<<(unsigned)nb, kTileThreads, 0, stream>>>(s->P, E, s->total, s->block_sums, s->S);
-        if (tc->nslot > 0)
+        const int64_t chunk_blocks = (nb + scan_ctas() - 1) / scan_ctas();
+        const int64_t nchunk = (nb + chunk_blocks - 1) / chunk_blocks;
+        unsigned* ctl = reinterpret_cast<unsigned*>(s->total + 2);
+        k_scan_exits<<<(unsigned)nchunk, kTileThreads, 0, stream>>>(s->P, E, chunk_blocks, s->total, ctl,
+                                                                    s->look_aggr, s->look_incl, s->S);
+        count_launches(1);
+        if (tc->nslot > 0) {
             k_slot_inflow<<<blocks_for(tc->nslot, 256), 256, 0, stream>>>(tc->nslot, tc->slot_at, tc->slot_first,
-                                                                          tc->slot_exit, tc->exit_pos, tc->exit_start,
-                                                                          s->S, s->inflow, s->total);
-        count_launches(4);
+                                                                          tc->slot_edge, s->S, s->inflow, s->total);
+            count_launches(1);
+        }
     }
     k_tile_accu<<<tile_grid, kTileThreads, sizeof(TileCallSmem), stream>>>(g, ext, ext_s, vec_in && vec_out, out, f,
                                                                            s->stat, s->total);

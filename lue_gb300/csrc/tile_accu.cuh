@@ -84,8 +84,10 @@ struct TileCore {
     // Inflow slots (border cells that receive flow from other tiles), per tile in border order:
     int64_t nslot = 0;
     int32_t* slot_at = nullptr;                // [nslot] tile * kSlotStride + border index
-    int32_t* slot_first = nullptr;             // [nslot + 1] first of the slot's upstream exits in slot_exit
-    int32_t* slot_exit = nullptr;              // [slot_first[nslot]] exit ids draining into the slot
+    int32_t* slot_first = nullptr;             // [nslot + 1] first of the slot's upstream exits in slot_edge
+    int2* slot_edge = nullptr;                 // [slot_first[nslot]] per exit draining into the slot: its
+                                               // exit-forest position, and the position before its subtree
+                                               // (-1: none)
     int64_t bytes = 0;
 };
 
@@ -104,9 +106,12 @@ struct TileScratch {
     uint4* S = nullptr;                        // [nexit] inclusive prefix sums (128-bit), post-order
     float* inflow = nullptr;                   // [ntiles * kSlotStride] what enters each border cell (0 where
                                                // nothing does), float, NaN when no-data enters
-    uint4* block_sums = nullptr;               // [scan blocks]
-    unsigned long long* total = nullptr;       // [2] material total bound (2^-16 units), fallback flag
-    unsigned long long* block_total = nullptr; // [ntiles] per-tile bounds
+    uint4* look_aggr = nullptr;                // [scan blocks] each block's sum (decoupled look-back)
+    uint4* look_incl = nullptr;                // [scan blocks] the sum up to and including the block
+    // Zeroed before each call, in one memset of ctl_bytes: total[0] = bound of the material total
+    // (2^-16 units, summed by pass 1), total[1] = fallback flag, then the scan's ticket and block flags.
+    unsigned long long* total = nullptr;
+    int64_t ctl_bytes = 0;
     TileStat* stat = nullptr;                  // [ntiles]
     int64_t bytes = 0;
 };
