@@ -957,7 +957,9 @@ __global__ void __launch_bounds__(NT) k_stage_flow(StageRunArgs a, StageFlowArgs
                     pv[j] = __ldcg(a.hist + (int64_t)L.in_rows[s] * ns + t);
                 }
             }
-        } else {
+        } else if (!ONE || r == 0) {
+            // one step: the barrier that ends each round orders its outflows before the next round's
+            // reads, so only round 0 (after the loads of the inputs) needs one here
             __syncthreads();
         }
         const int lo = L.rstart[max(0, r - ns + 1)], hi = L.rstart[min(rounds, r + 1)];

@@ -810,7 +810,7 @@ __device__ __forceinline__ bool tile_fallback(const unsigned long long* total)
 
 constexpr int kScanItems = 16;
 constexpr int kScanBlock = kTileThreads * kScanItems;
-constexpr int kScanPolls = 1 << 20;  // poll limit of one look-back wait (about 0.1 s)
+constexpr int kScanPolls = 1 << 20;  // poll limit of one look-back wait (a second at most)
 
 __device__ __forceinline__ u128 block_exclusive_u128(u128 v, u128* warp_tot, u128& block_total)
 {
@@ -859,7 +859,7 @@ __device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v)
 // ctl = the ticket, then the chunk flags, zeroed before the call.
 __global__ void __launch_bounds__(kTileThreads)
     k_scan_exits(const float2* __restrict__ P, int64_t n, int64_t chunk_blocks, unsigned long long* total,
-                 unsigned* ctl, uint4* look_aggr, uint4* look_incl, uint4* __restrict__ S)
+                 unsigned* ctl, uint4* look_aggr, uint4* look_incl, uint4* __restrict__ S, int polls)
 {
     __shared__ u128 warp_tot[kTileThreads / 32];
     __shared__ u128 prefix_sh;
@@ -906,13 +906,13 @@ __global__ void __launch_bounds__(kTileThreads)
                 u128 x = 0;
                 if (j >= 0) {
                     int k = 0;
-                    for (; k < kScanPolls; ++k) {
+                    for (; k < polls; ++k) {
                         f = ld_acquire_u32(flag + j);
                         if (f != 0u) break;
-                        if (*reinterpret_cast<volatile unsigned long long*>(total + 1)) k = kScanPolls - 1;
+                        if (*reinterpret_cast<volatile unsigned long long*>(total + 1)) k = polls - 1;
                         __nanosleep(64);
                     }
-                    if (k >= kScanPolls) f = 0u;
+                    if (k >= polls) f = 0u;
                 }
                 if (__ballot_sync(0xffffffffu, f == 0u)) {
                     failed = true;
@@ -1725,8 +1725,12 @@ int tile_accu_f32(const TopologyCore* core, TileScratch* s, const float* ext, fl
         const int64_t chunk_blocks = (nb + scan_ctas() - 1) / scan_ctas();
         const int64_t nchunk = (nb + chunk_blocks - 1) / chunk_blocks;
         unsigned* ctl = reinterpret_cast<unsigned*>(s->total + 2);
+        // test hook: LUE_GB300_TILE_POLLS (poll limit of a look-back wait; 0: every wait gives up at once,
+        // and the walk engine redoes the call)
+        int polls = kScanPolls;
+        if (const char* e = getenv("LUE_GB300_TILE_POLLS")) polls = std::max(0, atoi(e));
         k_scan_exits<<<(unsigned)nchunk, kTileThreads, 0, stream>>>(s->P, E, chunk_blocks, s->total, ctl,
-                                                                    s->look_aggr, s->look_incl, s->S);
+                                                                    s->look_aggr, s->look_incl, s->S, polls);
         count_launches(1);
         if (tc->nslot > 0) {
             k_slot_inflow<<<blocks_for(tc->nslot, 256), 256, 0, stream>>>(tc->nslot, tc->slot_at, tc->slot_first,

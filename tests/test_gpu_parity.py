@@ -256,6 +256,24 @@ def test_tile_engine_against_walk_engine_and_oracle(lfr, c1):
     parity.assert_close32(tiles, walk, "tiles vs walk")
 
 
+def test_tile_scan_waits_that_give_up_are_redone_by_the_walk_engine(lfr, c1, monkeypatch):
+    """Every look-back wait of the exit-forest scan gives up at once (LUE_GB300_TILE_POLLS=0): the scan
+    sets the redo flag, the walk engine redoes the call, and the results are the walk engine's bit for
+    bit; the next call is a normal one."""
+    fd, m, ps = c1["flow_direction"], c1["material"], c1["partition"]
+    a = lfr.from_numpy(fd, ps)
+    assert a.topology().stats()["tile_exits"] > 2 * 4096  # several scan chunks: some of them wait
+    md = lfr.from_numpy(m, ps)
+    normal = lfr.to_numpy(lfr.accu(a, md))
+    walk = _accu_with_engine(lfr, a, md, "walk")
+    assert not np.array_equal(normal, walk)  # the engines round differently: equality shows the redo
+    monkeypatch.setenv("LUE_GB300_TILE_POLLS", "0")
+    gave_up = lfr.to_numpy(lfr.accu(a, md))
+    monkeypatch.delenv("LUE_GB300_TILE_POLLS")
+    assert np.array_equal(gave_up, walk, equal_nan=True)
+    assert np.array_equal(lfr.to_numpy(lfr.accu(a, md)), normal)
+
+
 def test_tile_engine_ragged_with_no_data(lfr):
     fd, m, rng = ragged(777, 1001, 13)
     m = m.copy()
