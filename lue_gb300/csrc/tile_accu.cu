@@ -662,12 +662,17 @@ __device__ __forceinline__ unsigned long long float_to_fixed64(float x, int F)
 }
 
 // x * 2^F exactly, for x == 0 or a normal x >= 0 with x * 2^F >= 2^23 (no bit is shifted out).
-__device__ __forceinline__ unsigned long long float_to_fixed64_exact(float x, int F)
+__device__ __forceinline__ unsigned long long float_to_fixed64_exact(float x, float scale_hi)
 {
-    const unsigned b = __float_as_uint(x);
-    const unsigned m = (b & 0x7FFFFFu) | 0x800000u;
-    const int s = b ? (int)(b >> 23) - 150 + F : 0;
-    return b ? (unsigned long long)m << s : 0ull;
+    // scale_hi = 2^(F - 32).  The high and low 32-bit halves by float arithmetic, every step exact: a
+    // power-of-two scaling, the truncation of a value below 2^30 with at most 24 significant bits, its
+    // fraction (the bits under the binary point), and that fraction times 2^32 (an integer: no bit of
+    // x * 2^F lies below 2^0).  Three conversions and three float operations instead of a 64-bit shift.
+    const float y = __fmul_rn(x, scale_hi);
+    const unsigned hi = __float2uint_rz(y);
+    const float frac = __fsub_rn(y, __uint2float_rz(hi));
+    const unsigned lo = __float2uint_rz(__fmul_rn(frac, 4294967296.0f));
+    return ((unsigned long long)hi << 32) | lo;
 }
 
 // v * 2^-F rounded to float (to nearest, ties to even), for v * 2^-F in the normal float range.
@@ -1364,7 +1369,7 @@ __global__ void __launch_bounds__(kTileThreads, 4)
     unsigned long long a[kRun];
     if (exact) {
 #pragma unroll
-        for (int j = 0; j < kRun; ++j) a[j] = float_to_fixed64_exact(x[j], F);
+        for (int j = 0; j < kRun; ++j) a[j] = float_to_fixed64_exact(x[j], pow2f(F - 32));
     } else {
 #pragma unroll
         for (int j = 0; j < kRun; ++j) a[j] = float_to_fixed64(x[j], F);
