@@ -592,9 +592,9 @@ __global__ void __launch_bounds__(kTileThreads)
         const int s0 = st[i], p = s0 + sz[i] - 1;
         if (p >= kRunPositions || s0 > p) continue;  // reported above
         const bool head = (heads[p >> 5] >> (p & 31)) & 1u;
-        cell_at[T + run_table_index(p)] = (uint16_t)(i | (valid ? 0u : kNoValue) | (head ? kSegHead : 0u));
-        prev_at[T + run_table_index(p)] =
-            (uint16_t)((s0 > 0 ? scan_slot(s0 - 1) : kZeroSlot) | (s0 == p ? kPrevRidge : 0u));
+        cell_at[T + run_table_index(p)] =
+            (uint16_t)(i | (valid ? 0u : kNoValue) | (head ? kSegHead : 0u) | (s0 == p ? kLoneCell : 0u));
+        prev_at[T + run_table_index(p)] = (uint16_t)(8 * (s0 > 0 ? scan_slot(s0 - 1) : kZeroSlot));
     }
     __syncthreads();
     if (t < kRunPositions / 32 && seen[t] != 0xFFFFFFFFu) *error = 1;
@@ -1363,7 +1363,7 @@ __global__ void __launch_bounds__(kTileThreads, 4)
         const unsigned* C = reinterpret_cast<const unsigned*>(sm.S);
 #pragma unroll
         for (int j = 0; j < kRun; ++j)
-            if (C[kRunSlots * t + j] != C[run_at(pv, j) & kSlotMask]) poisoned |= 1u << j;
+            if (C[kRunSlots * t + j] != C[run_at(pv, j) >> 3]) poisoned |= 1u << j;
         __syncthreads();  // S and warp_tot are free for the value scan
     }
     unsigned long long a[kRun];
@@ -1380,22 +1380,41 @@ __global__ void __launch_bounds__(kTileThreads, 4)
     const float nan = __int_as_float(0x7fc00000);
     const float unscale = pow2f(-F);
     const ulonglong2* own = reinterpret_cast<const ulonglong2*>(sm.S + kRunSlots * t);
+    const unsigned char* Sb = reinterpret_cast<const unsigned char*>(sm.S);  // prev_at: byte offsets
+    // the subtree's sum (its prefix minus the prefix before it, < 2^62) to float: two 32-bit conversions,
+    // each rounded to nearest, and one fused rounding of their sum: within about one unit in the last
+    // place, and exact when it has at most 24 significant bits
+    auto result = [&](unsigned long long s_own, unsigned p) {
+        const unsigned long long v = s_own - *reinterpret_cast<const unsigned long long*>(Sb + p);
+        return __fmaf_rn(__uint2float_rn((unsigned)(v >> 32)), 4294967296.0f, __uint2float_rn((unsigned)v)) *
+               unscale;
+    };
+    if (clean) {  // uniform
 #pragma unroll
-    for (int i = 0; i < kRunWords; ++i) {
-        const ulonglong2 s2 = own[i];
+        for (int i = 0; i < kRunWords; ++i) {
+            const ulonglong2 s2 = own[i];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int j = 2 * i + h;
-            const unsigned w = run_at(ca, j), p = run_at(pv, j);
-            const bool none = (w & kNoValue) || ((poisoned >> j) & 1u);
-            const bool write = none || !clean || !(p & kPrevRidge);
-            if (!write) continue;
-            const unsigned long long v = (h ? s2.y : s2.x) - sm.S[p & kSlotMask];  // < 2^62
-            // two 32-bit conversions, each rounded to nearest, and one fused rounding of their sum: within
-            // about one unit in the last place, and exact when v has at most 24 significant bits
-            const float r = __fmaf_rn(__uint2float_rn((unsigned)(v >> 32)), 4294967296.0f,
-                                      __uint2float_rn((unsigned)v)) * unscale;
-            sm.M[w & kIndexMask] = none ? nan : r;
+            for (int h = 0; h < 2; ++h) {
+                const int j = 2 * i + h;
+                const unsigned w = run_at(ca, j);
+                const bool none = w & kNoValue;
+                if (!none && (w & kLoneCell)) continue;  // keeps its material (plus what enters) in M
+                const float r = result(h ? s2.y : s2.x, run_at(pv, j));
+                sm.M[w & kIndexMask] = none ? nan : r;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < kRunWords; ++i) {
+            const ulonglong2 s2 = own[i];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int j = 2 * i + h;
+                const unsigned w = run_at(ca, j);
+                const bool none = (w & kNoValue) || ((poisoned >> j) & 1u);
+                const float r = result(h ? s2.y : s2.x, run_at(pv, j));
+                sm.M[w & kIndexMask] = none ? nan : r;
+            }
         }
     }
     __syncthreads();

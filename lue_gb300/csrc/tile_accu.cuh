@@ -61,9 +61,9 @@ __host__ __device__ __forceinline__ int scan_slot(int p) { return p + 2 * (p / k
 constexpr unsigned kIndexMask = 0x0FFFu;
 constexpr unsigned kSegHead = 0x4000u;   // the first position of a root's subtree (a no-data cell is its own)
 constexpr unsigned kNoValue = 0x8000u;   // no-data flow direction or outside the array: result NaN / none
-// prev_at entries: the scan slot just before the node's subtree, and a flag.
-constexpr unsigned kSlotMask = 0x1FFFu;
-constexpr unsigned kPrevRidge = 0x8000u;  // the subtree is the cell alone
+constexpr unsigned kLoneCell = 0x1000u;  // the subtree is the cell alone (no in-tile upstream cell)
+// prev_at entries: the byte offset in the tile's scan array (8 bytes per scan slot) of the slot just
+// before the node's subtree, so that pass 3 addresses shared memory with the entry itself.
 
 struct TileCore {
     int64_t trows = 0, tcols = 0, ntiles = 0;  // tile grid
@@ -77,8 +77,8 @@ struct TileCore {
                                                // the tile, or -1
     // Per-tile flow forests in post-order (built once from the flow direction), by post-order position:
     uint16_t* cell_at = nullptr;               // [ntiles * kRunPositions] cell at the position (| kNoValue)
-    uint16_t* prev_at = nullptr;               // [ntiles * kRunPositions] scan slot before the subtree
-                                               // (kZeroSlot for a subtree at position 0) | kPrevRidge
+    uint16_t* prev_at = nullptr;               // [ntiles * kRunPositions] 8 x the scan slot before the
+                                               // subtree (kZeroSlot for a subtree at position 0)
     uint32_t* exit_span = nullptr;             // [nexit] scan slots of each exit cell: own | before << 16
     uint8_t* border_in = nullptr;              // [ntiles * kBorderCells] per border cell: outside neighbours draining in
     // Inflow slots (border cells that receive flow from other tiles), per tile in border order:
