@@ -1389,7 +1389,19 @@ __global__ void __launch_bounds__(kTileThreads, 4)
         return __fmaf_rn(__uint2float_rn((unsigned)(v >> 32)), 4294967296.0f, __uint2float_rn((unsigned)v)) *
                unscale;
     };
-    if (clean) {  // uniform
+    if (clean && exact) {  // uniform; a lone cell's sum is its own term, converted both ways exactly
+#pragma unroll
+        for (int i = 0; i < kRunWords; ++i) {
+            const ulonglong2 s2 = own[i];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int j = 2 * i + h;
+                const unsigned w = run_at(ca, j);
+                const float r = result(h ? s2.y : s2.x, run_at(pv, j));
+                sm.M[w & kIndexMask] = (w & kNoValue) ? nan : r;
+            }
+        }
+    } else if (clean) {
 #pragma unroll
         for (int i = 0; i < kRunWords; ++i) {
             const ulonglong2 s2 = own[i];
