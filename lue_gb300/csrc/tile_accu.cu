@@ -813,7 +813,7 @@ __device__ __forceinline__ bool tile_fallback(const unsigned long long* total)
     return *reinterpret_cast<const volatile unsigned long long*>(total + 1) != 0 || total[0] >= kTotalLimit;
 }
 
-constexpr int kScanItems = 16;
+constexpr int kScanItems = 8;
 constexpr int kScanBlock = kTileThreads * kScanItems;
 constexpr int kScanPolls = 1 << 20;  // poll limit of one look-back wait (a second at most)
 
