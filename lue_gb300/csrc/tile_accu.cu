@@ -762,10 +762,10 @@ struct TileForest {
 struct __align__(16) TileCallSmem {
     unsigned long long S[kScanSlotCount];  // inclusive prefix sums by scan slot; S[kZeroSlot] = 0
     float M[kTileCells];                   // material plus what enters, in cell order; then the results
-    unsigned long long warp_tot[kTileThreads / 32];
-    unsigned red[2][kTileThreads / 32];
-    unsigned warp_mn[kTileThreads / 32];
-    float warp_sum[kTileThreads / 32];
+    alignas(16) unsigned long long warp_tot[kTileThreads / 32];
+    alignas(16) unsigned red[2][kTileThreads / 32];
+    alignas(16) unsigned warp_mn[kTileThreads / 32];
+    alignas(16) float warp_sum[kTileThreads / 32];
     float seg_hi[kTileThreads / 32], seg_lo[kTileThreads / 32];  // pass 1: warp totals of the segmented scan
     int seg_head[kTileThreads / 32];
     float carry_hi[kTileThreads], carry_lo[kTileThreads];        // pass 1: what each run's first segment carries in
@@ -1042,8 +1042,12 @@ __device__ __forceinline__ void tile_prefix(TileCallSmem& sm, unsigned long long
     if (lane == 31) sm.warp_tot[warp] = x;
     __syncthreads();
     unsigned long long off = x - a[kRun - 1];
+    const ulonglong2* wt = reinterpret_cast<const ulonglong2*>(sm.warp_tot);  // 16-byte loads
 #pragma unroll
-    for (int w = 0; w < kTileThreads / 32; ++w) off += w < warp ? sm.warp_tot[w] : 0ull;
+    for (int w = 0; w < kTileThreads / 64; ++w) {
+        const ulonglong2 v = wt[w];
+        off += (2 * w < warp ? v.x : 0ull) + (2 * w + 1 < warp ? v.y : 0ull);
+    }
     ulonglong2* run = reinterpret_cast<ulonglong2*>(sm.S + kRunSlots * t);  // 144-byte runs
 #pragma unroll
     for (int i = 0; i < kRunWords; ++i) run[i] = make_ulonglong2(a[2 * i] + off, a[2 * i + 1] + off);
@@ -1338,14 +1342,16 @@ __global__ void __launch_bounds__(kTileThreads, 4)
         const float mat = sm.M[ecell];
         sm.M[ecell] = mat >= 0.0f ? mat + entering : __int_as_float(0x7fc00000);
     }
-    float in_total = 0.0f;
-    unsigned mn = st.min_bits, nan_in = 0;
-#pragma unroll
-    for (int w = 0; w < kTileThreads / 32; ++w) {  // the same order in every thread
-        in_total += sm.warp_sum[w];
-        mn = min(mn, sm.red[0][w]);
-        nan_in |= sm.red[1][w];
-    }
+    // over the eight warps, by 16-byte loads; the sum in the same order in every thread
+    static_assert(kTileThreads == 256, "eight warps per tile CTA");
+    const float4 s0 = *reinterpret_cast<const float4*>(sm.warp_sum);
+    const float4 s1 = *reinterpret_cast<const float4*>(sm.warp_sum + 4);
+    const uint4 m0 = *reinterpret_cast<const uint4*>(sm.red[0]), m1 = *reinterpret_cast<const uint4*>(sm.red[0] + 4);
+    const uint4 n0 = *reinterpret_cast<const uint4*>(sm.red[1]), n1 = *reinterpret_cast<const uint4*>(sm.red[1] + 4);
+    const float in_total = 0.0f + s0.x + s0.y + s0.z + s0.w + s1.x + s1.y + s1.z + s1.w;
+    const unsigned mn = min(min(min(min(st.min_bits, m0.x), min(m0.y, m0.z)), min(m0.w, m1.x)),
+                            min(min(m1.y, m1.z), m1.w));
+    const unsigned nan_in = n0.x | n0.y | n0.z | n0.w | n1.x | n1.y | n1.z | n1.w;
     const float bound = (st.bound + in_total) * 1.0009765625f;
     const int F = tile_scale(bound);
     if (!(bound < 1.0e38f) || (mn != 0xFFFFFFFFu && __uint_as_float(mn + 1u) * pow2f(F) < kMinQuantum)) {
