@@ -372,7 +372,7 @@ def bench_ours(args, world, rank, local):
     # host->device from a pinned numpy array, accu runs, and the outflow comes back device->host into a
     # pinned numpy array.  Three streams overlap the upload of step k+1 and the download of step k-1 with
     # the routing of step k; arrays made on one stream and used on another are recorded on it.
-    e2e_steps = max(3, min(args.steps, 8))
+    e2e_steps = max(3, min(args.steps, 20))
     m_np = lfr.pinned_empty((rows, cols), np.float32)
     m_np[...] = inputs["material"]
     out_np = [lfr.pinned_empty((rows, cols), np.float32) for _ in range(2)]
