@@ -1395,7 +1395,9 @@ __global__ void __launch_bounds__(kTileThreads, 4)
         return __fmaf_rn(__uint2float_rn((unsigned)(v >> 32)), 4294967296.0f, __uint2float_rn((unsigned)v)) *
                unscale;
     };
-    if (clean && exact) {  // uniform; a lone cell's sum is its own term, converted both ways exactly
+    if (clean && exact) {  // uniform
+        // a valid lone cell already holds its result (its material plus what enters) in M: its lanes skip
+        // the read of the prefix before it and the store (predicated, so no shared-memory traffic)
 #pragma unroll
         for (int i = 0; i < kRunWords; ++i) {
             const ulonglong2 s2 = own[i];
@@ -1403,8 +1405,13 @@ __global__ void __launch_bounds__(kTileThreads, 4)
             for (int h = 0; h < 2; ++h) {
                 const int j = 2 * i + h;
                 const unsigned w = run_at(ca, j);
-                const float r = result(h ? s2.y : s2.x, run_at(pv, j));
-                sm.M[w & kIndexMask] = (w & kNoValue) ? nan : r;
+                const bool keep = (w & (kLoneCell | kNoValue)) == kLoneCell;
+                unsigned long long before = 0ull;
+                if (!keep) before = *reinterpret_cast<const unsigned long long*>(Sb + run_at(pv, j));
+                const unsigned long long v = (h ? s2.y : s2.x) - before;
+                const float r = __fmaf_rn(__uint2float_rn((unsigned)(v >> 32)), 4294967296.0f,
+                                          __uint2float_rn((unsigned)v)) * unscale;
+                if (!keep) sm.M[w & kIndexMask] = (w & kNoValue) ? nan : r;
             }
         }
     } else if (clean) {
