@@ -758,7 +758,7 @@ struct TileForest {
     const float* inflow;
 };
 
-// Shared memory of a pass-3 tile CTA (dynamic: 53 KB, four CTAs per SM).
+// Shared memory of a tile CTA of pass 1 or pass 3 (dynamic: 53 KB, four CTAs per SM).
 struct __align__(16) TileCallSmem {
     unsigned long long S[kScanSlotCount];  // inclusive prefix sums by scan slot; S[kZeroSlot] = 0
     float M[kTileCells];                   // material plus what enters, in cell order; then the results
@@ -1048,9 +1048,12 @@ __device__ __forceinline__ void tile_prefix(TileCallSmem& sm, unsigned long long
         const ulonglong2 v = wt[w];
         off += (2 * w < warp ? v.x : 0ull) + (2 * w + 1 < warp ? v.y : 0ull);
     }
-    ulonglong2* run = reinterpret_cast<ulonglong2*>(sm.S + kRunSlots * t);  // 144-byte runs
+    unsigned long long* run = sm.S + kRunSlots * t;  // 136-byte runs
 #pragma unroll
-    for (int i = 0; i < kRunWords; ++i) run[i] = make_ulonglong2(a[2 * i] + off, a[2 * i + 1] + off);
+    for (int j = 0; j < kRun; ++j) {
+        a[j] += off;  // the thread keeps its own prefixes
+        run[j] = a[j];
+    }
     if (t == 0) sm.S[kZeroSlot] = 0ull;
     __syncthreads();
 }
@@ -1385,11 +1388,10 @@ __global__ void __launch_bounds__(kTileThreads, 4)
     // material (plus what enters) there on the fast path, which is its result
     const float nan = __int_as_float(0x7fc00000);
     const float unscale = pow2f(-F);
-    const ulonglong2* own = reinterpret_cast<const ulonglong2*>(sm.S + kRunSlots * t);
     const unsigned char* Sb = reinterpret_cast<const unsigned char*>(sm.S);  // prev_at: byte offsets
-    // the subtree's sum (its prefix minus the prefix before it, < 2^62) to float: two 32-bit conversions,
-    // each rounded to nearest, and one fused rounding of their sum: within about one unit in the last
-    // place, and exact when it has at most 24 significant bits
+    // the subtree's sum (its prefix, a[j], minus the prefix before it, < 2^62) to float: two 32-bit
+    // conversions, each rounded to nearest, and one fused rounding of their sum: within about one unit
+    // in the last place, and exact when it has at most 24 significant bits
     auto result = [&](unsigned long long s_own, unsigned p) {
         const unsigned long long v = s_own - *reinterpret_cast<const unsigned long long*>(Sb + p);
         return __fmaf_rn(__uint2float_rn((unsigned)(v >> 32)), 4294967296.0f, __uint2float_rn((unsigned)v)) *
@@ -1399,47 +1401,32 @@ __global__ void __launch_bounds__(kTileThreads, 4)
         // a valid lone cell already holds its result (its material plus what enters) in M: its lanes skip
         // the read of the prefix before it and the store (predicated, so no shared-memory traffic)
 #pragma unroll
-        for (int i = 0; i < kRunWords; ++i) {
-            const ulonglong2 s2 = own[i];
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int j = 2 * i + h;
-                const unsigned w = run_at(ca, j);
-                const bool keep = (w & (kLoneCell | kNoValue)) == kLoneCell;
-                unsigned long long before = 0ull;
-                if (!keep) before = *reinterpret_cast<const unsigned long long*>(Sb + run_at(pv, j));
-                const unsigned long long v = (h ? s2.y : s2.x) - before;
-                const float r = __fmaf_rn(__uint2float_rn((unsigned)(v >> 32)), 4294967296.0f,
-                                          __uint2float_rn((unsigned)v)) * unscale;
-                if (!keep) sm.M[w & kIndexMask] = (w & kNoValue) ? nan : r;
-            }
+        for (int j = 0; j < kRun; ++j) {
+            const unsigned w = run_at(ca, j);
+            const bool keep = (w & (kLoneCell | kNoValue)) == kLoneCell;
+            unsigned long long before = 0ull;
+            if (!keep) before = *reinterpret_cast<const unsigned long long*>(Sb + run_at(pv, j));
+            const unsigned long long v = a[j] - before;
+            const float r = __fmaf_rn(__uint2float_rn((unsigned)(v >> 32)), 4294967296.0f,
+                                      __uint2float_rn((unsigned)v)) * unscale;
+            if (!keep) sm.M[w & kIndexMask] = (w & kNoValue) ? nan : r;
         }
     } else if (clean) {
 #pragma unroll
-        for (int i = 0; i < kRunWords; ++i) {
-            const ulonglong2 s2 = own[i];
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int j = 2 * i + h;
-                const unsigned w = run_at(ca, j);
-                const bool none = w & kNoValue;
-                if (!none && (w & kLoneCell)) continue;  // keeps its material (plus what enters) in M
-                const float r = result(h ? s2.y : s2.x, run_at(pv, j));
-                sm.M[w & kIndexMask] = none ? nan : r;
-            }
+        for (int j = 0; j < kRun; ++j) {
+            const unsigned w = run_at(ca, j);
+            const bool none = w & kNoValue;
+            if (!none && (w & kLoneCell)) continue;  // keeps its material (plus what enters) in M
+            const float r = result(a[j], run_at(pv, j));
+            sm.M[w & kIndexMask] = none ? nan : r;
         }
     } else {
 #pragma unroll
-        for (int i = 0; i < kRunWords; ++i) {
-            const ulonglong2 s2 = own[i];
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int j = 2 * i + h;
-                const unsigned w = run_at(ca, j);
-                const bool none = (w & kNoValue) || ((poisoned >> j) & 1u);
-                const float r = result(h ? s2.y : s2.x, run_at(pv, j));
-                sm.M[w & kIndexMask] = none ? nan : r;
-            }
+        for (int j = 0; j < kRun; ++j) {
+            const unsigned w = run_at(ca, j);
+            const bool none = (w & kNoValue) || ((poisoned >> j) & 1u);
+            const float r = result(a[j], run_at(pv, j));
+            sm.M[w & kIndexMask] = none ? nan : r;
         }
     }
     __syncthreads();

@@ -38,24 +38,25 @@ constexpr int kBorderCells = 4 * kTile - 4;  // cells on the tile's border ring
 
 // Per-tile post-order: valid cells take positions 0 .. nvalid - 1, cells with a no-data flow direction
 // (or outside the array) the positions after them.  Scan thread t owns the run of positions 16 t ..
-// 16 t + 15.  Prefix sums are kept in shared memory by scan slot: position p has slot p + 2 (p / 16),
-// so that each thread's run is 144 bytes (16-byte stores of a quarter-warp fall on distinct banks);
-// slot kZeroSlot holds 0 (the prefix before position 0).  Per-position tables are stored
+// 16 t + 15.  Prefix sums are kept in shared memory by scan slot: position p has slot p + p / 16, so
+// that each thread's run is 136 bytes and the 8-byte accesses of a warp at one offset into the runs
+// (the stores of the scan, the reads of the prefix just before a small subtree) fall on distinct banks
+// in pairs of lanes; slot kZeroSlot holds 0 (the prefix before position 0).  Per-position tables are stored
 // word-transposed: the 16-bit entries of positions 16 t + 2 i and 16 t + 2 i + 1 form word i of thread
 // t, at word index 256 i + t, so that each of a thread's eight table loads is one coalesced 128-byte
 // line per warp.
 constexpr int kRun = 16;
 constexpr int kRunWords = kRun / 2;
 constexpr int kRunPositions = kRun * kTileThreads;  // 4096: every cell of the tile, nothing else
-constexpr int kRunSlots = kRun + 2;                 // scan slots per thread run (two pad slots)
-constexpr int kZeroSlot = kRunSlots * kTileThreads; // 4608
+constexpr int kRunSlots = kRun + 1;                 // scan slots per thread run (one pad slot)
+constexpr int kZeroSlot = kRunSlots * kTileThreads; // 4352
 constexpr int kScanSlotCount = kZeroSlot + 2;
 __host__ __device__ __forceinline__ int run_table_index(int p)
 {
     const int t = p / kRun, j = p - kRun * t;
     return ((j >> 1) * kTileThreads + t) * 2 + (j & 1);
 }
-__host__ __device__ __forceinline__ int scan_slot(int p) { return p + 2 * (p / kRun); }
+__host__ __device__ __forceinline__ int scan_slot(int p) { return p + p / kRun; }
 
 // cell_at entries: the cell (0..4095) and two flags.
 constexpr unsigned kIndexMask = 0x0FFFu;
