@@ -611,10 +611,14 @@ int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stre
         TRY(cudaGetLastError(), "producers");
         TRY(cudaStreamSynchronize(stream), "producers");  // po must outlive the copy
         sc->bytes += (sc->nstages + 1) * 8 + po[sc->nstages] * 8 + sc->nstages * 4;
-        // Ticket order: the stages sorted by their earliest start in a model of a one-step call (a stage
-        // starts kHandOffRounds after the last exit round of its last producer), so that CTAs take stages
-        // about in the order in which their inputs become ready.  A producer's start is always earlier
-        // than its consumers', so the order keeps every producer before the stages it feeds.
+        // Ticket order: the stages sorted by their latest start in a model of a one-step call (a stage
+        // can start kHandOffRounds after the last exit round of its last producer; its latest start is
+        // the last one that still lets every stage it feeds start in time for the whole call to finish at
+        // the model's earliest end), so that CTAs take the stages with least slack, the critical chain,
+        // first among those that can start at about the same time.  A producer's latest start is always
+        // earlier than its consumers', so the order keeps every producer before the stages it feeds.
+        // LUE_GB300_STAGE_ORDER=early sorts by the earliest start instead (measured slower: one
+        // kinematic-wave step at 8192^2 20.1 ms against 15.4 ms, 100 steps 1.55 against 1.36 ms per step).
         {
             constexpr int64_t kHandOffRounds = 2;
             const int64_t ns = sc->nstages, npairs = po[ns];
@@ -624,13 +628,27 @@ int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stre
             TRY(cudaMemcpy(mxr.data(), sc->max_exit_round, ns * sizeof(int32_t), cudaMemcpyDeviceToHost),
                 "stage order");
             std::vector<int64_t> start(ns, 0);
-            int64_t last = 0;
+            int64_t last = 0, finish = 0;
             for (int64_t k = 0; k < ns; ++k) {
                 int64_t s0 = 0;
                 for (int64_t j = po[k]; j < po[k + 1]; ++j)
                     s0 = std::max<int64_t>(s0, start[pr[j].x] + mxr[pr[j].x] + 1 + kHandOffRounds);
                 start[k] = s0;
                 last = std::max(last, s0);
+                finish = std::max<int64_t>(finish, s0 + (srec[ws[k]].z & 0xFFFF));
+            }
+            const char* order_env = getenv("LUE_GB300_STAGE_ORDER");
+            if (!(order_env && order_env[0] == 'e')) {
+                std::vector<int64_t> late(ns);
+                for (int64_t k = 0; k < ns; ++k) late[k] = finish - (srec[ws[k]].z & 0xFFFF);
+                for (int64_t k = ns - 1; k >= 0; --k)
+                    for (int64_t j = po[k]; j < po[k + 1]; ++j)
+                        late[pr[j].x] = std::min<int64_t>(late[pr[j].x], late[k] - mxr[pr[j].x] - 1 - kHandOffRounds);
+                last = 0;
+                for (int64_t k = 0; k < ns; ++k) {
+                    start[k] = std::max<int64_t>(0, late[k]);
+                    last = std::max(last, start[k]);
+                }
             }
             // counting sort by start, stable (ties keep the depth order)
             std::vector<int64_t> bucket(last + 2, 0);
