@@ -136,6 +136,17 @@ typedef struct lue_gpu_stage_schedule {
 int lue_gpu_topology_get_stage_schedule(const lue_gpu_topology* topology, lue_gpu_stage_schedule* schedule);
 int lue_gpu_topology_set_stage_schedule(lue_gpu_topology* topology, const lue_gpu_stage_schedule* schedule);
 
+/* Order in which the CTAs of a stage-engine call take the stages (no reference counterpart; results do not
+ * depend on it).  LATEST (the default): by the latest start that keeps the call's critical chain on time,
+ * the stages with least slack first; the fastest for one call on an otherwise idle GPU.  EARLIEST: by the
+ * earliest start, about the order in which the stages' inputs become ready; its CTAs wait less, which
+ * suits many calls running at the same time (a server).  Like the cap, the order belongs to the stage
+ * structures: setting another one frees them (they are rebuilt by the next call that needs them, after
+ * all work on the device) and is refused with LUE_GPU_EINVAL while clones exist. */
+enum { LUE_GPU_STAGE_ORDER_LATEST = 0, LUE_GPU_STAGE_ORDER_EARLIEST = 1 };
+int lue_gpu_topology_set_stage_order(lue_gpu_topology* topology, int order);
+int lue_gpu_topology_get_stage_order(const lue_gpu_topology* topology, int* order);
+
 /* A call to time: issues one routing call on `topology` on `stream` and returns its status. */
 typedef int (*lue_gpu_stage_call)(lue_gpu_topology* topology, void* user, void* stream);
 

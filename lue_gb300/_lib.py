@@ -92,6 +92,8 @@ def _declare(L):
         "lue_gpu_d8_flow_direction_f64": ([p, i64, i64, p, p], i32),
         "lue_gpu_topology_get_stage_schedule": ([p, ctypes.POINTER(StageSchedule)], i32),
         "lue_gpu_topology_set_stage_schedule": ([p, ctypes.POINTER(StageSchedule)], i32),
+        "lue_gpu_topology_set_stage_order": ([p, i32], i32),
+        "lue_gpu_topology_get_stage_order": ([p, ctypes.POINTER(i32)], i32),
         "lue_gpu_autotune_stage_schedule": ([p, STAGE_CALL, p, i32, p, ctypes.POINTER(StageSchedule)], i32),
     }
     for name, (args, res) in sig.items():

@@ -67,6 +67,19 @@ extern "C" int lue_gpu_topology_set_stage_schedule(lue_gpu_topology* topology, c
     return stage_schedule_set(topology, schedule->cap, schedule->threads, schedule->publish_every);
 }
 
+extern "C" int lue_gpu_topology_set_stage_order(lue_gpu_topology* topology, int order)
+{
+    if (!topology) return fail(LUE_GPU_EINVAL, "set_stage_order: NULL argument");
+    return stage_order_set(topology, order);
+}
+
+extern "C" int lue_gpu_topology_get_stage_order(const lue_gpu_topology* topology, int* order)
+{
+    if (!topology || !order) return fail(LUE_GPU_EINVAL, "get_stage_order: NULL argument");
+    *order = topology->core->stage_order;
+    return LUE_GPU_OK;
+}
+
 extern "C" int lue_gpu_autotune_stage_schedule(lue_gpu_topology* topology, lue_gpu_stage_call call, void* user,
                                                int repeats, void* stream_, lue_gpu_stage_schedule* best)
 {

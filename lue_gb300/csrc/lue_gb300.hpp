@@ -66,6 +66,15 @@ class Topology {
     {
         check(lue_gpu_topology_set_stage_schedule(_h, &s), "set_stage_schedule");
     }
+    // The order in which a stage-engine call takes its stages (lue_gpu_topology_{get,set}_stage_order):
+    // LUE_GPU_STAGE_ORDER_LATEST (default) or LUE_GPU_STAGE_ORDER_EARLIEST (for many calls at once).
+    int stage_order() const
+    {
+        int o = 0;
+        check(lue_gpu_topology_get_stage_order(_h, &o), "stage_order");
+        return o;
+    }
+    void set_stage_order(int order) { check(lue_gpu_topology_set_stage_order(_h, order), "set_stage_order"); }
 
     // Autotunes the stage schedule for `call`, a callable that issues one routing call over this topology on
     // `stream`; keeps the fastest schedule and returns it (lue_gpu_autotune_stage_schedule).  An exception

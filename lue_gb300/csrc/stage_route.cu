@@ -617,8 +617,10 @@ int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stre
         // the model's earliest end), so that CTAs take the stages with least slack, the critical chain,
         // first among those that can start at about the same time.  A producer's latest start is always
         // earlier than its consumers', so the order keeps every producer before the stages it feeds.
-        // LUE_GB300_STAGE_ORDER=early sorts by the earliest start instead (measured slower: one
-        // kinematic-wave step at 8192^2 20.1 ms against 15.4 ms, 100 steps 1.55 against 1.36 ms per step).
+        // LUE_GPU_STAGE_ORDER_EARLIEST sorts by the earliest start instead (about the order in which the
+        // stages' inputs become ready: fewer waiting CTAs, for servers that run many calls at once; alone
+        // on the GPU it is slower: one kinematic-wave step at 8192^2 20.1 ms against 15.4 ms, 100 steps
+        // 1.55 against 1.36 ms per step).
         {
             constexpr int64_t kHandOffRounds = 2;
             const int64_t ns = sc->nstages, npairs = po[ns];
@@ -637,8 +639,7 @@ int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stre
                 last = std::max(last, s0);
                 finish = std::max<int64_t>(finish, s0 + (srec[ws[k]].z & 0xFFFF));
             }
-            const char* order_env = getenv("LUE_GB300_STAGE_ORDER");
-            if (!(order_env && order_env[0] == 'e')) {
+            if (core->stage_order != LUE_GPU_STAGE_ORDER_EARLIEST) {
                 std::vector<int64_t> late(ns);
                 for (int64_t k = 0; k < ns; ++k) late[k] = finish - (srec[ws[k]].z & 0xFFFF);
                 for (int64_t k = ns - 1; k >= 0; --k)
@@ -1344,6 +1345,27 @@ int stage_schedule_set(lue_gpu_topology* t, int cap, int threads, int publish_ev
     }
     t->stage_threads = threads;
     t->publish_every = publish_every;
+    return LUE_GPU_OK;
+}
+
+int stage_order_set(lue_gpu_topology* t, int order)
+{
+    if (order != LUE_GPU_STAGE_ORDER_LATEST && order != LUE_GPU_STAGE_ORDER_EARLIEST)
+        return fail(LUE_GPU_EINVAL, "stage order: must be LUE_GPU_STAGE_ORDER_LATEST or _EARLIEST");
+    TopologyCore* core = t->core;
+    std::lock_guard<std::mutex> lock(core->stage_mutex);
+    if (order == core->stage_order) return LUE_GPU_OK;
+    if (core->refs.load() > 1)
+        return fail(LUE_GPU_EINVAL, "stage order: the stage structures are shared with " +
+                                        std::to_string(core->refs.load() - 1) + " clone(s); change the order before cloning");
+    if (core->stages) {
+        // the handle's streams are unknown here: wait for all work before the structures go
+        if (int rc = cuda_status(cudaDeviceSynchronize(), "stage order")) return rc;
+        core->bytes -= core->stages->bytes;
+        stage_core_free(core->stages);
+        core->stages = nullptr;
+    }
+    core->stage_order = order;  // rebuilt with it by the next call that needs them
     return LUE_GPU_OK;
 }
 

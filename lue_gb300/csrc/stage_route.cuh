@@ -89,6 +89,7 @@ int stage_prepare(lue_gpu_topology* t, cudaStream_t stream);
 // Setting another cap frees the stage structures (rebuilt by the next call); refused while clones share them.
 void stage_schedule_get(const lue_gpu_topology* t, int* cap, int* threads, int* publish_every);
 int stage_schedule_set(lue_gpu_topology* t, int cap, int threads, int publish_every);
+int stage_order_set(lue_gpu_topology* t, int order);
 int stage_route_f32(lue_gpu_topology* t, int rule, const float* a, float as, const float* b, float bs, float* out,
                     float* rem, cudaStream_t stream, bool* done);
 int stage_route_f64(lue_gpu_topology* t, int rule, const double* a, double as, const double* b, double bs,

@@ -23,6 +23,7 @@ struct TopologyCore {
     std::vector<int32_t> level_offsets;  // [levels + 1] start of each level in `order`
     StageCore* stages = nullptr;         // stage engine (acyclic rasters; built on first use)
     int stage_cap = 0;                   // most cells of one stage when built (0: LUE_GB300_STAGE_CAP or 128)
+    int stage_order = LUE_GPU_STAGE_ORDER_LATEST;  // ticket order of the stage structures when built
     bool stages_unavailable = false;     // the raster is beyond the stage engine's limits
     PathCore* paths = nullptr;           // path engine (acyclic rasters; built on first use)
     bool paths_unavailable = false;      // the raster is beyond the path engine's limits

@@ -106,6 +106,24 @@ class Topology:
         s = _lib.StageSchedule(int(cap), int(threads), int(publish_every), 0.0)
         _lib.check(_lib.lib().lue_gpu_topology_set_stage_schedule(self.handle, ctypes.byref(s)))
 
+    STAGE_ORDERS = {"latest": 0, "earliest": 1}
+
+    def stage_order(self):
+        """The order in which a stage-engine call's CTAs take the stages: "latest" (least slack first, the
+        fastest for one call alone on the GPU) or "earliest" (about the order in which inputs become
+        ready: fewer waiting CTAs when many calls run at once)."""
+        o = ctypes.c_int()
+        _lib.check(_lib.lib().lue_gpu_topology_get_stage_order(self.handle, ctypes.byref(o)))
+        return {v: k for k, v in self.STAGE_ORDERS.items()}[o.value]
+
+    def set_stage_order(self, order):
+        """Sets the stage order ("latest" or "earliest"); results do not depend on it.  Like another cap,
+        another order frees the stage structures (rebuilt by the next call) and is refused while clones
+        share them."""
+        if order not in self.STAGE_ORDERS:
+            raise ValueError(f"stage order must be one of {sorted(self.STAGE_ORDERS)}")
+        _lib.check(_lib.lib().lue_gpu_topology_set_stage_order(self.handle, self.STAGE_ORDERS[order]))
+
     def stats(self):
         s = _lib.TopologyStats()
         _lib.check(_lib.lib().lue_gpu_topology_get_stats(self.handle, ctypes.byref(s)))

@@ -90,9 +90,12 @@ class Server:
         self.grids = [lfr.from_numpy(fd, device=self.device) for fd in pool_fds]
         self.topologies = [g.topology() for g in self.grids]
         # everything a request would otherwise build or allocate on its first call: the stage
-        # structures of each grid, one handle (scratch) per grid, and pinned result buffers
+        # structures of each grid, one handle (scratch) per grid, and pinned result buffers.  Many
+        # requests run at once, so the stage engine takes its stages in about the order in which their
+        # inputs become ready (fewer CTAs waiting on others while other requests need the SMs).
         self.free_clones = collections.defaultdict(list)
         for g, t in enumerate(self.topologies):
+            t.set_stage_order("earliest")
             t.prepare()
             self.free_clones[g].append(t.clone())
         self._warm_pinned(slots)

@@ -61,6 +61,38 @@ def test_kinematic_wave_steps_do_not_depend_on_the_schedule(lfr):
         assert np.array_equal(got, want, equal_nan=True), (cap, threads, publish)
 
 
+def test_stage_order_round_trip_and_results_do_not_depend_on_it(lfr):
+    """Both ticket orders (latest start, the default; earliest start, for servers) give the same bits for
+    a one-step and a multi-step kinematic wave and for accu_threshold; another order is refused while
+    clones share the stage structures, and a bad order is refused."""
+    fd, q, lat, alpha = _kw_case(lfr)
+    t = fd.topology()
+    assert t.stage_order() == "latest"
+    want1 = lfr.to_numpy(lfr.kinematic_wave(fd, q, lat, alpha, 0.6, 3600.0, 100.0))
+    want9 = lfr.to_numpy(lfr.kinematic_wave_steps(fd, q, lat, alpha, 0.6, 3600.0, 100.0, 9))
+    t.set_stage_order("earliest")
+    assert t.stage_order() == "earliest"
+    assert np.array_equal(lfr.to_numpy(lfr.kinematic_wave(fd, q, lat, alpha, 0.6, 3600.0, 100.0)), want1,
+                          equal_nan=True)
+    assert np.array_equal(lfr.to_numpy(lfr.kinematic_wave_steps(fd, q, lat, alpha, 0.6, 3600.0, 100.0, 9)), want9,
+                          equal_nan=True)
+    c = t.clone()
+    with pytest.raises(_lib.LueGpuError) as e:
+        t.set_stage_order("latest")
+    assert "clone" in str(e.value)
+    c.close()
+    with pytest.raises(_lib.LueGpuError) as e:
+        _lib.check(_lib.lib().lue_gpu_topology_set_stage_order(t.handle, 7))
+    assert e.value.status == 1
+    t.set_stage_order("latest")
+    fdt, m, thr = _threshold_case(lfr, 300, 350, 9)
+    a = [lfr.to_numpy(x) for x in lfr.accu_threshold(fdt, m, thr)]
+    fdt.topology().set_stage_order("earliest")
+    b = [lfr.to_numpy(x) for x in lfr.accu_threshold(fdt, m, thr)]
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y, equal_nan=True)
+
+
 def test_bad_schedules_and_cap_changes_under_clones_are_refused(lfr):
     fd, m, thr = _threshold_case(lfr, 200, 300, 5)
     t = fd.topology()
