@@ -9,10 +9,10 @@
 //      subtree) to P, in the post-order of the exit forest, with per-tile statistics of the material for
 //      pass 3.  An exit is a root of the tile's forest, and the subtrees of the roots are consecutive runs
 //      of positions, so its value is a segmented sum (float-float, no cancellation).
-//   2. Exit forest: exit y's parent is the exit reached by following the flow from y's downstream
-//      cell through that cell's tile.  The final value of exit y is the sum of the local values over
-//      y's subtree of this forest, so an inclusive prefix sum over P in post-order gives every subtree
-//      sum as a difference of two prefix sums.  The sums are exact: 128-bit fixed point (96 value bits,
+//   2. k_scan_exits, over the exit forest: exit y's parent is the exit reached by following the flow
+//      from y's downstream cell through that cell's tile.  The final value of exit y is the sum of the
+//      local values over y's subtree of this forest, so an inclusive prefix sum over P in post-order
+//      gives every subtree sum as a difference of two prefix sums.  The sums are exact: 128-bit fixed point (96 value bits,
 //      32 bits counting no-data exits), so summation order cannot change the result.
 //   3. k_slot_inflow: per border cell that receives flow from other tiles, the exact sum of the subtree
 //      sums of the exits draining into it, rounded to float once.
