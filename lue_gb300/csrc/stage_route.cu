@@ -622,7 +622,12 @@ int stage_core_build(const TopologyCore* core, uint32_t* work, cudaStream_t stre
         // on the GPU it is slower: one kinematic-wave step at 8192^2 20.1 ms against 15.4 ms, 100 steps
         // 1.55 against 1.36 ms per step).
         {
-            constexpr int64_t kHandOffRounds = 2;
+            // the model's hand-off between a producer's last exit round and a consumer's start, in rounds:
+            // 2 for the earliest-start order; 32 for the latest-start order (measured at 8192^2, 100
+            // kinematic-wave steps: 136.0 ms at 2, 133.3 at 6, 131.1-131.5 from 16 to 128).
+            // LUE_GB300_STAGE_HANDOFF overrides it.
+            int64_t kHandOffRounds = core->stage_order == LUE_GPU_STAGE_ORDER_EARLIEST ? 2 : 32;
+            if (const char* e = getenv("LUE_GB300_STAGE_HANDOFF")) kHandOffRounds = std::max(0, atoi(e));
             const int64_t ns = sc->nstages, npairs = po[ns];
             std::vector<int2> pr(std::max<int64_t>(1, npairs));
             std::vector<int32_t> mxr(ns);
