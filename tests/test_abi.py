@@ -62,3 +62,7 @@ def test_schedule_and_autotune_entry_points_reject_bad_arguments_without_a_gpu()
     cb = _lib.STAGE_CALL(lambda handle, user, stream: 0)
     assert L.lue_gpu_autotune_stage_schedule(None, cb, None, 1, None, ctypes.byref(s)) == 1
     assert b"NULL" in L.lue_gpu_last_error()
+    order = ctypes.c_int(-1)
+    assert L.lue_gpu_topology_set_stage_order(None, 0) == 1
+    assert L.lue_gpu_topology_get_stage_order(None, ctypes.byref(order)) == 1
+    assert b"NULL" in L.lue_gpu_last_error() and order.value == -1
