@@ -84,14 +84,6 @@ __device__ __forceinline__ u128 exit_value_fixed(float2 v, int F)
     return float_to_fixed(v.x, F) + float_to_fixed(v.y, F);
 }
 
-__device__ __forceinline__ double fixed_to_double(u128 v, int F)
-{
-    u128 a = v & kValueMask;
-    double hi = (double)(unsigned long long)(a >> 64) * 18446744073709551616.0;
-    double lo = (double)(unsigned long long)a;
-    return ldexp(hi + lo, -F);
-}
-
 // ---------------------------------------------------------------------------------------------------
 // Build
 // ---------------------------------------------------------------------------------------------------
@@ -416,14 +408,6 @@ __device__ __forceinline__ void border_cell(int b, int& rin, int& cin)
     else { rin = b - (3 * kTile - 2) + 1; cin = kTile - 1; }
 }
 
-// Border index (0..251, see border_cell) of a border cell of the tile.
-__device__ __forceinline__ int border_index(int rin, int cin)
-{
-    if (rin == 0) return cin;
-    if (rin == kTile - 1) return kTile + cin;
-    return cin == 0 ? 2 * kTile + rin - 1 : 3 * kTile - 2 + rin - 1;
-}
-
 // Exclusive prefix of one int per thread over the block; `total` gets the block sum.
 __device__ __forceinline__ int block_exclusive_int(int v, int* warp_tot, int& total)
 {
@@ -675,31 +659,6 @@ __device__ __forceinline__ unsigned long long float_to_fixed64_exact(float x, fl
     return ((unsigned long long)hi << 32) | lo;
 }
 
-// v * 2^-F rounded to float (to nearest, ties to even), for v * 2^-F in the normal float range.
-__device__ __forceinline__ float u64_to_float_scaled(unsigned long long v, int F)
-{
-    if (v == 0) return 0.0f;
-    const int lz = __clzll((long long)v);
-    const unsigned long long n = v << lz;  // leading bit at 63
-    const unsigned hi = (unsigned)(n >> 32), lo = (unsigned)n;
-    unsigned mant = hi >> 8;  // 24 bits with the implicit one
-    const unsigned round = (hi >> 7) & 1u, sticky = ((hi & 0x7Fu) | lo) != 0u;
-    mant += round & (sticky | (mant & 1u));
-    // biased exponent 63 - lz - F + 127; a mantissa that rounds up to 2^24 carries into it
-    return __uint_as_float((unsigned)(63 - lz + 126 - F) * 0x800000u + mant);
-}
-__device__ __forceinline__ float u64_to_float(unsigned long long v) { return u64_to_float_scaled(v, 0); }
-
-// A fixed-point value V * 2^-F as float-float (hi, lo): hi holds the top 24 bits of V, lo the rest.
-__device__ __forceinline__ float2 fixed64_to_ff(unsigned long long V, int F)
-{
-    if (V == 0) return make_float2(0.0f, 0.0f);
-    const int lz = __clzll((long long)V);
-    const unsigned long long keep = lz >= 40 ? ~0ull : ~((1ull << (40 - lz)) - 1ull);
-    const float s = pow2f(-F);
-    return make_float2(u64_to_float(V & keep) * s, u64_to_float(V & ~keep) * s);
-}
-
 // A 96-bit fixed-point value v * 2^-F, rounded to float (the bits below the top 64 are dropped).
 __device__ __forceinline__ float fixed128_to_float(u128 v, int F)
 {
@@ -707,14 +666,6 @@ __device__ __forceinline__ float fixed128_to_float(u128 v, int F)
     if (hi == 0) return ldexpf(__ull2float_rn((unsigned long long)v), -F);
     const int shift = 64 - __clzll((long long)hi);
     return ldexpf(__ull2float_rn((unsigned long long)(v >> shift)), shift - F);
-}
-
-// v * 2^d rounded to the nearest integer (v < 2^96; the result is known to be < 2^62).
-__device__ __forceinline__ unsigned long long rescale_fixed(u128 v, int d)
-{
-    if (d >= 0) return d >= 64 ? 0ull : (unsigned long long)(v << d);  // d >= 62 leaves room only for v == 0
-    if (d <= -97) return 0;
-    return (unsigned long long)((v + ((u128)1 << (-d - 1))) >> (-d));
 }
 
 // Cells of a tile by thread in cell order: thread t holds the 4 x 4 cells (row (t + 256 j) / 16,
@@ -795,11 +746,6 @@ __device__ __forceinline__ void load_material(float4 (&x)[4], const float* __res
         x[j] = ext ? load_quad(ext, g, tr * kTile + (cell >> 6), tc * kTile + (cell & 63), vec, 0.0f)
                    : make_float4(ext_s, ext_s, ext_s, ext_s);
     }
-}
-
-__device__ __forceinline__ float quad_at(const float4& q, int k)
-{
-    return k == 0 ? q.x : (k == 1 ? q.y : (k == 2 ? q.z : q.w));
 }
 
 // The material total in 2^-16 units at or beyond this makes the tile engine hand the call to the walk
