@@ -38,15 +38,6 @@ __device__ __forceinline__ ffloat ff_fast_two_sum(float a, float b)  // |a| >= |
     const float s = __fadd_rn(a, b);
     return ffloat{s, __fsub_rn(b, __fsub_rn(s, a))};
 }
-__device__ __forceinline__ ffloat ff_add(ffloat a, ffloat b)
-{
-    ffloat s = ff_two_sum(a.hi, b.hi);
-    const ffloat t = ff_two_sum(a.lo, b.lo);
-    s.lo = __fadd_rn(s.lo, t.hi);
-    s = ff_fast_two_sum(s.hi, s.lo);
-    s.lo = __fadd_rn(s.lo, t.lo);
-    return ff_fast_two_sum(s.hi, s.lo);
-}
 __device__ __forceinline__ ffloat ff_neg(ffloat a) { return ffloat{-a.hi, -a.lo}; }
 __device__ __forceinline__ ffloat ff_prod(float a, float b)
 {
@@ -161,13 +152,6 @@ __device__ __forceinline__ void ff_powers_f(float x, int p, int m, ffloat& yp, f
         if (e == p) yp = r;
         if (e == m) ym = r;
     }
-}
-
-template <int P, int M>
-__device__ __forceinline__ ffloat kw_poly_g(ffloat y, float al, const ffloat& known, const KWConstFF& K)
-{
-    const ffloat ym = ff_pow_n<M>(y, K.br.m), yp = ff_pow_n<P>(y, K.br.p);
-    return ff_add_sloppy(ff_add_sloppy(ff_mul(K.k, ym), ff_mul_f(yp, al)), ff_neg(known));
 }
 
 // y = Q^(1/m) in float-float, for the state of a cell that starts from discharge Q (rare: once per call

@@ -86,12 +86,6 @@ struct StageSortSmem {
     int warp_tot[kStageBuildThreads / 32];
 };
 
-// Depth of in-tile cell p, or of the global cell gi when p < 0 (another tile).
-__device__ __forceinline__ int32_t depth_of(const StageSortSmem& sm, const int32_t* depth, int p, int64_t gi)
-{
-    return p >= 0 ? sm.d[p] : __ldg(depth + gi);
-}
-
 // Per tile: the order of its valid cells by (depth, distance to the depth group's most downstream cell),
 // cut into stages of at most `cap` consecutive cells of one depth; the rounds; and per position a flag
 // word (bit 0: first cell of a stage, bit 1: the outflow leaves the stage, bits 2-9: mask of the upstream
