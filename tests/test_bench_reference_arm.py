@@ -26,3 +26,21 @@ def test_reference_arm_prints_one_json_line():
     assert d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert d["config"]["workload"] == "accu_1k"
+
+
+def test_committed_profiles_carry_the_lines_the_bench_reads():
+    """bench.py takes the accu call's DRAM traffic and the multi-step kinematic wave's instructions per
+    cell step from the committed ncu summaries under profiles/: both lines exist and are plausible."""
+    sys.path.insert(0, ROOT)
+    try:
+        import bench
+    finally:
+        sys.path.remove(ROOT)
+    traffic = bench.profile_traffic("accu_f32_tiles")
+    assert traffic is not None
+    nbytes, cells = traffic
+    assert 9.0 <= nbytes / cells <= 40.0  # at least the algorithmic 9 B/cell
+    ipcs = bench.profile_value("warp_instructions_per_cell_step", "k_stage_flow_kw")
+    assert ipcs is not None and 1.0 < ipcs[0][0] < 100.0
+    fma = bench.profile_value("fma_pipe_pct", "k_stage_flow_kw")
+    assert fma is not None and 0.0 < fma[0][0] <= 100.0
